@@ -1,0 +1,115 @@
+/* turbotops_gb300.h — C-ABI of the GB300 front end of turbotops.
+ *
+ * Plain C: no exceptions, no C++ or torch types cross this boundary. Every
+ * entry point returns a TT_* status; tt_last_error() holds the message. The
+ * C++ host layer (turbotops_gb300/host) maps statuses back to the exception
+ * types and messages the reference throws (std::invalid_argument,
+ * std::overflow_error, std::length_error).
+ *
+ * Pointers named *_dev are device pointers; they are used in stream order on
+ * the context's stream. Entry points ending in _h take host pointers and
+ * synchronise before returning. Device results owned by the context (the
+ * tt_*_out structs) stay valid until the next call on the same context.
+ *
+ * Reference interfaces each entry point replaces are cited as
+ * file:line in dnbaker/turbotops v0.1.0.
+ */
+#ifndef TURBOTOPS_GB300_H
+#define TURBOTOPS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TT_OK 0
+#define TT_ERR_INVALID 1   /* std::invalid_argument */
+#define TT_ERR_OVERFLOW 2  /* std::overflow_error */
+#define TT_ERR_LENGTH 3    /* std::length_error (memory, capacity) */
+#define TT_ERR_CUDA 4      /* CUDA runtime error */
+#define TT_ERR_TIMEOUT 5   /* a bounded device wait ran out */
+#define TT_ERR_INTERNAL 6
+
+#define TT_METRIC_L1 0
+#define TT_METRIC_L2 1
+#define TT_METRIC_LINF 2
+#define TT_METRIC_LP 3
+
+typedef struct tt_ctx tt_ctx;
+
+/* Library version, "MAJOR.MINOR.PATCH" of the reference it mirrors. */
+const char* tt_version(void);
+
+/* Context: device, stream (a cudaStream_t used as given; NULL is the legacy
+ * default stream), reusable device arena. */
+int tt_ctx_create(int device, void* stream, tt_ctx** out);
+void tt_ctx_destroy(tt_ctx* ctx);
+const char* tt_last_error(const tt_ctx* ctx);
+/* Kernels launched through the context since creation. */
+uint64_t tt_ctx_launches(const tt_ctx* ctx);
+int tt_ctx_synchronize(tt_ctx* ctx);
+/* Stream-ordered copy of bytes between any two device or host addresses
+ * (lets bindings move context-owned results into their own buffers). */
+int tt_copy_async(tt_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+/* Metric::parse + Metric::minkowski (metric.hpp:227-253): "l1" | "l2" |
+ * "linf" | "euclidean" | "manhattan" | "chebyshev" | "lp:<p>", p >= 1. */
+int tt_metric_parse(const char* s, int* kind, float* p);
+
+/* make_dense, full layout (rips.hpp:391-403) + enclosing_radius
+ * (rips.hpp:370-380). x_dev: n x dim row-major; mat_dev: n x n.
+ * *enclosing (host, may be NULL) receives min_i max_j d(i, j) (+inf if n = 0). */
+int tt_dense_distances(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p,
+                       float* mat_dev, float* enclosing);
+
+/* Result of tt_dim0: device arrays owned by the context. */
+typedef struct tt_dim0_out {
+    uint64_t edges;                     /* kept edges (d <= threshold) */
+    const uint64_t* edge_keys_dev;      /* sorted: diameter bits << 33 | (2^33-1 - index) */
+    const uint8_t* apparent_dev;        /* per sorted edge: zero-apparent (maxdim >= 1) */
+    const uint8_t* tree_dev;            /* per sorted edge: in the spanning forest */
+    uint64_t columns;                   /* dim-1 columns, descending filtration order */
+    const uint64_t* col_index_dev;
+    const float* col_diameter_dev;
+    const uint64_t* col_cofacet_dev;    /* first zero cofacet (triangle index) or UINT64_MAX */
+    const uint8_t* col_cofacet_app_dev; /* that cofacet has a zero-apparent facet */
+    uint64_t h0_finite;                 /* finite H0 bars with death > 0, discovery order */
+    const float* h0_death_dev;
+    uint64_t essential;                 /* connected components: essential H0 bars */
+} tt_dim0_out;
+
+/* Reducer::dim0 (rips.hpp:685-870). The complex is the dense full matrix
+ * mat_dev (n x n) when it is not NULL, else the CSR graph rp/ci/w (device;
+ * CsrGraph layout core.hpp:92-98, rows sorted by neighbour id). Edges with
+ * d <= threshold are kept. maxdim >= 1 computes apparent flags and columns. */
+int tt_dim0(tt_ctx* ctx, const float* mat_dev, const uint64_t* rp_dev, const uint32_t* ci_dev,
+            const float* w_dev, uint32_t n, float threshold, uint32_t maxdim, tt_dim0_out* out);
+
+/* redzed::detail::build_edges (redzed.hpp:545-613): kept edges sorted by
+ * (diameter asc, combinatorial index asc); verts_dev holds (i, j), i < j.
+ * Same complex convention as tt_dim0. *count receives the edge count;
+ * TT_ERR_LENGTH if it exceeds cap (nothing written). */
+int tt_redzed_edges(tt_ctx* ctx, const float* mat_dev, const uint64_t* rp_dev, const uint32_t* ci_dev,
+                    const float* w_dev, uint32_t n, float threshold, float* diam_dev, int32_t* verts_dev,
+                    uint64_t cap, uint64_t* count);
+
+/* Front end of the dense full-Rips path with host buffers (the call the
+ * reference's rips::compute_dense front end binds, rips.hpp:1068-1075 +
+ * :685-870): points -> distances -> enclosing radius -> dim0, everything a
+ * host reducer needs, copied back.
+ *   mat_h      n x n distances (may be NULL)
+ *   h0_h       finite H0 deaths (capacity n)
+ *   col_idx_h / col_d_h / col_cf_h / col_cf_app_h   columns (capacity n(n-1)/2
+ *              or *ncols from a first call with col_idx_h == NULL)
+ *   thr_inout  threshold in (+inf: enclosing radius), effective threshold out */
+int tt_dense_front_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p,
+                     uint32_t maxdim, float* thr_inout, float* mat_h, float* h0_h, uint64_t* nh0,
+                     uint64_t* essential, uint64_t* col_idx_h, float* col_d_h, uint64_t* col_cf_h,
+                     uint8_t* col_cf_app_h, uint64_t col_cap, uint64_t* ncols, uint64_t* nedges);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,163 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs ``oracle/_ref/refprobe`` (the unmodified reference headers compiled by
+``make -C oracle ref``; only possible where the reference sources are present)
+on small seeded clouds and stores each stage's raw outputs as ``.npz``.
+The GPU machine never runs this script: it only reads the committed fixtures.
+
+    python tests/golden/make_golden.py            # small fixtures (seconds)
+    python tests/golden/make_golden.py --configs  # + checksums of the full workloads
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from turbotops_gb300 import synth  # noqa: E402
+
+PROBE = os.path.join(ROOT, "oracle", "_ref", "refprobe")
+CLI = os.path.join(ROOT, "oracle", "_ref", "turbotops")
+
+
+def probe(stage: str, x: np.ndarray, metric: str, *extra: str) -> dict[str, np.ndarray]:
+    n, dim = x.shape
+    with tempfile.TemporaryDirectory() as td:
+        pts = os.path.join(td, "p.bin")
+        np.ascontiguousarray(x, np.float32).tofile(pts)
+        pre = os.path.join(td, "o")
+        subprocess.run([PROBE, stage, pts, str(n), str(dim), metric, *extra, pre], check=True)
+        out = {}
+        types = {"mat": np.float32, "encl": np.float32, "eidx": np.uint64, "ed": np.float32,
+                 "app": np.uint8, "cidx": np.uint64, "cd": np.float32, "h0": np.float32,
+                 "emi": np.uint64, "emd": np.float32, "emf": np.uint8, "thr": np.float32,
+                 "piv": np.uint64, "c2idx": np.uint64, "c2d": np.float32, "app2n": np.uint64,
+                 "ids": np.uint32, "rp": np.uint64, "ci": np.uint32, "w": np.float32,
+                 "rd": np.float32, "rv": np.int32, "bars": np.float32}
+        for f in os.listdir(td):
+            if f.startswith("o."):
+                key = f[2:]
+                out[key] = np.fromfile(os.path.join(td, f), dtype=types[key])
+        return out
+
+
+def save(name: str, x: np.ndarray, metric: str, stage: str, params: dict, res: dict) -> None:
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), x=x, metric=np.array(metric),
+                        stage=np.array(stage), params=np.array(json.dumps(params)), **res)
+
+
+def small() -> None:
+    clouds = {
+        "u3": synth.uniform(200, 3, 11),
+        "g17": synth.gauss(150, 17, 12),
+        "g32": synth.gauss(120, 32, 13),
+        "g9": synth.gauss(140, 9, 14),
+        "grid4": synth.grid(300, 4, 6, 15),
+        "torus": synth.torus(240, 16),
+    }
+    # dense distance matrices + enclosing radius, every metric path
+    for cname in ["u3", "g17", "g32", "g9", "grid4"]:
+        for metric in ["l2", "l1", "linf", "lp:3", "lp:1.5"]:
+            x = clouds[cname]
+            save(f"dense_{cname}_{metric.replace(':', '')}", x, metric, "dense", {},
+                 probe("dense", x, metric))
+    # dim0 (sorted edges, apparent flags, columns, H0, emergent probe) and assemble
+    for cname, metric, thr in [("torus", "l2", "inf"), ("grid4", "l1", "inf"),
+                               ("grid4", "linf", "inf"), ("u3", "l2", "0.3"),
+                               ("grid4", "l2", "2.5")]:
+        x = clouds[cname]
+        tag = f"{cname}_{metric}_{thr.replace('.', 'p')}"
+        save(f"asm_{tag}", x, metric, "asm", {"thr": thr}, probe("asm", x, metric, thr))
+    # kNN lists, kNN graph, radius graph
+    knn_cases = [("g9", "l2", 7), ("g9", "l1", 7), ("g9", "linf", 5), ("grid4", "l1", 6),
+                 ("g32", "l2", 15), ("u3", "lp3", 6)]
+    for cname, metric, k in knn_cases:
+        x = clouds[cname]
+        m = "lp:3" if metric == "lp3" else metric
+        save(f"knn_{cname}_{metric}_{k}", x, m, "knn", {"k": k}, probe("knng", x, m, str(k)) |
+             probe("knn", x, m, str(k)))
+    for cname, metric, tau in [("u3", "l2", "0.2"), ("u3", "l1", "0.3"), ("grid4", "linf", "2"),
+                               ("g9", "l2", "3.0")]:
+        x = clouds[cname]
+        save(f"radius_{cname}_{metric}", x, metric, "radius", {"tau": tau},
+             probe("radius", x, metric, tau))
+    # H0 via MST (complete graph)
+    for cname, metric, thr in [("u3", "l2", "inf"), ("g32", "l2", "inf"), ("grid4", "l1", "inf"),
+                               ("g9", "linf", "1.0")]:
+        x = clouds[cname]
+        save(f"mst_{cname}_{metric}", x, metric, "mst", {"thr": thr}, probe("mst", x, metric, thr))
+    # RedZeD edge lists (dense and kNN graph) and sparse dim0
+    for cname, metric in [("grid4", "l1"), ("u3", "l2")]:
+        x = clouds[cname]
+        save(f"rzd_{cname}_{metric}", x, metric, "rzd", {}, probe("rzd", x, metric))
+    for cname, metric, k in [("g9", "l2", 8), ("grid4", "l1", 6)]:
+        x = clouds[cname]
+        save(f"rzs_{cname}_{metric}", x, metric, "rzs", {"k": k},
+             probe("rzs", x, metric, str(k)) | {"knn_" + a: b for a, b in probe("knng", x, metric, str(k)).items()})
+        save(f"sdim0_{cname}_{metric}", x, metric, "sdim0", {"k": k},
+             probe("sdim0", x, metric, str(k)) | {"g_" + a: b for a, b in probe("knng", x, metric, str(k)).items()})
+    # full diagrams (tops::persistence, dense, canonical order is applied by tests)
+    for cname, metric, maxdim in [("torus", "l2", 2), ("grid4", "l1", 2), ("u3", "l2", 1),
+                                  ("grid4", "linf", 1)]:
+        x = clouds[cname]
+        save(f"bars_{cname}_{metric}_{maxdim}", x, metric, "bars", {"maxdim": maxdim},
+             probe("bars", x, metric, str(maxdim)))
+
+
+def sha(*arrs: np.ndarray) -> str:
+    h = hashlib.sha256()
+    for a in arrs:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()[:16]
+
+
+def configs() -> None:
+    """Checksums of the full benchmark workloads' front-end outputs."""
+    res = {}
+    x = synth.torus()
+    r = probe("asm", x, "l2", "inf")
+    res["torus1000_l2"] = {"thr": float(r["thr"][0]), "edges": int(r["eidx"].size),
+                           "edges_sha": sha(r["eidx"], r["ed"]), "app_sha": sha(r["app"]),
+                           "app": int(r["app"].sum()), "cols": int(r["cidx"].size),
+                           "cols_sha": sha(r["cidx"], r["cd"]), "h0_sha": sha(r["h0"]),
+                           "piv_sha": sha(r["piv"]), "c2": int(r["c2idx"].size),
+                           "c2_sha": sha(r["c2idx"], r["c2d"]), "app2": int(r["app2n"][0])}
+    np.savez_compressed(os.path.join(HERE, "cfg_torus1000_piv.npz"), piv=r["piv"])
+    for metric in ["linf", "l1"]:
+        x = synth.lattice()
+        r = probe("asm", x, metric, "inf")
+        res[f"lattice3000_{metric}"] = {
+            "thr": float(r["thr"][0]), "edges": int(r["eidx"].size),
+            "edges_sha": sha(r["eidx"], r["ed"]), "app_sha": sha(r["app"]), "app": int(r["app"].sum()),
+            "cols": int(r["cidx"].size), "cols_sha": sha(r["cidx"], r["cd"]), "h0_sha": sha(r["h0"]),
+            "piv_sha": sha(r["piv"]), "c2": int(r["c2idx"].size), "c2_sha": sha(r["c2idx"], r["c2d"]),
+            "app2": int(r["app2n"][0])}
+        np.savez_compressed(os.path.join(HERE, f"cfg_lattice3000_{metric}_piv.npz"), piv=r["piv"])
+        print(metric, res[f"lattice3000_{metric}"], flush=True)
+    x = synth.gmm()
+    r = probe("knng", x, "l2", "15") | probe("knn", x, "l2", "15")
+    s = probe("rzs", x, "l2", "15")
+    res["gmm100k_l2_k15"] = {"ids_sha": sha(r["ids"]), "nnz": int(r["ci"].size),
+                             "csr_sha": sha(r["rp"], r["ci"], r["w"]), "rz_sha": sha(s["rd"], s["rv"])}
+    with open(os.path.join(HERE, "configs.json"), "w") as f:
+        json.dump(res, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--configs", action="store_true")
+    a = ap.parse_args()
+    if not os.path.exists(PROBE):
+        sys.exit("build the reference first: make -C oracle ref")
+    small()
+    if a.configs:
+        configs()

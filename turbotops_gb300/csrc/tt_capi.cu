@@ -1,0 +1,227 @@
+// tt_capi.cu — the C-ABI (include/turbotops_gb300.h): argument checks with the
+// reference's messages, exception -> status mapping, host-buffer entry points.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "tt_internal.cuh"
+
+using namespace tt;
+
+namespace {
+
+thread_local std::string g_error;   // errors of calls without a context
+
+template <typename F>
+int guard(tt_ctx* c, F&& f) {
+    try {
+        if (!c) throw Error(TT_ERR_INVALID, "gb300: null context");
+        TT_CUDA(cudaSetDevice(c->device));
+        f();
+        return TT_OK;
+    } catch (const Error& e) {
+        (c ? c->last_error : g_error) = e.what();
+        return e.status;
+    } catch (const std::exception& e) {
+        (c ? c->last_error : g_error) = e.what();
+        return TT_ERR_INTERNAL;
+    }
+}
+
+void check_metric(int kind, float p) {
+    if (kind < TT_METRIC_L1 || kind > TT_METRIC_LP) invalid("metric: unknown kind");
+    if (kind == TT_METRIC_LP && !(p >= 1.0f)) invalid("metric: p must be in [1, inf]");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tt_version(void) { return "0.1.0"; }
+
+int tt_ctx_create(int device, void* stream, tt_ctx** out) {
+    if (!out) return TT_ERR_INVALID;
+    *out = nullptr;
+    tt_ctx* c = new tt_ctx;
+    c->device = device;
+    const int st = guard(c, [&] {
+        cudaDeviceProp prop;
+        TT_CUDA(cudaGetDeviceProperties(&prop, device));
+        c->sms = prop.multiProcessorCount;
+        // The stream is used as given; NULL is the legacy default stream.
+        c->stream = static_cast<cudaStream_t>(stream);
+    });
+    if (st != TT_OK) {
+        g_error = c->last_error;
+        delete c;
+        return st;
+    }
+    *out = c;
+    return TT_OK;
+}
+
+void tt_ctx_destroy(tt_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->arena.release();
+    c->pinned.release();
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* tt_last_error(const tt_ctx* c) { return c ? c->last_error.c_str() : g_error.c_str(); }
+
+uint64_t tt_ctx_launches(const tt_ctx* c) { return c ? c->launches : 0; }
+
+int tt_ctx_synchronize(tt_ctx* c) {
+    return guard(c, [&] { TT_CUDA(cudaStreamSynchronize(c->stream)); });
+}
+
+int tt_copy_async(tt_ctx* c, void* dst, const void* src, size_t bytes) {
+    return guard(c, [&] {
+        if (bytes) TT_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));
+    });
+}
+
+int tt_metric_parse(const char* s, int* kind, float* p) {
+    // Metric::parse / Metric::minkowski (metric.hpp:227-253)
+    const std::string m = s ? s : "";
+    float q = NAN;
+    if (m == "l2" || m == "euclidean") q = 2.0f;
+    else if (m == "l1" || m == "manhattan") q = 1.0f;
+    else if (m == "linf" || m == "chebyshev") q = INFINITY;
+    else if (m.rfind("lp:", 0) == 0) {
+        const std::string v = m.substr(3);
+        if (v == "inf") q = INFINITY;
+        else {
+            char* end = nullptr;
+            const float t = std::strtof(v.c_str(), &end);
+            if (end && *end == '\0' && !v.empty()) q = t;
+            else goto unknown;
+        }
+    } else {
+        goto unknown;
+    }
+    if (!(q >= 1.0f)) {
+        g_error = "metric: p must be in [1, inf]";
+        return TT_ERR_INVALID;
+    }
+    *p = q;
+    *kind = q == 1.0f ? TT_METRIC_L1 : q == 2.0f ? TT_METRIC_L2 : std::isinf(q) ? TT_METRIC_LINF : TT_METRIC_LP;
+    return TT_OK;
+unknown:
+    g_error = "metric: unknown '" + m + "' (expected l1 | l2 | linf | lp:<p>, p >= 1)";
+    return TT_ERR_INVALID;
+}
+
+int tt_dense_distances(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, float* mat,
+                       float* enclosing) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (n && (!x || !mat)) invalid("gb300: null buffer");
+        u32* rowmax = enclosing ? c->arena.get<u32>(S_ROWMAX, u64(n) + 1) : nullptr;
+        dense_matrix(c, x, n, dim, kind, p, mat, rowmax);
+        if (enclosing) {
+            if (n == 0) {
+                *enclosing = INFINITY;
+                return;
+            }
+            min_bits(c, rowmax, n, rowmax + n);
+            u32 b = 0;
+            TT_CUDA(cudaMemcpyAsync(&b, rowmax + n, 4, cudaMemcpyDeviceToHost, c->stream));
+            TT_CUDA(cudaStreamSynchronize(c->stream));
+            *enclosing = bitsf(b);
+        }
+    });
+}
+
+int tt_dim0(tt_ctx* c, const float* mat, const uint64_t* rp, const uint32_t* ci, const float* w, uint32_t n,
+            float thr, uint32_t maxdim, tt_dim0_out* out) {
+    return guard(c, [&] {
+        if (!out) invalid("gb300: null output");
+        if (std::isnan(thr) || thr < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        if (n > 1 && !mat && !(rp && ci && w)) invalid("gb300: null complex");
+        Complex cx{mat, rp, ci, w, n, thr};
+        Dim0Out r;
+        dim0(c, cx, maxdim, r);
+        out->edges = r.m;
+        out->edge_keys_dev = r.keys;
+        out->apparent_dev = r.app;
+        out->tree_dev = r.tree;
+        out->columns = r.ncols;
+        out->col_index_dev = r.cidx;
+        out->col_diameter_dev = r.cd;
+        out->col_cofacet_dev = r.emi;
+        out->col_cofacet_app_dev = r.emf;
+        out->h0_finite = r.nh0;
+        out->h0_death_dev = r.h0;
+        out->essential = r.essential;
+    });
+}
+
+int tt_redzed_edges(tt_ctx* c, const float* mat, const uint64_t* rp, const uint32_t* ci, const float* w,
+                    uint32_t n, float thr, float* diam, int32_t* verts, uint64_t cap, uint64_t* count) {
+    return guard(c, [&] {
+        if (std::isnan(thr) || thr < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        Complex cx{mat, rp, ci, w, n, thr};
+        const u64 m = redzed_edges(c, cx, diam, verts, cap);
+        if (count) *count = m;
+        if (m > cap) throw Error(TT_ERR_LENGTH, "gb300: edge list exceeds the output capacity");
+    });
+}
+
+int tt_dense_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t maxdim,
+                     float* thr_inout, float* mat_h, float* h0_h, uint64_t* nh0, uint64_t* essential,
+                     uint64_t* col_idx_h, float* col_d_h, uint64_t* col_cf_h, uint8_t* col_cf_app_h,
+                     uint64_t col_cap, uint64_t* ncols, uint64_t* nedges) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (!thr_inout) invalid("gb300: null threshold");
+        const float t = *thr_inout;
+        if (std::isnan(t) || t < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        for (u64 i = 0; i < u64(n) * dim; ++i)
+            if (!std::isfinite(x_h[i])) invalid("persistence: non-finite coordinate");
+        f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
+        f32* mat = c->arena.get<f32>(S_MAT, u64(n) * n + 1);
+        if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
+        u32* rowmax = c->arena.get<u32>(S_ROWMAX, u64(n) + 1);
+        dense_matrix(c, x, n, dim, kind, p, mat, std::isinf(t) ? rowmax : nullptr);
+        float thr = t;
+        if (std::isinf(t)) {
+            if (n == 0) {
+                thr = INFINITY;
+            } else {
+                min_bits(c, rowmax, n, rowmax + n);
+                u32 b = 0;
+                TT_CUDA(cudaMemcpyAsync(&b, rowmax + n, 4, cudaMemcpyDeviceToHost, c->stream));
+                TT_CUDA(cudaStreamSynchronize(c->stream));
+                thr = bitsf(b);
+            }
+        }
+        *thr_inout = thr;
+        Complex cx{mat, nullptr, nullptr, nullptr, n, thr};
+        Dim0Out r;
+        dim0(c, cx, maxdim, r);
+        if (mat_h && n)
+            TT_CUDA(cudaMemcpyAsync(mat_h, mat, sizeof(f32) * n * n, cudaMemcpyDeviceToHost, c->stream));
+        if (h0_h && r.nh0)
+            TT_CUDA(cudaMemcpyAsync(h0_h, r.h0, sizeof(f32) * r.nh0, cudaMemcpyDeviceToHost, c->stream));
+        if (col_idx_h && r.ncols) {
+            if (r.ncols > col_cap) throw Error(TT_ERR_LENGTH, "gb300: columns exceed the output capacity");
+            TT_CUDA(cudaMemcpyAsync(col_idx_h, r.cidx, 8 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+            if (col_d_h) TT_CUDA(cudaMemcpyAsync(col_d_h, r.cd, 4 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+            if (col_cf_h) TT_CUDA(cudaMemcpyAsync(col_cf_h, r.emi, 8 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+            if (col_cf_app_h)
+                TT_CUDA(cudaMemcpyAsync(col_cf_app_h, r.emf, r.ncols, cudaMemcpyDeviceToHost, c->stream));
+        }
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+        if (nh0) *nh0 = r.nh0;
+        if (essential) *essential = r.essential;
+        if (ncols) *ncols = r.ncols;
+        if (nedges) *nedges = r.m;
+    });
+}
+
+}  // extern "C"

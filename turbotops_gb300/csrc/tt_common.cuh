@@ -1,0 +1,142 @@
+// tt_common.cuh — shared definitions of the GB300 front-end library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/turbotops_gb300.h"
+
+namespace tt {
+
+using u8 = uint8_t;
+using u32 = uint32_t;
+using u64 = uint64_t;
+using i64 = int64_t;
+using f32 = float;
+
+constexpr int kSMs = 152;          // GB300: 2 dies x 76 SMs
+constexpr u64 kNone = ~0ull;
+
+// Errors thrown inside the library and mapped to TT_* status codes at the
+// C-ABI boundary (tt_capi.cu). The message is the reference's message where
+// the reference has one for the same condition.
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess)
+        throw Error(TT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define TT_CUDA(x) ::tt::check((x), #x)
+#define TT_LAUNCH(what) ::tt::check(cudaGetLastError(), what)
+
+inline void invalid(const std::string& m) { throw Error(TT_ERR_INVALID, m); }
+
+inline u32 div_up(u64 a, u64 b) { return u32((a + b - 1) / b); }
+
+__host__ __device__ inline u32 fbits(f32 d) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(d);
+#else
+    u32 u;
+    __builtin_memcpy(&u, &d, 4);
+    return u;
+#endif
+}
+__host__ __device__ inline f32 bitsf(u32 u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    f32 d;
+    __builtin_memcpy(&d, &u, 4);
+    return d;
+#endif
+}
+
+// Device-memory arena owned by a context: one cudaMalloc'd slab per size
+// class, reused across calls, so steady-state calls allocate nothing.
+struct Arena {
+    struct Slab {
+        void* p = nullptr;
+        size_t bytes = 0;
+    };
+    std::vector<Slab> slabs;   // indexed by slot
+    void* get(int slot, size_t bytes) {
+        if (slot >= int(slabs.size())) slabs.resize(slot + 1);
+        Slab& s = slabs[slot];
+        if (s.bytes < bytes) {
+            if (s.p) TT_CUDA(cudaFree(s.p));
+            s.p = nullptr;
+            size_t b = bytes < 256 ? 256 : bytes;
+            b = (b + b / 8 + 255) & ~size_t(255);   // headroom against regrowth
+            cudaError_t e = cudaMalloc(&s.p, b);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                throw Error(TT_ERR_LENGTH, "device memory exhausted (" + std::to_string(b) + " bytes)");
+            }
+            s.bytes = b;
+        }
+        return s.p;
+    }
+    template <typename T>
+    T* get(int slot, size_t count) { return static_cast<T*>(get(slot, count * sizeof(T))); }
+    void release() {
+        for (auto& s : slabs)
+            if (s.p) cudaFree(s.p);
+        slabs.clear();
+    }
+};
+
+// Pinned host staging, grown on demand.
+struct Pinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void* get(size_t b) {
+        if (bytes < b) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            b = (b + b / 8 + 4095) & ~size_t(4095);
+            TT_CUDA(cudaMallocHost(&p, b));
+            bytes = b;
+        }
+        return p;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+// Arena slots. Each stage documents the slots it uses; a stage never holds a
+// slot across a call into another stage that uses the same slot.
+enum Slot : int {
+    S_SORT_A = 0, S_SORT_B, S_SORT_HIST, S_SORT_VA, S_SORT_VB,   // radix sort
+    S_SCAN, S_FLAGS, S_EDGE_KEYS, S_EDGE_TMP, S_COUNT,            // edges / compaction
+    S_UF_PARENT, S_UF_BEST, S_UF_WORK, S_UF_WORK2,                // Borůvka
+    S_MAT, S_PTS, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4,         // host-buffer entry points
+    S_KNN_D, S_KNN_I, S_GRAPH_KEYS, S_GRAPH_TMP, S_PIV,           // kNN / graph / pivots
+    S_MISC0, S_MISC1, S_MISC2, S_MISC3, S_ROWMAX, S_ASM0, S_ASM1, S_ASM2, S_ASM3, S_ASM4,
+    S_NSLOTS
+};
+
+}  // namespace tt
+
+// Opaque context behind the C-ABI.
+struct tt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    tt::Arena arena;
+    tt::Pinned pinned;
+    std::string last_error;
+    int sms = tt::kSMs;
+    double last_kernel_ms = 0.0;   // device time of the last stage (CUDA events)
+    uint64_t launches = 0;          // kernels launched through this context
+};

@@ -1,0 +1,512 @@
+// tt_dim0.cu — the dimension-0 stage of the cohomology reducer on the GPU.
+//
+// Replaces rips.hpp Reducer::dim0 (:685-870): the kept edges (d <= thr) are
+// packed into Ripser-order keys and radix-sorted (the reference's bucket sort
+// reproduces the plain (d asc, idx desc) order, :775-839, which is what the
+// key order is); every edge gets its zero-apparent-cofacet test (:844-849,
+// zero_apparent_cofacet_v :644-649); the spanning forest that the reference's
+// serial union-find selects over the sorted edges (:850-866) is computed by
+// Borůvka over the edge ranks — with distinct ranks the minimum spanning
+// forest is unique, so the tree/non-tree split is the same edge for edge.
+// H0 bars are the tree edges with d > 0 in sorted order; columns are the
+// non-tree, non-apparent edges in descending order (:867).
+//
+// For each non-apparent edge the kernel also records the column-local part of
+// the emergent-pair shortcut of compute_pairs (:903-928): the first cofacet in
+// descending order with the edge's diameter, and whether that cofacet has a
+// zero-apparent facet. Only the pivot lookup stays on the host.
+//
+// The same stage covers the sparse complex (rips.hpp SparseComplex :418-472):
+// cofacets of an edge are the common neighbours of its endpoints, walked from
+// the top of their sorted CSR rows.
+#include "tt_internal.cuh"
+
+namespace tt {
+
+namespace {
+
+constexpr u32 NOV = 0xffffffffu;   // no vertex
+
+__device__ __forceinline__ void decode_edge(u64 idx, u32& a, u32& b) {
+    // rips.hpp decode, nv = 2 closed form (:549-557): a > b
+    u64 v = u64((1.0 + sqrt(1.0 + 8.0 * double(idx))) * 0.5);
+    while (v * (v - 1) / 2 > idx) --v;
+    while ((v + 1) * v / 2 <= idx) ++v;
+    a = u32(v);
+    b = u32(idx - v * (v - 1) / 2);
+}
+__device__ __forceinline__ u64 edge_idx(u32 a, u32 b) {   // any order
+    if (a < b) { const u32 t = a; a = b; b = t; }
+    return u64(a) * (a - 1) / 2 + b;
+}
+__device__ __forceinline__ u64 tri_idx(u32 a, u32 b, u32 c) {   // a > b > c
+    return u64(a) * (a - 1) * (a - 2) / 6 + u64(b) * (b - 1) / 2 + c;
+}
+__device__ __forceinline__ void sort3(u32& a, u32& b, u32& c) {   // descending
+    if (a < b) { const u32 t = a; a = b; b = t; }
+    if (b < c) { const u32 t = b; b = c; c = t; }
+    if (a < b) { const u32 t = a; a = b; b = t; }
+}
+__device__ __forceinline__ f32 key_d(u64 k) { return __uint_as_float(u32(k >> kIdxBits)); }
+__device__ __forceinline__ u64 key_idx(u64 k) { return kIdxMask - (k & kIdxMask); }
+
+// --------------------------------------------------------------------------
+// Dense complex (full n x n matrix).
+// --------------------------------------------------------------------------
+struct DenseCx {
+    const f32* mat;
+    u32 n;
+    __device__ __forceinline__ f32 d(u32 i, u32 j) const { return i == j ? 0.0f : mat[u64(i) * n + j]; }
+};
+
+// Largest w not in {a, b} with D[a][w] <= cap and D[b][w] <= cap, scanning
+// candidates downward 32 at a time (coalesced row segments); NOV if none.
+// This is the first cofacet in descending index order (cofacets_full
+// rips.hpp:282-344 with all = true).
+__device__ __forceinline__ u32 warp_top_cofacet2(const DenseCx& cx, u32 a, u32 b, f32 cap) {
+    const int lane = threadIdx.x & 31;
+    const f32* ra = cx.mat + u64(a) * cx.n;
+    const f32* rb = cx.mat + u64(b) * cx.n;
+    for (int64_t hi = cx.n; hi > 0; hi -= 32) {
+        const int64_t w = hi - 32 + lane;
+        bool ok = false;
+        if (w >= 0 && u32(w) != a && u32(w) != b) ok = ra[w] <= cap && rb[w] <= cap;
+        const u32 bal = __ballot_sync(0xffffffffu, ok);
+        if (bal) return u32(hi - 32 + (31 - __clz(bal)));
+    }
+    return NOV;
+}
+
+// First facet of triangle (c0 > c1 > c2) in ascending index order with length
+// d (zero_pivot_facet_v rips.hpp:609-636 for nv = 3): removing c0 leaves
+// (c1, c2), removing c1 leaves (c0, c2), removing c2 leaves (c0, c1).
+template <typename Cx>
+__device__ __forceinline__ u64 tri_zero_facet(const Cx& cx, u32 c0, u32 c1, u32 c2, f32 d, u32& f0, u32& f1) {
+    if (cx.d(c1, c2) == d) { f0 = c1; f1 = c2; return edge_idx(c1, c2); }
+    if (cx.d(c0, c2) == d) { f0 = c0; f1 = c2; return edge_idx(c0, c2); }
+    if (cx.d(c0, c1) == d) { f0 = c0; f1 = c1; return edge_idx(c0, c1); }
+    return kNone;
+}
+
+__global__ void k_edges_dense(const f32* __restrict__ mat, u32 n, f32 thr, u64* __restrict__ keys,
+                              unsigned long long* __restrict__ count, int redzed) {
+    const int lane = threadIdx.x & 31;
+    const u32 warps = (gridDim.x * blockDim.x) >> 5;
+    for (u32 i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const f32* row = mat + u64(i) * n;
+        const u64 rbase = u64(i) * (i - 1) / 2;
+        for (u32 j0 = 0; j0 < i; j0 += 32) {
+            const u32 j = j0 + lane;
+            const f32 d = j < i ? row[j] : INFINITY;
+            const bool keep = j < i && d <= thr;
+            const u32 bal = __ballot_sync(0xffffffffu, keep);
+            if (!bal) continue;
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (keep) {
+                const u64 idx = rbase + j;
+                keys[base + __popc(bal & ((1u << lane) - 1))] =
+                    (u64(__float_as_uint(d)) << kIdxBits) | (redzed ? idx : kIdxMask - idx);
+            }
+        }
+    }
+}
+
+__global__ void k_apparent_dense(const f32* __restrict__ mat, u32 n, const u64* __restrict__ keys, u64 m,
+                                 u8* __restrict__ app, u32* __restrict__ emw, u8* __restrict__ emf) {
+    const DenseCx cx{mat, n};
+    const int lane = threadIdx.x & 31;
+    const u64 warps = (u64(gridDim.x) * blockDim.x) >> 5;
+    for (u64 e = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; e < m; e += warps) {
+        const u64 key = keys[e];
+        const f32 d = key_d(key);
+        const u64 idx = key_idx(key);
+        u32 a, b;
+        decode_edge(idx, a, b);
+        const u32 w = warp_top_cofacet2(cx, a, b, d);
+        bool apparent = false, em = false;
+        if (w != NOV) {
+            u32 c0 = a, c1 = b, c2 = w;
+            sort3(c0, c1, c2);
+            u32 f0 = 0, f1 = 0;
+            const u64 f = tri_zero_facet(cx, c0, c1, c2, d, f0, f1);
+            apparent = f == idx;
+            if (!apparent) {
+                // emergent probe: does the cofacet have a zero-apparent facet?
+                // Its zero facet is (f0, f1); that facet's zero cofacet must
+                // be the same triangle.
+                const u32 w2 = warp_top_cofacet2(cx, f0, f1, d);
+                if (w2 != NOV) {
+                    u32 g0 = f0, g1 = f1, g2 = w2;
+                    sort3(g0, g1, g2);
+                    em = g0 == c0 && g1 == c1 && g2 == c2;
+                }
+            }
+        }
+        if (lane == 0) {
+            app[e] = apparent;
+            emw[e] = w;
+            emf[e] = em;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// Sparse complex (CSR, rows ascending).
+// --------------------------------------------------------------------------
+struct CsrCx {
+    const u64* rp;
+    const u32* ci;
+    const f32* w;
+    __device__ __forceinline__ f32 d(u32 i, u32 j) const {
+        if (i == j) return 0.0f;
+        u64 lo = rp[i], hi = rp[i + 1];
+        while (lo < hi) {
+            const u64 mid = (lo + hi) >> 1;
+            if (ci[mid] < j) lo = mid + 1;
+            else hi = mid;
+        }
+        return (lo < rp[i + 1] && ci[lo] == j) ? w[lo] : INFINITY;
+    }
+    // Largest common neighbour x of a and b with both weights <= cap (the
+    // k-way intersection walked from the top, rips.hpp:429-471).
+    __device__ __forceinline__ u32 top_cofacet2(u32 a, u32 b, f32 cap) const {
+        u64 pa = rp[a + 1], pb = rp[b + 1];
+        const u64 la = rp[a], lb = rp[b];
+        while (pa > la && pb > lb) {
+            const u32 xa = ci[pa - 1], xb = ci[pb - 1];
+            if (xa > xb) { --pa; continue; }
+            if (xb > xa) { --pb; continue; }
+            if (w[pa - 1] <= cap && w[pb - 1] <= cap) return xa;
+            --pa;
+            --pb;
+        }
+        return NOV;
+    }
+};
+
+__global__ void k_edges_csr(const u64* __restrict__ rp, const u32* __restrict__ ci, const f32* __restrict__ w,
+                            u32 n, f32 thr, u64* __restrict__ keys, unsigned long long* __restrict__ count,
+                            int redzed) {
+    const int lane = threadIdx.x & 31;
+    const u32 warps = (gridDim.x * blockDim.x) >> 5;
+    for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        const u64 b = rp[v], e = rp[v + 1];
+        const u64 vbase = u64(v) * (v - 1) / 2;
+        for (u64 t0 = b; t0 < e; t0 += 32) {
+            const u64 t = t0 + lane;
+            bool keep = false;
+            u32 u = 0;
+            f32 d = 0.0f;
+            if (t < e) {
+                u = ci[t];
+                d = w[t];
+                keep = u < v && d <= thr;
+            }
+            const u32 bal = __ballot_sync(0xffffffffu, keep);
+            if (!bal) continue;
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (keep) {
+                const u64 idx = vbase + u;
+                keys[base + __popc(bal & ((1u << lane) - 1))] =
+                    (u64(__float_as_uint(d)) << kIdxBits) | (redzed ? idx : kIdxMask - idx);
+            }
+        }
+    }
+}
+
+__global__ void k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, u64 m, u8* __restrict__ app,
+                               u32* __restrict__ emw, u8* __restrict__ emf) {
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
+        const u64 key = keys[e];
+        const f32 d = key_d(key);
+        const u64 idx = key_idx(key);
+        u32 a, b;
+        decode_edge(idx, a, b);
+        const u32 w = cx.top_cofacet2(a, b, d);
+        bool apparent = false, em = false;
+        if (w != NOV) {
+            u32 c0 = a, c1 = b, c2 = w;
+            sort3(c0, c1, c2);
+            u32 f0 = 0, f1 = 0;
+            const u64 f = tri_zero_facet(cx, c0, c1, c2, d, f0, f1);
+            apparent = f == idx;
+            if (!apparent) {
+                const u32 w2 = cx.top_cofacet2(f0, f1, d);
+                if (w2 != NOV) {
+                    u32 g0 = f0, g1 = f1, g2 = w2;
+                    sort3(g0, g1, g2);
+                    em = g0 == c0 && g1 == c1 && g2 == c2;
+                }
+            }
+        }
+        app[e] = apparent;
+        emw[e] = w;
+        emf[e] = em;
+    }
+}
+
+// --------------------------------------------------------------------------
+// Borůvka over edge ranks (rank = position in the sorted array).
+// --------------------------------------------------------------------------
+__global__ void k_iota(u32* __restrict__ p, u32 n) {
+    for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) p[v] = v;
+}
+
+// For each live edge with endpoints in different components, offer its rank
+// to both components; edges inside a component are dropped from the list.
+__global__ void k_bv_offer(const u64* __restrict__ keys, const u32* __restrict__ live, u32 nlive, int all,
+                           const u32* __restrict__ comp, u32* __restrict__ best, u32* __restrict__ live_out,
+                           u32* __restrict__ nlive_out) {
+    for (u32 t = blockIdx.x * blockDim.x + threadIdx.x; t < nlive; t += gridDim.x * blockDim.x) {
+        const u32 r = all ? t : live[t];
+        u32 a, b;
+        decode_edge(key_idx(keys[r]), a, b);
+        const u32 ca = comp[a], cb = comp[b];
+        if (ca == cb) continue;
+        atomicMin(&best[ca], r);
+        atomicMin(&best[cb], r);
+        live_out[atomicAdd(nlive_out, 1u)] = r;
+    }
+}
+
+// Every component root with an offered edge takes it into the forest and
+// hooks onto the other side; of a mutual pair only the larger root hooks.
+__global__ void k_bv_hook(const u64* __restrict__ keys, const u32* __restrict__ comp, const u32* __restrict__ best,
+                          u32* __restrict__ parent, u8* __restrict__ tree, u32 n, u32* __restrict__ hooks) {
+    for (u32 c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        if (comp[c] != c) continue;
+        const u32 r = best[c];
+        if (r == NOV) continue;
+        u32 a, b;
+        decode_edge(key_idx(keys[r]), a, b);
+        const u32 o = comp[a] == c ? comp[b] : comp[a];
+        tree[r] = 1;
+        if (best[o] == r && c < o) continue;   // mutual: o hooks onto c
+        parent[c] = o;
+        atomicAdd(hooks, 1u);
+    }
+}
+
+__global__ void k_bv_flatten(const u32* __restrict__ parent, u32* __restrict__ comp, u32* __restrict__ best, u32 n) {
+    for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        u32 r = parent[v];
+        for (u32 s = 0; parent[r] != r && s < n; ++s) r = parent[r];
+        comp[v] = r;
+        best[v] = NOV;
+    }
+}
+
+// --------------------------------------------------------------------------
+// Ordered compaction of H0 bars and columns.
+// --------------------------------------------------------------------------
+__global__ void k_flags_dim0(const u64* __restrict__ keys, const u8* __restrict__ tree, const u8* __restrict__ app,
+                             u64 m, int want_cols, u64* __restrict__ fh, u64* __restrict__ fc) {
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
+        const bool t = tree[e];
+        fh[e] = t && key_d(keys[e]) > 0.0f;
+        fc[e] = want_cols && !t && !(app && app[e]);
+    }
+}
+
+__global__ void k_emit_dim0(const u64* __restrict__ keys, const u8* __restrict__ tree, const u8* __restrict__ app,
+                            const u32* __restrict__ emw, const u8* __restrict__ emf, u64 m, int want_cols,
+                            const u64* __restrict__ oh, const u64* __restrict__ oc, const u64* __restrict__ tot,
+                            f32* __restrict__ h0, u64* __restrict__ cidx, f32* __restrict__ cd,
+                            u64* __restrict__ emi, u8* __restrict__ emf_out) {
+    const u64 ncols = tot[1];
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
+        const u64 key = keys[e];
+        const f32 d = key_d(key);
+        const bool t = tree[e];
+        if (t && d > 0.0f) h0[oh[e]] = d;
+        if (want_cols && !t && !(app && app[e])) {
+            const u64 o = ncols - 1 - oc[e];   // descending order (rips.hpp:867)
+            const u64 idx = key_idx(key);
+            cidx[o] = idx;
+            cd[o] = d;
+            const u32 w = emw[e];
+            if (w == NOV) {
+                emi[o] = kNone;
+                emf_out[o] = 0;
+            } else {
+                u32 a, b;
+                decode_edge(idx, a, b);
+                u32 c0 = a, c1 = b, c2 = w;
+                sort3(c0, c1, c2);
+                emi[o] = tri_idx(c0, c1, c2);
+                emf_out[o] = emf[e];
+            }
+        }
+    }
+}
+
+__global__ void k_pair_totals(const u64* __restrict__ oh, const u64* __restrict__ oc, const u64* __restrict__ fh,
+                              const u64* __restrict__ fc, u64 m, u64* __restrict__ tot) {
+    tot[0] = m ? oh[m - 1] + fh[m - 1] : 0;
+    tot[1] = m ? oc[m - 1] + fc[m - 1] : 0;
+}
+
+inline u32 grid_for(u64 work, u32 per_block) {
+    const u64 g = (work + per_block - 1) / per_block;
+    return u32(std::max<u64>(1, std::min<u64>(g, 64ull * kSMs)));
+}
+
+}  // namespace
+
+// Kept edges as sorted keys (Ripser or RedZeD order); returns the count.
+static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys_out) {
+    const u64 cap = cx.mat ? u64(cx.n) * (cx.n ? cx.n - 1 : 0) / 2 : 0;
+    u64 capacity = cap;
+    if (!cx.mat) {
+        u64 nnz = 0;
+        TT_CUDA(cudaMemcpyAsync(&nnz, cx.rp + cx.n, sizeof(u64), cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+        capacity = nnz / 2 + 1;
+    }
+    u64* keys = c->arena.get<u64>(S_EDGE_KEYS, capacity + 1);
+    unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 4);
+    TT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream));
+    if (cx.n > 1) {
+        if (cx.mat)
+            k_edges_dense<<<grid_for(u64(cx.n) * 32, 256), 256, 0, c->stream>>>(cx.mat, cx.n, cx.thr, keys, cnt, redzed);
+        else
+            k_edges_csr<<<grid_for(u64(cx.n) * 32, 256), 256, 0, c->stream>>>(cx.rp, cx.ci, cx.w, cx.n, cx.thr, keys,
+                                                                              cnt, redzed);
+        TT_LAUNCH("k_edges");
+        ++c->launches;
+    }
+    unsigned long long m = 0;
+    TT_CUDA(cudaMemcpyAsync(&m, cnt, sizeof(m), cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaStreamSynchronize(c->stream));
+    radix_sort_inplace<u32>(c, keys, nullptr, m);
+    *keys_out = keys;
+    return m;
+}
+
+void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
+    if (cx.n > 131072) invalid("gb300: dim0 supports n <= 131072 vertices");
+    out = Dim0Out{};
+    const u64 m = sorted_edge_keys(c, cx, 0, &out.keys);
+    out.m = m;
+    if (m >= 0xffffffffull) invalid("gb300: more than 2^32 - 1 kept edges");
+    const u32 n = cx.n;
+    // per-edge flags
+    u8* app = c->arena.get<u8>(S_FLAGS, 2 * m + 16);
+    u8* tree = app + m + 8;
+    u32* emw = c->arena.get<u32>(S_EDGE_TMP, m + 1);
+    u8* emf = c->arena.get<u8>(S_MISC2, m + 1);
+    TT_CUDA(cudaMemsetAsync(tree, 0, m + 1, c->stream));
+    if (maxdim >= 1 && m) {
+        if (cx.mat)
+            k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, c->stream>>>(cx.mat, n, out.keys, m, app, emw, emf);
+        else
+            k_apparent_csr<<<grid_for(m, 256), 256, 0, c->stream>>>(CsrCx{cx.rp, cx.ci, cx.w}, out.keys, m, app, emw,
+                                                                     emf);
+        TT_LAUNCH("k_apparent");
+        ++c->launches;
+    }
+    out.app = maxdim >= 1 ? app : nullptr;
+    out.tree = tree;
+    // Borůvka spanning forest
+    u32* comp = c->arena.get<u32>(S_UF_PARENT, 2 * u64(n) + 2);
+    u32* parent = comp + n + 1;
+    u32* best = c->arena.get<u32>(S_UF_BEST, n + 1);
+    u32* live0 = c->arena.get<u32>(S_UF_WORK, m + 1);
+    u32* live1 = c->arena.get<u32>(S_UF_WORK2, m + 1);
+    u32* ctr = c->arena.get<u32>(S_MISC1, 4);   // [0] live count, [1] hooks
+    u64 total_hooks = 0;
+    if (n) {
+        k_iota<<<grid_for(n, 256), 256, 0, c->stream>>>(comp, n);
+        k_iota<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, n);
+        TT_CUDA(cudaMemsetAsync(best, 0xff, sizeof(u32) * n, c->stream));
+        c->launches += 2;
+        u32 nlive = u32(m);
+        bool all = true;
+        for (int round = 0; nlive && round < 64; ++round) {
+            TT_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(u32), c->stream));
+            k_bv_offer<<<grid_for(nlive, 256), 256, 0, c->stream>>>(out.keys, live0, nlive, all, comp, best, live1,
+                                                                     ctr);
+            k_bv_hook<<<grid_for(n, 256), 256, 0, c->stream>>>(out.keys, comp, best, parent, tree, n, ctr + 1);
+            k_bv_flatten<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, comp, best, n);
+            TT_LAUNCH("boruvka");
+            c->launches += 3;
+            u32 h[2];
+            TT_CUDA(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+            TT_CUDA(cudaStreamSynchronize(c->stream));
+            total_hooks += h[1];
+            std::swap(live0, live1);
+            all = false;
+            nlive = h[0];
+            if (h[1] == 0) break;
+        }
+    }
+    // ordered compaction of H0 deaths and columns
+    const int want_cols = maxdim >= 1;
+    u64* fh = c->arena.get<u64>(S_MISC0, 4 * m + 8);
+    u64* fc = fh + m + 2;
+    u64* oh = fc + m + 2;
+    u64* oc = oh + m + 2;
+    u64* tot = c->arena.get<u64>(S_COUNT, 4);
+    if (m) {
+        k_flags_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, m, want_cols, fh, fc);
+        TT_LAUNCH("k_flags_dim0");
+        scan_exclusive<u64>(c, fh, oh, m, nullptr);
+        scan_exclusive<u64>(c, fc, oc, m, nullptr);
+        k_pair_totals<<<1, 1, 0, c->stream>>>(oh, oc, fh, fc, m, tot);
+        c->launches += 2;
+    } else {
+        TT_CUDA(cudaMemsetAsync(tot, 0, 2 * sizeof(u64), c->stream));
+    }
+    u64 h[2];
+    TT_CUDA(cudaMemcpyAsync(h, tot, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaStreamSynchronize(c->stream));
+    out.nh0 = h[0];
+    out.ncols = h[1];
+    out.h0 = c->arena.get<f32>(S_OUT0, h[0] + 1);
+    out.cidx = c->arena.get<u64>(S_OUT1, h[1] + 1);
+    out.cd = c->arena.get<f32>(S_OUT2, h[1] + 1);
+    out.emi = c->arena.get<u64>(S_OUT3, h[1] + 1);
+    out.emf = c->arena.get<u8>(S_OUT4, h[1] + 1);
+    if (m) {
+        k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, emw, emf, m, want_cols, oh, oc,
+                                                             tot, out.h0, out.cidx, out.cd, out.emi, out.emf);
+        TT_LAUNCH("k_emit_dim0");
+        ++c->launches;
+    }
+    // every hook merged two components through one tree edge
+    out.essential = n - total_hooks;
+}
+
+namespace {
+__global__ void k_emit_redzed(const u64* __restrict__ keys, u64 m, f32* __restrict__ d, int32_t* __restrict__ v) {
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
+        const u64 k = keys[e];
+        u32 a, b;
+        decode_edge(k & kIdxMask, a, b);
+        d[e] = key_d(k);
+        v[2 * e] = int32_t(b);
+        v[2 * e + 1] = int32_t(a);
+    }
+}
+}  // namespace
+
+// redzed::detail::build_edges (redzed.hpp:545-613): kept edges in
+// (d asc, combinatorial index asc) order, vertices (i < j). Writes up to cap
+// edges to the device buffers d / verts and returns the edge count.
+u64 redzed_edges(tt_ctx* c, const Complex& cx, f32* d, int32_t* verts, u64 cap) {
+    if (cx.n > 131072) invalid("gb300: edge lists support n <= 131072 vertices");
+    u64* keys = nullptr;
+    const u64 m = sorted_edge_keys(c, cx, 1, &keys);
+    if (m && m <= cap) {
+        k_emit_redzed<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, m, d, verts);
+        TT_LAUNCH("k_emit_redzed");
+        ++c->launches;
+    }
+    return m;
+}
+
+}  // namespace tt

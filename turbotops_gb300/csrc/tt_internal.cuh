@@ -1,0 +1,73 @@
+// tt_internal.cuh — declarations shared by the library's translation units.
+#pragma once
+#include "tt_common.cuh"
+
+namespace tt {
+
+// Packed filtration keys for edges and triangles: the float bits of the
+// diameter (non-negative, so integer order == float order; < 2^31) above a
+// 33-bit simplex index. Ripser order (rips.hpp:114-118) is (d asc, idx desc):
+// the index field holds kIdxMask - idx. RedZeD order (redzed.hpp:477-480) is
+// (d asc, combinatorial index asc): the field holds idx. Indices must be
+// < 2^33 (edges: n <= 131072; triangles: C(n, 3) < 2^33).
+constexpr int kIdxBits = 33;
+constexpr u64 kIdxMask = (1ull << kIdxBits) - 1;
+__host__ __device__ inline u64 key_rips(f32 d, u64 idx) {
+    return (u64(fbits(d)) << kIdxBits) | (kIdxMask - idx);
+}
+
+// ---- tt_dense.cu
+void dense_matrix(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32* mat, u32* rowmax);
+void min_bits(tt_ctx* c, const u32* v, u32 n, u32* out);
+
+// ---- tt_sort.cu
+template <typename T>
+void scan_exclusive(tt_ctx* c, const T* in, T* out, u64 n, T* total, int depth = 0);
+template <typename V>
+bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits = 0);
+template <typename V>
+void radix_sort_inplace(tt_ctx* c, u64* keys, V* vals, u64 n, int force_bits = 0);
+
+// ---- tt_dim0.cu
+struct Dim0Out {
+    u64 m = 0;            // kept edges
+    u64* keys = nullptr;  // m sorted Ripser keys (device)
+    u8* app = nullptr;    // m apparent flags (device), maxdim >= 1
+    u8* tree = nullptr;   // m spanning-tree flags (device)
+    u64 ncols = 0;        // dim-1 columns
+    u64* cidx = nullptr;  // columns (device), descending filtration order
+    f32* cd = nullptr;
+    u64* emi = nullptr;   // emergent probe per column: first zero cofacet index or kNone
+    u8* emf = nullptr;    //   and whether that cofacet has a zero-apparent facet
+    u64 nh0 = 0;          // finite H0 bars (d > 0), sorted edge order
+    f32* h0 = nullptr;    // deaths (device)
+    u64 essential = 0;    // connected components
+};
+// Graph is either a dense full matrix (mat != nullptr) or a CSR.
+struct Complex {
+    const f32* mat = nullptr;
+    const u64* rp = nullptr;
+    const u32* ci = nullptr;
+    const f32* w = nullptr;
+    u32 n = 0;
+    f32 thr = 0;
+};
+void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out);
+// RedZeD EdgeList (d asc, comb asc): diam + vertex pairs (i < j).
+u64 redzed_edges(tt_ctx* c, const Complex& cx, f32* d, int32_t* verts, u64 cap);
+
+// ---- tt_assemble.cu
+u64 assemble2(tt_ctx* c, const Complex& cx, const u64* keys, u64 m, const u64* piv_sorted, u64 npiv,
+              u64** cidx, f32** cd, u64* napp);
+
+// ---- tt_knn.cu
+void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists);
+u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* ids, u32 k,
+              u64* rp, u32** ci, f32** w);
+u64 radius_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32 tau, u64* rp,
+                 u32** ci, f32** w);
+
+// ---- tt_mst.cu
+u64 mst_deaths(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32* deaths);
+
+}  // namespace tt

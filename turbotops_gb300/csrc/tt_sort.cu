@@ -1,0 +1,286 @@
+// tt_sort.cu — device-wide primitives: exclusive scan, stream compaction and a
+// stable LSD radix sort of 64-bit keys with an optional 32- or 64-bit payload.
+//
+// The filtration sorts (rips.hpp:775-839, redzed.hpp:545-613) are total
+// orders on (diameter, index) and are reproduced exactly by sorting a packed
+// 64-bit key, so ties never depend on sort stability or thread count.
+//
+// Radix sort: 8-bit digits, 4096-key tiles (256 threads x 16 keys). Per pass:
+//   k_rs_upsweep   per-tile digit histogram -> hist[digit * tiles + tile]
+//   scan           exclusive scan of hist (digit-major gives global offsets)
+//   k_rs_scatter   stable in-tile ranking (warp match + per-warp counters,
+//                  warp-major order), scatter to offsets
+// Only the bits in which min key and max key differ are sorted (keys share
+// every bit above the highest differing one), which is usually 4-6 passes.
+#include "tt_internal.cuh"
+
+namespace tt {
+
+namespace {
+
+constexpr int RS_THREADS = 256, RS_ITEMS = 16, RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int SCAN_THREADS = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// ---------------------------------------------------------------------------
+// Scan (exclusive, u64): tile sums, recursive scan of the sums, tile scan.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ T block_exclusive_scan(T v, T* warp_tot, T* total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const T t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        T x = lane < nw ? warp_tot[lane] : T(0);
+        T xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const T t = __shfl_up_sync(0xffffffffu, xi, o);
+            if (lane >= o) xi += t;
+        }
+        if (lane < nw) warp_tot[lane] = xi - x;
+        if (lane == nw - 1) *total = xi;
+    }
+    __syncthreads();
+    const T r = inc - v + warp_tot[w];
+    __syncthreads();
+    return r;
+}
+
+template <typename T>
+__global__ void k_tile_sums(const T* __restrict__ in, u64 n, T* __restrict__ sums) {
+    __shared__ T wt[32];
+    __shared__ T tot;
+    const u64 base = u64(blockIdx.x) * SCAN_TILE;
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        const u64 k = base + u64(i) * SCAN_THREADS + threadIdx.x;
+        if (k < n) s += in[k];
+    }
+    block_exclusive_scan<T>(s, wt, &tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+template <typename T>
+__global__ void k_tile_scan(const T* __restrict__ in, u64 n, const T* __restrict__ offs,
+                            T* __restrict__ out, T* __restrict__ total) {
+    __shared__ T wt[32];
+    __shared__ T tot;
+    const u64 base = u64(blockIdx.x) * SCAN_TILE + u64(threadIdx.x) * SCAN_ITEMS;
+    T v[SCAN_ITEMS];
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        v[i] = (base + i < n) ? in[base + i] : T(0);
+        s += v[i];
+    }
+    T run = block_exclusive_scan<T>(s, wt, &tot) + (offs ? offs[blockIdx.x] : T(0));
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        if (base + i < n) out[base + i] = run;
+        run += v[i];
+    }
+    if (total && blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) *total = run;
+}
+
+// ---------------------------------------------------------------------------
+// Radix sort kernels.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RS_THREADS)
+k_rs_upsweep(const u64* __restrict__ keys, u64 n, int shift, u32* __restrict__ hist, u32 tiles) {
+    __shared__ u32 h[RS_WARPS][256];
+    for (int t = threadIdx.x; t < RS_WARPS * 256; t += RS_THREADS) (&h[0][0])[t] = 0;
+    __syncthreads();
+    const int w = threadIdx.x >> 5;
+    const u64 base = u64(blockIdx.x) * RS_TILE;
+#pragma unroll 4
+    for (int i = 0; i < RS_ITEMS; ++i) {
+        const u64 k = base + u64(i) * RS_THREADS + threadIdx.x;
+        if (k < n) atomicAdd(&h[w][(keys[k] >> shift) & 0xff], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
+        u32 s = 0;
+#pragma unroll
+        for (int q = 0; q < RS_WARPS; ++q) s += h[q][d];
+        hist[u64(d) * tiles + blockIdx.x] = s;
+    }
+}
+
+template <typename V>
+__global__ void __launch_bounds__(RS_THREADS)
+k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __restrict__ vin,
+             V* __restrict__ vout, u64 n, int shift, const u32* __restrict__ offs, u32 tiles) {
+    __shared__ u32 cnt[RS_WARPS][256];   // per-warp running count, then warp prefix
+    __shared__ u32 gbase[256];
+    for (int t = threadIdx.x; t < RS_WARPS * 256; t += RS_THREADS) (&cnt[0][0])[t] = 0;
+    for (int d = threadIdx.x; d < 256; d += RS_THREADS) gbase[d] = offs[u64(d) * tiles + blockIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const u32 lt = (1u << lane) - 1u;
+    // Warp w owns keys [base + w*32*ITEMS, base + (w+1)*32*ITEMS), item-major:
+    // key (w, i, lane) precedes (w, i', lane') iff (i, lane) < (i', lane').
+    const u64 base = u64(blockIdx.x) * RS_TILE + u64(w) * 32 * RS_ITEMS;
+    u64 key[RS_ITEMS];
+    u32 rank[RS_ITEMS];
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; ++i) {
+        const u64 k = base + u64(i) * 32 + lane;
+        const bool ok = k < n;
+        key[i] = ok ? kin[k] : ~0ull;
+        const u32 dg = ok ? u32(key[i] >> shift) & 0xffu : 0x100u;   // 0x100: no key
+        const u32 peers = __match_any_sync(0xffffffffu, dg);
+        const u32 before = __popc(peers & lt);
+        const int leader = __ffs(peers) - 1;
+        u32 prev = 0;
+        if (lane == leader && dg < 256) {
+            prev = cnt[w][dg];
+            cnt[w][dg] = prev + __popc(peers);
+        }
+        prev = __shfl_sync(0xffffffffu, prev, leader);
+        rank[i] = prev + before;
+        __syncwarp();
+    }
+    __syncthreads();
+    // exclusive prefix over warps, per digit
+    for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
+        u32 s = 0;
+#pragma unroll
+        for (int q = 0; q < RS_WARPS; ++q) {
+            const u32 c = cnt[q][d];
+            cnt[q][d] = s;
+            s += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; ++i) {
+        const u64 k = base + u64(i) * 32 + lane;
+        if (k < n) {
+            const u32 dg = u32(key[i] >> shift) & 0xffu;
+            const u32 pos = gbase[dg] + cnt[w][dg] + rank[i];
+            kout[pos] = key[i];
+            if (vin) vout[pos] = vin[k];
+        }
+    }
+}
+
+__global__ void k_minmax(const u64* __restrict__ keys, u64 n, unsigned long long* __restrict__ mm) {
+    u64 lo = ~0ull, hi = 0;
+    for (u64 i = u64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x) {
+        const u64 k = keys[i];
+        lo = min(lo, k);
+        hi = max(hi, k);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        lo = min(lo, (u64)__shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, (u64)__shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&mm[0], (unsigned long long)lo);
+        atomicMax(&mm[1], (unsigned long long)hi);
+    }
+}
+
+}  // namespace
+
+template <typename T>
+void scan_exclusive(tt_ctx* c, const T* in, T* out, u64 n, T* total, int depth) {
+    if (n == 0) {
+        if (total) TT_CUDA(cudaMemsetAsync(total, 0, sizeof(T), c->stream));
+        return;
+    }
+    const u64 tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (tiles == 1) {
+        k_tile_scan<T><<<1, SCAN_THREADS, 0, c->stream>>>(in, n, nullptr, out, total);
+        TT_LAUNCH("k_tile_scan");
+        c->launches += 1;
+        return;
+    }
+    if (depth > 4) invalid("scan: input too large");
+    T* sums = c->arena.get<T>(S_SCAN + 0, 2 * tiles + 2) ;
+    // sums[0..tiles) tile totals, sums[tiles..2 tiles) their exclusive scan
+    // (a deeper level reuses a fresh stack slot through recursion on a copy)
+    k_tile_sums<T><<<u32(tiles), SCAN_THREADS, 0, c->stream>>>(in, n, sums);
+    TT_LAUNCH("k_tile_sums");
+    if (tiles <= SCAN_TILE) {
+        k_tile_scan<T><<<1, SCAN_THREADS, 0, c->stream>>>(sums, tiles, nullptr, sums + tiles, nullptr);
+        TT_LAUNCH("k_tile_scan");
+    } else {
+        invalid("scan: more than 33M tiles");
+    }
+    k_tile_scan<T><<<u32(tiles), SCAN_THREADS, 0, c->stream>>>(in, n, sums + tiles, out, total);
+    TT_LAUNCH("k_tile_scan");
+    c->launches += 3;
+}
+
+template void scan_exclusive<u64>(tt_ctx*, const u64*, u64*, u64, u64*, int);
+template void scan_exclusive<u32>(tt_ctx*, const u32*, u32*, u64, u32*, int);
+
+// Sorts keys[0..n) ascending (stable, with the optional payload). Returns the
+// buffers that hold the result: the caller's (keys, vals) or the arena
+// scratch (kbuf, vbuf) — 'swapped' tells which.
+template <typename V>
+bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits) {
+    if (n <= 1) return false;
+    int bits = force_bits;
+    if (bits <= 0) {
+        unsigned long long* mm = c->arena.get<unsigned long long>(S_MISC3, 2);
+        const unsigned long long init[2] = {~0ull, 0ull};
+        TT_CUDA(cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+        k_minmax<<<std::min<u32>(div_up(n, 256), 8 * kSMs), 256, 0, c->stream>>>(keys, n, mm);
+        TT_LAUNCH("k_minmax");
+        ++c->launches;
+        unsigned long long h[2];
+        TT_CUDA(cudaMemcpyAsync(h, mm, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+        const u64 diff = h[0] ^ h[1];
+        bits = diff ? 64 - __builtin_clzll(diff) : 0;
+    }
+    const u32 tiles = div_up(n, RS_TILE);
+    u32* hist = c->arena.get<u32>(S_SORT_HIST, u64(tiles) * 256 + 1);
+    u64 *ka = keys, *kb = kbuf;
+    V *va = vals, *vb = vbuf;
+    bool swapped = false;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_rs_upsweep<<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, shift, hist, tiles);
+        TT_LAUNCH("k_rs_upsweep");
+        scan_exclusive<u32>(c, hist, hist, u64(tiles) * 256, nullptr, 0);
+        k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, shift, hist, tiles);
+        TT_LAUNCH("k_rs_scatter");
+        c->launches += 2;
+        std::swap(ka, kb);
+        std::swap(va, vb);
+        swapped = !swapped;
+    }
+    return swapped;
+}
+
+template bool radix_sort<u32>(tt_ctx*, u64*, u32*, u64, u64*, u32*, int);
+template bool radix_sort<u64>(tt_ctx*, u64*, u64*, u64, u64*, u64*, int);
+
+// Sort keys in place (result always back in `keys`, payload in `vals`).
+template <typename V>
+void radix_sort_inplace(tt_ctx* c, u64* keys, V* vals, u64 n, int force_bits) {
+    if (n <= 1) return;
+    u64* kb = c->arena.get<u64>(S_SORT_A, n);
+    V* vb = vals ? c->arena.get<V>(S_SORT_VA, n) : nullptr;
+    if (radix_sort<V>(c, keys, vals, n, kb, vb, force_bits)) {
+        TT_CUDA(cudaMemcpyAsync(keys, kb, n * sizeof(u64), cudaMemcpyDeviceToDevice, c->stream));
+        if (vals) TT_CUDA(cudaMemcpyAsync(vals, vb, n * sizeof(V), cudaMemcpyDeviceToDevice, c->stream));
+    }
+}
+
+template void radix_sort_inplace<u32>(tt_ctx*, u64*, u32*, u64, int);
+template void radix_sort_inplace<u64>(tt_ctx*, u64*, u64*, u64, int);
+
+}  // namespace tt

@@ -1,0 +1,93 @@
+"""Device-resident front-end stages on torch tensors (all on one CUDA device).
+
+Each function calls exactly one C-ABI entry point; results are torch tensors
+on the device. Names follow the reference functions they replace.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import torch
+
+from . import capi
+from .capi import Context, ptr
+
+
+def _f32(x: torch.Tensor) -> torch.Tensor:
+    if x.dtype != torch.float32 or not x.is_cuda:
+        raise ValueError("expected a float32 CUDA tensor")
+    return x.contiguous()
+
+
+def make_dense(ctx: Context, x: torch.Tensor, metric: str = "l2") -> tuple[torch.Tensor, float]:
+    """rips.hpp make_dense (full layout) + enclosing_radius: (n x n matrix, radius)."""
+    x = _f32(x)
+    n, dim = x.shape
+    kind, p = capi.metric_parse(metric)
+    mat = torch.empty((n, n), dtype=torch.float32, device=x.device)
+    enc = C.c_float()
+    ctx.check(ctx.L.tt_dense_distances(ctx.h, ptr(x), n, dim, kind, p, ptr(mat), C.byref(enc)))
+    return mat, enc.value
+
+
+def _view(ctx: Context, addr: int, count: int, dtype: torch.dtype, device) -> torch.Tensor:
+    """Copy a context-owned device array into a fresh torch tensor (stream-ordered)."""
+    out = torch.empty(count, dtype=dtype, device=device)
+    if count:
+        ctx.check(ctx.L.tt_copy_async(ctx.h, C.c_void_p(out.data_ptr()), C.c_void_p(addr),
+                                      count * out.element_size()))
+    return out
+
+
+def dim0(ctx: Context, mat: torch.Tensor | None = None, csr: tuple | None = None, n: int | None = None,
+         threshold: float = math.inf, maxdim: int = 1) -> dict:
+    """rips.hpp Reducer::dim0 on a dense matrix or a CSR graph (rp u64, ci u32, w f32)."""
+    if mat is not None:
+        n = mat.shape[0]
+        rp = ci = w = None
+        dev = mat.device
+    else:
+        rp, ci, w = csr
+        dev = rp.device
+        if n is None:
+            n = rp.numel() - 1
+    out = capi.Dim0Out()
+    ctx.check(ctx.L.tt_dim0(ctx.h, ptr(mat), ptr(rp), ptr(ci), ptr(w), n, float(threshold), maxdim,
+                            C.byref(out)))
+    m, c, h = out.edges, out.columns, out.h0_finite
+    r = {
+        "keys": _view(ctx, out.edge_keys_dev, m, torch.int64, dev),
+        "tree": _view(ctx, out.tree_dev, m, torch.uint8, dev),
+        "cidx": _view(ctx, out.col_index_dev, c, torch.int64, dev),
+        "cd": _view(ctx, out.col_diameter_dev, c, torch.float32, dev),
+        "emi": _view(ctx, out.col_cofacet_dev, c, torch.int64, dev),
+        "emf": _view(ctx, out.col_cofacet_app_dev, c, torch.uint8, dev),
+        "h0": _view(ctx, out.h0_death_dev, h, torch.float32, dev),
+        "essential": out.essential,
+    }
+    r["app"] = _view(ctx, out.apparent_dev, m, torch.uint8, dev) if out.apparent_dev else None
+    torch.cuda.current_stream(dev).synchronize()
+    return r
+
+
+def redzed_edges(ctx: Context, mat: torch.Tensor | None = None, csr: tuple | None = None, n: int | None = None,
+                 threshold: float = math.inf) -> tuple[torch.Tensor, torch.Tensor]:
+    """redzed::detail::build_edges: (diameters, vertex pairs) in (d asc, comb asc) order."""
+    if mat is not None:
+        n = mat.shape[0]
+        rp = ci = w = None
+        dev = mat.device
+        cap = n * (n - 1) // 2
+    else:
+        rp, ci, w = csr
+        dev = rp.device
+        n = rp.numel() - 1 if n is None else n
+        cap = ci.numel() // 2
+    d = torch.empty(max(cap, 1), dtype=torch.float32, device=dev)
+    v = torch.empty(2 * max(cap, 1), dtype=torch.int32, device=dev)
+    cnt = C.c_uint64()
+    ctx.check(ctx.L.tt_redzed_edges(ctx.h, ptr(mat), ptr(rp), ptr(ci), ptr(w), n, float(threshold), ptr(d),
+                                    ptr(v), cap, C.byref(cnt)))
+    m = cnt.value
+    return d[:m], v[: 2 * m]
