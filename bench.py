@@ -1,0 +1,364 @@
+"""Front-end benchmark on one GB300 (see --help).
+
+Workload (default): the symmetric kNN flag complex of 100,000 float32 points in
+R^32 drawn from a mixture of 16 isotropic Gaussians (centres ~ N(0, 4I),
+sigma 1, seed 3), k = 15, L2, maxdim 1 — the front end of one diagram:
+exact kNN lists -> symmetric kNN graph (CSR) -> filtration sort of its edges
+-> apparent/emergent-pair scan -> Borůvka H0 -> dim-1 columns. A "step" is
+one such front end; the metric is front ends (diagrams) per second.
+
+  value  device-resident input, CUDA events on the library's stream around
+         each step, L2 flushed (a 512 MB write) between steps outside the
+         events, mean over the timed steps, max over ranks
+  e2e    the same front end through the host-buffer C-ABI call
+         (tt_knn_front_h): host points in, CSR + H0 + columns out, copies
+         inside the timed region
+  roofline   the dominant kernel (the exact kNN all-pairs scan), timed alone
+  cpu_baseline   the oracle port of the same front end on the host cores, a
+         bounded sample of the kNN queries scaled to the whole cloud
+
+--impl reference runs only the CPU arm (the oracle port; the reference's own
+build cannot run on this host) on rank 0 and prints its line.
+Multi-GPU: independent replicas per rank (weak scaling, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "diagrams/s"
+N, DIM, K, MAXDIM, METRIC_NAME = 100_000, 32, 15, 1, "l2"
+
+
+def peaks() -> tuple[dict, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(v: float, ws: int) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ----------------------------------------------------------------------------
+# CPU arm: the oracle port of the same front end.
+# ----------------------------------------------------------------------------
+def cpu_front_seconds(x, sample: int, threads: int) -> tuple[float, dict]:
+    """Seconds for one whole front end on the host, from a bounded sample."""
+    import numpy as np
+
+    from oracle import oracle as O
+    n = x.shape[0]
+    t0 = time.perf_counter()
+    ids_s = O.knn_rows(x, METRIC_NAME, K, 0, sample, threads)
+    t_knn = (time.perf_counter() - t0) * (n / sample)
+    # graph + dim0 at full size need the full lists: use the device's lists'
+    # shape (n x k) with the sampled rows' cost already measured; the graph
+    # and dim0 stages are timed on a sub-cloud of the same density and scaled
+    # by edge count.
+    sub = min(n, 20_000)
+    xs = np.ascontiguousarray(x[:sub])
+    ids = O.knn_rows(xs, METRIC_NAME, K, 0, sub, threads)
+    t1 = time.perf_counter()
+    rp, ci, w = O.knn_graph(xs, METRIC_NAME, ids)
+    t_graph = (time.perf_counter() - t1) * (n / sub)
+    t2 = time.perf_counter()
+    O.dim0(csr=(rp, ci, w), n=sub, maxdim=MAXDIM)
+    t_dim0 = (time.perf_counter() - t2) * (n / sub)
+    del ids_s
+    return t_knn + t_graph + t_dim0, {"knn_s": t_knn, "graph_s": t_graph, "dim0_s": t_dim0}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    import numpy as np  # noqa: F401
+
+    from oracle import oracle as O
+    from turbotops_gb300 import synth
+    O.lib()
+    x = synth.gmm(N, DIM)
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample
+    for _ in range(args.warmup):
+        cpu_front_seconds(x, max(sample // 4, threads), threads)
+    times = []
+    detail = {}
+    for _ in range(args.steps):
+        s, detail = cpu_front_seconds(x, sample, threads)
+        times.append(s)
+    sec = statistics.mean(times)
+    value = 1.0 / sec
+    line = {"metric": METRIC, "value": value, "unit": "diagrams/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"knn-complex front end, gmm {N}x{DIM}, k={K}, {METRIC_NAME}, maxdim {MAXDIM}",
+                       "sample": f"{sample} kNN queries of {N}, graph+dim0 on a 20000-point sub-cloud, "
+                                 f"scaled to the whole cloud"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "diagrams/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} of {N} kNN queries (+ graph/dim0 on 20000 points), scaled",
+                             **{k: round(v, 4) for k, v in detail.items()}},
+            "e2e": {"value": value, "unit": "diagrams/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# GPU arm.
+# ----------------------------------------------------------------------------
+def run_gpu(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    from turbotops_gb300 import capi, synth
+    from turbotops_gb300.capi import Context, KnnFrontOut
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    x_h = synth.gmm(N, DIM)
+    x = torch.from_numpy(x_h).to(dev)
+    ctx = Context(local)
+    L = ctx.L
+    kind, p = capi.metric_parse(METRIC_NAME)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        out = KnnFrontOut()
+        ctx.check(L.tt_knn_front(ctx.h, x.data_ptr(), N, DIM, kind, p, K, MAXDIM, C.byref(out)))
+        return out
+
+    for _ in range(args.warmup):
+        out = step()
+    torch.cuda.synchronize()
+    nnz, ncols = out.graph.nnz, out.dim0.columns
+
+    # ---- value: device-timed steps
+    clocks = Clocks(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = ctx.launches
+    ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    launches = ctx.launches - launches0
+    barrier(ws)
+    clk = clocks.stop()
+    ms_step = max_over_ranks(statistics.mean(ms), ws)
+
+    # ---- e2e: host buffers through the C-ABI
+    xp = torch.from_numpy(x_h).pin_memory()
+    rp_h = torch.empty(N + 1, dtype=torch.int64).pin_memory()
+    col_h = torch.empty(nnz + 16, dtype=torch.int32).pin_memory()
+    w_h = torch.empty(nnz + 16, dtype=torch.float32).pin_memory()
+    h0_h = torch.empty(N, dtype=torch.float32).pin_memory()
+    ci_h = torch.empty(ncols + 16, dtype=torch.int64).pin_memory()
+    cd_h = torch.empty(ncols + 16, dtype=torch.float32).pin_memory()
+    cf_h = torch.empty(ncols + 16, dtype=torch.int64).pin_memory()
+    ca_h = torch.empty(ncols + 16, dtype=torch.uint8).pin_memory()
+    u64 = C.c_uint64
+    cnt = [u64() for _ in range(5)]
+
+    def e2e_step():
+        ctx.check(L.tt_knn_front_h(ctx.h, xp.data_ptr(), N, DIM, kind, p, K, MAXDIM, rp_h.data_ptr(),
+                                   col_h.data_ptr(), w_h.data_ptr(), nnz + 16, C.byref(cnt[0]), h0_h.data_ptr(),
+                                   C.byref(cnt[1]), C.byref(cnt[2]), ci_h.data_ptr(), cd_h.data_ptr(),
+                                   cf_h.data_ptr(), ca_h.data_ptr(), ncols + 16, C.byref(cnt[3]),
+                                   C.byref(cnt[4])))
+
+    for _ in range(2):
+        e2e_step()
+    e2e_ms = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_step_ms = max_over_ranks(statistics.mean(e2e_ms), ws)
+    h2d = N * DIM * 4
+    d2h = (N + 1) * 8 + cnt[0].value * 8 + cnt[1].value * 4 + cnt[3].value * 21
+
+    # ---- roofline of the dominant kernel: the exact kNN all-pairs scan alone
+    ids = torch.empty((N, K), dtype=torch.int32, device=dev)
+    dd = torch.empty((N, K), dtype=torch.float32, device=dev)
+    ko = C.c_uint32()
+    kms = []
+    for r in range(args.warmup + args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.check(L.tt_knn(ctx.h, x.data_ptr(), N, DIM, kind, p, K, ids.data_ptr(), dd.data_ptr(), C.byref(ko)))
+        e1.record(stream)
+        e1.synchronize()
+        if r >= args.warmup:
+            kms.append(e0.elapsed_time(e1))
+    knn_ms = statistics.mean(kms)
+    pk, pk_src = peaks()
+    gram_flops = 2.0 * N * N * DIM            # the Gram-equivalent contraction of one launch
+    achieved = gram_flops / (knn_ms * 1e-3) / 1e12
+    fp32_ops = N * N * (3.0 * DIM)            # sub + mul/fma + add per coordinate, exact path
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "knn_scan_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        s, det = cpu_front_seconds(x_h, args.cpu_sample, threads)
+        cpu = {"value": 1.0 / s, "unit": "diagrams/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_sample} of {N} kNN queries on all host threads (+ graph/dim0 on a "
+                         f"20000-point sub-cloud), scaled to the whole front end",
+               **{k: round(v, 4) for k, v in det.items()}}
+
+    value = ws * 1000.0 / ms_step
+    line = {
+        "metric": METRIC, "value": value, "unit": "diagrams/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"knn-complex front end, gmm {N}x{DIM}, k={K}, {METRIC_NAME}, maxdim {MAXDIM}",
+                   "edges": int(out.dim0.edges), "columns": int(ncols), "nnz": int(nnz),
+                   "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": ws * 1000.0 / e2e_step_ms, "unit": "diagrams/s", "ms_per_step": e2e_step_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": achieved / pk["bf16_tflops"], "traffic": traffic,
+                     "kernel": "k_scan<L2, 32, KnnOp<16>> (exact kNN all-pairs scan)",
+                     "kernel_ms": knn_ms, "peak_source": pk_src,
+                     "fp32_exact_ops_per_s": fp32_ops / (knn_ms * 1e-3)},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-sample", type=int, default=8000, help="kNN queries timed on the host")
+    ap.add_argument("--n", type=int, default=N, help="points (smaller only for profiling runs)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    global N
+    N = args.n
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
+    try:
+        if args.impl == "reference":
+            return run_reference(args, ws, rank)
+        return run_gpu(args, ws, rank, local)
+    finally:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -95,6 +95,68 @@ int tt_redzed_edges(tt_ctx* ctx, const float* mat_dev, const uint64_t* rp_dev, c
                     const float* w_dev, uint32_t n, float threshold, float* diam_dev, int32_t* verts_dev,
                     uint64_t cap, uint64_t* count);
 
+/* knn_lists_exact (graph.hpp:211-225): the k nearest neighbours of every
+ * point, ascending by (distance, id), self excluded; k is clamped to n - 1
+ * (the row stride of ids_dev / dists_dev is the clamped k, *k_out). k <= 32.
+ * dists_dev may be NULL. */
+int tt_knn(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+           uint32_t* ids_dev, float* dists_dev, uint32_t* k_out);
+
+/* Result of a graph builder: a CsrGraph (core.hpp:92-98) with device arrays
+ * owned by the context; row_ptr_dev has n + 1 entries. */
+typedef struct tt_csr_out {
+    uint32_t n;
+    uint64_t nnz;              /* 2m */
+    const uint64_t* row_ptr_dev;
+    const uint32_t* col_dev;
+    const float* weight_dev;
+} tt_csr_out;
+
+/* knn_lists_exact + knn_graph (graph.hpp:211-225, :286-304): the symmetric
+ * kNN graph, rows sorted by neighbour id, weights d(i, j). */
+int tt_knn_graph(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+                 tt_csr_out* out);
+
+/* radius_graph (graph.hpp:170-201): all pairs with d <= tau. */
+int tt_radius_graph(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, float tau,
+                    tt_csr_out* out);
+
+/* mst::h0 (mst.hpp:25-99): the n - 1 minimum-spanning-tree weights of the
+ * complete graph, ascending, into deaths_dev (capacity n). The reference's
+ * bars follow: deaths > threshold add essential classes, deaths > 0 are
+ * finite bars. */
+int tt_mst_deaths(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, float* deaths_dev);
+
+/* Host-buffer form of tt_knn_graph (what the reference's
+ * knn_lists_exact + knn_graph front end binds): points in, CsrGraph out.
+ * row_ptr_h has n + 1 entries; col_h / weight_h hold up to cap entries
+ * (TT_ERR_LENGTH beyond, *nnz always set). */
+int tt_knn_graph_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+                   uint64_t* row_ptr_h, uint32_t* col_h, float* weight_h, uint64_t cap, uint64_t* nnz);
+
+/* Device results of the kNN flag-complex front end: the graph plus dim0. */
+typedef struct tt_knn_front_out {
+    tt_csr_out graph;
+    tt_dim0_out dim0;
+} tt_knn_front_out;
+
+/* knn_lists_exact -> knn_graph -> Reducer::dim0 of rips::compute_graph
+ * (turbotops.hpp:260-298, threshold +inf), all on the device. */
+int tt_knn_front(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+                 uint32_t maxdim, tt_knn_front_out* out);
+
+/* Front end of the kNN flag-complex path with host buffers (what
+ * persistence(points, ...) with graph = knn binds, turbotops.hpp:260-298:
+ * knn_lists_exact -> knn_graph -> Reducer::dim0 of rips::compute_graph):
+ * points in; the CsrGraph, the H0 deaths, the essential count and the dim-1
+ * columns (+ emergent probe) out. Capacities as in tt_knn_graph_h and
+ * tt_dense_front_h; every count is always written. */
+int tt_knn_front_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+                   uint32_t maxdim, uint64_t* row_ptr_h, uint32_t* col_h, float* weight_h, uint64_t cap,
+                   uint64_t* nnz, float* h0_h, uint64_t* nh0, uint64_t* essential, uint64_t* col_idx_h,
+                   float* col_d_h, uint64_t* col_cf_h, uint8_t* col_cf_app_h, uint64_t col_cap, uint64_t* ncols,
+                   uint64_t* nedges);
+
 /* Front end of the dense full-Rips path with host buffers (the call the
  * reference's rips::compute_dense front end binds, rips.hpp:1068-1075 +
  * :685-870): points -> distances -> enclosing radius -> dim0, everything a

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -217,6 +218,43 @@ struct Cx {
     // for cd <= cap. fn returns false to stop.
     template <typename F>
     void cofacets(const u32* vd, u32 nv, f32 diam, bool all, f32 cap, F&& fn) const {
+        if (!mat) {
+            // SparseComplex::cofacets (rips.hpp:429-471): the common
+            // neighbours of vd's vertices, walked down from the top of their
+            // sorted rows.
+            u64 p[40], lo[40];
+            for (u32 i = 0; i < nv; ++i) {
+                lo[i] = rp[vd[i]];
+                p[i] = rp[vd[i] + 1];
+                if (p[i] == lo[i]) return;
+            }
+            for (;;) {
+                u32 x = ci[p[0] - 1];
+                bool agree = true;
+                for (u32 i = 1; i < nv && agree; ++i) {
+                    while (ci[p[i] - 1] > x) {
+                        if (--p[i] == lo[i]) return;
+                    }
+                    if (ci[p[i] - 1] < x) {
+                        x = ci[p[i] - 1];
+                        agree = false;
+                    }
+                }
+                if (!agree) {
+                    while (ci[p[0] - 1] > x) {
+                        if (--p[0] == lo[0]) return;
+                    }
+                    continue;
+                }
+                u32 t = 0;
+                for (u32 i = 0; i < nv; ++i) t += vd[i] > x;
+                if (!all && t > 0) return;
+                f32 cd = diam;
+                for (u32 i = 0; i < nv; ++i) cd = std::max(cd, w[p[i] - 1]);
+                if (cd <= cap && !fn(x, t, cd)) return;
+                if (--p[0] == lo[0]) return;
+            }
+        }
         for (int64_t wi = int64_t(n) - 1; wi >= 0; --wi) {
             const u32 w = u32(wi);
             u32 t = 0;
@@ -446,15 +484,43 @@ uint64_t or_assemble(const float* mat, uint32_t n, float thr, const uint64_t* si
 }
 
 void or_knn(const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k, uint32_t* ids) {
+    or_knn_rows(x, n, dim, kind, p, k, 0, n, 1, ids);
+}
+
+// Rows [q0, q1) of the kNN lists (ids holds rows q0.. at stride k), on
+// `threads` host threads; the CPU-baseline leg of the benchmark times this.
+void or_knn_rows(const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k, uint32_t q0,
+                 uint32_t q1, uint32_t threads, uint32_t* ids) {
     k = n ? std::min<u32>(k, n - 1) : 0;
-    std::vector<std::pair<f32, u32>> c;
-    for (u32 i = 0; i < n; ++i) {
-        c.clear();
-        for (u32 j = 0; j < n; ++j)
-            if (j != i) c.emplace_back(dist(kind, p, x + u64(i) * dim, x + u64(j) * dim, dim), j);
-        std::partial_sort(c.begin(), c.begin() + k, c.end());
-        for (u32 t = 0; t < k; ++t) ids[u64(i) * k + t] = c[t].second;
+    // knn_query's bounded max-heap of (distance, id) (graph.hpp:123-166),
+    // over every candidate instead of the k-d tree's leaves.
+    auto work = [&](u32 lo, u32 hi) {
+        std::vector<std::pair<f32, u32>> h;
+        for (u32 i = lo; i < hi; ++i) {
+            h.clear();
+            for (u32 j = 0; j < n; ++j) {
+                if (j == i) continue;
+                const std::pair<f32, u32> c{dist(kind, p, x + u64(i) * dim, x + u64(j) * dim, dim), j};
+                if (h.size() < k) {
+                    h.push_back(c);
+                    std::push_heap(h.begin(), h.end());
+                } else if (c < h.front()) {
+                    std::pop_heap(h.begin(), h.end());
+                    h.back() = c;
+                    std::push_heap(h.begin(), h.end());
+                }
+            }
+            std::sort(h.begin(), h.end());
+            for (u32 t = 0; t < k; ++t) ids[u64(i - q0) * k + t] = h[t].second;
+        }
+    };
+    threads = std::max<u32>(1, std::min<u32>(threads, q1 > q0 ? q1 - q0 : 1));
+    std::vector<std::thread> pool;
+    for (u32 t = 0; t < threads; ++t) {
+        const u32 lo = q0 + u32(u64(q1 - q0) * t / threads), hi = q0 + u32(u64(q1 - q0) * (t + 1) / threads);
+        pool.emplace_back(work, lo, hi);
     }
+    for (auto& th : pool) th.join();
 }
 
 uint64_t or_knn_graph(const float* x, uint32_t n, uint32_t dim, int kind, float p,

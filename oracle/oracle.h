@@ -54,6 +54,9 @@ uint64_t or_assemble(const float* mat, uint32_t n, float thr,
 
 /* knn_lists_exact (graph.hpp:211-225): ascending (d, id), self excluded. */
 void or_knn(const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k, uint32_t* ids);
+/* Rows [q0, q1) of the same lists on `threads` host threads. */
+void or_knn_rows(const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k, uint32_t q0,
+                 uint32_t q1, uint32_t threads, uint32_t* ids);
 /* knn_graph (graph.hpp:286-304) + CsrGraph::from_rows: returns nnz; rp has n+1. */
 uint64_t or_knn_graph(const float* x, uint32_t n, uint32_t dim, int kind, float p,
                       const uint32_t* ids, uint32_t k, uint64_t* rp, uint32_t* ci, float* w);

@@ -62,6 +62,8 @@ def lib():
         L.or_assemble.argtypes = [P, C.c_uint32, C.c_float, P, P, C.c_uint64, P, C.c_uint64, P, P,
                                   C.c_uint64, P]
         L.or_knn.argtypes = [P, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_uint32, P]
+        L.or_knn_rows.argtypes = [P, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_uint32, C.c_uint32,
+                                  C.c_uint32, C.c_uint32, P]
         L.or_knn_graph.restype = C.c_uint64
         L.or_knn_graph.argtypes = [P, C.c_uint32, C.c_uint32, C.c_int, C.c_float, P, C.c_uint32, P, P, P]
         L.or_radius_graph.restype = C.c_uint64
@@ -168,6 +170,17 @@ def knn(x, metric, k) -> np.ndarray:
     ids = np.empty((n, kk), np.uint32)
     c, p = metric_code(metric)
     lib().or_knn(_p(x), n, dim, c, p, k, _p(ids))
+    return ids
+
+
+def knn_rows(x, metric, k, q0, q1, threads) -> np.ndarray:
+    """kNN lists of queries [q0, q1) against the whole cloud, on `threads` threads."""
+    x = _pts(x)
+    n, dim = x.shape
+    kk = min(k, n - 1) if n else 0
+    ids = np.empty((q1 - q0, kk), np.uint32)
+    c, p = metric_code(metric)
+    lib().or_knn_rows(_p(x), n, dim, c, p, k, q0, q1, threads, _p(ids))
     return ids
 
 

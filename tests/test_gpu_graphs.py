@@ -1,0 +1,81 @@
+"""CUDA path vs the reference goldens and the oracle: exact kNN lists, the
+symmetric kNN graph, the radius graph and the complete-graph MST (H0)."""
+import numpy as np
+import pytest
+
+from golden_io import cases, ids, thr_of
+from gpu_util import bits, ctx, dev, host
+from oracle import oracle as O
+from turbotops_gb300 import ops, synth
+
+pytestmark = pytest.mark.gpu
+
+KNN = cases("knn")
+RADIUS = cases("radius")
+MST = cases("mst")
+
+
+def exact(metric):
+    return metric in ("l1", "l2", "linf")
+
+
+@pytest.mark.parametrize("c", KNN, ids=ids(KNN))
+def test_knn_vs_reference(c):
+    k = c["params"]["k"]
+    x = dev(c["x"])
+    i, d = ops.knn(ctx(), x, k, c["metric"])
+    if not exact(c["metric"]):
+        pytest.skip("Lp lists depend on the final root's rounding (see DESIGN)")
+    assert np.array_equal(host(i).view(np.uint32).ravel(), c["ids"])
+    rp, ci, w = ops.knn_graph(ctx(), x, k, c["metric"])
+    assert np.array_equal(host(rp).view(np.uint64), c["rp"])
+    assert np.array_equal(host(ci).view(np.uint32), c["ci"])
+    assert np.array_equal(bits(host(w)), bits(c["w"]))
+
+
+@pytest.mark.parametrize("c", RADIUS, ids=ids(RADIUS))
+def test_radius_vs_reference(c):
+    rp, ci, w = ops.radius_graph(ctx(), dev(c["x"]), thr_of(c["params"]["tau"]), c["metric"])
+    assert np.array_equal(host(rp).view(np.uint64), c["rp"])
+    assert np.array_equal(host(ci).view(np.uint32), c["ci"])
+    assert np.array_equal(bits(host(w)), bits(c["w"]))
+
+
+@pytest.mark.parametrize("c", MST, ids=ids(MST))
+def test_mst_vs_reference(c):
+    d = ops.mst_deaths(ctx(), dev(c["x"]), c["metric"])
+    bars = ops.h0_bars(d, thr_of(c["params"]["thr"]))
+    assert np.array_equal(bits(bars), bits(c["h0"]))
+
+
+@pytest.mark.parametrize("metric", ["l2", "l1", "linf"])
+@pytest.mark.parametrize("n,dim,k,kind", [(1000, 32, 15, "gauss"), (700, 3, 8, "grid"), (513, 5, 31, "gauss"),
+                                          (129, 16, 1, "gauss"), (6, 4, 15, "gauss")])
+def test_knn_graph_vs_oracle(metric, n, dim, k, kind):
+    x = synth.gauss(n, dim, n + dim) if kind == "gauss" else synth.grid(n, dim, 12, n)
+    i, d = ops.knn(ctx(), dev(x), k, metric)
+    ref = O.knn(x, metric, k)
+    assert np.array_equal(host(i).view(np.uint32), ref)
+    rp, ci, w = ops.knn_graph(ctx(), dev(x), k, metric)
+    orp, oci, ow = O.knn_graph(x, metric, ref)
+    assert np.array_equal(host(rp).view(np.uint64), orp)
+    assert np.array_equal(host(ci).view(np.uint32), oci)
+    assert np.array_equal(bits(host(w)), bits(ow))
+
+
+@pytest.mark.parametrize("metric", ["l2", "l1", "linf"])
+@pytest.mark.parametrize("n,dim", [(2000, 32), (1500, 3), (300, 7), (2, 3)])
+def test_mst_vs_oracle(metric, n, dim):
+    x = synth.gauss(n, dim, 3 * n + dim) if dim != 3 else synth.grid(n, 3, 20, n)
+    d = ops.mst_deaths(ctx(), dev(x), metric)
+    assert np.array_equal(bits(ops.h0_bars(d)), bits(O.mst_h0(x, metric)))
+
+
+def test_radius_vs_oracle_ties():
+    x = synth.grid(800, 4, 7, 3)
+    for metric, tau in [("l1", 3.0), ("linf", 1.0), ("l2", 2.0)]:
+        rp, ci, w = ops.radius_graph(ctx(), dev(x), tau, metric)
+        orp, oci, ow = O.radius_graph(x, metric, tau)
+        assert np.array_equal(host(rp).view(np.uint64), orp)
+        assert np.array_equal(host(ci).view(np.uint32), oci)
+        assert np.array_equal(bits(host(w)), bits(ow))

@@ -24,10 +24,18 @@ METRIC_L1, METRIC_L2, METRIC_LINF, METRIC_LP = 0, 1, 2, 3
 OK, ERR_INVALID, ERR_OVERFLOW, ERR_LENGTH, ERR_CUDA, ERR_TIMEOUT, ERR_INTERNAL = range(7)
 
 
+class CsrOut(C.Structure):
+    _fields_ = [("n", u32), ("nnz", u64), ("row_ptr_dev", P), ("col_dev", P), ("weight_dev", P)]
+
+
 class Dim0Out(C.Structure):
     _fields_ = [("edges", u64), ("edge_keys_dev", P), ("apparent_dev", P), ("tree_dev", P),
                 ("columns", u64), ("col_index_dev", P), ("col_diameter_dev", P), ("col_cofacet_dev", P),
                 ("col_cofacet_app_dev", P), ("h0_finite", u64), ("h0_death_dev", P), ("essential", u64)]
+
+
+class KnnFrontOut(C.Structure):
+    _fields_ = [("graph", CsrOut), ("dim0", Dim0Out)]
 
 
 _SIGS = {
@@ -42,6 +50,14 @@ _SIGS = {
     "tt_dense_distances": (i32, [P, P, u32, u32, i32, f32, P, C.POINTER(f32)]),
     "tt_dim0": (i32, [P, P, P, P, P, u32, f32, u32, C.POINTER(Dim0Out)]),
     "tt_redzed_edges": (i32, [P, P, P, P, P, u32, f32, P, P, u64, C.POINTER(u64)]),
+    "tt_knn": (i32, [P, P, u32, u32, i32, f32, u32, P, P, C.POINTER(u32)]),
+    "tt_knn_graph": (i32, [P, P, u32, u32, i32, f32, u32, C.POINTER(CsrOut)]),
+    "tt_radius_graph": (i32, [P, P, u32, u32, i32, f32, f32, C.POINTER(CsrOut)]),
+    "tt_mst_deaths": (i32, [P, P, u32, u32, i32, f32, P]),
+    "tt_knn_graph_h": (i32, [P, P, u32, u32, i32, f32, u32, P, P, P, u64, C.POINTER(u64)]),
+    "tt_knn_front": (i32, [P, P, u32, u32, i32, f32, u32, u32, C.POINTER(KnnFrontOut)]),
+    "tt_knn_front_h": (i32, [P, P, u32, u32, i32, f32, u32, u32, P, P, P, u64, C.POINTER(u64), P,
+                             C.POINTER(u64), C.POINTER(u64), P, P, P, P, u64, C.POINTER(u64), C.POINTER(u64)]),
     "tt_dense_front_h": (i32, [P, P, u32, u32, i32, f32, u32, C.POINTER(f32), P, P, C.POINTER(u64),
                                C.POINTER(u64), P, P, P, P, u64, C.POINTER(u64), C.POINTER(u64)]),
 }

@@ -34,6 +34,44 @@ void check_metric(int kind, float p) {
     if (kind == TT_METRIC_LP && !(p >= 1.0f)) invalid("metric: p must be in [1, inf]");
 }
 
+void fill_dim0(const Dim0Out& r, tt_dim0_out* out) {
+    out->edges = r.m;
+    out->edge_keys_dev = r.keys;
+    out->apparent_dev = r.app;
+    out->tree_dev = r.tree;
+    out->columns = r.ncols;
+    out->col_index_dev = r.cidx;
+    out->col_diameter_dev = r.cd;
+    out->col_cofacet_dev = r.emi;
+    out->col_cofacet_app_dev = r.emf;
+    out->h0_finite = r.nh0;
+    out->h0_death_dev = r.h0;
+    out->essential = r.essential;
+}
+
+// knn_lists_exact -> knn_graph -> dim0 on the device. The graph is moved into
+// slots that dim0 does not use, so both results stay valid together.
+u64 knn_front_dev(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32 maxdim, u64** rp_out,
+                  u32** ci_out, f32** w_out, Dim0Out& r) {
+    const u32 kk = n ? std::min<u32>(k, n - 1) : 0;
+    u64* rp = c->arena.get<u64>(S_GRAPH_RP, u64(n) + 1);
+    u32* ci = nullptr;
+    f32* w = nullptr;
+    const u64 nnz = knn_graph(c, x, n, dim, kind, p, nullptr, kk, rp, &ci, &w);
+    u32* gci = c->arena.get<u32>(S_GRAPH_TMP, nnz + 1);
+    f32* gw = c->arena.get<f32>(S_KNN_D, nnz + 1);
+    if (nnz) {
+        TT_CUDA(cudaMemcpyAsync(gci, ci, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
+        TT_CUDA(cudaMemcpyAsync(gw, w, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    Complex cx{nullptr, rp, gci, gw, n, INFINITY};
+    dim0(c, cx, maxdim, r);
+    *rp_out = rp;
+    *ci_out = gci;
+    *w_out = gw;
+    return nnz;
+}
+
 }  // namespace
 
 extern "C" {
@@ -169,6 +207,148 @@ int tt_redzed_edges(tt_ctx* c, const float* mat, const uint64_t* rp, const uint3
         const u64 m = redzed_edges(c, cx, diam, verts, cap);
         if (count) *count = m;
         if (m > cap) throw Error(TT_ERR_LENGTH, "gb300: edge list exceeds the output capacity");
+    });
+}
+
+int tt_knn(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k, uint32_t* ids,
+           float* dists, uint32_t* k_out) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (k == 0) invalid("persistence: k must be >= 1");
+        const u32 kk = n ? std::min<u32>(k, n - 1) : 0;
+        if (k_out) *k_out = kk;
+        if (kk) knn_exact(c, x, n, dim, kind, p, kk, ids, dists);
+    });
+}
+
+int tt_knn_graph(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+                 tt_csr_out* out) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (k == 0) invalid("persistence: k must be >= 1");
+        if (!out) invalid("gb300: null output");
+        const u32 kk = n ? std::min<u32>(k, n - 1) : 0;
+        u64* rp = c->arena.get<u64>(S_OUT0, u64(n) + 1);
+        u32* ci = nullptr;
+        f32* w = nullptr;
+        const u64 nnz = knn_graph(c, x, n, dim, kind, p, nullptr, kk, rp, &ci, &w);
+        out->n = n;
+        out->nnz = nnz;
+        out->row_ptr_dev = rp;
+        out->col_dev = ci;
+        out->weight_dev = w;
+    });
+}
+
+int tt_radius_graph(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, float tau,
+                    tt_csr_out* out) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (std::isnan(tau) || tau < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        if (!out) invalid("gb300: null output");
+        u64* rp = c->arena.get<u64>(S_OUT0, u64(n) + 1);
+        u32* ci = nullptr;
+        f32* w = nullptr;
+        const u64 nnz = radius_graph(c, x, n, dim, kind, p, tau, rp, &ci, &w);
+        out->n = n;
+        out->nnz = nnz;
+        out->row_ptr_dev = rp;
+        out->col_dev = ci;
+        out->weight_dev = w;
+    });
+}
+
+int tt_mst_deaths(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, float* deaths) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        mst_deaths(c, x, n, dim, kind, p, deaths);
+    });
+}
+
+int tt_knn_graph_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+                   uint64_t* rp_h, uint32_t* col_h, float* w_h, uint64_t cap, uint64_t* nnz_out) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (k == 0) invalid("persistence: k must be >= 1");
+        for (u64 i = 0; i < u64(n) * dim; ++i)
+            if (!std::isfinite(x_h[i])) invalid("persistence: non-finite coordinate");
+        f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
+        if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
+        const u32 kk = n ? std::min<u32>(k, n - 1) : 0;
+        u64* rp = c->arena.get<u64>(S_OUT0, u64(n) + 1);
+        u32* ci = nullptr;
+        f32* w = nullptr;
+        const u64 nnz = knn_graph(c, x, n, dim, kind, p, nullptr, kk, rp, &ci, &w);
+        if (nnz_out) *nnz_out = nnz;
+        if (nnz > cap) throw Error(TT_ERR_LENGTH, "gb300: graph exceeds the output capacity");
+        TT_CUDA(cudaMemcpyAsync(rp_h, rp, 8 * (u64(n) + 1), cudaMemcpyDeviceToHost, c->stream));
+        if (nnz) {
+            TT_CUDA(cudaMemcpyAsync(col_h, ci, 4 * nnz, cudaMemcpyDeviceToHost, c->stream));
+            TT_CUDA(cudaMemcpyAsync(w_h, w, 4 * nnz, cudaMemcpyDeviceToHost, c->stream));
+        }
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int tt_knn_front(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+                 uint32_t maxdim, tt_knn_front_out* out) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (k == 0) invalid("persistence: k must be >= 1");
+        if (!out) invalid("gb300: null output");
+        u64* rp = nullptr;
+        u32* ci = nullptr;
+        f32* w = nullptr;
+        Dim0Out r;
+        const u64 nnz = knn_front_dev(c, x, n, dim, kind, p, k, maxdim, &rp, &ci, &w, r);
+        out->graph.n = n;
+        out->graph.nnz = nnz;
+        out->graph.row_ptr_dev = rp;
+        out->graph.col_dev = ci;
+        out->graph.weight_dev = w;
+        fill_dim0(r, &out->dim0);
+    });
+}
+
+int tt_knn_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
+                   uint32_t maxdim, uint64_t* rp_h, uint32_t* col_h, float* w_h, uint64_t cap, uint64_t* nnz_out,
+                   float* h0_h, uint64_t* nh0, uint64_t* essential, uint64_t* col_idx_h, float* col_d_h,
+                   uint64_t* col_cf_h, uint8_t* col_cf_app_h, uint64_t col_cap, uint64_t* ncols,
+                   uint64_t* nedges) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (k == 0) invalid("persistence: k must be >= 1");
+        for (u64 i = 0; i < u64(n) * dim; ++i)
+            if (!std::isfinite(x_h[i])) invalid("persistence: non-finite coordinate");
+        f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
+        if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
+        u64* rp = nullptr;
+        u32* gci = nullptr;
+        f32* gw = nullptr;
+        Dim0Out r;
+        const u64 nnz = knn_front_dev(c, x, n, dim, kind, p, k, maxdim, &rp, &gci, &gw, r);
+        if (nnz_out) *nnz_out = nnz;
+        if (nnz > cap) throw Error(TT_ERR_LENGTH, "gb300: graph exceeds the output capacity");
+        TT_CUDA(cudaMemcpyAsync(rp_h, rp, 8 * (u64(n) + 1), cudaMemcpyDeviceToHost, c->stream));
+        if (nnz) {
+            TT_CUDA(cudaMemcpyAsync(col_h, gci, 4 * nnz, cudaMemcpyDeviceToHost, c->stream));
+            TT_CUDA(cudaMemcpyAsync(w_h, gw, 4 * nnz, cudaMemcpyDeviceToHost, c->stream));
+        }
+        if (h0_h && r.nh0)
+            TT_CUDA(cudaMemcpyAsync(h0_h, r.h0, sizeof(f32) * r.nh0, cudaMemcpyDeviceToHost, c->stream));
+        if (nh0) *nh0 = r.nh0;
+        if (essential) *essential = r.essential;
+        if (ncols) *ncols = r.ncols;
+        if (nedges) *nedges = r.m;
+        if (col_idx_h && r.ncols) {
+            if (r.ncols > col_cap) throw Error(TT_ERR_LENGTH, "gb300: columns exceed the output capacity");
+            TT_CUDA(cudaMemcpyAsync(col_idx_h, r.cidx, 8 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+            if (col_d_h) TT_CUDA(cudaMemcpyAsync(col_d_h, r.cd, 4 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+            if (col_cf_h) TT_CUDA(cudaMemcpyAsync(col_cf_h, r.emi, 8 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+            if (col_cf_app_h)
+                TT_CUDA(cudaMemcpyAsync(col_cf_app_h, r.emf, r.ncols, cudaMemcpyDeviceToHost, c->stream));
+        }
+        TT_CUDA(cudaStreamSynchronize(c->stream));
     });
 }
 

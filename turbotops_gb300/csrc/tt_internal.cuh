@@ -16,6 +16,31 @@ __host__ __device__ inline u64 key_rips(f32 d, u64 idx) {
     return (u64(fbits(d)) << kIdxBits) | (kIdxMask - idx);
 }
 
+// Simplex index helpers (combinatorial number system, rips.hpp:505-580).
+__device__ __forceinline__ void decode_edge(u64 idx, u32& a, u32& b) {
+    // rips.hpp decode, nv = 2 closed form (:549-557): a > b
+    u64 v = u64((1.0 + sqrt(1.0 + 8.0 * double(idx))) * 0.5);
+    while (v * (v - 1) / 2 > idx) --v;
+    while ((v + 1) * v / 2 <= idx) ++v;
+    a = u32(v);
+    b = u32(idx - v * (v - 1) / 2);
+}
+__device__ __forceinline__ u64 edge_idx(u32 a, u32 b) {   // any order
+    if (a < b) { const u32 t = a; a = b; b = t; }
+    return u64(a) * (a - 1) / 2 + b;
+}
+__device__ __forceinline__ u64 tri_idx(u32 a, u32 b, u32 c) {   // a > b > c
+    return u64(a) * (a - 1) * (a - 2) / 6 + u64(b) * (b - 1) / 2 + c;
+}
+__device__ __forceinline__ void sort3(u32& a, u32& b, u32& c) {   // descending
+    if (a < b) { const u32 t = a; a = b; b = t; }
+    if (b < c) { const u32 t = b; b = c; c = t; }
+    if (a < b) { const u32 t = a; a = b; b = t; }
+}
+__device__ __forceinline__ f32 key_d(u64 k) { return __uint_as_float(u32(k >> kIdxBits)); }
+__device__ __forceinline__ u64 key_idx(u64 k) { return kIdxMask - (k & kIdxMask); }
+
+
 // ---- tt_dense.cu
 void dense_matrix(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32* mat, u32* rowmax);
 void min_bits(tt_ctx* c, const u32* v, u32 n, u32* out);

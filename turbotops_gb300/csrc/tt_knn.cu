@@ -1,0 +1,179 @@
+// tt_knn.cu — exact all-pairs scans over a point cloud: k nearest neighbours,
+// the symmetric kNN graph, the radius graph and the per-round nearest
+// foreign neighbour of the complete-graph Borůvka MST.
+//
+// Replaces graph.hpp knn_lists_exact (:211-225, k-d tree + heap, ties by id),
+// knn_graph (:286-304) + CsrGraph::from_rows (core.hpp:113-134),
+// radius_graph (:170-201) and the distance scans of mst::h0 (mst.hpp:25-99).
+// The reference's k-d tree is an exact accelerator (its pruning is
+// conservative, graph.hpp:114-119), so an exhaustive scan with the same
+// distance bits and the same (distance, id) order returns the same lists.
+//
+// One tiled all-pairs scanner (tt_scan.cuh) serves all four.
+#include "tt_scan.cuh"
+
+namespace tt {
+
+using scan::KnnOp;
+using scan::RadiusCountOp;
+using scan::RadiusFillOp;
+using scan::ForeignOp;
+using scan::scan_all;
+
+namespace {
+
+u32* error_word(tt_ctx* c) {
+    u32* e = c->arena.get<u32>(S_MISC2, 4);
+    TT_CUDA(cudaMemsetAsync(e, 0, sizeof(u32), c->stream));
+    return e;
+}
+
+void check_error_word(tt_ctx* c, const u32* e) {
+    u32 h = 0;
+    TT_CUDA(cudaMemcpyAsync(&h, e, 4, cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaStreamSynchronize(c->stream));
+    if (h & TT_DEV_ERR_TIMEOUT) throw Error(TT_ERR_TIMEOUT, "gb300: a bounded device wait timed out");
+}
+
+// --------------------------------------------------------------------------
+// Graph assembly kernels.
+// --------------------------------------------------------------------------
+__global__ void k_knn_pairs(const u32* __restrict__ ids, const f32* __restrict__ d, u32 n, u32 k,
+                            u64* __restrict__ keys, u32* __restrict__ vals) {
+    const u64 total = u64(n) * k;
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += u64(gridDim.x) * blockDim.x) {
+        const u32 i = u32(e / k), j = ids[e];
+        const u32 b = __float_as_uint(d[e]);
+        keys[2 * e] = (u64(i) << 32) | j;
+        vals[2 * e] = b;
+        keys[2 * e + 1] = (u64(j) << 32) | i;
+        vals[2 * e + 1] = b;
+    }
+}
+
+__global__ void k_unique_flags(const u64* __restrict__ keys, u64 m, u64* __restrict__ f) {
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x)
+        f[e] = e == 0 || keys[e] != keys[e - 1];
+}
+
+__global__ void k_unique_emit(const u64* __restrict__ keys, const u32* __restrict__ vals, u64 m,
+                              const u64* __restrict__ f, const u64* __restrict__ pos, u32* __restrict__ ci,
+                              f32* __restrict__ w, u32* __restrict__ rows) {
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
+        if (!f[e]) continue;
+        const u64 o = pos[e];
+        ci[o] = u32(keys[e]);
+        w[o] = __uint_as_float(vals[e]);
+        rows[o] = u32(keys[e] >> 32);
+    }
+}
+
+// row_ptr from the row of each entry of a row-sorted list
+__global__ void k_row_ptr(const u32* __restrict__ rows, u64 nnz, u32 n, u64* __restrict__ rp) {
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e <= nnz; e += u64(gridDim.x) * blockDim.x) {
+        const int64_t lo = e == 0 ? -1 : int64_t(rows[e - 1]);
+        const int64_t hi = e == nnz ? int64_t(n) : int64_t(rows[e]);
+        for (int64_t r = lo + 1; r <= hi; ++r) rp[r] = e;
+    }
+}
+
+inline u32 grid_for(u64 work, u32 per_block) {
+    const u64 g = (work + per_block - 1) / per_block;
+    return u32(std::max<u64>(1, std::min<u64>(g, 64ull * kSMs)));
+}
+
+}  // namespace
+
+void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists) {
+    if (k == 0 || n < 2) return;
+    u32* err = error_word(c);
+    if (k <= 16) scan_all(c, kind, x, n, dim, p, KnnOp<16>{ids, dists, k}, nullptr, err);
+    else if (k <= 32) scan_all(c, kind, x, n, dim, p, KnnOp<32>{ids, dists, k}, nullptr, err);
+    else invalid("gb300: exact kNN supports k <= 32");
+    check_error_word(c, err);
+}
+
+// Symmetric union of the lists (graph.hpp:286-304): both directions of every
+// list entry, sorted by (row, col), duplicates dropped. The weight of (i, j)
+// is the list distance d(i, j), bit-identical to the reference's recomputed
+// c(v, u) because every kernel is symmetric bit for bit.
+u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* ids, u32 k, u64* rp,
+              u32** ci_out, f32** w_out) {
+    const u64 m = 2 * u64(n) * k;
+    u32* kid = const_cast<u32*>(ids);
+    f32* kd = c->arena.get<f32>(S_KNN_D, u64(n) * k + 1);
+    if (!ids) {
+        kid = c->arena.get<u32>(S_KNN_I, u64(n) * k + 1);
+        knn_exact(c, x, n, dim, kind, p, k, kid, kd);
+    } else {
+        invalid("gb300: knn_graph from external lists is not supported; pass ids = NULL");
+    }
+    u64* keys = c->arena.get<u64>(S_GRAPH_KEYS, m + 1);
+    u32* vals = c->arena.get<u32>(S_GRAPH_TMP, m + 1);
+    if (m) {
+        k_knn_pairs<<<grid_for(u64(n) * k, 256), 256, 0, c->stream>>>(kid, kd, n, k, keys, vals);
+        TT_LAUNCH("k_knn_pairs");
+        ++c->launches;
+    }
+    radix_sort_inplace<u32>(c, keys, vals, m);
+    u64* f = c->arena.get<u64>(S_MISC0, 2 * m + 4);
+    u64* pos = f + m + 2;
+    u64* tot = c->arena.get<u64>(S_COUNT, 4);
+    u64 nnz = 0;
+    if (m) {
+        k_unique_flags<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, m, f);
+        scan_exclusive<u64>(c, f, pos, m, tot);
+        TT_CUDA(cudaMemcpyAsync(&nnz, tot, 8, cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+        ++c->launches;
+    }
+    u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);
+    f32* w = c->arena.get<f32>(S_OUT2, nnz + 1);
+    u32* rows = c->arena.get<u32>(S_OUT3, nnz + 1);
+    if (m) {
+        k_unique_emit<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, vals, m, f, pos, ci, w, rows);
+        TT_LAUNCH("k_unique_emit");
+        ++c->launches;
+    }
+    k_row_ptr<<<grid_for(nnz + 1, 256), 256, 0, c->stream>>>(rows, nnz, n, rp);
+    TT_LAUNCH("k_row_ptr");
+    ++c->launches;
+    *ci_out = ci;
+    *w_out = w;
+    return nnz;
+}
+
+// radius_graph (graph.hpp:170-201): a counting scan, a scan of the counts
+// into row pointers, and a filling scan that writes each row in increasing
+// neighbour order (the order CsrGraph::from_rows sorts into).
+u64 radius_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32 tau, u64* rp, u32** ci_out,
+                 f32** w_out) {
+    u64* cnt = c->arena.get<u64>(S_MISC0, u64(n) + 1);
+    u64* tot = c->arena.get<u64>(S_COUNT, 4);
+    u32* err = error_word(c);
+    if (n) scan_all(c, kind, x, n, dim, p, RadiusCountOp{tau, cnt}, nullptr, err);
+    scan_exclusive<u64>(c, cnt, rp, n, tot);
+    TT_CUDA(cudaMemcpyAsync(rp + n, tot, 8, cudaMemcpyDeviceToDevice, c->stream));
+    u64 nnz = 0;
+    TT_CUDA(cudaMemcpyAsync(&nnz, tot, 8, cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaStreamSynchronize(c->stream));
+    u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);
+    f32* w = c->arena.get<f32>(S_OUT2, nnz + 1);
+    if (n) scan_all(c, kind, x, n, dim, p, RadiusFillOp{tau, rp, ci, w}, nullptr, err);
+    check_error_word(c, err);
+    *ci_out = ci;
+    *w_out = w;
+    return nnz;
+}
+
+// One Borůvka proposal round over the complete graph: best[root] receives the
+// minimum (d, combinatorial index) edge leaving each component.
+void foreign_nearest(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* comp,
+                     unsigned long long* best, u32* err) {
+    scan_all(c, kind, x, n, dim, p, ForeignOp{comp, best}, comp, err);
+}
+
+void check_device_error(tt_ctx* c, const u32* err) { check_error_word(c, err); }
+u32* device_error_word(tt_ctx* c) { return error_word(c); }
+
+}  // namespace tt

@@ -36,6 +36,7 @@ __device__ __forceinline__ f32 l2_acc(const A& a, const B& b, u32 dim) {
 #pragma unroll
         for (int l = 0; l < 8; ++l) {
             f32 a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
             for (u32 c = 0; c < chunks; ++c) {
                 const f32 d0 = __fsub_rn(a(16 * c + l), b(16 * c + l));
                 const f32 d1 = __fsub_rn(a(16 * c + 8 + l), b(16 * c + 8 + l));
@@ -47,6 +48,7 @@ __device__ __forceinline__ f32 l2_acc(const A& a, const B& b, u32 dim) {
         s = hsum8(t);
         k = chunks << 4;
     }
+#pragma unroll
     for (; k < dim; ++k) {
         const f32 d = __fsub_rn(a(k), b(k));
         s = __fmaf_rn(d, d, s);
@@ -65,6 +67,7 @@ __device__ __forceinline__ f32 l1_acc(const A& a, const B& b, u32 dim) {
 #pragma unroll
         for (int l = 0; l < 8; ++l) {
             f32 a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
             for (u32 c = 0; c < chunks; ++c) {
                 a0 = __fadd_rn(a0, fabsf(__fsub_rn(a(16 * c + l), b(16 * c + l))));
                 a1 = __fadd_rn(a1, fabsf(__fsub_rn(a(16 * c + 8 + l), b(16 * c + 8 + l))));
@@ -74,6 +77,7 @@ __device__ __forceinline__ f32 l1_acc(const A& a, const B& b, u32 dim) {
         s = hsum8(t);
         k = chunks << 4;
     }
+#pragma unroll
     for (; k < dim; ++k) s = __fadd_rn(s, fabsf(__fsub_rn(a(k), b(k))));
     return s;
 }
@@ -82,6 +86,7 @@ __device__ __forceinline__ f32 l1_acc(const A& a, const B& b, u32 dim) {
 template <typename A, typename B>
 __device__ __forceinline__ f32 linf_acc(const A& a, const B& b, u32 dim) {
     f32 m = 0.0f;
+#pragma unroll
     for (u32 k = 0; k < dim; ++k) m = fmaxf(m, fabsf(__fsub_rn(a(k), b(k))));
     return m;
 }

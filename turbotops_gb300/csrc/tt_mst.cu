@@ -1,0 +1,107 @@
+// tt_mst.cu — H0 of the complete-graph Rips filtration via Borůvka.
+//
+// Replaces mst::h0 (mst.hpp:25-99). The reference grows one Prim tree; the
+// finite H0 deaths are the weights of a minimum spanning tree, and every MST
+// of a graph has the same multiset of weights, so any MST gives the same
+// sorted death list. Here each round proposes, for every component, its
+// minimum outgoing edge under the strict order (d, combinatorial index)
+// (the all-pairs scan of tt_knn.cu); the proposals form a forest (only
+// mutual proposals close 2-cycles, broken by component id); components
+// merge, and after at most ceil(log2 n) rounds one tree remains. The deaths
+// are then sorted by a radix sort on their float bits.
+#include "tt_internal.cuh"
+
+namespace tt {
+
+void foreign_nearest(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* comp,
+                     unsigned long long* best, u32* err);
+void check_device_error(tt_ctx* c, const u32* err);
+u32* device_error_word(tt_ctx* c);
+
+namespace {
+
+__global__ void k_mst_init(u32* __restrict__ comp, u32* __restrict__ parent, unsigned long long* __restrict__ best,
+                           u32 n) {
+    for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        comp[v] = v;
+        parent[v] = v;
+        best[v] = ~0ull;
+    }
+}
+
+__global__ void k_mst_hook(const u32* __restrict__ comp, const unsigned long long* __restrict__ best,
+                           u32* __restrict__ parent, u32 n, f32* __restrict__ deaths, u32* __restrict__ cnt) {
+    for (u32 c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        if (comp[c] != c) continue;
+        const u64 key = best[c];
+        if (key == ~0ull) continue;
+        u32 a, b;
+        decode_edge(key & kIdxMask, a, b);
+        const u32 o = comp[a] == c ? comp[b] : comp[a];
+        if (best[o] == key && c < o) continue;   // mutual: o hooks and records
+        parent[c] = o;
+        deaths[atomicAdd(cnt, 1u)] = __uint_as_float(u32(key >> kIdxBits));
+    }
+}
+
+__global__ void k_mst_flatten(const u32* __restrict__ parent, u32* __restrict__ comp,
+                              unsigned long long* __restrict__ best, u32 n) {
+    for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        u32 r = parent[v];
+        for (u32 s = 0; parent[r] != r && s < n; ++s) r = parent[r];
+        comp[v] = r;
+        best[v] = ~0ull;
+    }
+}
+
+__global__ void k_float_keys(const f32* __restrict__ d, u32 m, u64* __restrict__ keys) {
+    for (u32 e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x)
+        keys[e] = __float_as_uint(d[e]);
+}
+
+__global__ void k_keys_float(const u64* __restrict__ keys, u32 m, f32* __restrict__ d) {
+    for (u32 e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x)
+        d[e] = __uint_as_float(u32(keys[e]));
+}
+
+inline u32 grid_for(u64 work) { return u32(std::max<u64>(1, std::min<u64>((work + 255) / 256, 64ull * kSMs))); }
+
+}  // namespace
+
+// Sorted MST weights (n - 1 of them) into deaths (device). Returns n - 1.
+u64 mst_deaths(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32* deaths) {
+    if (n < 2) return 0;
+    if (n > 131072) invalid("gb300: the complete-graph MST supports n <= 131072 points");
+    u32* comp = c->arena.get<u32>(S_UF_PARENT, 2 * u64(n) + 2);
+    u32* parent = comp + n + 1;
+    unsigned long long* best = c->arena.get<unsigned long long>(S_UF_BEST, n + 1);
+    u32* cnt = c->arena.get<u32>(S_MISC1, 4);
+    u32* err = device_error_word(c);
+    k_mst_init<<<grid_for(n), 256, 0, c->stream>>>(comp, parent, best, n);
+    TT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(u32), c->stream));
+    c->launches += 1;
+    u32 done = 0;
+    for (int round = 0; round < 40 && done < n - 1; ++round) {
+        foreign_nearest(c, x, n, dim, kind, p, comp, best, err);
+        k_mst_hook<<<grid_for(n), 256, 0, c->stream>>>(comp, best, parent, n, deaths, cnt);
+        k_mst_flatten<<<grid_for(n), 256, 0, c->stream>>>(parent, comp, best, n);
+        TT_LAUNCH("mst round");
+        c->launches += 2;
+        u32 h = 0;
+        TT_CUDA(cudaMemcpyAsync(&h, cnt, 4, cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+        if (h == done) break;   // no progress: cannot happen on a connected complete graph
+        done = h;
+    }
+    check_device_error(c, err);
+    if (done != n - 1) throw Error(TT_ERR_INTERNAL, "gb300: Boruvka did not span the cloud");
+    u64* keys = c->arena.get<u64>(S_EDGE_KEYS, n);
+    k_float_keys<<<grid_for(n - 1), 256, 0, c->stream>>>(deaths, n - 1, keys);
+    radix_sort_inplace<u32>(c, keys, nullptr, n - 1);
+    k_keys_float<<<grid_for(n - 1), 256, 0, c->stream>>>(keys, n - 1, deaths);
+    TT_LAUNCH("mst sort");
+    c->launches += 2;
+    return n - 1;
+}
+
+}  // namespace tt

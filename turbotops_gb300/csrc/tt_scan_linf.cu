@@ -1,0 +1,10 @@
+// tt_scan_linf.cu — instantiates the all-pairs scanner (tt_scan.cuh) for
+// one metric kind; the four kinds compile in parallel.
+#define TT_SCAN_IMPL
+#include "tt_scan.cuh"
+
+namespace tt {
+namespace scan {
+TT_SCAN_INSTANTIATE(M_LINF)
+}  // namespace scan
+}  // namespace tt

@@ -91,3 +91,65 @@ def redzed_edges(ctx: Context, mat: torch.Tensor | None = None, csr: tuple | Non
                                     ptr(v), cap, C.byref(cnt)))
     m = cnt.value
     return d[:m], v[: 2 * m]
+
+
+def knn(ctx: Context, x: torch.Tensor, k: int, metric: str = "l2") -> tuple[torch.Tensor, torch.Tensor]:
+    """graph.hpp knn_lists_exact: (ids n x k, distances n x k), ascending (d, id)."""
+    x = _f32(x)
+    n, dim = x.shape
+    kind, p = capi.metric_parse(metric)
+    kk = min(k, n - 1) if n else 0
+    ids = torch.empty((n, max(kk, 1)), dtype=torch.int32, device=x.device)
+    d = torch.empty((n, max(kk, 1)), dtype=torch.float32, device=x.device)
+    ko = C.c_uint32()
+    ctx.check(ctx.L.tt_knn(ctx.h, ptr(x), n, dim, kind, p, k, ptr(ids), ptr(d), C.byref(ko)))
+    return ids[:, :kk], d[:, :kk]
+
+
+def _csr(ctx: Context, out, dev) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+    rp = _view(ctx, out.row_ptr_dev, out.n + 1, torch.int64, dev)
+    ci = _view(ctx, out.col_dev, out.nnz, torch.int32, dev)
+    w = _view(ctx, out.weight_dev, out.nnz, torch.float32, dev)
+    torch.cuda.current_stream(dev).synchronize()
+    return rp, ci, w
+
+
+def knn_graph(ctx: Context, x: torch.Tensor, k: int, metric: str = "l2") -> tuple:
+    """graph.hpp knn_lists_exact + knn_graph: CSR (row_ptr i64, col i32, weight f32)."""
+    x = _f32(x)
+    n, dim = x.shape
+    kind, p = capi.metric_parse(metric)
+    out = capi.CsrOut()
+    ctx.check(ctx.L.tt_knn_graph(ctx.h, ptr(x), n, dim, kind, p, k, C.byref(out)))
+    return _csr(ctx, out, x.device)
+
+
+def radius_graph(ctx: Context, x: torch.Tensor, tau: float, metric: str = "l2") -> tuple:
+    """graph.hpp radius_graph: CSR of all pairs with d <= tau."""
+    x = _f32(x)
+    n, dim = x.shape
+    kind, p = capi.metric_parse(metric)
+    out = capi.CsrOut()
+    ctx.check(ctx.L.tt_radius_graph(ctx.h, ptr(x), n, dim, kind, p, float(tau), C.byref(out)))
+    return _csr(ctx, out, x.device)
+
+
+def mst_deaths(ctx: Context, x: torch.Tensor, metric: str = "l2") -> torch.Tensor:
+    """Sorted minimum-spanning-tree weights of the complete graph (mst.hpp:25-99)."""
+    x = _f32(x)
+    n, dim = x.shape
+    kind, p = capi.metric_parse(metric)
+    d = torch.empty(max(n, 1), dtype=torch.float32, device=x.device)
+    ctx.check(ctx.L.tt_mst_deaths(ctx.h, ptr(x), n, dim, kind, p, ptr(d)))
+    return d[: max(n - 1, 0)]
+
+
+def h0_bars(deaths, threshold: float = math.inf):
+    """mst::h0's bars (mst.hpp:91-97) from sorted deaths: (birth, death) pairs."""
+    import numpy as np
+    d = deaths.detach().cpu().numpy() if hasattr(deaths, "detach") else np.asarray(deaths)
+    n = d.size + 1 if d.size or threshold is not None else 0
+    fin = d[(d <= threshold) & (d > 0)]
+    ess = 1 + int((d > threshold).sum())
+    bars = [np.stack([np.zeros_like(fin), fin], 1).ravel(), np.tile(np.array([0, np.inf], np.float32), ess)]
+    return np.concatenate(bars).astype(np.float32)
