@@ -335,6 +335,7 @@ def run_gpu(args, ws, rank, local):
 
 
 def main():
+    global N
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -344,7 +345,6 @@ def main():
     ap.add_argument("--n", type=int, default=N, help="points (smaller only for profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
-    global N
     N = args.n
     ws, rank, local = dist_env()
     if ws > 1:
