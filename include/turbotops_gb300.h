@@ -64,6 +64,22 @@ int tt_metric_parse(const char* s, int* kind, float* p);
 int tt_dense_distances(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p,
                        float* mat_dev, float* enclosing);
 
+/* No counterpart in the reference. tt_dense_distances for callers that
+ * cannot allocate device memory during the call (all device memory already
+ * handed to their own pool, or a loop that must not take the
+ * synchronisation cudaMalloc/cudaFree imply): no context, no cudaMalloc,
+ * cudaFree or allocating library call. The per-row maxima live in a fixed
+ * 1 MiB array in the library's device memory, so n <= 262144 (larger n
+ * returns TT_ERR_LENGTH before any work). Outputs: mat_dev (n x n) and
+ * radius_dev (one float, device memory), in stream order on `stream`
+ * (cudaStream_t; NULL = legacy default stream) of the current device.
+ * The first call on each device resolves the array's address (make it
+ * before any stream capture). All calls on a device share the array; calls
+ * that overlap on the GPU race and must be serialised by the caller.
+ * Errors: tt_last_error(NULL). */
+int tt_dense_distances_static(const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, float* mat_dev,
+                              float* radius_dev, void* stream);
+
 /* Result of tt_dim0: device arrays owned by the context. */
 typedef struct tt_dim0_out {
     uint64_t edges;                     /* kept edges (d <= threshold) */

@@ -48,6 +48,7 @@ _SIGS = {
     "tt_copy_async": (i32, [P, P, P, C.c_size_t]),
     "tt_metric_parse": (i32, [C.c_char_p, C.POINTER(i32), C.POINTER(f32)]),
     "tt_dense_distances": (i32, [P, P, u32, u32, i32, f32, P, C.POINTER(f32)]),
+    "tt_dense_distances_static": (i32, [P, u32, u32, i32, f32, P, P, P]),
     "tt_dim0": (i32, [P, P, P, P, P, u32, f32, u32, C.POINTER(Dim0Out)]),
     "tt_redzed_edges": (i32, [P, P, P, P, P, u32, f32, P, P, u64, C.POINTER(u64)]),
     "tt_knn": (i32, [P, P, u32, u32, i32, f32, u32, P, P, C.POINTER(u32)]),

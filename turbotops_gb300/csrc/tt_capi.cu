@@ -74,6 +74,11 @@ u64 knn_front_dev(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 
 
 }  // namespace
 
+namespace tt {
+// Error text for context-free entry points (read back by tt_last_error(NULL)).
+void set_thread_error(const std::string& msg) { g_error = msg; }
+}  // namespace tt
+
 extern "C" {
 
 const char* tt_version(void) { return "0.1.0"; }
