@@ -187,6 +187,44 @@ int tt_dense_front_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, in
                      uint64_t* essential, uint64_t* col_idx_h, float* col_d_h, uint64_t* col_cf_h,
                      uint8_t* col_cf_app_h, uint64_t col_cap, uint64_t* ncols, uint64_t* nedges);
 
+/* Reducer::assemble(1) (rips.hpp:981-1023) over the dense matrix mat_dev:
+ * the dimension-2 columns generated from the sorted kept edges
+ * (edge_keys_dev, m Ripser keys as tt_dim0 returns them), minus the
+ * dimension-1 pivots (pivots_dev, npiv triangle indices, any order) and the
+ * triangles in zero-apparent pairs, in descending filtration order.
+ * *columns receives the count; *col_index_dev / *col_diameter_dev point at
+ * context-owned arrays; *apparent receives the skipped-apparent count.
+ * Requires C(n, 3) < 2^33. */
+int tt_assemble(tt_ctx* ctx, const float* mat_dev, uint32_t n, float threshold, const uint64_t* edge_keys_dev,
+                uint64_t m, const uint64_t* pivots_dev, uint64_t npiv, uint64_t* columns,
+                const uint64_t** col_index_dev, const float** col_diameter_dev, uint64_t* apparent);
+
+/* A persistence diagram (rips.hpp Barcode :52-67) in discovery order plus the
+ * reference's telemetry (turbotops.hpp Stats :85-96). Host memory owned by
+ * the library: release with tt_barcode_free. */
+typedef struct tt_barcode {
+    uint32_t ndims;
+    uint64_t total;
+    uint64_t* count;     /* bars per dimension (ndims entries) */
+    float* birth;        /* all bars, dimension-major, discovery order */
+    float* death;        /* +inf for essential classes */
+    char method[32];     /* "dense", "sparse" or "mst" */
+    float threshold;     /* effective filtration cutoff */
+    uint64_t edges;
+    uint64_t columns[32], apparent[32], emergent[32];
+} tt_barcode;
+
+/* tops::persistence(points, n, dim, Options) (turbotops.hpp:211-303) with
+ * the front end on the GPU and compute_pairs on the host:
+ *   knn = 0, maxdim = 0          complete-graph MST H0 (mst::h0)
+ *   knn = 0, threshold = +inf    dense full Rips cut at the enclosing radius
+ *   knn = 0, threshold < inf     radius graph, sparse flag complex
+ *   knn = 1                      exact kNN graph (k neighbours), sparse flag complex
+ * GPU front end limits: maxdim <= 2 (dense) / <= 1 (graph input). */
+int tt_persistence_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t maxdim,
+                     float threshold, int knn, uint32_t k, tt_barcode** out);
+void tt_barcode_free(tt_barcode* b);
+
 #ifdef __cplusplus
 }
 #endif

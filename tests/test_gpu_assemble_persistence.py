@@ -1,0 +1,120 @@
+"""CUDA path vs the reference: dim-2 assemble (with the reference's own
+dimension-1 pivots) and whole diagrams through tt_persistence_h (GPU front
+end + host reduction), compared bar for bar in the CLI's canonical order."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from golden_io import GOLDEN, canonical, cases, ids, thr_of
+from gpu_util import bits, ctx, decode_keys, dev, host
+from oracle import oracle as O
+import turbotops_gb300 as tg
+from turbotops_gb300 import ops, synth
+
+pytestmark = pytest.mark.gpu
+
+ASM = cases("asm")
+BARS = cases("bars")
+
+
+def sha(*arrs):
+    h = hashlib.sha256()
+    for a in arrs:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()[:16]
+
+
+@pytest.mark.parametrize("c", ASM, ids=ids(ASM))
+def test_assemble_vs_reference(c):
+    mat, enc = ops.make_dense(ctx(), dev(c["x"]), c["metric"])
+    thr = thr_of(c["params"]["thr"])
+    thr = enc if np.isinf(thr) else thr
+    r = ops.dim0(ctx(), mat=mat, threshold=thr, maxdim=2)
+    piv = dev(c["piv"].view(np.int64))
+    ci, cd, napp = ops.assemble(ctx(), mat, thr, r["keys"], piv)
+    assert np.array_equal(host(ci).view(np.uint64), c["c2idx"])
+    assert np.array_equal(bits(host(cd)), bits(c["c2d"]))
+    assert napp == int(c["app2n"][0])
+
+
+@pytest.mark.parametrize("c", BARS, ids=ids(BARS))
+def test_persistence_vs_reference(c):
+    dgms, info = tg.persistence(c["x"], maxdim=c["params"]["maxdim"], metric=c["metric"])
+    got = tg.canonical(dgms)
+    ref = canonical(c["bars"])
+    assert got.shape == ref.shape
+    assert np.array_equal(bits(got), bits(ref))
+
+
+@pytest.mark.parametrize("name,metric", [("lattice3000_linf", "linf"), ("lattice3000_l1", "l1")])
+def test_lattice_config_front_end_checksums(name, metric):
+    """Full-size tie-heavy configuration: every front-end output of the
+    reference (sorted edges, apparent flags, columns, H0, dim-2 columns built
+    from the reference's pivots) reproduced bit for bit (checksums)."""
+    cfg = json.load(open(os.path.join(GOLDEN, "configs.json")))[name]
+    x = synth.lattice()
+    mat, enc = ops.make_dense(ctx(), dev(x), metric)
+    assert np.float32(enc) == np.float32(cfg["thr"])
+    r = ops.dim0(ctx(), mat=mat, threshold=enc, maxdim=2)
+    idx, d = decode_keys(r["keys"])
+    assert idx.size == cfg["edges"] and sha(idx, d) == cfg["edges_sha"]
+    assert sha(host(r["app"])) == cfg["app_sha"]
+    assert sha(host(r["cidx"]).view(np.uint64), host(r["cd"])) == cfg["cols_sha"]
+    piv = np.load(os.path.join(GOLDEN, f"cfg_{name}_piv.npz"))["piv"]
+    ci, cd, napp = ops.assemble(ctx(), mat, enc, r["keys"], dev(piv.view(np.int64)))
+    assert ci.numel() == cfg["c2"] and napp == cfg["app2"]
+    assert sha(host(ci).view(np.uint64), host(cd)) == cfg["c2_sha"]
+
+
+def test_torus_config_front_end_checksums():
+    cfg = json.load(open(os.path.join(GOLDEN, "configs.json")))["torus1000_l2"]
+    x = synth.torus()
+    mat, enc = ops.make_dense(ctx(), dev(x), "l2")
+    assert np.float32(enc) == np.float32(cfg["thr"])
+    r = ops.dim0(ctx(), mat=mat, threshold=enc, maxdim=2)
+    idx, d = decode_keys(r["keys"])
+    assert sha(idx, d) == cfg["edges_sha"] and sha(host(r["app"])) == cfg["app_sha"]
+    assert sha(host(r["cidx"]).view(np.uint64), host(r["cd"])) == cfg["cols_sha"]
+    piv = np.load(os.path.join(GOLDEN, "cfg_torus1000_piv.npz"))["piv"]
+    ci, cd, napp = ops.assemble(ctx(), mat, enc, r["keys"], dev(piv.view(np.int64)))
+    assert sha(host(ci).view(np.uint64), host(cd)) == cfg["c2_sha"] and napp == cfg["app2"]
+
+
+@pytest.mark.parametrize("metric,maxdim,graph,thr", [("l2", 1, "full", "inf"), ("l1", 2, "full", "inf"),
+                                                    ("l2", 1, "full", "0.3"), ("l2", 1, "knn", "inf"),
+                                                    ("linf", 0, "full", "inf"), ("l2", 0, "full", "0.2")])
+def test_persistence_paths_vs_oracle_h0_and_counts(metric, maxdim, graph, thr):
+    """Every dispatch path runs; H0 agrees with the oracle's dim0 / MST."""
+    x = synth.uniform(400, 3, 77)
+    t = thr_of(thr)
+    dgms, info = tg.persistence(x, maxdim=maxdim, metric=metric, graph=graph, threshold=t, k=8)
+    assert len(dgms) == maxdim + 1
+    if maxdim == 0 and graph == "full":
+        ref = O.mst_h0(x, metric, t)
+    elif graph == "full" and np.isinf(t):
+        m = O.dense(x, metric)
+        ref = O.dim0(mat=m, thr=O.enclosing_radius(m), maxdim=maxdim)["h0"]
+    elif graph == "full":
+        ref = O.dim0(csr=O.radius_graph(x, metric, t), n=400, thr=t, maxdim=maxdim)["h0"]
+    else:
+        ids_ = O.knn(x, metric, 8)
+        ref = O.dim0(csr=O.knn_graph(x, metric, ids_), n=400, maxdim=maxdim)["h0"]
+    assert np.array_equal(bits(dgms[0].ravel()), bits(ref))
+
+
+def test_persistence_validation_messages():
+    x = synth.uniform(10, 2, 1)
+    with pytest.raises(ValueError, match="threshold must be non-negative"):
+        tg.persistence(x, threshold=-1.0)
+    with pytest.raises(ValueError, match="k must be >= 1"):
+        tg.persistence(x, graph="knn", k=0)
+    with pytest.raises(ValueError, match="non-finite coordinate"):
+        y = x.copy()
+        y[3, 1] = np.nan
+        tg.persistence(y)
+    with pytest.raises(ValueError, match="unknown 'cosine'"):
+        tg.persistence(x, metric="cosine")

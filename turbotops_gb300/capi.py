@@ -34,6 +34,12 @@ class Dim0Out(C.Structure):
                 ("col_cofacet_app_dev", P), ("h0_finite", u64), ("h0_death_dev", P), ("essential", u64)]
 
 
+class Barcode(C.Structure):
+    _fields_ = [("ndims", u32), ("total", u64), ("count", C.POINTER(u64)), ("birth", C.POINTER(f32)),
+                ("death", C.POINTER(f32)), ("method", C.c_char * 32), ("threshold", f32), ("edges", u64),
+                ("columns", u64 * 32), ("apparent", u64 * 32), ("emergent", u64 * 32)]
+
+
 class KnnFrontOut(C.Structure):
     _fields_ = [("graph", CsrOut), ("dim0", Dim0Out)]
 
@@ -56,6 +62,10 @@ _SIGS = {
     "tt_radius_graph": (i32, [P, P, u32, u32, i32, f32, f32, C.POINTER(CsrOut)]),
     "tt_mst_deaths": (i32, [P, P, u32, u32, i32, f32, P]),
     "tt_knn_graph_h": (i32, [P, P, u32, u32, i32, f32, u32, P, P, P, u64, C.POINTER(u64)]),
+    "tt_assemble": (i32, [P, P, u32, f32, P, u64, P, u64, C.POINTER(u64), C.POINTER(P), C.POINTER(P),
+                          C.POINTER(u64)]),
+    "tt_persistence_h": (i32, [P, P, u32, u32, i32, f32, u32, f32, i32, u32, C.POINTER(C.POINTER(Barcode))]),
+    "tt_barcode_free": (None, [C.POINTER(Barcode)]),
     "tt_knn_front": (i32, [P, P, u32, u32, i32, f32, u32, u32, C.POINTER(KnnFrontOut)]),
     "tt_knn_front_h": (i32, [P, P, u32, u32, i32, f32, u32, u32, P, P, P, u64, C.POINTER(u64), P,
                              C.POINTER(u64), C.POINTER(u64), P, P, P, P, u64, C.POINTER(u64), C.POINTER(u64)]),

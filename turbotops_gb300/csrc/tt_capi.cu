@@ -215,6 +215,23 @@ int tt_redzed_edges(tt_ctx* c, const float* mat, const uint64_t* rp, const uint3
     });
 }
 
+int tt_assemble(tt_ctx* c, const float* mat, uint32_t n, float thr, const uint64_t* keys, uint64_t m,
+                const uint64_t* piv, uint64_t npiv, uint64_t* columns, const uint64_t** cidx, const float** cd,
+                uint64_t* apparent) {
+    return guard(c, [&] {
+        if (std::isnan(thr) || thr < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        if (!columns || !cidx || !cd) invalid("gb300: null output");
+        Complex cx{mat, nullptr, nullptr, nullptr, n, thr};
+        u64* ci = nullptr;
+        f32* d = nullptr;
+        u64 napp = 0;
+        *columns = assemble2(c, cx, keys, m, piv, npiv, &ci, &d, &napp);
+        *cidx = ci;
+        *cd = d;
+        if (apparent) *apparent = napp;
+    });
+}
+
 int tt_knn(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k, uint32_t* ids,
            float* dists, uint32_t* k_out) {
     return guard(c, [&] {

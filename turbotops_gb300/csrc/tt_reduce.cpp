@@ -1,0 +1,387 @@
+// tt_reduce.cpp — host cohomology reduction of the columns the GPU front end
+// leaves (rips.hpp Reducer::compute_pairs, :874-978: the reduction stays
+// sequential on the host by design).
+//
+// The algorithm is Ripser's (U. Bauer, J. Appl. Comput. Topol. 2021) as the
+// reference runs it: columns in descending filtration order (d desc, index
+// asc); each column's coboundary in a binary heap ordered by (d asc, index
+// desc) with mod-2 cancellation at the top; a pivot already owned by an
+// earlier column adds that column's stored reduction; a pivot with a
+// zero-apparent facet adds that facet's coboundary; otherwise the pivot pairs
+// the column (a bar if it is longer than zero). The emergent-pair shortcut
+// (:903-928) pairs a column with its first zero cofacet when no earlier
+// column owns it and it has no zero-apparent facet; for dimension 1 the GPU
+// supplies that cofacet and flag per column, and only the ownership lookup
+// runs here.
+#include "tt_reduce.h"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <stdexcept>
+#include <string>
+
+namespace tt {
+namespace host {
+
+namespace {
+
+constexpr uint64_t kNone = std::numeric_limits<uint64_t>::max();
+
+inline bool precedes(const Entry& a, const Entry& b) { return a.d < b.d || (a.d == b.d && a.idx > b.idx); }
+
+// C(v, k) for v <= n, k <= K, overflow-checked.
+struct Binom {
+    uint32_t n = 0, K = 0;
+    std::vector<uint64_t> t;   // t[k * (n + 1) + v]
+    Binom(uint32_t nn, uint32_t KK) : n(nn), K(KK), t(uint64_t(nn + 1) * (KK + 1), 0) {
+        for (uint32_t v = 0; v <= n; ++v) {
+            at(v, 0) = 1;
+            for (uint32_t k = 1; k <= std::min(v, K); ++k) {
+                uint64_t s;
+                if (__builtin_add_overflow(at(v - 1, k - 1), at(v - 1, k), &s))
+                    throw std::overflow_error("rips: simplex index overflow");
+                at(v, k) = s;
+            }
+        }
+    }
+    uint64_t& at(uint32_t v, uint32_t k) { return t[uint64_t(k) * (n + 1) + v]; }
+    uint64_t operator()(uint32_t v, uint32_t k) const { return k > K ? 0 : t[uint64_t(k) * (n + 1) + v]; }
+};
+
+struct Cx {
+    const HostComplex& c;
+    const Binom& B;
+
+    float dist(uint32_t i, uint32_t j) const {
+        if (i == j) return 0.0f;
+        if (c.mat) return c.mat[uint64_t(i) * c.n + j];
+        const uint32_t* b = c.ci + c.rp[i];
+        const uint32_t* e = c.ci + c.rp[i + 1];
+        const uint32_t* it = std::lower_bound(b, e, j);
+        return (it != e && *it == j) ? c.w[it - c.ci] : INFINITY;
+    }
+
+    // vertices of the simplex with nv vertices, descending (rips.hpp decode)
+    void decode(uint64_t idx, uint32_t nv, uint32_t* vd) const {
+        uint32_t top = c.n;
+        for (uint32_t i = 0; i < nv; ++i) {
+            const uint32_t k = nv - i;
+            uint32_t lo = k - 1, hi = top;
+            while (hi - lo > 1) {
+                const uint32_t mid = lo + (hi - lo) / 2;
+                if (B(mid, k) <= idx) lo = mid;
+                else hi = mid;
+            }
+            vd[i] = lo;
+            idx -= B(lo, k);
+            top = lo;
+        }
+    }
+
+    // Cofacets of vd (nv vertices, descending, diameter diam) with diameter
+    // <= cap, in descending index order: fn(Entry, w, t) -> continue?
+    template <typename F>
+    void cofacets(const uint32_t* vd, uint32_t nv, float diam, float cap, F&& fn) const {
+        uint64_t A[34], S[34];
+        A[0] = 0;
+        for (uint32_t i = 0; i < nv; ++i) A[i + 1] = A[i] + B(vd[i], nv + 1 - i);
+        S[nv] = 0;
+        for (uint32_t i = nv; i-- > 0;) S[i] = S[i + 1] + B(vd[i], nv - i);
+        if (c.mat) {
+            uint32_t t = 0;
+            for (int64_t wi = int64_t(c.n) - 1; wi >= 0; --wi) {
+                const uint32_t w = uint32_t(wi);
+                while (t < nv && vd[t] > w) ++t;
+                if (t < nv && vd[t] == w) continue;
+                float cd = diam;
+                bool ok = true;
+                for (uint32_t i = 0; i < nv; ++i) {
+                    const float dv = c.mat[uint64_t(vd[i]) * c.n + w];
+                    if (dv > cd) {
+                        cd = dv;
+                        if (cd > cap) { ok = false; break; }
+                    }
+                }
+                if (ok && !fn(Entry{A[t] + B(w, nv + 1 - t) + S[t], cd}, w, t)) return;
+            }
+            return;
+        }
+        // CSR: common neighbours walked down from the top of the sorted rows
+        uint64_t p[34], lo[34];
+        for (uint32_t i = 0; i < nv; ++i) {
+            lo[i] = c.rp[vd[i]];
+            p[i] = c.rp[vd[i] + 1];
+            if (p[i] == lo[i]) return;
+        }
+        for (;;) {
+            uint32_t x = c.ci[p[0] - 1];
+            bool agree = true;
+            for (uint32_t i = 1; i < nv && agree; ++i) {
+                while (c.ci[p[i] - 1] > x)
+                    if (--p[i] == lo[i]) return;
+                if (c.ci[p[i] - 1] < x) {
+                    x = c.ci[p[i] - 1];
+                    agree = false;
+                }
+            }
+            if (!agree) {
+                while (c.ci[p[0] - 1] > x)
+                    if (--p[0] == lo[0]) return;
+                continue;
+            }
+            uint32_t t = 0;
+            while (t < nv && vd[t] > x) ++t;
+            float cd = diam;
+            for (uint32_t i = 0; i < nv; ++i) cd = std::max(cd, c.w[p[i] - 1]);
+            if (cd <= cap && !fn(Entry{A[t] + B(x, nv + 1 - t) + S[t], cd}, x, t)) return;
+            if (--p[0] == lo[0]) return;
+        }
+    }
+
+    // first cofacet in descending order with diameter d (its vertices in cv)
+    uint64_t zero_cofacet(const uint32_t* vd, uint32_t nv, float d, uint32_t* cv) const {
+        uint64_t found = kNone;
+        cofacets(vd, nv, d, d, [&](const Entry& e, uint32_t w, uint32_t t) {
+            found = e.idx;
+            for (uint32_t i = 0; i < t; ++i) cv[i] = vd[i];
+            cv[t] = w;
+            for (uint32_t i = t; i < nv; ++i) cv[i + 1] = vd[i];
+            return false;
+        });
+        return found;
+    }
+
+    // first facet in ascending order with diameter d (its vertices in fv)
+    uint64_t zero_facet(const uint32_t* vd, uint32_t nv, float d, uint32_t* fv) const {
+        if (nv < 2) return kNone;
+        float dm[33][33];
+        for (uint32_t a = 0; a < nv; ++a)
+            for (uint32_t b = a + 1; b < nv; ++b) dm[a][b] = dist(vd[a], vd[b]);
+        for (uint32_t j = 0; j < nv; ++j) {
+            bool hit = false;
+            for (uint32_t a = 0; a < nv && !hit; ++a)
+                for (uint32_t b = a + 1; b < nv && !hit; ++b) hit = a != j && b != j && dm[a][b] == d;
+            if (hit) {
+                uint64_t idx = 0;
+                for (uint32_t i = 0, o = 0; i < nv; ++i)
+                    if (i != j) {
+                        fv[o] = vd[i];
+                        idx += B(vd[i], nv - 1 - o);
+                        ++o;
+                    }
+                return idx;
+            }
+        }
+        return kNone;
+    }
+
+    // zero_apparent_facet: the zero facet whose zero cofacet is s
+    Entry zero_apparent_facet(const Entry& s, uint32_t nv) const {
+        uint32_t vd[34], fv[34], cv[34];
+        decode(s.idx, nv, vd);
+        const uint64_t f = zero_facet(vd, nv, s.d, fv);
+        if (f == kNone) return Entry{kNone, 0};
+        return zero_cofacet(fv, nv - 1, s.d, cv) == s.idx ? Entry{f, s.d} : Entry{kNone, 0};
+    }
+};
+
+// Open-addressing map: simplex index -> column.
+struct PivotMap {
+    std::vector<uint64_t> k, v;
+    uint64_t mask = 0, count = 0;
+    explicit PivotMap(uint64_t cap) {
+        uint64_t c = 16;
+        while (c < 2 * cap + 2) c <<= 1;
+        k.assign(c, kNone);
+        v.assign(c, 0);
+        mask = c - 1;
+    }
+    static uint64_t h(uint64_t x) {
+        x ^= x >> 33;
+        x *= 0xff51afd7ed558ccdull;
+        x ^= x >> 33;
+        return x;
+    }
+    uint64_t find(uint64_t key) const {
+        for (uint64_t s = h(key) & mask;; s = (s + 1) & mask) {
+            if (k[s] == key) return v[s];
+            if (k[s] == kNone) return kNone;
+        }
+    }
+    void insert(uint64_t key, uint64_t val) {
+        if (2 * (count + 1) > k.size()) grow();
+        uint64_t s = h(key) & mask;
+        while (k[s] != kNone && k[s] != key) s = (s + 1) & mask;
+        if (k[s] == kNone) ++count;
+        k[s] = key;
+        v[s] = val;
+    }
+    void grow() {
+        std::vector<uint64_t> ok, ov;
+        ok.swap(k);
+        ov.swap(v);
+        k.assign(ok.size() * 2, kNone);
+        v.assign(ok.size() * 2, 0);
+        mask = k.size() - 1;
+        count = 0;
+        for (uint64_t i = 0; i < ok.size(); ++i)
+            if (ok[i] != kNone) insert(ok[i], ov[i]);
+    }
+};
+
+// Min-heap in filtration order with pairwise cancellation of equal indices.
+struct Heap {
+    std::vector<Entry> h;
+    static bool later(const Entry& a, const Entry& b) { return precedes(b, a); }
+    void clear() { h.clear(); }
+    void push(const Entry& e) {
+        h.push_back(e);
+        std::push_heap(h.begin(), h.end(), later);
+    }
+    void heapify(std::vector<Entry>& v) {
+        std::make_heap(v.begin(), v.end(), later);
+        h.swap(v);
+    }
+    Entry pop_pivot() {
+        Entry piv{kNone, 0};
+        while (!h.empty()) {
+            if (piv.idx == kNone) {
+                piv = h.front();
+                std::pop_heap(h.begin(), h.end(), later);
+                h.pop_back();
+            } else if (h.front().idx == piv.idx) {
+                std::pop_heap(h.begin(), h.end(), later);
+                h.pop_back();
+                piv.idx = kNone;
+            } else {
+                break;
+            }
+        }
+        return piv;
+    }
+    Entry get_pivot() {
+        const Entry p = pop_pivot();
+        if (p.idx != kNone) push(p);
+        return p;
+    }
+};
+
+}  // namespace
+
+Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const std::vector<Entry>& cols,
+                   const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
+                   ReduceStats& st) {
+    const Binom B(hc.n, maxdim + 2);
+    const Cx cx{hc, B};
+    const uint32_t nv = dim + 1;
+    Bars bars;
+    PivotMap pivots(cols.size() + 16);
+    std::vector<uint64_t> off{0};
+    std::vector<Entry> red, wr, buf;
+    Heap wc;
+    uint32_t vd[34];
+    auto push_coboundary = [&](const Entry& s) {
+        cx.decode(s.idx, nv, vd);
+        cx.cofacets(vd, nv, s.d, hc.thr, [&](const Entry& e, uint32_t, uint32_t) {
+            wc.push(e);
+            return true;
+        });
+    };
+    for (uint64_t c = 0; c < cols.size(); ++c) {
+        const Entry col = cols[c];
+        const float birth = col.d;
+        wc.clear();
+        wr.clear();
+        Entry pivot{kNone, 0};
+        bool emergent = false;
+        if (em_idx) {
+            // GPU-supplied first zero cofacet and its zero-apparent-facet flag
+            if (em_idx[c] != kNone && !em_app[c] && pivots.find(em_idx[c]) == kNone) {
+                pivot = Entry{em_idx[c], col.d};
+                emergent = true;
+            }
+            if (!emergent) {
+                buf.clear();
+                cx.decode(col.idx, nv, vd);
+                cx.cofacets(vd, nv, col.d, hc.thr, [&](const Entry& e, uint32_t, uint32_t) {
+                    buf.push_back(e);
+                    return true;
+                });
+            }
+        } else {
+            bool check = true;
+            buf.clear();
+            cx.decode(col.idx, nv, vd);
+            cx.cofacets(vd, nv, col.d, hc.thr, [&](const Entry& cf, uint32_t, uint32_t) {
+                if (check && cf.d == col.d) {
+                    if (pivots.find(cf.idx) == kNone && cx.zero_apparent_facet(cf, nv + 1).idx == kNone) {
+                        pivot = cf;
+                        emergent = true;
+                        return false;
+                    }
+                    check = false;
+                }
+                buf.push_back(cf);
+                return true;
+            });
+        }
+        if (emergent) {
+            ++st.emergent;
+        } else {
+            wc.heapify(buf);
+            pivot = wc.get_pivot();
+        }
+        bool fresh = emergent;
+        for (;;) {
+            if (pivot.idx == kNone) {
+                bars.birth.push_back(birth);
+                bars.death.push_back(INFINITY);
+                break;
+            }
+            if (fresh) {
+                pivots.insert(pivot.idx, c);
+                break;
+            }
+            const uint64_t j = pivots.find(pivot.idx);
+            if (j != kNone) {
+                wr.push_back(cols[j]);
+                push_coboundary(cols[j]);
+                for (uint64_t t = off[j]; t < off[j + 1]; ++t) {
+                    wr.push_back(red[t]);
+                    push_coboundary(red[t]);
+                }
+                pivot = wc.get_pivot();
+                continue;
+            }
+            const Entry fa = cx.zero_apparent_facet(pivot, nv + 1);
+            if (fa.idx != kNone) {
+                wr.push_back(fa);
+                push_coboundary(fa);
+                pivot = wc.get_pivot();
+                continue;
+            }
+            if (pivot.d > birth) {
+                bars.birth.push_back(birth);
+                bars.death.push_back(pivot.d);
+            }
+            pivots.insert(pivot.idx, c);
+            std::sort(wr.begin(), wr.end(), precedes);
+            for (size_t x = 0; x < wr.size();) {
+                if (x + 1 < wr.size() && wr[x].idx == wr[x + 1].idx) x += 2;
+                else red.push_back(wr[x++]);
+            }
+            break;
+        }
+        off.push_back(red.size());
+    }
+    st.columns = cols.size();
+    pivot_list.clear();
+    for (uint64_t s = 0; s < pivots.k.size(); ++s)
+        if (pivots.k[s] != kNone) pivot_list.push_back(pivots.k[s]);
+    std::sort(pivot_list.begin(), pivot_list.end());
+    return bars;
+}
+
+}  // namespace host
+}  // namespace tt

@@ -1,0 +1,46 @@
+// tt_reduce.h — the host reduction of the remaining columns (the part of the
+// reference that stays sequential on the CPU).
+#pragma once
+#include <stdint.h>
+
+#include <vector>
+
+namespace tt {
+namespace host {
+
+struct Entry {
+    uint64_t idx;
+    float d;
+};
+
+// The complex the reducer enumerates cofacets in: a dense full matrix or a
+// CSR graph (host copies), with the filtration threshold.
+struct HostComplex {
+    const float* mat = nullptr;   // n x n, or nullptr
+    const uint64_t* rp = nullptr;
+    const uint32_t* ci = nullptr;
+    const float* w = nullptr;
+    uint32_t n = 0;
+    float thr = 0;
+};
+
+struct Bars {
+    std::vector<float> birth, death;
+};
+
+struct ReduceStats {
+    uint64_t columns = 0, emergent = 0;
+};
+
+// compute_pairs(dim) of the cohomology reducer. `cols` are the dimension-dim
+// simplices to reduce, in descending filtration order. For dim == 1 the
+// column-local part of the emergent-pair test may be supplied precomputed
+// (em_idx / em_app per column, UINT64_MAX = no zero cofacet); otherwise the
+// reducer evaluates it. Returns the bars; `pivots` receives the index of every
+// pivot (dimension-(dim+1) simplex) found.
+Bars compute_pairs(const HostComplex& cx, uint32_t dim, uint32_t maxdim, const std::vector<Entry>& cols,
+                   const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivots,
+                   ReduceStats& st);
+
+}  // namespace host
+}  // namespace tt

@@ -153,3 +153,20 @@ def h0_bars(deaths, threshold: float = math.inf):
     ess = 1 + int((d > threshold).sum())
     bars = [np.stack([np.zeros_like(fin), fin], 1).ravel(), np.tile(np.array([0, np.inf], np.float32), ess)]
     return np.concatenate(bars).astype(np.float32)
+
+
+def assemble(ctx: Context, mat: torch.Tensor, threshold: float, edge_keys: torch.Tensor,
+             pivots: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor, int]:
+    """rips.hpp Reducer::assemble(1): dim-2 columns (index i64, diameter f32), descending; apparent count."""
+    n = mat.shape[0]
+    cnt, app = C.c_uint64(), C.c_uint64()
+    ci, cd = C.c_void_p(), C.c_void_p()
+    piv = pivots.contiguous()
+    ctx.check(ctx.L.tt_assemble(ctx.h, ptr(mat), n, float(threshold), ptr(edge_keys), edge_keys.numel(),
+                                ptr(piv) if piv.numel() else None, piv.numel(), C.byref(cnt), C.byref(ci),
+                                C.byref(cd), C.byref(app)))
+    c = cnt.value
+    idx = _view(ctx, ci.value or 0, c, torch.int64, mat.device)
+    d = _view(ctx, cd.value or 0, c, torch.float32, mat.device)
+    torch.cuda.current_stream(mat.device).synchronize()
+    return idx, d, app.value
