@@ -199,6 +199,34 @@ int tt_assemble(tt_ctx* ctx, const float* mat_dev, uint32_t n, float threshold, 
                 uint64_t m, const uint64_t* pivots_dev, uint64_t npiv, uint64_t* columns,
                 const uint64_t** col_index_dev, const float** col_diameter_dev, uint64_t* apparent);
 
+/* ---- Batched dense front end, replayed from a captured CUDA graph ----
+ * The front end the reference runs per full-Rips cloud (turbotops.hpp:230-259
+ * with RedZeD: make_dense, enclosing_radius, build_edges) for a whole batch of
+ * clouds of uneven size in one pass: a persistent work-queue kernel over every
+ * cloud's distance tiles, per-cloud enclosing radii, and one sort of all
+ * clouds' kept edges. Buffers are sized for the worst case at creation, so a
+ * run has no host round trip and (use_graph != 0) is one graph launch. */
+typedef struct tt_batch tt_batch;
+typedef struct tt_batch_out {
+    uint32_t clouds;
+    uint64_t total_points;
+    const float* radius_dev;          /* per cloud: enclosing radius (the threshold) */
+    const uint64_t* edge_offset_dev;  /* clouds + 1 offsets into diam/verts */
+    const float* diam_dev;            /* per cloud: kept edges, (d asc, comb asc) */
+    const int32_t* verts_dev;         /* (i, j) local vertex ids, i < j */
+    const float* mats_dev;            /* per cloud: n x n distances, back to back */
+    void* stream;                     /* the batch's own stream (cudaStream_t) */
+} tt_batch_out;
+/* sizes: points per cloud (host). Points go into tt_batch_points(b):
+ * clouds back to back, row-major (sum of sizes) x dim float32 on the device. */
+int tt_batch_create(tt_ctx* ctx, const uint32_t* sizes, uint32_t count, uint32_t dim, int kind, float p,
+                    int use_graph, tt_batch** out);
+float* tt_batch_points(tt_batch* b);
+/* Runs the batch on its stream; wait != 0 synchronises before returning. */
+int tt_batch_run(tt_batch* b, int wait);
+int tt_batch_result(tt_batch* b, tt_batch_out* out);
+void tt_batch_destroy(tt_batch* b);
+
 /* A persistence diagram (rips.hpp Barcode :52-67) in discovery order plus the
  * reference's telemetry (turbotops.hpp Stats :85-96). Host memory owned by
  * the library: release with tt_barcode_free. */

@@ -122,7 +122,7 @@ enum Slot : int {
     S_UF_PARENT, S_UF_BEST, S_UF_WORK, S_UF_WORK2,                // Borůvka
     S_MAT, S_PTS, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4,         // host-buffer entry points
     S_KNN_D, S_KNN_I, S_GRAPH_KEYS, S_GRAPH_TMP, S_PIV,           // kNN / graph / pivots
-    S_MISC0, S_MISC1, S_MISC2, S_MISC3, S_ROWMAX, S_GRAPH_RP, S_ASM0, S_ASM1, S_ASM2, S_ASM3, S_ASM4,
+    S_SCAN2, S_SCAN3, S_MISC0, S_MISC1, S_MISC2, S_MISC3, S_ROWMAX, S_GRAPH_RP, S_ASM0, S_ASM1, S_ASM2, S_ASM3, S_ASM4,
     S_NSLOTS
 };
 

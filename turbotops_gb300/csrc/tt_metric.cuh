@@ -27,7 +27,7 @@ __device__ __forceinline__ f32 hsum8(const f32 t[8]) {
 // from that sum; dim < 16 is one fma chain from 0. A generic accessor lets
 // the same code read points from global or shared memory.
 template <typename A, typename B>
-__device__ __forceinline__ f32 l2_acc(const A& a, const B& b, u32 dim) {
+__device__ __forceinline__ f32 l2_sq_acc(const A& a, const B& b, u32 dim) {
     u32 k = 0;
     f32 s = 0.0f;
     if (dim >= 16) {
@@ -53,7 +53,22 @@ __device__ __forceinline__ f32 l2_acc(const A& a, const B& b, u32 dim) {
         const f32 d = __fsub_rn(a(k), b(k));
         s = __fmaf_rn(d, d, s);
     }
-    return __fsqrt_rn(s);
+    return s;
+}
+
+// The reference's l2 is the IEEE square root of l2_sq_acc's sum.
+template <typename A, typename B>
+__device__ __forceinline__ f32 l2_acc(const A& a, const B& b, u32 dim) {
+    return __fsqrt_rn(l2_sq_acc(a, b, dim));
+}
+
+// Every s >= 0 with sqrt_rn(s) <= d satisfies s <= sq_bound(d): sqrt(s) must
+// lie below the next float above d, so s is below that float squared
+// (rounded up). Lets a scan reject most candidates before the square root.
+__device__ __forceinline__ f32 sq_bound(f32 d) {
+    if (!(d < INFINITY)) return INFINITY;
+    const f32 up = __uint_as_float(__float_as_uint(d) + 1u);
+    return __fmul_ru(up, up);
 }
 
 // kern::l1 (metric.hpp:144-159).

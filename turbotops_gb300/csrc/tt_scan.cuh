@@ -45,6 +45,7 @@ struct KnnOp {
     struct State {
         f32 d[K];
         u32 j[K];
+        f32 thr_s;   // sq_bound of the current K-th distance
     };
     __device__ __forceinline__ void init(State& s, u32) const {
 #pragma unroll
@@ -52,6 +53,14 @@ struct KnnOp {
             s.d[t] = INFINITY;
             s.j[t] = 0xffffffffu;
         }
+        s.thr_s = INFINITY;
+    }
+    // L2 fast path: the squared sum decides most candidates; only those that
+    // can still enter the list take the IEEE square root.
+    __device__ __forceinline__ void visit_sq(State& s, u32 i, u32 j, f32 sq, const u32*) const {
+        if (j == i || sq > s.thr_s) return;
+        visit(s, i, j, __fsqrt_rn(sq), nullptr);
+        s.thr_s = sq_bound(s.d[K - 1]);
     }
     __device__ __forceinline__ static bool lt(f32 d, u32 j, f32 e, u32 i) { return d < e || (d == e && j < i); }
     __device__ __forceinline__ void visit(State& s, u32 i, u32 j, f32 d, const u32*) const {
@@ -125,10 +134,17 @@ struct ForeignOp {
     struct State {
         u64 key;
         u32 c;
+        f32 thr_s;
     };
     __device__ __forceinline__ void init(State& s, u32 i) const {
         s.key = ~0ull;
         s.c = comp[i];
+        s.thr_s = INFINITY;
+    }
+    __device__ __forceinline__ void visit_sq(State& s, u32 i, u32 j, f32 sq, const u32* tcomp) const {
+        if (tcomp[0] == s.c || sq > s.thr_s) return;
+        visit(s, i, j, __fsqrt_rn(sq), tcomp);
+        s.thr_s = sq_bound(__uint_as_float(u32(s.key >> kIdxBits)));
     }
     __device__ __forceinline__ void visit(State& s, u32 i, u32 j, f32 d, const u32* tcomp) const {
         if (tcomp[0] == s.c) return;
@@ -145,6 +161,14 @@ template <typename Op>
 struct NeedsComp : std::false_type {};
 template <>
 struct NeedsComp<ForeignOp> : std::true_type {};
+
+// Visitors that accept the L2 squared sum (visit_sq) before the root.
+template <typename Op>
+struct TakesSq : std::false_type {};
+template <int K>
+struct TakesSq<KnnOp<K>> : std::true_type {};
+template <>
+struct TakesSq<ForeignOp> : std::true_type {};
 
 // --------------------------------------------------------------------------
 // The scanner (compiled only in the tt_scan_<kind>.cu translation units).
@@ -212,6 +236,24 @@ k_scan(const f32* __restrict__ x, u32 n, u32 dim_rt, f32 p, Op op, const u32* __
                 for (u32 r = 0; r < rows; ++r) {
                     const f32 d = metric_dist(KIND, p, Row{qg}, Row{tile + r * dim}, dim);
                     op.visit(st, i, j0 + r, d, kComp ? tc + r : nullptr);
+                }
+            } else if constexpr (KIND == M_L2 && TakesSq<Op>::value && QN % 4 == 0) {
+                // candidate row through 128-bit shared loads, squared sum
+                // first (sq_bound pre-test), root only for survivors
+#pragma unroll 2
+                for (u32 r = 0; r < rows; ++r) {
+                    f32 cr[QN];
+                    const float4* c4 = reinterpret_cast<const float4*>(tile + r * QN);
+#pragma unroll
+                    for (int v = 0; v < QN / 4; ++v) {
+                        const float4 t4 = c4[v];
+                        cr[4 * v] = t4.x;
+                        cr[4 * v + 1] = t4.y;
+                        cr[4 * v + 2] = t4.z;
+                        cr[4 * v + 3] = t4.w;
+                    }
+                    const f32 sq = l2_sq_acc(RegRow<QN>{q}, RegRow<QN>{cr}, QN);
+                    op.visit_sq(st, i, j0 + r, sq, kComp ? tc + r : nullptr);
                 }
             } else {
 #pragma unroll 2

@@ -206,21 +206,22 @@ void scan_exclusive(tt_ctx* c, const T* in, T* out, u64 n, T* total, int depth) 
         c->launches += 1;
         return;
     }
-    if (depth > 4) invalid("scan: input too large");
-    T* sums = c->arena.get<T>(S_SCAN + 0, 2 * tiles + 2) ;
-    // sums[0..tiles) tile totals, sums[tiles..2 tiles) their exclusive scan
-    // (a deeper level reuses a fresh stack slot through recursion on a copy)
+    if (depth > 2) invalid("scan: input too large");
+    // sums[0..tiles) tile totals, sums[tiles..2 tiles) their exclusive scan;
+    // each recursion level has its own scratch slot
+    T* sums = c->arena.get<T>(depth == 0 ? S_SCAN : depth == 1 ? S_SCAN2 : S_SCAN3, 2 * tiles + 2);
     k_tile_sums<T><<<u32(tiles), SCAN_THREADS, 0, c->stream>>>(in, n, sums);
     TT_LAUNCH("k_tile_sums");
     if (tiles <= SCAN_TILE) {
         k_tile_scan<T><<<1, SCAN_THREADS, 0, c->stream>>>(sums, tiles, nullptr, sums + tiles, nullptr);
         TT_LAUNCH("k_tile_scan");
+        c->launches += 1;
     } else {
-        invalid("scan: more than 33M tiles");
+        scan_exclusive<T>(c, sums, sums + tiles, tiles, nullptr, depth + 1);
     }
     k_tile_scan<T><<<u32(tiles), SCAN_THREADS, 0, c->stream>>>(in, n, sums + tiles, out, total);
     TT_LAUNCH("k_tile_scan");
-    c->launches += 3;
+    c->launches += 2;
 }
 
 template void scan_exclusive<u64>(tt_ctx*, const u64*, u64*, u64, u64*, int);
