@@ -170,3 +170,17 @@ def ptr(t) -> int | None:
 
 def fthr(t: float) -> float:
     return math.inf if t is None else float(t)
+
+
+class BatchOut(C.Structure):
+    _fields_ = [("clouds", u32), ("total_points", u64), ("radius_dev", P), ("edge_offset_dev", P),
+                ("diam_dev", P), ("verts_dev", P), ("mats_dev", P), ("stream", P)]
+
+
+_SIGS.update({
+    "tt_batch_create": (i32, [P, P, u32, u32, i32, f32, i32, C.POINTER(P)]),
+    "tt_batch_points": (P, [P]),
+    "tt_batch_run": (i32, [P, i32]),
+    "tt_batch_result": (i32, [P, C.POINTER(BatchOut)]),
+    "tt_batch_destroy": (None, [P]),
+})

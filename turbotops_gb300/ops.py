@@ -170,3 +170,56 @@ def assemble(ctx: Context, mat: torch.Tensor, threshold: float, edge_keys: torch
     d = _view(ctx, cd.value or 0, c, torch.float32, mat.device)
     torch.cuda.current_stream(mat.device).synchronize()
     return idx, d, app.value
+
+
+class DenseBatch:
+    """The dense front end of a batch of clouds (tt_batch_*): per-cloud
+    enclosing radius and RedZeD edge list from one captured CUDA graph."""
+
+    def __init__(self, ctx: Context, sizes, dim: int, metric: str = "l2", use_graph: bool = True):
+        import numpy as np
+        self.ctx = ctx
+        self.sizes = np.ascontiguousarray(sizes, np.uint32)
+        self.dim = dim
+        kind, p = capi.metric_parse(metric)
+        h = C.c_void_p()
+        ctx.check(ctx.L.tt_batch_create(ctx.h, self.sizes.ctypes.data, len(self.sizes), dim, kind, p,
+                                        1 if use_graph else 0, C.byref(h)))
+        self.h = h
+        self.total = int(self.sizes.sum())
+
+    def load(self, points: torch.Tensor) -> None:
+        """Copy the clouds (sum(sizes) x dim, back to back) into the batch's input buffer."""
+        pts = _f32(points)
+        dst = self.ctx.L.tt_batch_points(self.h)
+        self.ctx.check(self.ctx.L.tt_copy_async(self.ctx.h, C.c_void_p(dst), C.c_void_p(pts.data_ptr()),
+                                                self.total * self.dim * 4))
+        self.ctx.synchronize()
+
+    def run(self, wait: bool = True) -> None:
+        self.ctx.check(self.ctx.L.tt_batch_run(self.h, 1 if wait else 0))
+
+    def result(self) -> dict:
+        out = capi.BatchOut()
+        self.ctx.check(self.ctx.L.tt_batch_result(self.h, C.byref(out)))
+        dev = torch.device("cuda", self.ctx.device)
+        c = out.clouds
+        off = _view(self.ctx, out.edge_offset_dev, c + 1, torch.int64, dev)
+        torch.cuda.current_stream(dev).synchronize()
+        m = int(off[-1].item())
+        r = {"radius": _view(self.ctx, out.radius_dev, c, torch.float32, dev), "edge_offset": off,
+             "diam": _view(self.ctx, out.diam_dev, m, torch.float32, dev),
+             "verts": _view(self.ctx, out.verts_dev, 2 * m, torch.int32, dev)}
+        torch.cuda.current_stream(dev).synchronize()
+        return r
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.tt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
