@@ -310,6 +310,11 @@ def run_gpu(args, ws, rank, local):
                          f"20000-point sub-cloud), scaled to the whole front end",
                **{k: round(v, 4) for k, v in det.items()}}
 
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras["batch"] = batch_block(ctx, dev)
+        extras["topo"] = topo_block(dev)
+
     value = ws * 1000.0 / ms_step
     line = {
         "metric": METRIC, "value": value, "unit": "diagrams/s", "n_gpus": ws, "steps": args.steps,
@@ -328,10 +333,116 @@ def run_gpu(args, ws, rank, local):
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": int(launches),
+        "other_workloads": extras,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def batch_block(ctx, dev, reps: int = 5) -> dict:
+    """The batched form (512 circle / figure-eight clouds of 64..2048 points,
+    seed 4): one CUDA-graph replay of the batched dense front end vs the plain
+    per-cloud GPU path (tt_dense_distances + tt_redzed_edges per cloud)."""
+    import numpy as np
+    import torch
+
+    from turbotops_gb300 import capi, ops, synth
+    clouds = synth.circle_batch()
+    sizes = [c.shape[0] for c in clouds]
+    b = ops.DenseBatch(ctx, sizes, 3, "l2", use_graph=True)
+    b.load(torch.from_numpy(np.concatenate(clouds)).to(dev))
+    b.run()   # capture
+    out = capi.BatchOut()
+    ctx.check(ctx.L.tt_batch_result(b.h, C.byref(out)))
+    bs = torch.cuda.ExternalStream(out.stream, device=dev)
+    ms = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(bs)
+        b.run(wait=False)
+        e1.record(bs)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    batch_ms = statistics.mean(ms)
+    r = b.result()
+    edges = int(r["edge_offset"][-1].item())
+    b.close()
+    # plain per-cloud path
+    xs = [torch.from_numpy(c).to(dev) for c in clouds]
+    kind, p = capi.metric_parse("l2")
+    nmax = max(sizes)
+    mat = torch.empty(nmax * nmax, dtype=torch.float32, device=dev)
+    dd = torch.empty(nmax * (nmax - 1) // 2 + 1, dtype=torch.float32, device=dev)
+    vv = torch.empty(nmax * (nmax - 1) + 2, dtype=torch.int32, device=dev)
+    enc = C.c_float()
+    cnt = C.c_uint64()
+
+    def plain():
+        for x in xs:
+            n = x.shape[0]
+            ctx.check(ctx.L.tt_dense_distances(ctx.h, x.data_ptr(), n, 3, kind, p, mat.data_ptr(), C.byref(enc)))
+            ctx.check(ctx.L.tt_redzed_edges(ctx.h, mat.data_ptr(), None, None, None, n, enc.value, dd.data_ptr(),
+                                            vv.data_ptr(), dd.numel(), C.byref(cnt)))
+        torch.cuda.synchronize()
+
+    plain()
+    t0 = time.perf_counter()
+    plain()
+    plain_ms = (time.perf_counter() - t0) * 1e3
+    pairs = sum(n * (n - 1) // 2 for n in sizes)
+    return {"workload": "512 clouds (circle / figure-eight, 64..2048 points, R^3, seed 4), L2: distances, "
+                        "enclosing radii, RedZeD edge lists", "clouds": len(sizes), "points": int(sum(sizes)),
+            "pairs": pairs, "kept_edges": edges, "batched_graph_ms": batch_ms,
+            "batched_diagrams_per_s": len(sizes) * 1000.0 / batch_ms, "per_cloud_ms": plain_ms,
+            "per_cloud_diagrams_per_s": len(sizes) * 1000.0 / plain_ms,
+            "batched_over_per_cloud": plain_ms / batch_ms,
+            "hbm_bytes_written_matrices": 4 * sum(n * n for n in sizes)}
+
+
+def topo_block(dev, reps: int = 2, plain_clouds: int = 8) -> dict:
+    """The differentiable form: loss = sum over 64 noisy circles (512 points,
+    sigma 0.1, seed 5) of -sum(top-4 H1 persistence) + sum(H0 death^2);
+    a step = forward + hand-written adjoint backward. Batched: all clouds in
+    one call (host reductions on every core) vs the plain per-cloud path (one
+    cloud per call, one host thread), the latter timed on `plain_clouds`
+    clouds and scaled to 64."""
+    import numpy as np
+    import torch
+
+    from turbotops_gb300 import synth, topo
+    clouds = synth.circles()
+    sizes = [c.shape[0] for c in clouds]
+    x = torch.from_numpy(np.concatenate(clouds)).to(dev)
+
+    def batched_step():
+        xx = x.clone().requires_grad_(True)
+        topo.topo_loss(xx, sizes).backward()
+        torch.cuda.synchronize()
+        return xx.grad
+
+    batched_step()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        batched_step()
+    bt = (time.perf_counter() - t0) / reps
+
+    def plain_step(q):
+        xq = torch.from_numpy(clouds[q]).to(dev).requires_grad_(True)
+        topo.topo_loss(xq, [sizes[q]], threads=1).backward()
+        torch.cuda.synchronize()
+
+    plain_step(0)
+    t0 = time.perf_counter()
+    for q in range(plain_clouds):
+        plain_step(q)
+    pt = (time.perf_counter() - t0) / plain_clouds * len(clouds)
+    return {"workload": "topo loss fwd+bwd, 64 noisy circles x 512 points (R^3, sigma 0.1, seed 5), L2, maxdim 1",
+            "batched_s_per_step": bt, "batched_steps_per_s": 1.0 / bt,
+            "per_cloud_s_per_step": pt, "per_cloud_steps_per_s": 1.0 / pt,
+            "per_cloud_sample": f"{plain_clouds} of 64 clouds timed, scaled",
+            "host_threads": os.cpu_count(), "batched_over_per_cloud": pt / bt}
 
 
 def main():
@@ -344,6 +455,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=8000, help="kNN queries timed on the host")
     ap.add_argument("--n", type=int, default=N, help="points (smaller only for profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched / differentiable blocks")
     args = ap.parse_args()
     N = args.n
     ws, rank, local = dist_env()

@@ -227,6 +227,36 @@ int tt_batch_run(tt_batch* b, int wait);
 int tt_batch_result(tt_batch* b, tt_batch_out* out);
 void tt_batch_destroy(tt_batch* b);
 
+/* ---- Differentiable persistence (no counterpart in the reference) ----
+ * tt_topo_forward: for clouds stored back to back in x_dev (sizes[q] points
+ * each, dim coordinates), the dense full-Rips diagram up to H1 with each bar's
+ * critical edge(s), as global point ids (host arrays owned by the result;
+ * release with tt_topo_free). H0: finite bars only. H1: every bar; essential
+ * bars have death +inf and death edge (UINT32_MAX, UINT32_MAX). The front end
+ * runs on the GPU, the column reductions of all clouds on `threads` host
+ * threads (0 = all cores). */
+typedef struct tt_topo_out {
+    uint32_t clouds;
+    const uint64_t* h0_offset;      /* clouds + 1 */
+    const float* h0_death;
+    const uint32_t* h0_edge;        /* 2 per bar */
+    const uint64_t* h1_offset;      /* clouds + 1 */
+    const float* h1_birth;
+    const float* h1_death;
+    const uint32_t* h1_birth_edge;  /* 2 per bar */
+    const uint32_t* h1_death_edge;  /* 2 per bar */
+    void* opaque;
+} tt_topo_out;
+int tt_topo_forward(tt_ctx* ctx, const float* x_dev, const uint32_t* sizes, uint32_t count, uint32_t dim, int kind,
+                    float p, int threads, tt_topo_out** out);
+void tt_topo_free(tt_topo_out* out);
+/* The adjoint: grad_x_dev[u] += g_e * dd/dx_u, grad_x_dev[v] -= g_e * dd/dx_u
+ * for every edge e = (u, v) of edges_dev (2 per edge, point ids) with
+ * upstream gradient grad_d_dev[e], for the metric (kind, p). Accumulates
+ * (float atomics) into grad_x_dev, which the caller zeroes. */
+int tt_topo_adjoint(tt_ctx* ctx, const float* x_dev, uint32_t dim, int kind, float p, const uint32_t* edges_dev,
+                    const float* grad_d_dev, uint64_t m, float* grad_x_dev);
+
 /* A persistence diagram (rips.hpp Barcode :52-67) in discovery order plus the
  * reference's telemetry (turbotops.hpp Stats :85-96). Host memory owned by
  * the library: release with tt_barcode_free. */

@@ -184,3 +184,17 @@ _SIGS.update({
     "tt_batch_result": (i32, [P, C.POINTER(BatchOut)]),
     "tt_batch_destroy": (None, [P]),
 })
+
+
+class TopoOut(C.Structure):
+    _fields_ = [("clouds", u32), ("h0_offset", C.POINTER(u64)), ("h0_death", C.POINTER(f32)),
+                ("h0_edge", C.POINTER(u32)), ("h1_offset", C.POINTER(u64)), ("h1_birth", C.POINTER(f32)),
+                ("h1_death", C.POINTER(f32)), ("h1_birth_edge", C.POINTER(u32)), ("h1_death_edge", C.POINTER(u32)),
+                ("opaque", P)]
+
+
+_SIGS.update({
+    "tt_topo_forward": (i32, [P, P, P, u32, u32, i32, f32, i32, C.POINTER(C.POINTER(TopoOut))]),
+    "tt_topo_free": (None, [C.POINTER(TopoOut)]),
+    "tt_topo_adjoint": (i32, [P, P, u32, i32, f32, P, P, u64, P]),
+})

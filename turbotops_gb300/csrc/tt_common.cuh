@@ -120,7 +120,7 @@ enum Slot : int {
     S_SORT_A = 0, S_SORT_B, S_SORT_HIST, S_SORT_VA, S_SORT_VB,   // radix sort
     S_SCAN, S_FLAGS, S_EDGE_KEYS, S_EDGE_TMP, S_COUNT,            // edges / compaction
     S_UF_PARENT, S_UF_BEST, S_UF_WORK, S_UF_WORK2,                // Borůvka
-    S_MAT, S_PTS, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4,         // host-buffer entry points
+    S_MAT, S_PTS, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4, S_OUT5,         // host-buffer entry points
     S_KNN_D, S_KNN_I, S_GRAPH_KEYS, S_GRAPH_TMP, S_PIV,           // kNN / graph / pivots
     S_SCAN2, S_SCAN3, S_MISC0, S_MISC1, S_MISC2, S_MISC3, S_ROWMAX, S_GRAPH_RP, S_ASM0, S_ASM1, S_ASM2, S_ASM3, S_ASM4,
     S_NSLOTS

@@ -292,14 +292,17 @@ __global__ void k_flags_dim0(const u64* __restrict__ keys, const u8* __restrict_
 __global__ void k_emit_dim0(const u64* __restrict__ keys, const u8* __restrict__ tree, const u8* __restrict__ app,
                             const u32* __restrict__ emw, const u8* __restrict__ emf, u64 m, int want_cols,
                             const u64* __restrict__ oh, const u64* __restrict__ oc, const u64* __restrict__ tot,
-                            f32* __restrict__ h0, u64* __restrict__ cidx, f32* __restrict__ cd,
-                            u64* __restrict__ emi, u8* __restrict__ emf_out) {
+                            f32* __restrict__ h0, u64* __restrict__ h0_edge, u64* __restrict__ cidx,
+                            f32* __restrict__ cd, u64* __restrict__ emi, u8* __restrict__ emf_out) {
     const u64 ncols = tot[1];
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
         const u64 key = keys[e];
         const f32 d = key_d(key);
         const bool t = tree[e];
-        if (t && d > 0.0f) h0[oh[e]] = d;
+        if (t && d > 0.0f) {
+            h0[oh[e]] = d;
+            h0_edge[oh[e]] = key_idx(key);   // the bar's critical (death) edge
+        }
         if (want_cols && !t && !(app && app[e])) {
             const u64 o = ncols - 1 - oc[e];   // descending order (rips.hpp:867)
             const u64 idx = key_idx(key);
@@ -448,9 +451,11 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
     out.cd = c->arena.get<f32>(S_OUT2, h[1] + 1);
     out.emi = c->arena.get<u64>(S_OUT3, h[1] + 1);
     out.emf = c->arena.get<u8>(S_OUT4, h[1] + 1);
+    out.h0_edge = c->arena.get<u64>(S_OUT5, h[0] + 1);
     if (m) {
         k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, emw, emf, m, want_cols, oh, oc,
-                                                             tot, out.h0, out.cidx, out.cd, out.emi, out.emf);
+                                                             tot, out.h0, out.h0_edge, out.cidx, out.cd, out.emi,
+                                                             out.emf);
         TT_LAUNCH("k_emit_dim0");
         ++c->launches;
     }

@@ -66,6 +66,7 @@ struct Dim0Out {
     u8* emf = nullptr;    //   and whether that cofacet has a zero-apparent facet
     u64 nh0 = 0;          // finite H0 bars (d > 0), sorted edge order
     f32* h0 = nullptr;    // deaths (device)
+    u64* h0_edge = nullptr;   // each finite H0 bar's tree edge (edge index, device)
     u64 essential = 0;    // connected components
 };
 // Graph is either a dense full matrix (mat != nullptr) or a CSR.

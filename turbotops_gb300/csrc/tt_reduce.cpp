@@ -337,6 +337,8 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
             if (pivot.idx == kNone) {
                 bars.birth.push_back(birth);
                 bars.death.push_back(INFINITY);
+                bars.birth_idx.push_back(col.idx);
+                bars.death_idx.push_back(kNone);
                 break;
             }
             if (fresh) {
@@ -364,6 +366,8 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
             if (pivot.d > birth) {
                 bars.birth.push_back(birth);
                 bars.death.push_back(pivot.d);
+                bars.birth_idx.push_back(col.idx);
+                bars.death_idx.push_back(pivot.idx);
             }
             pivots.insert(pivot.idx, c);
             std::sort(wr.begin(), wr.end(), precedes);

@@ -26,6 +26,9 @@ struct HostComplex {
 
 struct Bars {
     std::vector<float> birth, death;
+    // critical simplices of each bar: the column's simplex (birth) and the
+    // pivot (death; UINT64_MAX for essential bars)
+    std::vector<uint64_t> birth_idx, death_idx;
 };
 
 struct ReduceStats {
