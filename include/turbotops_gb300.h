@@ -50,6 +50,13 @@ const char* tt_last_error(const tt_ctx* ctx);
 /* Kernels launched through the context since creation. */
 uint64_t tt_ctx_launches(const tt_ctx* ctx);
 int tt_ctx_synchronize(tt_ctx* ctx);
+/* Exact-kNN engine: 0 = automatic (the tcgen05 tensor-core Gram filter for
+ * L2 in R^32 with k <= 16 and n >= 1024, else the exhaustive scan),
+ * 1 = always the exhaustive scan, 2 = the filter wherever it applies.
+ * Every engine returns the same lists. */
+int tt_ctx_set_knn_mode(tt_ctx* ctx, int mode);
+/* Exact distance evaluations the last filtered kNN let through. */
+uint64_t tt_ctx_filter_evals(const tt_ctx* ctx);
 /* Stream-ordered copy of bytes between any two device or host addresses
  * (lets bindings move context-owned results into their own buffers). */
 int tt_copy_async(tt_ctx* ctx, void* dst, const void* src, size_t bytes);

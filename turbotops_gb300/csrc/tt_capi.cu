@@ -122,6 +122,15 @@ int tt_ctx_synchronize(tt_ctx* c) {
     return guard(c, [&] { TT_CUDA(cudaStreamSynchronize(c->stream)); });
 }
 
+int tt_ctx_set_knn_mode(tt_ctx* c, int mode) {
+    return guard(c, [&] {
+        if (mode < 0 || mode > 2) invalid("gb300: knn mode must be 0, 1 or 2");
+        c->knn_mode = mode;
+    });
+}
+
+uint64_t tt_ctx_filter_evals(const tt_ctx* c) { return c ? c->filter_evals : 0; }
+
 int tt_copy_async(tt_ctx* c, void* dst, const void* src, size_t bytes) {
     return guard(c, [&] {
         if (bytes) TT_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));

@@ -139,4 +139,6 @@ struct tt_ctx {
     int sms = tt::kSMs;
     double last_kernel_ms = 0.0;   // device time of the last stage (CUDA events)
     uint64_t launches = 0;          // kernels launched through this context
+    int knn_mode = 0;               // 0 auto, 1 exhaustive scan, 2 tensor-core filter where applicable
+    uint64_t filter_evals = 0;      // exact evaluations the last tensor-core kNN let through
 };

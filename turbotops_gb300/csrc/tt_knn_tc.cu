@@ -1,0 +1,361 @@
+// tt_knn_tc.cu — exact L2 k nearest neighbours in R^32 with a tensor-core
+// (tcgen05) Gram filter.
+//
+// Same result as the exhaustive scan (tt_scan.cuh KnnOp, which replaces
+// graph.hpp knn_lists_exact :211-225): the k smallest (distance, id) pairs
+// per query, every distance the reference's lane-ordered float32 l2
+// (metric.hpp:92-112). The Gram product only decides which candidates are
+// worth that exact evaluation:
+//
+//   s~(q, c) = |q|^2 + |c|^2 - 2 G~(q, c),   G~ = TF32 tensor-core Gram, FP32 sum
+//
+// TF32 keeps 10 mantissa bits of each operand, so |G~ - q.c| <= 2^-9 |q||c|
+// <= 2^-10 (|q|^2 + |c|^2); with the FP32 norms and the final fma the error of
+// s~ stays below 2^-8 (|q|^2 + |c|^2). A candidate is evaluated exactly when
+//
+//   s~ - 2^-7 (|q|^2 + |c|^2) <= T_q,   T_q = sq_bound(d_k) (1 + 2^-16)
+//
+// where d_k is the query's current k-th exact distance: every candidate
+// whose exact distance could enter the list passes (the 2^-16 covers the
+// lane-ordered sum's own rounding), so the filter never changes a result.
+//
+// Pipeline per CTA (128 threads = 4 warps, one query row per thread, 128
+// queries per block, persistent over query blocks):
+//   TMA (cp.async.bulk.tensor, 128-byte swizzle) loads the query tile once
+//   and candidate tiles of 128 points into two shared-memory stages;
+//   thread 0 issues tcgen05.mma.kind::tf32 (M = 128, N = 128, 4 x K = 8)
+//   into one of two TMEM accumulators and commits to an mbarrier; while
+//   the tensor core works on tile t + 1 the four warps read tile t's Gram
+//   rows (tcgen05.ld 32x32b.x32), run the filter and the exact path.
+// TMEM: 2 x 128 columns per CTA; shared memory is padded so that at most two
+// CTAs share an SM, so tcgen05.alloc never waits. Every mbarrier wait is
+// bounded (tt_tma.cuh); on a timeout the kernel records the error, stops,
+// and still frees its TMEM.
+#include <cuda.h>
+
+#include "tt_internal.cuh"
+#include "tt_metric.cuh"
+#include "tt_tma.cuh"
+
+namespace tt {
+
+namespace {
+
+constexpr int TC_DIM = 32;      // coordinates per point (one 128-byte swizzle row)
+constexpr int TC_M = 128;       // queries per block (TMEM lanes)
+constexpr int TC_N = 128;       // candidates per tile (accumulator columns)
+constexpr int TC_K = 16;        // register top-k capacity
+constexpr u32 TILE_BYTES = TC_M * TC_DIM * 4;   // 16 KiB (query and candidate tiles alike)
+constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
+
+struct Shared {
+    alignas(1024) unsigned char a[TILE_BYTES];
+    alignas(1024) unsigned char b[2][TILE_BYTES];
+    alignas(8) u64 bar_a;
+    alignas(8) u64 bar_b[2];
+    alignas(8) u64 bar_mma[2];
+    u32 tmem_base;
+    u32 block;
+    u32 stop;
+};
+
+// UMMA shared-memory descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes in 1024-byte groups of 8 (stride byte offset 1024), version 1.
+__device__ __forceinline__ u64 sw128_desc(u32 saddr) {
+    return u64((saddr >> 4) & 0x3fff) | (u64(1) << 16) | (u64(1024 >> 4) << 32) | (u64(1) << 46) |
+           (u64(2) << 61);
+}
+
+// Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, N, M.
+constexpr u32 kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (u32(TC_N >> 3) << 17) | (u32(TC_M >> 4) << 24);
+
+__device__ __forceinline__ void tma_tile(void* dst, const CUtensorMap* map, int row, u64* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_addr(dst)),
+        "l"(map), "r"(0), "r"(row), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_tile(u32 d_tmem, u32 a_saddr, u32 b_saddr) {
+#pragma unroll
+    for (int ks = 0; ks < TC_DIM / 8; ++ks) {   // K = 8 tf32 = 32 bytes per step
+        const u64 da = sw128_desc(a_saddr + 32 * ks);
+        const u64 db = sw128_desc(b_saddr + 32 * ks);
+        const u32 acc = ks > 0;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+            "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+            : "memory");
+    }
+}
+
+__device__ __forceinline__ void mma_commit(u64* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(u32 taddr, u32 (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+template <int DIM>
+struct RegVec {
+    const f32 (&q)[DIM];
+    __device__ __forceinline__ f32 operator()(u32 k) const { return q[k]; }
+};
+
+__global__ void k_norms(const f32* __restrict__ x, u32 n, f32* __restrict__ nq, f32* __restrict__ wc) {
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        f32 s = 0.0f;
+#pragma unroll
+        for (int k = 0; k < TC_DIM; ++k) s = fmaf(x[u64(i) * TC_DIM + k], x[u64(i) * TC_DIM + k], s);
+        nq[i] = s;
+        wc[i] = s * (1.0f - 1.0f / 128.0f);
+    }
+}
+
+__global__ void __launch_bounds__(128, 2)
+k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32 n, u32 k,
+         const f32* __restrict__ nq, const f32* __restrict__ wc, u32* __restrict__ ids, f32* __restrict__ dists,
+         u32* __restrict__ next_block, u32* __restrict__ err, unsigned long long* __restrict__ exact_count) {
+    extern __shared__ unsigned char smem_raw[];
+    Shared& S = *reinterpret_cast<Shared*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const u32 tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const u32 nblocks = (n + TC_M - 1) / TC_M;
+    const u32 ntiles = (n + TC_N - 1) / TC_N;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem_base)),
+                     "r"(2 * TC_N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(&S.bar_a, 1);
+        mbar_init(&S.bar_b[0], 1);
+        mbar_init(&S.bar_b[1], 1);
+        mbar_init(&S.bar_mma[0], 1);
+        mbar_init(&S.bar_mma[1], 1);
+        fence_mbar_init();
+        S.stop = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const u32 tmem = S.tmem_base;
+    u32 ph_a = 0, uses_b[2] = {0, 0}, uses_mma[2] = {0, 0};
+    unsigned long long exact_evals = 0;
+    bool failed = false;
+
+    for (;;) {
+        if (tid == 0) S.block = atomicAdd(next_block, 1u);
+        __syncthreads();
+        const u32 blk = S.block;
+        if (blk >= nblocks || failed) break;
+        const u32 q0 = blk * TC_M;
+        if (tid == 0) {
+            mbar_expect_tx(&S.bar_a, TILE_BYTES);
+            tma_tile(S.a, &map, int(q0), &S.bar_a);
+            for (u32 t = 0; t < 2 && t < ntiles; ++t) {
+                mbar_expect_tx(&S.bar_b[t], TILE_BYTES);
+                tma_tile(S.b[t], &map, int(t * TC_N), &S.bar_b[t]);
+            }
+        }
+        // this thread's query in registers; its list; its filter bound
+        const u32 i = q0 + warp * 32 + lane;
+        const bool active = i < n;
+        f32 q[TC_DIM];
+#pragma unroll
+        for (int c = 0; c < TC_DIM; ++c) q[c] = active ? x[u64(i) * TC_DIM + c] : 0.0f;
+        const f32 nqi = active ? nq[i] : 0.0f;
+        f32 ld[TC_K];
+        u32 lj[TC_K];
+#pragma unroll
+        for (int t = 0; t < TC_K; ++t) {
+            ld[t] = INFINITY;
+            lj[t] = 0xffffffffu;
+        }
+        f32 rq = INFINITY;   // pass iff fma(-2, G, wc) <= rq
+        if (tid == 0) {
+            mbar_wait(&S.bar_a, ph_a, err);
+            mbar_wait(&S.bar_b[0], uses_b[0] & 1, err);
+            tc_fence_after();
+            mma_tile(tmem, smem_addr(S.a), smem_addr(S.b[0]));
+            mma_commit(&S.bar_mma[0]);
+        }
+        ph_a ^= 1;
+        for (u32 t = 0; t < ntiles; ++t) {
+            const int sb = int(t & 1);
+            mbar_wait(&S.bar_mma[sb], uses_mma[sb] & 1, err);
+            tc_fence_after();
+            if (tid == 0 && t + 1 < ntiles) {   // tensor core works on t + 1 during this epilogue
+                const int nb = sb ^ 1;
+                // uses_b[nb] = phases of stage nb consumed so far = tile t+1's phase
+                mbar_wait(&S.bar_b[nb], uses_b[nb] & 1, err);
+                tc_fence_after();
+                mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[nb]));
+                mma_commit(&S.bar_mma[nb]);
+            }
+            // epilogue of tile t; every thread acquires the stage's TMA phase
+            // (already complete) before reading the tile through generic loads
+            mbar_wait(&S.bar_b[sb], uses_b[sb] & 1, err);
+            const u32 j0 = t * TC_N;
+            const unsigned char* bt = S.b[sb];
+#pragma unroll 1
+            for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+                u32 v[32];
+                tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
+                if (!active) continue;
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) {
+                    const u32 j = j0 + u32(chunk * 32 + jj);
+                    if (j >= n) break;
+                    if (!(fmaf(-2.0f, __uint_as_float(v[jj]), wc[j]) <= rq) || j == i) continue;
+                    // exact lane-ordered distance from the swizzled shared tile
+                    const u32 rr = u32(chunk * 32 + jj);
+                    f32 cv[TC_DIM];
+#pragma unroll
+                    for (int ch = 0; ch < 8; ++ch) {
+                        const float4 t4 = *reinterpret_cast<const float4*>(bt + rr * 128 + ((ch ^ (rr & 7)) << 4));
+                        cv[4 * ch] = t4.x;
+                        cv[4 * ch + 1] = t4.y;
+                        cv[4 * ch + 2] = t4.z;
+                        cv[4 * ch + 3] = t4.w;
+                    }
+                    ++exact_evals;
+                    const f32 d = __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cv}, TC_DIM));
+                    if (!(d < ld[TC_K - 1] || (d == ld[TC_K - 1] && j < lj[TC_K - 1]))) continue;
+                    bool placed = false;
+#pragma unroll
+                    for (int s = TC_K - 1; s >= 1; --s) {
+                        if (!placed) {
+                            if (d < ld[s - 1] || (d == ld[s - 1] && j < lj[s - 1])) {
+                                ld[s] = ld[s - 1];
+                                lj[s] = lj[s - 1];
+                            } else {
+                                ld[s] = d;
+                                lj[s] = j;
+                                placed = true;
+                            }
+                        }
+                    }
+                    if (!placed) {
+                        ld[0] = d;
+                        lj[0] = j;
+                    }
+                    // bound from the k-th entry (k <= TC_K); +inf until the list holds k
+                    f32 dk = INFINITY;
+#pragma unroll
+                    for (int s = 0; s < TC_K; ++s)
+                        if (s == int(k) - 1) dk = ld[s];
+                    const f32 tq = dk < INFINITY ? sq_bound(dk) * (1.0f + 1.0f / 65536.0f) : INFINITY;
+                    rq = tq - nqi * (1.0f - 1.0f / 128.0f);
+                }
+            }
+            ++uses_mma[sb];
+            tc_fence_before();
+            __syncthreads();   // TMEM buffer sb and shared stage sb are free again
+            ++uses_b[sb];
+            if (tid == 0) {
+                if (t + 2 < ntiles) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_expect_tx(&S.bar_b[sb], TILE_BYTES);
+                    tma_tile(S.b[sb], &map, int((t + 2) * TC_N), &S.bar_b[sb]);
+                }
+                S.stop = *((volatile u32*)err);   // one reader: the decision is block-uniform
+            }
+            __syncthreads();
+            if (S.stop) {
+                failed = true;
+                break;
+            }
+        }
+        if (active) {
+#pragma unroll
+            for (int s = 0; s < TC_K; ++s)
+                if (s < int(k)) {
+                    ids[u64(i) * k + s] = lj[s];
+                    if (dists) dists[u64(i) * k + s] = ld[s];
+                }
+        }
+        __syncthreads();
+    }
+    if (exact_count && exact_evals) atomicAdd(exact_count, exact_evals);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_N) : "memory");
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        TT_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (!p || q != cudaDriverEntryPointSuccess) throw Error(TT_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+}  // namespace
+
+bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x) {
+    return kind == M_L2 && dim == u32(TC_DIM) && k >= 1 && k <= u32(TC_K) && n >= 2 &&
+           (reinterpret_cast<uintptr_t>(x) & 15) == 0;
+}
+
+// Exact kNN lists through the tensor-core filter; returns the number of
+// exact distance evaluations the filter let through.
+u64 knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
+    f32* nq = c->arena.get<f32>(S_MISC0, 2 * u64(n) + 2);
+    f32* wc = nq + n + 1;
+    u32* ctl = c->arena.get<u32>(S_MISC1, 4);   // [0] next block, [1] error word
+    unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 1);
+    TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
+    TT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream));
+    k_norms<<<div_up(n, 256), 256, 0, c->stream>>>(x, n, nq, wc);
+    TT_LAUNCH("k_norms");
+    CUtensorMap map;
+    const cuuint64_t gdim[2] = {cuuint64_t(TC_DIM), cuuint64_t(n)};
+    const cuuint64_t gstride[1] = {cuuint64_t(TC_DIM) * 4};
+    const cuuint32_t box[2] = {cuuint32_t(TC_DIM), cuuint32_t(TC_M)};
+    const cuuint32_t estride[2] = {1, 1};
+    const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<f32*>(x), gdim, gstride, box,
+                                   estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(TT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
+    TT_CUDA(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)));
+    const u32 nblocks = div_up(n, TC_M);
+    const u32 grid = std::min<u32>(nblocks, 2 * u32(c->sms));
+    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, x, n, k, nq, wc, ids, dists, ctl, ctl + 1, cnt);
+    TT_LAUNCH("k_knn_tc");
+    c->launches += 2;
+    u32 e = 0;
+    unsigned long long evals = 0;
+    TT_CUDA(cudaMemcpyAsync(&e, ctl + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaMemcpyAsync(&evals, cnt, 8, cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaStreamSynchronize(c->stream));
+    if (e) throw Error(TT_ERR_TIMEOUT, "gb300: a bounded device wait timed out in the tensor-core kNN");
+    return evals;
+}
+
+}  // namespace tt
