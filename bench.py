@@ -290,6 +290,10 @@ def run_gpu(args, ws, rank, local):
         if r >= args.warmup:
             kms.append(e0.elapsed_time(e1))
     knn_ms = statistics.mean(kms)
+    evals = int(L.tt_ctx_filter_evals(ctx.h))
+    tc_path = evals > 0
+    kernel_name = ("k_knn_tc (tcgen05 TF32 Gram filter, exact lane-ordered recompute of the survivors)" if tc_path
+                   else "k_scan<L2, 32, KnnOp<16>> (exact kNN all-pairs scan)")
     pk, pk_src = peaks()
     gram_flops = 2.0 * N * N * DIM            # the Gram-equivalent contraction of one launch
     achieved = gram_flops / (knn_ms * 1e-3) / 1e12
@@ -327,7 +331,8 @@ def run_gpu(args, ws, rank, local):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": achieved / pk["bf16_tflops"], "traffic": traffic,
-                     "kernel": "k_scan<L2, 32, KnnOp<16>> (exact kNN all-pairs scan)",
+                     "kernel": kernel_name, "exact_evaluations": evals,
+                     "exact_fraction_of_pairs": evals / float(N) / float(N),
                      "kernel_ms": knn_ms, "peak_source": pk_src,
                      "fp32_exact_ops_per_s": fp32_ops / (knn_ms * 1e-3)},
         "cpu_baseline": cpu,

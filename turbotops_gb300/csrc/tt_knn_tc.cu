@@ -48,9 +48,15 @@ constexpr int TC_K = 16;        // register top-k capacity
 constexpr u32 TILE_BYTES = TC_M * TC_DIM * 4;   // 16 KiB (query and candidate tiles alike)
 constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
 
+constexpr u32 WC_BYTES = TC_N * 4;               // candidate norm terms per tile
+constexpr int QCAP = 32 * 32;                    // exact-path queue per warp and 32-column chunk
+
 struct Shared {
     alignas(1024) unsigned char a[TILE_BYTES];
     alignas(1024) unsigned char b[2][TILE_BYTES];
+    alignas(16) f32 wcs[2][TC_N];                // |c|^2 (1 - 2^-7) of the tile's candidates
+    alignas(16) u16 qcol[4][QCAP];               // queued (row << 7 | column) per warp
+    alignas(16) f32 qd[4][QCAP];                 // their exact distances
     alignas(8) u64 bar_a;
     alignas(8) u64 bar_b[2];
     alignas(8) u64 bar_mma[2];
@@ -58,6 +64,19 @@ struct Shared {
     u32 block;
     u32 stop;
 };
+
+// Row r (0..127) of a 128-byte-swizzled tile: 16-byte chunk c of the row sits
+// at chunk position c ^ (r & 7) (the TMA / UMMA 128-byte swizzle).
+__device__ __forceinline__ void swz_row(const unsigned char* tile, u32 r, f32 (&o)[TC_DIM]) {
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+        const float4 t4 = *reinterpret_cast<const float4*>(tile + r * 128 + ((ch ^ (r & 7)) << 4));
+        o[4 * ch] = t4.x;
+        o[4 * ch + 1] = t4.y;
+        o[4 * ch + 2] = t4.z;
+        o[4 * ch + 3] = t4.w;
+    }
+}
 
 // UMMA shared-memory descriptor: K-major operand, 128-byte swizzle, rows of
 // 128 bytes in 1024-byte groups of 8 (stride byte offset 1024), version 1.
@@ -159,6 +178,15 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
     u32 ph_a = 0, uses_b[2] = {0, 0}, uses_mma[2] = {0, 0};
     unsigned long long exact_evals = 0;
     bool failed = false;
+    u16* qcol = S.qcol[warp];
+    f32* qd = S.qd[warp];
+
+    // stage s <- candidate tile t: the points (TMA, swizzled) and their norm terms
+    auto load_stage = [&](int s, u32 t) {
+        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + WC_BYTES);
+        tma_tile(S.b[s], &map, int(t * TC_N), &S.bar_b[s]);
+        bulk_g2s(S.wcs[s], wc + u64(t) * TC_N, WC_BYTES, &S.bar_b[s]);
+    };
 
     for (;;) {
         if (tid == 0) S.block = atomicAdd(next_block, 1u);
@@ -169,17 +197,11 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         if (tid == 0) {
             mbar_expect_tx(&S.bar_a, TILE_BYTES);
             tma_tile(S.a, &map, int(q0), &S.bar_a);
-            for (u32 t = 0; t < 2 && t < ntiles; ++t) {
-                mbar_expect_tx(&S.bar_b[t], TILE_BYTES);
-                tma_tile(S.b[t], &map, int(t * TC_N), &S.bar_b[t]);
-            }
+            for (u32 t = 0; t < 2 && t < ntiles; ++t) load_stage(int(t), t);
         }
-        // this thread's query in registers; its list; its filter bound
-        const u32 i = q0 + warp * 32 + lane;
+        const u32 row = warp * 32 + lane;
+        const u32 i = q0 + row;
         const bool active = i < n;
-        f32 q[TC_DIM];
-#pragma unroll
-        for (int c = 0; c < TC_DIM; ++c) q[c] = active ? x[u64(i) * TC_DIM + c] : 0.0f;
         const f32 nqi = active ? nq[i] : 0.0f;
         f32 ld[TC_K];
         u32 lj[TC_K];
@@ -188,7 +210,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
             ld[t] = INFINITY;
             lj[t] = 0xffffffffu;
         }
-        f32 rq = INFINITY;   // pass iff fma(-2, G, wc) <= rq
+        f32 rq = INFINITY;   // candidate passes iff fma(-2, G, wc) <= rq
         if (tid == 0) {
             mbar_wait(&S.bar_a, ph_a, err);
             mbar_wait(&S.bar_b[0], uses_b[0] & 1, err);
@@ -196,47 +218,72 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
             mma_tile(tmem, smem_addr(S.a), smem_addr(S.b[0]));
             mma_commit(&S.bar_mma[0]);
         }
+        // every thread reads the query tile below: acquire its TMA phase
+        mbar_wait(&S.bar_a, ph_a, err);
         ph_a ^= 1;
         for (u32 t = 0; t < ntiles; ++t) {
             const int sb = int(t & 1);
             mbar_wait(&S.bar_mma[sb], uses_mma[sb] & 1, err);
             tc_fence_after();
-            if (tid == 0 && t + 1 < ntiles) {   // tensor core works on t + 1 during this epilogue
+            if (tid == 0 && t + 1 < ntiles) {   // the tensor core works on t + 1 during this epilogue
                 const int nb = sb ^ 1;
-                // uses_b[nb] = phases of stage nb consumed so far = tile t+1's phase
-                mbar_wait(&S.bar_b[nb], uses_b[nb] & 1, err);
+                mbar_wait(&S.bar_b[nb], uses_b[nb] & 1, err);   // tile t+1's phase
                 tc_fence_after();
                 mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[nb]));
                 mma_commit(&S.bar_mma[nb]);
             }
-            // epilogue of tile t; every thread acquires the stage's TMA phase
-            // (already complete) before reading the tile through generic loads
+            // every thread acquires the stage's (complete) TMA phase before
+            // reading the candidate tile and its norm terms
             mbar_wait(&S.bar_b[sb], uses_b[sb] & 1, err);
             const u32 j0 = t * TC_N;
             const unsigned char* bt = S.b[sb];
+            const f32* wcs = S.wcs[sb];
 #pragma unroll 1
             for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+                // (A) filter 32 candidates into a bit mask, branch-free
                 u32 v[32];
                 tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
-                if (!active) continue;
+                u32 m = 0;
 #pragma unroll
-                for (int jj = 0; jj < 32; ++jj) {
-                    const u32 j = j0 + u32(chunk * 32 + jj);
-                    if (j >= n) break;
-                    if (!(fmaf(-2.0f, __uint_as_float(v[jj]), wc[j]) <= rq) || j == i) continue;
-                    // exact lane-ordered distance from the swizzled shared tile
-                    const u32 rr = u32(chunk * 32 + jj);
-                    f32 cv[TC_DIM];
+                for (int g = 0; g < 8; ++g) {
+                    const float4 w4 = *reinterpret_cast<const float4*>(wcs + chunk * 32 + 4 * g);
+                    const f32 wv[4] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
-                    for (int ch = 0; ch < 8; ++ch) {
-                        const float4 t4 = *reinterpret_cast<const float4*>(bt + rr * 128 + ((ch ^ (rr & 7)) << 4));
-                        cv[4 * ch] = t4.x;
-                        cv[4 * ch + 1] = t4.y;
-                        cv[4 * ch + 2] = t4.z;
-                        cv[4 * ch + 3] = t4.w;
-                    }
-                    ++exact_evals;
-                    const f32 d = __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cv}, TC_DIM));
+                    for (int h = 0; h < 4; ++h)
+                        m |= u32(fmaf(-2.0f, __uint_as_float(v[4 * g + h]), wv[h]) <= rq) << (4 * g + h);
+                }
+                const u32 cbase = j0 + u32(chunk * 32);
+                if (!active) m = 0;
+                if (cbase + 32 > n) m &= cbase < n ? (1u << (n - cbase)) - 1u : 0u;
+                if (i >= cbase && i < cbase + 32) m &= ~(1u << (i - cbase));
+                if (!__any_sync(0xffffffffu, m != 0)) continue;
+                // (B) warp queue of (row, column) pairs, each thread's entries contiguous
+                const u32 cnt = __popc(m);
+                u32 off = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const u32 y = __shfl_up_sync(0xffffffffu, off, o);
+                    if (lane >= u32(o)) off += y;
+                }
+                const u32 total = __shfl_sync(0xffffffffu, off, 31);
+                off -= cnt;
+                for (u32 mm = m, e = off; mm; mm &= mm - 1, ++e)
+                    qcol[e] = u16((lane << 7) | u32(chunk * 32 + __ffs(mm) - 1));
+                __syncwarp();
+                // (C) all lanes: exact lane-ordered distances of the queue
+                for (u32 e = lane; e < total; e += 32) {
+                    const u32 qc = qcol[e];
+                    f32 qa[TC_DIM], cb[TC_DIM];
+                    swz_row(S.a, warp * 32 + (qc >> 7), qa);
+                    swz_row(bt, qc & 127u, cb);
+                    qd[e] = __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{qa}, RegVec<TC_DIM>{cb}, TC_DIM));
+                }
+                exact_evals += total;
+                __syncwarp();
+                // (D) each thread inserts its own results
+                for (u32 e = off; e < off + cnt; ++e) {
+                    const f32 d = qd[e];
+                    const u32 j = j0 + (qcol[e] & 127u);
                     if (!(d < ld[TC_K - 1] || (d == ld[TC_K - 1] && j < lj[TC_K - 1]))) continue;
                     bool placed = false;
 #pragma unroll
@@ -256,7 +303,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
                         ld[0] = d;
                         lj[0] = j;
                     }
-                    // bound from the k-th entry (k <= TC_K); +inf until the list holds k
+                }
+                if (cnt) {   // bound from the k-th entry; +inf until the list holds k
                     f32 dk = INFINITY;
 #pragma unroll
                     for (int s = 0; s < TC_K; ++s)
@@ -264,6 +312,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
                     const f32 tq = dk < INFINITY ? sq_bound(dk) * (1.0f + 1.0f / 65536.0f) : INFINITY;
                     rq = tq - nqi * (1.0f - 1.0f / 128.0f);
                 }
+                __syncwarp();
             }
             ++uses_mma[sb];
             tc_fence_before();
@@ -272,8 +321,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
             if (tid == 0) {
                 if (t + 2 < ntiles) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    mbar_expect_tx(&S.bar_b[sb], TILE_BYTES);
-                    tma_tile(S.b[sb], &map, int((t + 2) * TC_N), &S.bar_b[sb]);
+                    load_stage(sb, t + 2);
                 }
                 S.stop = *((volatile u32*)err);   // one reader: the decision is block-uniform
             }
@@ -293,7 +341,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         }
         __syncthreads();
     }
-    if (exact_count && exact_evals) atomicAdd(exact_count, exact_evals);
+    if (exact_count && exact_evals && lane == 0) atomicAdd(exact_count, exact_evals);
     tc_fence_before();
     __syncthreads();
     if (warp == 0)
@@ -326,8 +374,11 @@ bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x) {
 // Exact kNN lists through the tensor-core filter; returns the number of
 // exact distance evaluations the filter let through.
 u64 knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
-    f32* nq = c->arena.get<f32>(S_MISC0, 2 * u64(n) + 2);
-    f32* wc = nq + n + 1;
+    f32* nq = c->arena.get<f32>(S_MISC0, u64(n) + 1);
+    // the norm terms are bulk-copied 128 per tile: pad to whole tiles
+    const u64 wpad = (u64(n) + TC_N - 1) / TC_N * TC_N;
+    f32* wc = c->arena.get<f32>(S_MISC3, wpad);
+    TT_CUDA(cudaMemsetAsync(wc, 0, wpad * sizeof(f32), c->stream));
     u32* ctl = c->arena.get<u32>(S_MISC1, 4);   // [0] next block, [1] error word
     unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 1);
     TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
