@@ -458,7 +458,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-sample", type=int, default=8000, help="kNN queries timed on the host")
-    ap.add_argument("--n", type=int, default=N, help="points (smaller only for profiling runs)")
+    ap.add_argument("--points", "--n", dest="n", type=int, default=N,
+                    help="points (smaller only for profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / differentiable blocks")
     args = ap.parse_args()

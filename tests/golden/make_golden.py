@@ -161,3 +161,27 @@ if __name__ == "__main__":
     small()
     if a.configs:
         configs()
+
+
+def cli_cases() -> None:
+    """Exact-text diagrams of the reference CLI on small hand-checkable inputs."""
+    inputs = {"sq": "0 0\n1 0\n1 1\n0 1\n", "tri": "0 0\n1 0\n0 1\n"}
+    runs = [("sq", ["--maxdim", "1"]), ("sq", ["--maxdim", "1", "--metric", "l1"]),
+            ("sq", ["--maxdim", "1", "--metric", "linf"]), ("sq", ["--maxdim", "1", "--metric", "lp:3"]),
+            ("sq", ["--maxdim", "1", "--threshold", "1"]), ("tri", []),
+            ("sq", ["--graph", "knn", "-k", "2", "--maxdim", "1"]), ("sq", ["--maxdim", "2"])]
+    out = []
+    with tempfile.TemporaryDirectory() as td:
+        for name, text in inputs.items():
+            with open(os.path.join(td, name + ".txt"), "w") as f:
+                f.write(text)
+        for name, args in runs:
+            r = subprocess.run([CLI, "run", os.path.join(td, name + ".txt"), *args, "--quiet"], check=True,
+                               capture_output=True, text=True)
+            out.append({"input": inputs[name], "args": args, "stdout": r.stdout})
+    with open(os.path.join(HERE, "cli_cases.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__" and os.path.exists(CLI):
+    cli_cases()

@@ -1,0 +1,190 @@
+"""``python -m turbotops_gb300 run <input> [options]`` — the ``turbotops run`` CLI
+(src/turbotops.cpp:30-80, :784-935) on the GB300 front end.
+
+Same input formats (text: one point per line, commas/spaces/tabs/semicolons,
+'#' comments, UTF-8 BOM stripped; .bin: raw little-endian float32 with
+--dim), same options for this path, same output (one bar per line,
+'dim birth death' with %.9g, 'inf' for essential classes, canonical order),
+same failure convention ('turbotops: <message>' on stderr, exit code 2).
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+USAGE = """usage:
+  python -m turbotops_gb300 run <input> [options]   compute a persistence diagram
+  python -m turbotops_gb300 --version               print the version and exit
+
+input (run):
+  text   one point per line, coordinates separated by commas or spaces ('#' starts a comment)
+  .bin   raw little-endian float32, row-major; requires --dim
+
+options:
+  --maxdim D          highest homology dimension (default 1)
+  --threshold T       filtration cutoff, inclusive (default inf)
+  --metric M          l1 | l2 | linf | lp:<p>, p >= 1 (default l2)
+  --graph full|knn    complex: all pairs, or the kNN graph (default full)
+  -k N                neighbors for --graph knn (default 15)
+  --dim D             coordinates per point for .bin input
+  --mode M            boundary | coboundary | auto (diagrams never depend on it)
+  --coboundary, --boundary, --no-coboundary, --engine E   accepted, as --mode
+  --threads N         accepted (results never depend on it)
+  --output FILE       write the diagram to FILE instead of stdout
+  --quiet             no summary on stderr
+"""
+
+
+class CliError(Exception):
+    pass
+
+
+def _parse_f32(tok: str, what: str) -> float:
+    try:
+        v = float(tok)
+    except ValueError:
+        raise CliError(f"bad {what} '{tok}'") from None
+    return float(np.float32(v))
+
+
+def _parse_u32(tok: str, what: str) -> int:
+    if not tok.isdigit():
+        raise CliError(f"bad {what} '{tok}'")
+    v = int(tok)
+    if v > 0xFFFFFFFF:
+        raise CliError(f"bad {what} '{tok}' (out of range)")
+    return v
+
+
+def read_text_points(path: str) -> np.ndarray:
+    try:
+        raw = open(path, "rb").read()
+    except OSError:
+        raise CliError(f"cannot open {path}") from None
+    if raw.startswith(b"\xef\xbb\xbf"):
+        raw = raw[3:]
+    rows, dim = [], 0
+    for line in raw.decode("utf-8", "replace").splitlines():
+        line = line.split("#", 1)[0]
+        for ch in ",\t;":
+            line = line.replace(ch, " ")
+        toks = line.split()
+        if not toks:
+            continue
+        vals = [_parse_f32(t, "coordinate") for t in toks]
+        if not dim:
+            dim = len(vals)
+        elif len(vals) != dim:
+            raise CliError(f"{path}: inconsistent row length at point {len(rows)}")
+        rows.append(vals)
+    return np.asarray(rows, dtype=np.float32).reshape(len(rows), dim if rows else 0)
+
+
+def read_bin_points(path: str, dim: int) -> np.ndarray:
+    if not dim:
+        raise CliError("--dim is required for .bin input")
+    try:
+        raw = np.fromfile(path, dtype="<f4")
+    except OSError:
+        raise CliError(f"cannot open {path}") from None
+    if raw.size % dim:
+        raise CliError(f"{path}: size is not a multiple of 4 * dim")
+    return raw.reshape(-1, dim).astype(np.float32)
+
+
+def run(argv: list[str]) -> int:
+    from . import api
+    if not argv:
+        raise CliError("run: missing <input>\n" + USAGE)
+    path = argv[0]
+    o = {"maxdim": 1, "threshold": math.inf, "metric": "l2", "graph": "full", "k": 15, "dim": 0,
+         "output": None, "quiet": False}
+    it = iter(argv[1:])
+    for a in it:
+        def val():
+            try:
+                return next(it)
+            except StopIteration:
+                raise CliError(f"{a} needs a value") from None
+        if a == "--maxdim":
+            o["maxdim"] = _parse_u32(val(), "maxdim")
+        elif a == "--threshold":
+            v = val()
+            o["threshold"] = math.inf if v == "inf" else _parse_f32(v, "threshold")
+        elif a == "--metric":
+            o["metric"] = val()
+        elif a == "--graph":
+            g = val()
+            if g not in ("full", "knn"):
+                raise CliError("--graph must be full or knn")
+            o["graph"] = g
+        elif a == "-k":
+            o["k"] = _parse_u32(val(), "k")
+        elif a == "--dim":
+            o["dim"] = _parse_u32(val(), "dim")
+        elif a in ("--mode", "--engine"):
+            m = val()
+            ok = ("auto", "boundary", "coboundary") if a == "--mode" else ("auto", "reducer", "redzed")
+            if m not in ok:
+                raise CliError(("mode must be auto, boundary or coboundary" if a == "--mode"
+                                else "engine must be auto, reducer or redzed"))
+        elif a in ("--coboundary", "--boundary", "--no-coboundary", "--quiet"):
+            if a == "--quiet":
+                o["quiet"] = True
+        elif a == "--threads":
+            _parse_u32(val(), "threads")
+        elif a == "--output":
+            o["output"] = val()
+        elif a == "--edges" or a == "--approximate":
+            raise CliError(f"{a} is not offered by the GPU front end")
+        else:
+            raise CliError(f"unknown option '{a}'")
+    out_f = None
+    if o["output"]:
+        try:
+            out_f = open(o["output"], "w")
+        except OSError:
+            raise CliError(f"cannot open {o['output']} for writing") from None
+    x = read_bin_points(path, o["dim"]) if path.endswith(".bin") else read_text_points(path)
+    try:
+        dgms, info = api.persistence(x, maxdim=o["maxdim"], threshold=o["threshold"], metric=o["metric"],
+                                     graph=o["graph"], k=o["k"])
+    except (ValueError, OverflowError, MemoryError) as e:
+        raise CliError(str(e)) from None
+    text = api.format_diagram(dgms)
+    (out_f or sys.stdout).write(text)
+    if out_f:
+        out_f.close()
+    if not o["quiet"]:
+        n, d = x.shape if x.size else (0, 0)
+        sys.stderr.write(f"turbotops: {n} points in R^{d}, method {info['method']}, threshold {info['threshold']:.9g}, "
+                         f"{info['edges']} edges, {info['seconds_total']:.3f} s\n")
+        for dd, g in enumerate(dgms):
+            sys.stderr.write(f"  H{dd}: {len(g)} bars\n")
+    return 0
+
+
+def main(argv=None) -> int:
+    argv = sys.argv[1:] if argv is None else argv
+    try:
+        if not argv:
+            raise CliError("usage\n" + USAGE)
+        if argv[0] in ("--version", "version"):
+            print("turbotops 0.1.0 (gb300)")
+            return 0
+        if argv[0] in ("--help", "help", "-h"):
+            print(USAGE)
+            return 0
+        if argv[0] == "run":
+            return run(argv[1:])
+        raise CliError(f"unknown command '{argv[0]}'\n" + USAGE)
+    except CliError as e:
+        sys.stderr.write(f"turbotops: {e}\n")
+        return 2
+
+
+if __name__ == "__main__":
+    sys.exit(main())
