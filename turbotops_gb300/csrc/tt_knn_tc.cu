@@ -46,6 +46,7 @@ constexpr int TC_M = 128;       // queries per block (TMEM lanes)
 constexpr int TC_N = 128;       // candidates per tile (accumulator columns)
 constexpr int TC_K = 16;        // register top-k capacity
 constexpr u32 TILE_BYTES = TC_M * TC_DIM * 4;   // 16 KiB (query and candidate tiles alike)
+constexpr int NSTAGE = 2;                       // candidate tiles in flight (TMA ring)
 constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
 
 constexpr u32 WC_BYTES = TC_N * 4;               // candidate norm terms per tile
@@ -53,12 +54,12 @@ constexpr int QCAP = 32 * 32;                    // exact-path queue per warp an
 
 struct Shared {
     alignas(1024) unsigned char a[TILE_BYTES];
-    alignas(1024) unsigned char b[2][TILE_BYTES];
-    alignas(16) f32 wcs[2][TC_N];                // |c|^2 (1 - 2^-7) of the tile's candidates
+    alignas(1024) unsigned char b[NSTAGE][TILE_BYTES];
+    alignas(16) f32 wcs[NSTAGE][TC_N];                // |c|^2 (1 - 2^-7) of the tile's candidates
     alignas(16) u16 qcol[4][QCAP];               // queued (row << 7 | column) per warp
     alignas(16) f32 qd[4][QCAP];                 // their exact distances
     alignas(8) u64 bar_a;
-    alignas(8) u64 bar_b[2];
+    alignas(8) u64 bar_b[NSTAGE];
     alignas(8) u64 bar_mma[2];
     u32 tmem_base;
     u32 block;
@@ -136,8 +137,14 @@ struct RegVec {
     __device__ __forceinline__ f32 operator()(u32 k) const { return q[k]; }
 };
 
-__global__ void k_norms(const f32* __restrict__ x, u32 n, f32* __restrict__ nq, f32* __restrict__ wc) {
-    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+// |x_i|^2 and the filter's candidate term |x_i|^2 (1 - 2^-7); padding
+// candidates (i in [n, wpad)) get +inf so that they never pass the filter.
+__global__ void k_norms(const f32* __restrict__ x, u32 n, u32 wpad, f32* __restrict__ nq, f32* __restrict__ wc) {
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < wpad; i += gridDim.x * blockDim.x) {
+        if (i >= n) {
+            wc[i] = INFINITY;
+            continue;
+        }
         f32 s = 0.0f;
 #pragma unroll
         for (int k = 0; k < TC_DIM; ++k) s = fmaf(x[u64(i) * TC_DIM + k], x[u64(i) * TC_DIM + k], s);
@@ -164,8 +171,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
     }
     if (tid == 0) {
         mbar_init(&S.bar_a, 1);
-        mbar_init(&S.bar_b[0], 1);
-        mbar_init(&S.bar_b[1], 1);
+        for (int q = 0; q < NSTAGE; ++q) mbar_init(&S.bar_b[q], 1);
         mbar_init(&S.bar_mma[0], 1);
         mbar_init(&S.bar_mma[1], 1);
         fence_mbar_init();
@@ -175,7 +181,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
     __syncthreads();
     tc_fence_after();
     const u32 tmem = S.tmem_base;
-    u32 ph_a = 0, uses_b[2] = {0, 0}, uses_mma[2] = {0, 0};
+    u32 ph_a = 0, uses_b[NSTAGE] = {}, uses_mma[2] = {0, 0};
     unsigned long long exact_evals = 0;
     bool failed = false;
     u16* qcol = S.qcol[warp];
@@ -197,7 +203,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         if (tid == 0) {
             mbar_expect_tx(&S.bar_a, TILE_BYTES);
             tma_tile(S.a, &map, int(q0), &S.bar_a);
-            for (u32 t = 0; t < 2 && t < ntiles; ++t) load_stage(int(t), t);
+            for (u32 t = 0; t < u32(NSTAGE) && t < ntiles; ++t) load_stage(int(t), t);
         }
         const u32 row = warp * 32 + lane;
         const u32 i = q0 + row;
@@ -222,40 +228,60 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         mbar_wait(&S.bar_a, ph_a, err);
         ph_a ^= 1;
         for (u32 t = 0; t < ntiles; ++t) {
-            const int sb = int(t & 1);
+            const int sb = int(t & 1);            // accumulator buffer
+            const int st = int(t % NSTAGE);       // candidate stage
             mbar_wait(&S.bar_mma[sb], uses_mma[sb] & 1, err);
             tc_fence_after();
             if (tid == 0 && t + 1 < ntiles) {   // the tensor core works on t + 1 during this epilogue
-                const int nb = sb ^ 1;
-                mbar_wait(&S.bar_b[nb], uses_b[nb] & 1, err);   // tile t+1's phase
+                const int nb = sb ^ 1, ns = int((t + 1) % NSTAGE);
+                mbar_wait(&S.bar_b[ns], uses_b[ns] & 1, err);   // tile t+1's phase (issued NSTAGE-1 tiles ago)
                 tc_fence_after();
-                mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[nb]));
+                mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]));
                 mma_commit(&S.bar_mma[nb]);
             }
             // every thread acquires the stage's (complete) TMA phase before
             // reading the candidate tile and its norm terms
-            mbar_wait(&S.bar_b[sb], uses_b[sb] & 1, err);
+            mbar_wait(&S.bar_b[st], uses_b[st] & 1, err);
             const u32 j0 = t * TC_N;
-            const unsigned char* bt = S.b[sb];
-            const f32* wcs = S.wcs[sb];
+            const unsigned char* bt = S.b[st];
+            const f32* wcs = S.wcs[st];
 #pragma unroll 1
             for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
-                // (A) filter 32 candidates into a bit mask, branch-free
+                // (A) filter 32 candidates. Survivors are rare, so the common
+                // case is one min-tree (32 independent fmas, depth-5 fminf)
+                // per thread and a warp vote; the bit mask is built only by
+                // threads that hold a survivor. Padding candidates beyond n
+                // carry +inf norm terms and never pass.
                 u32 v[32];
                 tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
-                u32 m = 0;
+                f32 e[32];
 #pragma unroll
                 for (int g = 0; g < 8; ++g) {
                     const float4 w4 = *reinterpret_cast<const float4*>(wcs + chunk * 32 + 4 * g);
-                    const f32 wv[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-                    for (int h = 0; h < 4; ++h)
-                        m |= u32(fmaf(-2.0f, __uint_as_float(v[4 * g + h]), wv[h]) <= rq) << (4 * g + h);
+                    e[4 * g] = fmaf(-2.0f, __uint_as_float(v[4 * g]), w4.x);
+                    e[4 * g + 1] = fmaf(-2.0f, __uint_as_float(v[4 * g + 1]), w4.y);
+                    e[4 * g + 2] = fmaf(-2.0f, __uint_as_float(v[4 * g + 2]), w4.z);
+                    e[4 * g + 3] = fmaf(-2.0f, __uint_as_float(v[4 * g + 3]), w4.w);
                 }
-                const u32 cbase = j0 + u32(chunk * 32);
-                if (!active) m = 0;
-                if (cbase + 32 > n) m &= cbase < n ? (1u << (n - cbase)) - 1u : 0u;
-                if (i >= cbase && i < cbase + 32) m &= ~(1u << (i - cbase));
+                f32 lo[16];
+#pragma unroll
+                for (int h = 0; h < 16; ++h) lo[h] = fminf(e[h], e[h + 16]);
+#pragma unroll
+                for (int h = 0; h < 8; ++h) lo[h] = fminf(lo[h], lo[h + 8]);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) lo[h] = fminf(lo[h], lo[h + 4]);
+                const f32 emin = fminf(fminf(lo[0], lo[2]), fminf(lo[1], lo[3]));
+                const bool any = active && emin <= rq;
+                if (!__any_sync(0xffffffffu, any)) continue;
+                u32 m = 0;
+                if (any) {
+#pragma unroll
+                    for (int h = 0; h < 32; ++h) m |= u32(e[h] <= rq) << h;
+                    const u32 cbase = j0 + u32(chunk * 32);
+                    // +inf terms still pass while rq is +inf (list not full)
+                    if (cbase + 32 > n) m &= cbase < n ? (1u << (n - cbase)) - 1u : 0u;
+                    if (i >= cbase && i < cbase + 32) m &= ~(1u << (i - cbase));
+                }
                 if (!__any_sync(0xffffffffu, m != 0)) continue;
                 // (B) warp queue of (row, column) pairs, each thread's entries contiguous
                 const u32 cnt = __popc(m);
@@ -317,11 +343,11 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
             ++uses_mma[sb];
             tc_fence_before();
             __syncthreads();   // TMEM buffer sb and shared stage sb are free again
-            ++uses_b[sb];
+            ++uses_b[st];
             if (tid == 0) {
-                if (t + 2 < ntiles) {
+                if (t + NSTAGE < ntiles) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    load_stage(sb, t + 2);
+                    load_stage(st, t + NSTAGE);
                 }
                 S.stop = *((volatile u32*)err);   // one reader: the decision is block-uniform
             }
@@ -378,12 +404,11 @@ u64 knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     // the norm terms are bulk-copied 128 per tile: pad to whole tiles
     const u64 wpad = (u64(n) + TC_N - 1) / TC_N * TC_N;
     f32* wc = c->arena.get<f32>(S_MISC3, wpad);
-    TT_CUDA(cudaMemsetAsync(wc, 0, wpad * sizeof(f32), c->stream));
     u32* ctl = c->arena.get<u32>(S_MISC1, 4);   // [0] next block, [1] error word
     unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 1);
     TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
     TT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream));
-    k_norms<<<div_up(n, 256), 256, 0, c->stream>>>(x, n, nq, wc);
+    k_norms<<<div_up(wpad, 256), 256, 0, c->stream>>>(x, n, u32(wpad), nq, wc);
     TT_LAUNCH("k_norms");
     CUtensorMap map;
     const cuuint64_t gdim[2] = {cuuint64_t(TC_DIM), cuuint64_t(n)};
