@@ -50,14 +50,11 @@ constexpr int NSTAGE = 2;                       // candidate tiles in flight (TM
 constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
 
 constexpr u32 WC_BYTES = TC_N * 4;               // candidate norm terms per tile
-constexpr int QCAP = 32 * 32;                    // exact-path queue per warp and 32-column chunk
 
 struct Shared {
     alignas(1024) unsigned char a[TILE_BYTES];
     alignas(1024) unsigned char b[NSTAGE][TILE_BYTES];
     alignas(16) f32 wcs[NSTAGE][TC_N];                // |c|^2 (1 - 2^-7) of the tile's candidates
-    alignas(16) u16 qcol[4][QCAP];               // queued (row << 7 | column) per warp
-    alignas(16) f32 qd[4][QCAP];                 // their exact distances
     alignas(8) u64 bar_a;
     alignas(8) u64 bar_b[NSTAGE];
     alignas(8) u64 bar_mma[2];
@@ -184,8 +181,6 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
     u32 ph_a = 0, uses_b[NSTAGE] = {}, uses_mma[2] = {0, 0};
     unsigned long long exact_evals = 0;
     bool failed = false;
-    u16* qcol = S.qcol[warp];
-    f32* qd = S.qd[warp];
 
     // stage s <- candidate tile t: the points (TMA, swizzled) and their norm terms
     auto load_stage = [&](int s, u32 t) {
@@ -209,6 +204,9 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         const u32 i = q0 + row;
         const bool active = i < n;
         const f32 nqi = active ? nq[i] : 0.0f;
+        f32 q[TC_DIM];
+#pragma unroll
+        for (int c = 0; c < TC_DIM; ++c) q[c] = active ? x[u64(i) * TC_DIM + c] : 0.0f;
         f32 ld[TC_K];
         u32 lj[TC_K];
 #pragma unroll
@@ -245,13 +243,13 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
             const u32 j0 = t * TC_N;
             const unsigned char* bt = S.b[st];
             const f32* wcs = S.wcs[st];
-#pragma unroll 1
+            // (A) filter the tile's 128 candidates, 32 per TMEM load. Survivors
+            // are rare, so the common case is a min-tree (32 independent fmas,
+            // depth-5 fminf) per chunk; the bit mask is built only by threads
+            // holding a survivor. Padding candidates carry +inf terms.
+            u32 mk[TC_N / 32];
+#pragma unroll
             for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
-                // (A) filter 32 candidates. Survivors are rare, so the common
-                // case is one min-tree (32 independent fmas, depth-5 fminf)
-                // per thread and a warp vote; the bit mask is built only by
-                // threads that hold a survivor. Padding candidates beyond n
-                // carry +inf norm terms and never pass.
                 u32 v[32];
                 tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
                 f32 e[32];
@@ -271,66 +269,54 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
 #pragma unroll
                 for (int h = 0; h < 4; ++h) lo[h] = fminf(lo[h], lo[h + 4]);
                 const f32 emin = fminf(fminf(lo[0], lo[2]), fminf(lo[1], lo[3]));
-                const bool any = active && emin <= rq;
-                if (!__any_sync(0xffffffffu, any)) continue;
                 u32 m = 0;
-                if (any) {
+                if (active && emin <= rq) {
 #pragma unroll
                     for (int h = 0; h < 32; ++h) m |= u32(e[h] <= rq) << h;
                     const u32 cbase = j0 + u32(chunk * 32);
-                    // +inf terms still pass while rq is +inf (list not full)
+                    // +inf terms still pass while rq is +inf (list not yet full)
                     if (cbase + 32 > n) m &= cbase < n ? (1u << (n - cbase)) - 1u : 0u;
                     if (i >= cbase && i < cbase + 32) m &= ~(1u << (i - cbase));
                 }
-                if (!__any_sync(0xffffffffu, m != 0)) continue;
-                // (B) warp queue of (row, column) pairs, each thread's entries contiguous
-                const u32 cnt = __popc(m);
-                u32 off = cnt;
+                mk[chunk] = m;
+            }
+            // (B) survivors of the whole tile, by their owner: the query is in
+            // registers, the candidate row in the swizzled shared tile
+            if (__any_sync(0xffffffffu, (mk[0] | mk[1] | mk[2] | mk[3]) != 0)) {
+                bool changed = false;
+#pragma unroll 1
+                for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+#pragma unroll 1
+                    for (u32 mm = mk[chunk]; mm; mm &= mm - 1) {
+                        const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
+                        const u32 j = j0 + rr;
+                        f32 cb[TC_DIM];
+                        swz_row(bt, rr, cb);
+                        const f32 d = __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM));
+                        ++exact_evals;
+                        if (!(d < ld[TC_K - 1] || (d == ld[TC_K - 1] && j < lj[TC_K - 1]))) continue;
+                        bool placed = false;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const u32 y = __shfl_up_sync(0xffffffffu, off, o);
-                    if (lane >= u32(o)) off += y;
-                }
-                const u32 total = __shfl_sync(0xffffffffu, off, 31);
-                off -= cnt;
-                for (u32 mm = m, e = off; mm; mm &= mm - 1, ++e)
-                    qcol[e] = u16((lane << 7) | u32(chunk * 32 + __ffs(mm) - 1));
-                __syncwarp();
-                // (C) all lanes: exact lane-ordered distances of the queue
-                for (u32 e = lane; e < total; e += 32) {
-                    const u32 qc = qcol[e];
-                    f32 qa[TC_DIM], cb[TC_DIM];
-                    swz_row(S.a, warp * 32 + (qc >> 7), qa);
-                    swz_row(bt, qc & 127u, cb);
-                    qd[e] = __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{qa}, RegVec<TC_DIM>{cb}, TC_DIM));
-                }
-                exact_evals += total;
-                __syncwarp();
-                // (D) each thread inserts its own results
-                for (u32 e = off; e < off + cnt; ++e) {
-                    const f32 d = qd[e];
-                    const u32 j = j0 + (qcol[e] & 127u);
-                    if (!(d < ld[TC_K - 1] || (d == ld[TC_K - 1] && j < lj[TC_K - 1]))) continue;
-                    bool placed = false;
-#pragma unroll
-                    for (int s = TC_K - 1; s >= 1; --s) {
-                        if (!placed) {
-                            if (d < ld[s - 1] || (d == ld[s - 1] && j < lj[s - 1])) {
-                                ld[s] = ld[s - 1];
-                                lj[s] = lj[s - 1];
-                            } else {
-                                ld[s] = d;
-                                lj[s] = j;
-                                placed = true;
+                        for (int s = TC_K - 1; s >= 1; --s) {
+                            if (!placed) {
+                                if (d < ld[s - 1] || (d == ld[s - 1] && j < lj[s - 1])) {
+                                    ld[s] = ld[s - 1];
+                                    lj[s] = lj[s - 1];
+                                } else {
+                                    ld[s] = d;
+                                    lj[s] = j;
+                                    placed = true;
+                                }
                             }
                         }
-                    }
-                    if (!placed) {
-                        ld[0] = d;
-                        lj[0] = j;
+                        if (!placed) {
+                            ld[0] = d;
+                            lj[0] = j;
+                        }
+                        changed = true;
                     }
                 }
-                if (cnt) {   // bound from the k-th entry; +inf until the list holds k
+                if (changed) {   // bound from the k-th entry; +inf until the list holds k
                     f32 dk = INFINITY;
 #pragma unroll
                     for (int s = 0; s < TC_K; ++s)
@@ -338,7 +324,6 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
                     const f32 tq = dk < INFINITY ? sq_bound(dk) * (1.0f + 1.0f / 65536.0f) : INFINITY;
                     rq = tq - nqi * (1.0f - 1.0f / 128.0f);
                 }
-                __syncwarp();
             }
             ++uses_mma[sb];
             tc_fence_before();
@@ -367,7 +352,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         }
         __syncthreads();
     }
-    if (exact_count && exact_evals && lane == 0) atomicAdd(exact_count, exact_evals);
+    if (exact_count && exact_evals) atomicAdd(exact_count, exact_evals);
     tc_fence_before();
     __syncthreads();
     if (warp == 0)
