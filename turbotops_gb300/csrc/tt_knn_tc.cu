@@ -46,6 +46,7 @@ constexpr int TC_M = 128;       // queries per block (TMEM lanes)
 constexpr int TC_N = 128;       // candidates per tile (accumulator columns)
 constexpr int TC_K = 16;        // register top-k capacity
 constexpr u32 TILE_BYTES = TC_M * TC_DIM * 4;   // 16 KiB (query and candidate tiles alike)
+constexpr int TC_BUF = 16;                      // deferred survivors per thread
 constexpr int NSTAGE = 2;                       // candidate tiles in flight (TMA ring)
 constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
 
@@ -55,6 +56,7 @@ struct Shared {
     alignas(1024) unsigned char a[TILE_BYTES];
     alignas(1024) unsigned char b[NSTAGE][TILE_BYTES];
     alignas(16) f32 wcs[NSTAGE][TC_N];                // |c|^2 (1 - 2^-7) of the tile's candidates
+    u32 buf[16][128];                            // deferred survivors, entry-major (conflict-free)
     alignas(8) u64 bar_a;
     alignas(8) u64 bar_b[NSTAGE];
     alignas(8) u64 bar_mma[2];
@@ -215,6 +217,61 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
             lj[t] = 0xffffffffu;
         }
         f32 rq = INFINITY;   // candidate passes iff fma(-2, G, wc) <= rq
+        u32 nbuf = 0;        // deferred survivors of this thread (S.buf[.][tid])
+        // insert (d, j) into the sorted top-TC_K list; true if it entered
+        auto consider = [&](u32 j, f32 d) -> bool {
+            ++exact_evals;
+            if (!(d < ld[TC_K - 1] || (d == ld[TC_K - 1] && j < lj[TC_K - 1]))) return false;
+            bool placed = false;
+#pragma unroll
+            for (int s = TC_K - 1; s >= 1; --s) {
+                if (!placed) {
+                    if (d < ld[s - 1] || (d == ld[s - 1] && j < lj[s - 1])) {
+                        ld[s] = ld[s - 1];
+                        lj[s] = lj[s - 1];
+                    } else {
+                        ld[s] = d;
+                        lj[s] = j;
+                        placed = true;
+                    }
+                }
+            }
+            if (!placed) {
+                ld[0] = d;
+                lj[0] = j;
+            }
+            return true;
+        };
+        // filter bound from the k-th entry; +inf until the list holds k
+        auto update_rq = [&]() {
+            f32 dk = INFINITY;
+#pragma unroll
+            for (int s = 0; s < TC_K; ++s)
+                if (s == int(k) - 1) dk = ld[s];
+            const f32 tq = dk < INFINITY ? sq_bound(dk) * (1.0f + 1.0f / 65536.0f) : INFINITY;
+            rq = tq - nqi * (1.0f - 1.0f / 128.0f);
+        };
+        // evaluate the deferred survivors (coordinates from global memory / L2)
+        auto flush = [&]() {
+            bool changed = false;
+#pragma unroll 1
+            for (u32 e = 0; e < nbuf; ++e) {
+                const u32 j = S.buf[e][tid];
+                const float4* xr = reinterpret_cast<const float4*>(x + u64(j) * TC_DIM);
+                f32 cb[TC_DIM];
+#pragma unroll
+                for (int ch = 0; ch < 8; ++ch) {
+                    const float4 t4 = __ldg(xr + ch);
+                    cb[4 * ch] = t4.x;
+                    cb[4 * ch + 1] = t4.y;
+                    cb[4 * ch + 2] = t4.z;
+                    cb[4 * ch + 3] = t4.w;
+                }
+                changed |= consider(j, __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM)));
+            }
+            nbuf = 0;
+            if (changed) update_rq();
+        };
         if (tid == 0) {
             mbar_wait(&S.bar_a, ph_a, err);
             mbar_wait(&S.bar_b[0], uses_b[0] & 1, err);
@@ -280,49 +337,34 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
                 }
                 mk[chunk] = m;
             }
-            // (B) survivors of the whole tile, by their owner: the query is in
-            // registers, the candidate row in the swizzled shared tile
-            if (__any_sync(0xffffffffu, (mk[0] | mk[1] | mk[2] | mk[3]) != 0)) {
-                bool changed = false;
+            // (B) survivors. Few per tile, and at different lanes: they are
+            // deferred into a per-thread buffer and evaluated in lockstep when
+            // some lane's buffer would overflow (exact distance from the
+            // L2-resident coordinates, then insertion). A tile with more
+            // survivors than a buffer holds (the first tile of a block, while
+            // the lists fill) is evaluated directly from the shared tile.
+            const u32 tcnt = __popc(mk[0]) + __popc(mk[1]) + __popc(mk[2]) + __popc(mk[3]);
+            if (__any_sync(0xffffffffu, tcnt != 0)) {
+                if (__any_sync(0xffffffffu, tcnt > u32(TC_BUF))) {
+                    flush();
+                    bool changed = false;
 #pragma unroll 1
-                for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+                    for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
 #pragma unroll 1
-                    for (u32 mm = mk[chunk]; mm; mm &= mm - 1) {
-                        const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
-                        const u32 j = j0 + rr;
-                        f32 cb[TC_DIM];
-                        swz_row(bt, rr, cb);
-                        const f32 d = __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM));
-                        ++exact_evals;
-                        if (!(d < ld[TC_K - 1] || (d == ld[TC_K - 1] && j < lj[TC_K - 1]))) continue;
-                        bool placed = false;
-#pragma unroll
-                        for (int s = TC_K - 1; s >= 1; --s) {
-                            if (!placed) {
-                                if (d < ld[s - 1] || (d == ld[s - 1] && j < lj[s - 1])) {
-                                    ld[s] = ld[s - 1];
-                                    lj[s] = lj[s - 1];
-                                } else {
-                                    ld[s] = d;
-                                    lj[s] = j;
-                                    placed = true;
-                                }
-                            }
+                        for (u32 mm = mk[chunk]; mm; mm &= mm - 1) {
+                            const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
+                            f32 cb[TC_DIM];
+                            swz_row(bt, rr, cb);
+                            changed |= consider(j0 + rr, __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM)));
                         }
-                        if (!placed) {
-                            ld[0] = d;
-                            lj[0] = j;
-                        }
-                        changed = true;
                     }
-                }
-                if (changed) {   // bound from the k-th entry; +inf until the list holds k
-                    f32 dk = INFINITY;
-#pragma unroll
-                    for (int s = 0; s < TC_K; ++s)
-                        if (s == int(k) - 1) dk = ld[s];
-                    const f32 tq = dk < INFINITY ? sq_bound(dk) * (1.0f + 1.0f / 65536.0f) : INFINITY;
-                    rq = tq - nqi * (1.0f - 1.0f / 128.0f);
+                    if (changed) update_rq();
+                } else {
+                    if (__any_sync(0xffffffffu, nbuf + tcnt > u32(TC_BUF))) flush();
+#pragma unroll 1
+                    for (int chunk = 0; chunk < TC_N / 32; ++chunk)
+                        for (u32 mm = mk[chunk]; mm; mm &= mm - 1)
+                            S.buf[nbuf++][tid] = j0 + u32(chunk * 32 + __ffs(mm) - 1);
                 }
             }
             ++uses_mma[sb];
@@ -342,6 +384,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
                 break;
             }
         }
+        flush();
         if (active) {
 #pragma unroll
             for (int s = 0; s < TC_K; ++s)
