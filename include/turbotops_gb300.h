@@ -57,6 +57,9 @@ int tt_ctx_synchronize(tt_ctx* ctx);
 int tt_ctx_set_knn_mode(tt_ctx* ctx, int mode);
 /* Exact distance evaluations the last filtered kNN let through. */
 uint64_t tt_ctx_filter_evals(const tt_ctx* ctx);
+/* Candidate tiles (128 x 128 Gram blocks) the last filtered kNN computed;
+ * the exhaustive product is ceil(n / 128)^2. */
+uint64_t tt_ctx_filter_tiles(const tt_ctx* ctx);
 /* Stream-ordered copy of bytes between any two device or host addresses
  * (lets bindings move context-owned results into their own buffers). */
 int tt_copy_async(tt_ctx* ctx, void* dst, const void* src, size_t bytes);

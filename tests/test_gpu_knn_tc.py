@@ -57,3 +57,51 @@ def test_tensor_filter_full_config_checksum():
     i2, _, evals = _knn(synth.gmm(), 15, 0)   # automatic selection: the tensor path
     assert hashlib.sha256(np.ascontiguousarray(i2).tobytes()).hexdigest()[:16] == cfg["ids_sha"]
     assert evals > 0
+
+
+def _cases_tile_order():
+    rng = np.random.default_rng(7)
+    g = synth.gmm(30001, 32, seed=11)
+    out = {
+        # ragged last tile, shuffled rows (the regrouping must undo any input order)
+        "gmm_ragged_shuffled": (g[rng.permutation(len(g))], 15),
+        # every point repeated: k-th distances are 0 and ties are broken by id
+        "duplicates": (np.repeat(synth.gauss(1500, 32, 3), 20, axis=0), 15),
+        # integer lattice: massive distance ties across tiles
+        "lattice": (rng.integers(0, 3, (6000, 32)).astype(np.float32), 12),
+        # large common offset: the Gram-form margins dominate
+        "offset": (synth.gmm(8000, 32, seed=5) + np.float32(1000.0), 15),
+        # tiny coordinates: subnormal squares
+        "tiny": (synth.gauss(5000, 32, 9) * np.float32(1e-21), 7),
+        # well separated clusters, k = 1
+        "far_clusters": (synth.gmm(12000, 32, centres=4, seed=2) * np.float32(50.0), 1),
+    }
+    return out
+
+
+TILE_CASES = _cases_tile_order()
+
+
+@pytest.mark.parametrize("name", sorted(TILE_CASES))
+def test_tile_order_equals_exhaustive_scan(name):
+    x, k = TILE_CASES[name]
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    i1, d1, _ = _knn(x, k, 1)
+    i2, d2, _ = _knn(x, k, 2)
+    assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
+    assert np.array_equal(i1, i2)
+
+
+def test_tile_order_prunes_and_matches_at_scale():
+    """400,003 points: the pivot count reaches its cap and the last tile is
+    ragged; the lists equal the exhaustive scan's and most Gram tiles are
+    never computed."""
+    x = synth.gmm(400003, 32, seed=21)
+    i1, d1, _ = _knn(x, 10, 1)
+    c = ctx()
+    i2, d2, _ = _knn(x, 10, 2)
+    tiles = int(c.L.tt_ctx_filter_tiles(c.h))
+    nt = (len(x) + 127) // 128
+    assert np.array_equal(i1, i2)
+    assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
+    assert 0 < tiles < 0.5 * nt * nt, (tiles, nt * nt)

@@ -21,7 +21,8 @@ dist.init_process_group("gloo")
 ws, rank, _ = bench.dist_env()
 bench.barrier(ws)
 v = bench.max_over_ranks(float(rank + 1) * 10.0, ws)
-print("RESULT", rank, ws, v, flush=True)
+with open(os.path.join({out!r}, "rank%d.txt" % rank), "w") as f:   # one file per rank: no interleaving
+    f.write("RESULT %d %d %r\n" % (rank, ws, v))
 dist.destroy_process_group()
 """
 
@@ -35,10 +36,10 @@ def _torchrun(args, timeout=600):
 
 def test_max_over_ranks_and_barrier_gloo(tmp_path):
     w = tmp_path / "worker.py"
-    w.write_text(WORKER.format(root=ROOT))
+    w.write_text(WORKER.format(root=ROOT, out=str(tmp_path)))
     r = _torchrun([str(w)])
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = [ln.split() for ln in r.stdout.splitlines() if ln.startswith("RESULT")]
+    lines = [(tmp_path / f"rank{q}.txt").read_text().split() for q in range(2)]
     assert len(lines) == 2
     assert all(float(ln[3]) == 20.0 and ln[2] == "2" for ln in lines)
 

@@ -130,6 +130,7 @@ int tt_ctx_set_knn_mode(tt_ctx* c, int mode) {
 }
 
 uint64_t tt_ctx_filter_evals(const tt_ctx* c) { return c ? c->filter_evals : 0; }
+uint64_t tt_ctx_filter_tiles(const tt_ctx* c) { return c ? c->filter_tiles : 0; }
 
 int tt_copy_async(tt_ctx* c, void* dst, const void* src, size_t bytes) {
     return guard(c, [&] {

@@ -124,6 +124,7 @@ enum Slot : int {
     S_MAT, S_PTS, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4, S_OUT5,         // host-buffer entry points
     S_KNN_D, S_KNN_I, S_GRAPH_KEYS, S_GRAPH_TMP, S_PIV,           // kNN / graph / pivots
     S_SCAN2, S_SCAN3, S_MISC0, S_MISC1, S_MISC2, S_MISC3, S_ROWMAX, S_GRAPH_RP, S_ASM0, S_ASM1, S_ASM2, S_ASM3, S_ASM4,
+    S_TC_X, S_TC_PERM, S_TC_STATS, S_TC_KEYS, S_TC_VALS, S_TC_PIV,   // tensor-core kNN (tile order)
     S_NSLOTS
 };
 
@@ -142,4 +143,5 @@ struct tt_ctx {
     uint64_t launches = 0;          // kernels launched through this context
     int knn_mode = 0;               // 0 auto, 1 exhaustive scan, 2 tensor-core filter where applicable
     uint64_t filter_evals = 0;      // exact evaluations the last tensor-core kNN let through
+    uint64_t filter_tiles = 0;      // 128 x 128 Gram tiles the last tensor-core kNN computed
 };

@@ -85,14 +85,14 @@ inline u32 grid_for(u64 work, u32 per_block) {
 }  // namespace
 
 bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x);
-u64 knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists);
+void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists);
 
 void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists) {
     if (k == 0 || n < 2) return;
     // L2 in R^32: the tensor-core Gram filter (tt_knn_tc.cu) unless the
     // context asks for the exhaustive scan; both give the same lists
     if (c->knn_mode != 1 && knn_tc_applicable(n, dim, kind, k, x) && (c->knn_mode == 2 || n >= 1024)) {
-        c->filter_evals = knn_tc(c, x, n, k, ids, dists);
+        knn_tc(c, x, n, k, ids, dists);
         return;
     }
     u32* err = error_word(c);

@@ -1,37 +1,48 @@
 // tt_knn_tc.cu — exact L2 k nearest neighbours in R^32 with a tensor-core
-// (tcgen05) Gram filter.
+// (tcgen05) Gram filter and a bounding-ball tile order.
 //
 // Same result as the exhaustive scan (tt_scan.cuh KnnOp, which replaces
 // graph.hpp knn_lists_exact :211-225): the k smallest (distance, id) pairs
 // per query, every distance the reference's lane-ordered float32 l2
-// (metric.hpp:92-112). The Gram product only decides which candidates are
-// worth that exact evaluation:
+// (metric.hpp:92-112), ties broken by the smaller original id. Two exact
+// tests decide which candidates are worth that evaluation; neither can
+// change a list.
 //
-//   s~(q, c) = |q|^2 + |c|^2 - 2 G~(q, c),   G~ = TF32 tensor-core Gram, FP32 sum
-//
-// TF32 keeps 10 mantissa bits of each operand, so |G~ - q.c| <= 2^-9 |q||c|
-// <= 2^-10 (|q|^2 + |c|^2); with the FP32 norms and the final fma the error of
-// s~ stays below 2^-8 (|q|^2 + |c|^2). A candidate is evaluated exactly when
-//
-//   s~ - 2^-7 (|q|^2 + |c|^2) <= T_q,   T_q = sq_bound(d_k) (1 + 2^-16)
-//
-// where d_k is the query's current k-th exact distance: every candidate
-// whose exact distance could enter the list passes (the 2^-16 covers the
-// lane-ordered sum's own rounding), so the filter never changes a result.
+// 1. Tiles. The points are regrouped (a stable sort by nearest pivot, the
+//    pivots strided samples chained nearest-first) so that a 128-point tile
+//    is compact; every tile keeps its centroid c and radius R = max |x - c|.
+//    A query q with current k-th distance d_k skips a tile when
+//    |q - c| > d_k + R (with margins for every rounding, tile_needed below):
+//    by the triangle inequality no point of the tile can then enter the
+//    list. A query block visits the tiles outward from its own (B, B+1,
+//    B-1, ...), tests them 16 at a time, and loads only the tiles some query
+//    of the block still needs; a warp skips a loaded tile that none of its
+//    queries needs.
+// 2. Gram filter. For a loaded tile,
+//      s~(q, c) = |q|^2 + |c|^2 - 2 G~(q, c),   G~ = TF32 tensor-core Gram, FP32 sum
+//    TF32 keeps 10 mantissa bits of each operand, so |G~ - q.c| <= 2^-9 |q||c|
+//    <= 2^-10 (|q|^2 + |c|^2); with the FP32 norms and the final fma the error
+//    of s~ stays below 2^-8 (|q|^2 + |c|^2). A candidate is evaluated exactly
+//    when
+//      s~ - 2^-7 (|q|^2 + |c|^2) <= T_q,   T_q = sq_bound(d_k) (1 + 2^-16)
+//    so every candidate whose exact distance could enter the list passes
+//    (the 2^-16 covers the lane-ordered sum's own rounding).
 //
 // Pipeline per CTA (128 threads = 4 warps, one query row per thread, 128
 // queries per block, persistent over query blocks):
 //   TMA (cp.async.bulk.tensor, 128-byte swizzle) loads the query tile once
-//   and candidate tiles of 128 points into two shared-memory stages;
-//   thread 0 issues tcgen05.mma.kind::tf32 (M = 128, N = 128, 4 x K = 8)
-//   into one of two TMEM accumulators and commits to an mbarrier; while
-//   the tensor core works on tile t + 1 the four warps read tile t's Gram
-//   rows (tcgen05.ld 32x32b.x32), run the filter and the exact path.
+//   and the chosen candidate tiles into two shared-memory stages; thread 0
+//   issues tcgen05.mma.kind::tf32 (M = 128, N = 128, 4 x K = 8) into one of
+//   two TMEM accumulators and commits to an mbarrier; while the tensor core
+//   works on the next tile the four warps read this tile's Gram rows
+//   (tcgen05.ld 32x32b.x32), run the filter and the exact path.
 // TMEM: 2 x 128 columns per CTA; shared memory is padded so that at most two
 // CTAs share an SM, so tcgen05.alloc never waits. Every mbarrier wait is
-// bounded (tt_tma.cuh); on a timeout the kernel records the error, stops,
-// and still frees its TMEM.
+// bounded (tt_tma.cuh); on a timeout the kernel records the error, waits
+// (bounded) for its copies and products in flight, and still frees its TMEM.
 #include <cuda.h>
+
+#include <algorithm>
 
 #include "tt_internal.cuh"
 #include "tt_metric.cuh"
@@ -48,15 +59,23 @@ constexpr int TC_K = 16;        // register top-k capacity
 constexpr u32 TILE_BYTES = TC_M * TC_DIM * 4;   // 16 KiB (query and candidate tiles alike)
 constexpr int TC_BUF = 16;                      // deferred survivors per thread
 constexpr int NSTAGE = 2;                       // candidate tiles in flight (TMA ring)
+constexpr u32 TC_TEST = 16;                     // tiles tested per lookahead batch
+constexpr int ST_STRIDE = 36;                   // floats per tile record: centroid, R, |centroid|^2, pad
+constexpr int MAX_PIV = 256;
 constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
+static_assert(NSTAGE == 2, "the stage bookkeeping below assumes two stages");
+static_assert(TC_M == TC_N, "query blocks and candidate tiles share one tiling");
 
-constexpr u32 WC_BYTES = TC_N * 4;               // candidate norm terms per tile
+constexpr u32 WC_BYTES = TC_N * 4;   // candidate norm terms per tile
+constexpr u32 ID_BYTES = TC_N * 4;   // original ids per tile
 
 struct Shared {
     alignas(1024) unsigned char a[TILE_BYTES];
     alignas(1024) unsigned char b[NSTAGE][TILE_BYTES];
-    alignas(16) f32 wcs[NSTAGE][TC_N];                // |c|^2 (1 - 2^-7) of the tile's candidates
-    u32 buf[16][128];                            // deferred survivors, entry-major (conflict-free)
+    alignas(16) f32 wcs[NSTAGE][TC_N];   // |c|^2 (1 - 2^-7) of the tile's candidates
+    alignas(16) u32 oid[NSTAGE][TC_N];   // original ids of the tile's candidates
+    u32 buf[TC_BUF][TC_M];               // deferred survivors, entry-major (conflict-free)
+    u32 need[2][4];                      // per-warp lookahead masks (double-buffered)
     alignas(8) u64 bar_a;
     alignas(8) u64 bar_b[NSTAGE];
     alignas(8) u64 bar_mma[2];
@@ -130,37 +149,230 @@ __device__ __forceinline__ void tmem_ld32(u32 taddr, u32 (&v)[32]) {
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 
+// m[c] for a run-time c without dynamic register indexing (keeps m in registers)
+__device__ __forceinline__ u32 pick4(const u32 (&m)[4], int c) {
+    return c == 0 ? m[0] : c == 1 ? m[1] : c == 2 ? m[2] : m[3];
+}
+
 template <int DIM>
 struct RegVec {
     const f32 (&q)[DIM];
     __device__ __forceinline__ f32 operator()(u32 k) const { return q[k]; }
 };
 
-// |x_i|^2 and the filter's candidate term |x_i|^2 (1 - 2^-7); padding
-// candidates (i in [n, wpad)) get +inf so that they never pass the filter.
-__global__ void k_norms(const f32* __restrict__ x, u32 n, u32 wpad, f32* __restrict__ nq, f32* __restrict__ wc) {
-    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < wpad; i += gridDim.x * blockDim.x) {
-        if (i >= n) {
-            wc[i] = INFINITY;
-            continue;
-        }
-        f32 s = 0.0f;
+// Tile visited at step s by query block B: B, B+1, B-1, B+2, B-2, ... and,
+// once one side is exhausted, the rest of the other side in order.
+__device__ __forceinline__ u32 spiral_tile(u32 B, u32 s, u32 ntiles) {
+    const u32 left = B, right = ntiles - 1 - B;
+    const u32 m = min(left, right);
+    if (s <= 2 * m) return s == 0 ? B : (s & 1) ? B + (s + 1) / 2 : B - s / 2;
+    const u32 u = s - 2 * m;
+    return right > left ? B + m + u : B - m - u;
+}
+
+// May a point of the tile with record `st` (centroid c, radius R, |c|^2)
+// still enter the list of a query q (|q|^2 = nqi) whose k-th distance is dk?
+// False only when |q - c| > dk + R with room for every rounding:
+//  * the Gram form |q|^2 + |c|^2 - 2 q.c of |q - c|^2 (FP32 sums of 32 terms
+//    and two additions) is within 2^-17 (|q|^2 + |c|^2) of the real value,
+//    so `lower` (2^-16 of it and 2^-120 absolute taken off) is a lower
+//    bound; the absolute part covers subnormal products;
+//  * rhs = (dk + R)^2 (1 + 2^-10) in FP32 exceeds (dk + R~)^2 (1 + 2^-11),
+//    and the computed radius R~ is within 2^-18 of the true max distance;
+// so every point x of the tile has |q - x| >= |q - c| - R > dk (1 + 2^-12.5)
+// and its lane-ordered FP32 distance (relative error < 2^-18) exceeds dk:
+// it can neither beat nor tie the k-th entry. dk below 2^-50 (where
+// underflow defeats relative bounds), any non-finite value and any NaN
+// keep the tile.
+__device__ __forceinline__ bool tile_needed(const f32 (&q)[TC_DIM], f32 nqi, f32 dk, const f32* __restrict__ st) {
+    if (!(dk >= 0x1p-50f) || !(dk < INFINITY)) return true;
+    const float4* c4 = reinterpret_cast<const float4*>(st);
+    f32 g0 = 0.0f, g1 = 0.0f;
 #pragma unroll
-        for (int k = 0; k < TC_DIM; ++k) s = fmaf(x[u64(i) * TC_DIM + k], x[u64(i) * TC_DIM + k], s);
-        nq[i] = s;
-        wc[i] = s * (1.0f - 1.0f / 128.0f);
+    for (int ch = 0; ch < 8; ch += 2) {
+        const float4 a = __ldg(c4 + ch), b = __ldg(c4 + ch + 1);
+        g0 = fmaf(q[4 * ch], a.x, g0);
+        g1 = fmaf(q[4 * ch + 4], b.x, g1);
+        g0 = fmaf(q[4 * ch + 1], a.y, g0);
+        g1 = fmaf(q[4 * ch + 5], b.y, g1);
+        g0 = fmaf(q[4 * ch + 2], a.z, g0);
+        g1 = fmaf(q[4 * ch + 6], b.z, g1);
+        g0 = fmaf(q[4 * ch + 3], a.w, g0);
+        g1 = fmaf(q[4 * ch + 7], b.w, g1);
+    }
+    const float2 rc = __ldg(reinterpret_cast<const float2*>(st + 32));   // R, |c|^2
+    const f32 s = nqi + rc.y;
+    const f32 lower = fmaf(-2.0f, g0 + g1, s) - fmaf(s, 0x1p-16f, 0x1p-120f);
+    const f32 t = dk + rc.x;
+    const f32 rhs = t * t * (1.0f + 0x1p-10f);
+    return !(lower > rhs && lower <= 3.4e38f);
+}
+
+// ---- tile order ------------------------------------------------------------
+
+// Pivots: rows floor(p n / P) of x; rank[p] = position of pivot p on a
+// nearest-first chain from pivot 0 (ties to the lower index), so that
+// pivots of one region of space sit next to each other in the order.
+__global__ void __launch_bounds__(256) k_tc_pivots(const f32* __restrict__ x, u32 n, u32 P, f32* __restrict__ piv,
+                                                   u32* __restrict__ rank) {
+    __shared__ f32 pv[MAX_PIV][TC_DIM + 1];
+    __shared__ unsigned long long red[8];
+    __shared__ u32 cur_s;
+    const u32 p = threadIdx.x;
+    if (p < P) {
+        const u64 r = u64(p) * n / P;
+#pragma unroll 4
+        for (int k = 0; k < TC_DIM; ++k) {
+            pv[p][k] = x[r * TC_DIM + k];
+            piv[u64(p) * TC_DIM + k] = pv[p][k];
+        }
+    }
+    bool visited = p == 0;
+    if (p == 0) {
+        rank[0] = 0;
+        cur_s = 0;
+    }
+    __syncthreads();
+    for (u32 step = 1; step < P; ++step) {
+        const u32 cur = cur_s;
+        unsigned long long key = ~0ull;
+        if (p < P && !visited) {
+            f32 d = 0.0f;
+#pragma unroll 8
+            for (int k = 0; k < TC_DIM; ++k) {
+                const f32 t = pv[p][k] - pv[cur][k];
+                d = fmaf(t, t, d);
+            }
+            key = (u64(fbits(d)) << 32) | p;
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) key = min(key, (unsigned long long)__shfl_xor_sync(0xffffffffu, key, o));
+        if ((p & 31) == 0) red[p >> 5] = key;
+        __syncthreads();
+        if (p == 0) {
+            unsigned long long b = red[0];
+            for (int w = 1; w < 8; ++w) b = min(b, red[w]);
+            const u32 best = u32(b & 0xffffffffu);
+            rank[best] = step;
+            cur_s = best;
+        }
+        __syncthreads();
+        if (p == cur_s) visited = true;
     }
 }
 
+// key[i] = chain rank of the nearest pivot of point i (ties to the lower
+// pivot index), val[i] = i.
+__global__ void k_tc_assign(const f32* __restrict__ x, u32 n, const f32* __restrict__ piv, const u32* __restrict__ rank,
+                            u32 P, u64* __restrict__ key, u32* __restrict__ val) {
+    extern __shared__ f32 sp[];
+    for (u32 t = threadIdx.x; t < P * TC_DIM; t += blockDim.x) sp[t] = piv[t];
+    __syncthreads();
+    const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f32 q[TC_DIM];
+    const float4* xr = reinterpret_cast<const float4*>(x + u64(i) * TC_DIM);
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+        const float4 t4 = __ldg(xr + ch);
+        q[4 * ch] = t4.x;
+        q[4 * ch + 1] = t4.y;
+        q[4 * ch + 2] = t4.z;
+        q[4 * ch + 3] = t4.w;
+    }
+    u32 best = 0;
+    f32 bd = INFINITY;
+    for (u32 p = 0; p < P; ++p) {
+        const f32* c = sp + p * TC_DIM;
+        f32 d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < TC_DIM; k += 2) {
+            const f32 t0 = q[k] - c[k], t1 = q[k + 1] - c[k + 1];
+            d0 = fmaf(t0, t0, d0);
+            d1 = fmaf(t1, t1, d1);
+        }
+        const f32 d = d0 + d1;
+        if (d < bd) {
+            bd = d;
+            best = p;
+        }
+    }
+    key[i] = rank[best];
+    val[i] = i;
+}
+
+// Regrouped copy: xp[r] = x[perm[r]], its norms and filter terms, the
+// original ids; rows [n, wpad) are padding (+inf terms, id ~0).
+__global__ void k_tc_gather(const f32* __restrict__ x, u32 n, u32 wpad, const u32* __restrict__ perm,
+                            f32* __restrict__ xp, u32* __restrict__ ids, f32* __restrict__ nq, f32* __restrict__ wc) {
+    const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= wpad) return;
+    if (r >= n) {
+        wc[r] = INFINITY;
+        ids[r] = 0xffffffffu;
+        return;
+    }
+    const u32 src = perm[r];
+    const float4* xr = reinterpret_cast<const float4*>(x + u64(src) * TC_DIM);
+    float4* xo = reinterpret_cast<float4*>(xp + u64(r) * TC_DIM);
+    f32 s = 0.0f;
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+        const float4 t4 = __ldg(xr + ch);
+        xo[ch] = t4;
+        s = fmaf(t4.x, t4.x, s);
+        s = fmaf(t4.y, t4.y, s);
+        s = fmaf(t4.z, t4.z, s);
+        s = fmaf(t4.w, t4.w, s);
+    }
+    nq[r] = s;
+    wc[r] = s * (1.0f - 1.0f / 128.0f);
+    ids[r] = src;
+}
+
+// One warp per tile: centroid (lane k holds coordinate k), |centroid|^2,
+// radius = sqrt(max_x |x - c|^2).
+__global__ void k_tc_stats(const f32* __restrict__ xp, u32 n, u32 ntiles, f32* __restrict__ stats) {
+    const u32 w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= ntiles) return;
+    const u32 r0 = w * TC_N, r1 = min(r0 + TC_N, n);
+    f32 sum = 0.0f;
+    for (u32 r = r0; r < r1; ++r) sum += xp[u64(r) * TC_DIM + lane];
+    const f32 c = sum / f32(r1 - r0);
+    f32 cc = c * c;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(0xffffffffu, cc, o);
+    f32 r2 = 0.0f;
+    for (u32 r = r0; r < r1; ++r) {
+        const f32 t = xp[u64(r) * TC_DIM + lane] - c;
+        f32 d = t * t;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        // a NaN coordinate makes the radius NaN (sticky): the tile is then never skipped
+        r2 = (d != d || r2 != r2) ? d + r2 : fmaxf(r2, d);
+    }
+    f32* o = stats + u64(w) * ST_STRIDE;
+    o[lane] = c;
+    if (lane == 0) {
+        o[32] = sqrtf(r2);
+        o[33] = cc;
+        o[34] = 0.0f;
+        o[35] = 0.0f;
+    }
+}
+
+// ---- the kNN kernel ---------------------------------------------------------
+
 __global__ void __launch_bounds__(128, 2)
-k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32 n, u32 k,
-         const f32* __restrict__ nq, const f32* __restrict__ wc, u32* __restrict__ ids, f32* __restrict__ dists,
-         u32* __restrict__ next_block, u32* __restrict__ err, unsigned long long* __restrict__ exact_count) {
+k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, const f32* __restrict__ xp,
+         const u32* __restrict__ oids, u32 n, u32 k, const f32* __restrict__ nq, const f32* __restrict__ wc,
+         const f32* __restrict__ stats, u32* __restrict__ ids, f32* __restrict__ dists, u32* __restrict__ next_block,
+         u32* __restrict__ err, unsigned long long* __restrict__ counters) {
     extern __shared__ unsigned char smem_raw[];
     Shared& S = *reinterpret_cast<Shared*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const u32 tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const u32 nblocks = (n + TC_M - 1) / TC_M;
-    const u32 ntiles = (n + TC_N - 1) / TC_N;
+    const u32 ntiles = nblocks;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem_base)),
@@ -180,15 +392,17 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
     __syncthreads();
     tc_fence_after();
     const u32 tmem = S.tmem_base;
-    u32 ph_a = 0, uses_b[NSTAGE] = {}, uses_mma[2] = {0, 0};
-    unsigned long long exact_evals = 0;
+    u32 ph_a = 0, ub0 = 0, ub1 = 0, um0 = 0, um1 = 0;   // completed phases per stage / accumulator
+    unsigned long long exact_evals = 0, tiles_done = 0;
+    u32 npar = 0;   // S.need buffer of the next lookahead
     bool failed = false;
 
-    // stage s <- candidate tile t: the points (TMA, swizzled) and their norm terms
-    auto load_stage = [&](int s, u32 t) {
-        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + WC_BYTES);
-        tma_tile(S.b[s], &map, int(t * TC_N), &S.bar_b[s]);
-        bulk_g2s(S.wcs[s], wc + u64(t) * TC_N, WC_BYTES, &S.bar_b[s]);
+    // stage s <- candidate tile T: the points (TMA, swizzled), their norm terms and ids
+    auto load_stage = [&](int s, u32 T) {
+        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + WC_BYTES + ID_BYTES);
+        tma_tile(S.b[s], &map, int(T * TC_N), &S.bar_b[s]);
+        bulk_g2s(S.wcs[s], wc + u64(T) * TC_N, WC_BYTES, &S.bar_b[s]);
+        bulk_g2s(S.oid[s], oids + u64(T) * TC_N, ID_BYTES, &S.bar_b[s]);
     };
 
     for (;;) {
@@ -200,15 +414,14 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         if (tid == 0) {
             mbar_expect_tx(&S.bar_a, TILE_BYTES);
             tma_tile(S.a, &map, int(q0), &S.bar_a);
-            for (u32 t = 0; t < u32(NSTAGE) && t < ntiles; ++t) load_stage(int(t), t);
         }
         const u32 row = warp * 32 + lane;
-        const u32 i = q0 + row;
+        const u32 i = q0 + row;   // regrouped index of this thread's query
         const bool active = i < n;
         const f32 nqi = active ? nq[i] : 0.0f;
         f32 q[TC_DIM];
 #pragma unroll
-        for (int c = 0; c < TC_DIM; ++c) q[c] = active ? x[u64(i) * TC_DIM + c] : 0.0f;
+        for (int c = 0; c < TC_DIM; ++c) q[c] = active ? xp[u64(i) * TC_DIM + c] : 0.0f;
         f32 ld[TC_K];
         u32 lj[TC_K];
 #pragma unroll
@@ -217,6 +430,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
             lj[t] = 0xffffffffu;
         }
         f32 rq = INFINITY;   // candidate passes iff fma(-2, G, wc) <= rq
+        f32 dk = INFINITY;   // current k-th distance
         u32 nbuf = 0;        // deferred survivors of this thread (S.buf[.][tid])
         // insert (d, j) into the sorted top-TC_K list; true if it entered
         auto consider = [&](u32 j, f32 d) -> bool {
@@ -244,14 +458,15 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         };
         // filter bound from the k-th entry; +inf until the list holds k
         auto update_rq = [&]() {
-            f32 dk = INFINITY;
+            f32 d = INFINITY;
 #pragma unroll
             for (int s = 0; s < TC_K; ++s)
-                if (s == int(k) - 1) dk = ld[s];
-            const f32 tq = dk < INFINITY ? sq_bound(dk) * (1.0f + 1.0f / 65536.0f) : INFINITY;
+                if (s == int(k) - 1) d = ld[s];
+            dk = d;
+            const f32 tq = d < INFINITY ? sq_bound(d) * (1.0f + 1.0f / 65536.0f) : INFINITY;
             rq = tq - nqi * (1.0f - 1.0f / 128.0f);
         };
-        // evaluate the deferred survivors (coordinates from global memory / L2)
+        // evaluate the deferred survivors (original ids; coordinates from x, L2-resident)
         auto flush = [&]() {
             bool changed = false;
 #pragma unroll 1
@@ -272,9 +487,60 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
             nbuf = 0;
             if (changed) update_rq();
         };
+
+        // Lookahead over the outward order (block-uniform state): `bmask`
+        // holds the tiles of the current batch that some query of the block
+        // needs, `mymask` the ones this thread's query needs.
+        u32 sp = 0, bbase = 0, bmask = 0, mymask = 0;
+        auto refill = [&]() {
+            const u32 w = sp == 0 ? u32(NSTAGE) : TC_TEST;
+            u32 m = 0;
+            if (active) {
+#pragma unroll 1
+                for (u32 b = 0; b < w; ++b) {
+                    const u32 s = sp + b;
+                    if (s < ntiles && tile_needed(q, nqi, dk, stats + u64(spiral_tile(blk, s, ntiles)) * ST_STRIDE))
+                        m |= 1u << b;
+                }
+            }
+            const u32 wm = __reduce_or_sync(0xffffffffu, m);
+            if (lane == 0) S.need[npar][warp] = wm;
+            __syncthreads();
+            bmask = S.need[npar][0] | S.need[npar][1] | S.need[npar][2] | S.need[npar][3];
+            npar ^= 1;
+            bbase = sp;
+            mymask = m;
+            sp += w;
+        };
+        // next tile some query of the block needs (block-uniform); false when
+        // the order is exhausted
+        auto next_tile = [&](u32& T, bool& mine) -> bool {
+            for (;;) {
+                if (bmask) {
+                    const u32 b = u32(__ffs(bmask) - 1);
+                    bmask &= bmask - 1;
+                    T = spiral_tile(blk, bbase + b, ntiles);
+                    mine = (mymask >> b) & 1u;
+                    return true;
+                }
+                if (sp >= ntiles) return false;
+                refill();
+            }
+        };
+
+        u32 tl0 = 0, tl1 = 0, nbits = 0, nl = 0;   // stage tiles, this thread's need bits, tiles loaded
+        for (int s = 0; s < NSTAGE; ++s) {
+            u32 T;
+            bool mine;
+            if (!next_tile(T, mine)) break;
+            if (tid == 0) load_stage(s, T);
+            if (s == 0) tl0 = T; else tl1 = T;
+            nbits = (nbits & ~(1u << s)) | (u32(mine) << s);
+            ++nl;
+        }
         if (tid == 0) {
             mbar_wait(&S.bar_a, ph_a, err);
-            mbar_wait(&S.bar_b[0], uses_b[0] & 1, err);
+            mbar_wait(&S.bar_b[0], ub0 & 1, err);
             tc_fence_after();
             mma_tile(tmem, smem_addr(S.a), smem_addr(S.b[0]));
             mma_commit(&S.bar_mma[0]);
@@ -282,120 +548,148 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, u32
         // every thread reads the query tile below: acquire its TMA phase
         mbar_wait(&S.bar_a, ph_a, err);
         ph_a ^= 1;
-        for (u32 t = 0; t < ntiles; ++t) {
-            const int sb = int(t & 1);            // accumulator buffer
-            const int st = int(t % NSTAGE);       // candidate stage
-            mbar_wait(&S.bar_mma[sb], uses_mma[sb] & 1, err);
+        u32 it = 0;
+        for (; it < nl; ++it) {
+            const int sb = int(it & 1);            // accumulator buffer
+            const int st = int(it % NSTAGE);       // candidate stage
+            mbar_wait(&S.bar_mma[sb], (sb ? um1 : um0) & 1, err);
             tc_fence_after();
-            if (tid == 0 && t + 1 < ntiles) {   // the tensor core works on t + 1 during this epilogue
-                const int nb = sb ^ 1, ns = int((t + 1) % NSTAGE);
-                mbar_wait(&S.bar_b[ns], uses_b[ns] & 1, err);   // tile t+1's phase (issued NSTAGE-1 tiles ago)
+            if (tid == 0 && it + 1 < nl) {   // the tensor core works on the next tile during this epilogue
+                const int nb = sb ^ 1, ns = int((it + 1) % NSTAGE);
+                mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err);
                 tc_fence_after();
                 mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]));
                 mma_commit(&S.bar_mma[nb]);
             }
             // every thread acquires the stage's (complete) TMA phase before
-            // reading the candidate tile and its norm terms
-            mbar_wait(&S.bar_b[st], uses_b[st] & 1, err);
-            const u32 j0 = t * TC_N;
-            const unsigned char* bt = S.b[st];
-            const f32* wcs = S.wcs[st];
-            // (A) filter the tile's 128 candidates, 32 per TMEM load. Survivors
-            // are rare, so the common case is a min-tree (32 independent fmas,
-            // depth-5 fminf) per chunk; the bit mask is built only by threads
-            // holding a survivor. Padding candidates carry +inf terms.
-            u32 mk[TC_N / 32];
+            // reading the candidate tile, its norm terms and ids
+            mbar_wait(&S.bar_b[st], (st ? ub1 : ub0) & 1, err);
+            const u32 T = st == 0 ? tl0 : tl1;
+            const bool mine = (nbits >> st) & 1u;
+            const u32 j0 = T * TC_N;
+            if (__any_sync(0xffffffffu, mine)) {
+                const unsigned char* bt = S.b[st];
+                const f32* wcs = S.wcs[st];
+                const u32* oid = S.oid[st];
+                const f32 rqt = mine ? rq : -INFINITY;
+                // (A) filter the tile's 128 candidates, 32 per TMEM load. Survivors
+                // are rare, so the common case is a min-tree (32 independent fmas,
+                // depth-5 fminf) per chunk; the bit mask is built only by threads
+                // holding a survivor. Padding candidates carry +inf terms.
+                u32 mk[TC_N / 32];
 #pragma unroll
-            for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
-                u32 v[32];
-                tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
-                f32 e[32];
+                for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+                    u32 v[32];
+                    tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
+                    f32 e[32];
 #pragma unroll
-                for (int g = 0; g < 8; ++g) {
-                    const float4 w4 = *reinterpret_cast<const float4*>(wcs + chunk * 32 + 4 * g);
-                    e[4 * g] = fmaf(-2.0f, __uint_as_float(v[4 * g]), w4.x);
-                    e[4 * g + 1] = fmaf(-2.0f, __uint_as_float(v[4 * g + 1]), w4.y);
-                    e[4 * g + 2] = fmaf(-2.0f, __uint_as_float(v[4 * g + 2]), w4.z);
-                    e[4 * g + 3] = fmaf(-2.0f, __uint_as_float(v[4 * g + 3]), w4.w);
-                }
-                f32 lo[16];
-#pragma unroll
-                for (int h = 0; h < 16; ++h) lo[h] = fminf(e[h], e[h + 16]);
-#pragma unroll
-                for (int h = 0; h < 8; ++h) lo[h] = fminf(lo[h], lo[h + 8]);
-#pragma unroll
-                for (int h = 0; h < 4; ++h) lo[h] = fminf(lo[h], lo[h + 4]);
-                const f32 emin = fminf(fminf(lo[0], lo[2]), fminf(lo[1], lo[3]));
-                u32 m = 0;
-                if (active && emin <= rq) {
-#pragma unroll
-                    for (int h = 0; h < 32; ++h) m |= u32(e[h] <= rq) << h;
-                    const u32 cbase = j0 + u32(chunk * 32);
-                    // +inf terms still pass while rq is +inf (list not yet full)
-                    if (cbase + 32 > n) m &= cbase < n ? (1u << (n - cbase)) - 1u : 0u;
-                    if (i >= cbase && i < cbase + 32) m &= ~(1u << (i - cbase));
-                }
-                mk[chunk] = m;
-            }
-            // (B) survivors. Few per tile, and at different lanes: they are
-            // deferred into a per-thread buffer and evaluated in lockstep when
-            // some lane's buffer would overflow (exact distance from the
-            // L2-resident coordinates, then insertion). A tile with more
-            // survivors than a buffer holds (the first tile of a block, while
-            // the lists fill) is evaluated directly from the shared tile.
-            const u32 tcnt = __popc(mk[0]) + __popc(mk[1]) + __popc(mk[2]) + __popc(mk[3]);
-            if (__any_sync(0xffffffffu, tcnt != 0)) {
-                if (__any_sync(0xffffffffu, tcnt > u32(TC_BUF))) {
-                    flush();
-                    bool changed = false;
-#pragma unroll 1
-                    for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
-#pragma unroll 1
-                        for (u32 mm = mk[chunk]; mm; mm &= mm - 1) {
-                            const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
-                            f32 cb[TC_DIM];
-                            swz_row(bt, rr, cb);
-                            changed |= consider(j0 + rr, __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM)));
-                        }
+                    for (int g = 0; g < 8; ++g) {
+                        const float4 w4 = *reinterpret_cast<const float4*>(wcs + chunk * 32 + 4 * g);
+                        e[4 * g] = fmaf(-2.0f, __uint_as_float(v[4 * g]), w4.x);
+                        e[4 * g + 1] = fmaf(-2.0f, __uint_as_float(v[4 * g + 1]), w4.y);
+                        e[4 * g + 2] = fmaf(-2.0f, __uint_as_float(v[4 * g + 2]), w4.z);
+                        e[4 * g + 3] = fmaf(-2.0f, __uint_as_float(v[4 * g + 3]), w4.w);
                     }
-                    if (changed) update_rq();
-                } else {
-                    if (__any_sync(0xffffffffu, nbuf + tcnt > u32(TC_BUF))) flush();
+                    f32 lo[16];
+#pragma unroll
+                    for (int h = 0; h < 16; ++h) lo[h] = fminf(e[h], e[h + 16]);
+#pragma unroll
+                    for (int h = 0; h < 8; ++h) lo[h] = fminf(lo[h], lo[h + 8]);
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) lo[h] = fminf(lo[h], lo[h + 4]);
+                    const f32 emin = fminf(fminf(lo[0], lo[2]), fminf(lo[1], lo[3]));
+                    u32 m = 0;
+                    if (active && emin <= rqt) {
+#pragma unroll
+                        for (int h = 0; h < 32; ++h) m |= u32(e[h] <= rqt) << h;
+                        const u32 cbase = j0 + u32(chunk * 32);
+                        // +inf terms still pass while rq is +inf (list not yet full)
+                        if (cbase + 32 > n) m &= cbase < n ? (1u << (n - cbase)) - 1u : 0u;
+                        if (i >= cbase && i < cbase + 32) m &= ~(1u << (i - cbase));
+                    }
+                    mk[chunk] = m;
+                }
+                // (B) survivors. Few per tile, and at different lanes: they are
+                // deferred into a per-thread buffer and evaluated in lockstep when
+                // some lane's buffer would overflow (exact distance from the
+                // L2-resident coordinates, then insertion). A tile with more
+                // survivors than a buffer holds (the first tile of a block, while
+                // the lists fill) is evaluated directly from the shared tile.
+                const u32 tcnt = __popc(mk[0]) + __popc(mk[1]) + __popc(mk[2]) + __popc(mk[3]);
+                if (__any_sync(0xffffffffu, tcnt != 0)) {
+                    if (__any_sync(0xffffffffu, tcnt > u32(TC_BUF))) {
+                        flush();
+                        bool changed = false;
 #pragma unroll 1
-                    for (int chunk = 0; chunk < TC_N / 32; ++chunk)
-                        for (u32 mm = mk[chunk]; mm; mm &= mm - 1)
-                            S.buf[nbuf++][tid] = j0 + u32(chunk * 32 + __ffs(mm) - 1);
+                        for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+#pragma unroll 1
+                            for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1) {
+                                const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
+                                f32 cb[TC_DIM];
+                                swz_row(bt, rr, cb);
+                                changed |= consider(oid[rr], __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM)));
+                            }
+                        }
+                        if (changed) update_rq();
+                    } else {
+                        if (__any_sync(0xffffffffu, nbuf + tcnt > u32(TC_BUF))) flush();
+#pragma unroll 1
+                        for (int chunk = 0; chunk < TC_N / 32; ++chunk)
+                            for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1)
+                                S.buf[nbuf++][tid] = oid[chunk * 32 + __ffs(mm) - 1];
+                    }
                 }
             }
-            ++uses_mma[sb];
+            if (sb) ++um1; else ++um0;
             tc_fence_before();
-            __syncthreads();   // TMEM buffer sb and shared stage sb are free again
-            ++uses_b[st];
-            if (tid == 0) {
-                if (t + NSTAGE < ntiles) {
+            __syncthreads();   // TMEM buffer sb and shared stage st are free again
+            if (st) ++ub1; else ++ub0;
+            u32 Tn;
+            bool mn;
+            if (next_tile(Tn, mn)) {   // block-uniform (may test a batch)
+                if (tid == 0) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    load_stage(st, t + NSTAGE);
+                    load_stage(st, Tn);
                 }
-                S.stop = *((volatile u32*)err);   // one reader: the decision is block-uniform
+                if (st == 0) tl0 = Tn; else tl1 = Tn;
+                nbits = (nbits & ~(1u << st)) | (u32(mn) << st);
+                ++nl;
             }
+            if (tid == 0) S.stop = *((volatile u32*)err);   // one reader: the decision is block-uniform
             __syncthreads();
             if (S.stop) {
                 failed = true;
                 break;
             }
         }
+        if (failed) {
+            // bounded drain of what is still in flight: the product for tile
+            // it + 1 and the copies of tiles (it, nl)
+            if (tid == 0) {
+                const u32 u1 = (it + 1) & 1;
+                if (it + 1 < nl) mbar_wait(&S.bar_mma[u1], (u1 ? um1 : um0) & 1, nullptr);
+                for (u32 u = it + 1; u < nl; ++u) mbar_wait(&S.bar_b[u & 1], ((u & 1) ? ub1 : ub0) & 1, nullptr);
+            }
+            __syncthreads();
+            break;
+        }
+        tiles_done += nl;
         flush();
         if (active) {
+            const u32 oi = oids[i];
 #pragma unroll
             for (int s = 0; s < TC_K; ++s)
                 if (s < int(k)) {
-                    ids[u64(i) * k + s] = lj[s];
-                    if (dists) dists[u64(i) * k + s] = ld[s];
+                    ids[u64(oi) * k + s] = lj[s];
+                    if (dists) dists[u64(oi) * k + s] = ld[s];
                 }
         }
         __syncthreads();
     }
-    if (exact_count && exact_evals) atomicAdd(exact_count, exact_evals);
+    if (counters) {
+        if (exact_evals) atomicAdd(&counters[0], exact_evals);
+        if (tid == 0 && tiles_done) atomicAdd(&counters[1], tiles_done);
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0)
@@ -425,41 +719,69 @@ bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x) {
            (reinterpret_cast<uintptr_t>(x) & 15) == 0;
 }
 
-// Exact kNN lists through the tensor-core filter; returns the number of
-// exact distance evaluations the filter let through.
-u64 knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
-    f32* nq = c->arena.get<f32>(S_MISC0, u64(n) + 1);
-    // the norm terms are bulk-copied 128 per tile: pad to whole tiles
-    const u64 wpad = (u64(n) + TC_N - 1) / TC_N * TC_N;
+// Exact kNN lists through the tile order and the tensor-core filter; sets
+// the context's counts of exact evaluations and computed Gram tiles.
+// Slots: S_TC_* (regrouped copy and tile records), S_MISC0/1/3, S_COUNT, and
+// the radix sort's own (S_SORT_*, S_SCAN*).
+void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
+    const u32 ntiles = div_up(n, TC_N);
+    const u64 wpad = u64(ntiles) * TC_N;
+    // about 12 tiles per pivot region
+    const u32 P = std::max<u32>(1, std::min<u32>(MAX_PIV, n / (12 * TC_N)));
+    u32* perm = nullptr;
+    {
+        f32* piv = c->arena.get<f32>(S_TC_PIV, u64(P) * TC_DIM + MAX_PIV);
+        u32* rank = reinterpret_cast<u32*>(piv + u64(P) * TC_DIM);
+        u64* key = c->arena.get<u64>(S_TC_KEYS, n);
+        u32* val = c->arena.get<u32>(S_TC_VALS, n);
+        k_tc_pivots<<<1, 256, 0, c->stream>>>(x, n, P, piv, rank);
+        TT_LAUNCH("k_tc_pivots");
+        k_tc_assign<<<div_up(n, 256), 256, P * TC_DIM * sizeof(f32), c->stream>>>(x, n, piv, rank, P, key, val);
+        TT_LAUNCH("k_tc_assign");
+        c->launches += 2;
+        perm = val;
+        if (P > 1) {
+            u64* kb = c->arena.get<u64>(S_SORT_A, n);
+            u32* vb = c->arena.get<u32>(S_SORT_VA, n);
+            const int bits = 32 - __builtin_clz(P - 1);
+            if (radix_sort<u32>(c, key, val, n, kb, vb, bits)) perm = vb;
+        }
+    }
+    f32* xp = c->arena.get<f32>(S_TC_X, u64(n) * TC_DIM);
+    u32* oid = c->arena.get<u32>(S_TC_PERM, wpad);
+    f32* nq = c->arena.get<f32>(S_MISC0, wpad);
     f32* wc = c->arena.get<f32>(S_MISC3, wpad);
+    f32* stats = c->arena.get<f32>(S_TC_STATS, u64(ntiles) * ST_STRIDE);
     u32* ctl = c->arena.get<u32>(S_MISC1, 4);   // [0] next block, [1] error word
-    unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 1);
+    unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 2);
     TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
-    TT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream));
-    k_norms<<<div_up(wpad, 256), 256, 0, c->stream>>>(x, n, u32(wpad), nq, wc);
-    TT_LAUNCH("k_norms");
+    TT_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
+    k_tc_gather<<<div_up(wpad, 256), 256, 0, c->stream>>>(x, n, u32(wpad), perm, xp, oid, nq, wc);
+    TT_LAUNCH("k_tc_gather");
+    k_tc_stats<<<div_up(u64(ntiles) * 32, 256), 256, 0, c->stream>>>(xp, n, ntiles, stats);
+    TT_LAUNCH("k_tc_stats");
     CUtensorMap map;
     const cuuint64_t gdim[2] = {cuuint64_t(TC_DIM), cuuint64_t(n)};
     const cuuint64_t gstride[1] = {cuuint64_t(TC_DIM) * 4};
     const cuuint32_t box[2] = {cuuint32_t(TC_DIM), cuuint32_t(TC_M)};
     const cuuint32_t estride[2] = {1, 1};
-    const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<f32*>(x), gdim, gstride, box,
-                                   estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+    const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, xp, gdim, gstride, box, estride,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(TT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
     TT_CUDA(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)));
-    const u32 nblocks = div_up(n, TC_M);
-    const u32 grid = std::min<u32>(nblocks, 2 * u32(c->sms));
-    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, x, n, k, nq, wc, ids, dists, ctl, ctl + 1, cnt);
+    const u32 grid = std::min<u32>(ntiles, 2 * u32(c->sms));
+    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, x, xp, oid, n, k, nq, wc, stats, ids, dists, ctl, ctl + 1, cnt);
     TT_LAUNCH("k_knn_tc");
-    c->launches += 2;
+    c->launches += 3;
     u32 e = 0;
-    unsigned long long evals = 0;
+    unsigned long long h[2] = {0, 0};
     TT_CUDA(cudaMemcpyAsync(&e, ctl + 1, 4, cudaMemcpyDeviceToHost, c->stream));
-    TT_CUDA(cudaMemcpyAsync(&evals, cnt, 8, cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
     TT_CUDA(cudaStreamSynchronize(c->stream));
     if (e) throw Error(TT_ERR_TIMEOUT, "gb300: a bounded device wait timed out in the tensor-core kNN");
-    return evals;
+    c->filter_evals = h[0];
+    c->filter_tiles = h[1];
 }
 
 }  // namespace tt
