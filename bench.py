@@ -13,7 +13,8 @@ one such front end; the metric is front ends (diagrams) per second.
   e2e    the same front end through the host-buffer C-ABI call
          (tt_knn_front_h): host points in, CSR + H0 + columns out, copies
          inside the timed region
-  roofline   the dominant kernel (the exact kNN all-pairs scan), timed alone
+  roofline   the dominant stage (exact kNN lists: tile order + k_knn_tc), timed
+             alone; tensor work counted over the Gram tiles actually computed
   cpu_baseline   the oracle port of the same front end on the host cores, a
          bounded sample of the kNN queries scaled to the whole cloud
 
@@ -291,18 +292,23 @@ def run_gpu(args, ws, rank, local):
             kms.append(e0.elapsed_time(e1))
     knn_ms = statistics.mean(kms)
     evals = int(L.tt_ctx_filter_evals(ctx.h))
+    tiles = int(L.tt_ctx_filter_tiles(ctx.h))
     tc_path = evals > 0
-    kernel_name = ("k_knn_tc (tcgen05 TF32 Gram filter, exact lane-ordered recompute of the survivors)" if tc_path
-                   else "k_scan<L2, 32, KnnOp<16>> (exact kNN all-pairs scan)")
+    kernel_name = ("k_knn_tc (tile-ordered tcgen05 TF32 Gram filter, exact lane-ordered recompute of the survivors)"
+                   if tc_path else "k_scan<L2, 32, KnnOp<16>> (exact kNN all-pairs scan)")
     pk, pk_src = peaks()
-    gram_flops = 2.0 * N * N * DIM            # the Gram-equivalent contraction of one launch
+    ntiles = (N + 127) // 128
+    # tensor work actually issued: 128 x 128 x 32 Gram tiles the pruning kept
+    gram_flops = 2.0 * 128 * 128 * DIM * (tiles if tc_path else ntiles * ntiles)
     achieved = gram_flops / (knn_ms * 1e-3) / 1e12
-    fp32_ops = N * N * (3.0 * DIM)            # sub + mul/fma + add per coordinate, exact path
+    fp32_ops = N * N * (3.0 * DIM)            # sub + mul/fma + add per coordinate, exhaustive exact path
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "knn_scan_traffic.json")
-    if os.path.exists(tf):
+    tf = os.path.join(ROOT, "profiles", "knn_tc_traffic.json")
+    if tc_path and os.path.exists(tf):
         with open(tf) as f:
-            traffic = json.load(f).get("bytes_per_launch")
+            tj = json.load(f)
+        # DRAM bytes of one k_knn_tc launch (ncu) scaled by the tiles computed here
+        traffic = tj["dram_bytes"] * (tiles / tj["tiles"]) if tj.get("tiles") else tj["dram_bytes"]
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
@@ -331,9 +337,11 @@ def run_gpu(args, ws, rank, local):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": achieved / pk["bf16_tflops"], "traffic": traffic,
-                     "kernel": kernel_name, "exact_evaluations": evals,
+                     "kernel": kernel_name, "gram_tiles": tiles, "gram_tiles_exhaustive": ntiles * ntiles,
+                     "exact_evaluations": evals,
                      "exact_fraction_of_pairs": evals / float(N) / float(N),
-                     "kernel_ms": knn_ms, "peak_source": pk_src,
+                     "stage_ms": knn_ms, "peak_source": pk_src,
+                     "exhaustive_equivalent_tflops": 2.0 * N * N * DIM / (knn_ms * 1e-3) / 1e12,
                      "fp32_exact_ops_per_s": fp32_ops / (knn_ms * 1e-3)},
         "cpu_baseline": cpu,
         "clocks": clk,

@@ -79,3 +79,22 @@ def test_radius_vs_oracle_ties():
         assert np.array_equal(host(rp).view(np.uint64), orp)
         assert np.array_equal(host(ci).view(np.uint32), oci)
         assert np.array_equal(bits(host(w)), bits(ow))
+
+
+@pytest.mark.parametrize("m", [1500, 3000])
+def test_knn_graph_hub_rows(m):
+    """A hub: the origin is in every list of m points on a sphere, so its row
+    holds m + k entries — the row-local sort below 2048 entries, the global
+    sort of all entries above; both must give the oracle's CSR."""
+    rng = np.random.default_rng(m)
+    s = rng.normal(size=(m, 64))   # in R^64 random unit vectors are ~sqrt(2) apart
+    s /= np.linalg.norm(s, axis=1, keepdims=True)
+    x = np.ascontiguousarray(np.vstack([np.zeros((1, 64)), s]), dtype=np.float32)
+    k = 4
+    ref = O.knn(x, "l2", k)
+    rp, ci, w = ops.knn_graph(ctx(), dev(x), k, "l2")
+    orp, oci, ow = O.knn_graph(x, "l2", ref)
+    assert np.diff(orp)[0] >= m
+    assert np.array_equal(host(rp).view(np.uint64), orp)
+    assert np.array_equal(host(ci).view(np.uint32), oci)
+    assert np.array_equal(bits(host(w)), bits(ow))

@@ -65,28 +65,94 @@ __device__ __forceinline__ u64 tri_zero_facet(const Cx& cx, u32 c0, u32 c1, u32 
     return kNone;
 }
 
-__global__ void k_edges_dense(const f32* __restrict__ mat, u32 n, f32 thr, u64* __restrict__ keys,
-                              unsigned long long* __restrict__ count, int redzed) {
+// Rows of the complex as edge sources: row v lists its neighbours u < v in
+// increasing u (the dense matrix's row prefix, or the sorted CSR row).
+struct DenseRows {
+    const f32* mat;
+    u32 n;
+    __device__ __forceinline__ u64 begin(u32) const { return 0; }
+    __device__ __forceinline__ u64 end(u32 v) const { return v; }
+    __device__ __forceinline__ void at(u32 v, u64 t, u32& u, f32& d) const {
+        u = u32(t);
+        d = mat[u64(v) * n + t];
+    }
+};
+struct CsrRows {
+    const u64* rp;
+    const u32* ci;
+    const f32* w;
+    __device__ __forceinline__ u64 begin(u32 v) const { return rp[v]; }
+    __device__ __forceinline__ u64 end(u32 v) const { return rp[v + 1]; }
+    __device__ __forceinline__ void at(u32, u64 t, u32& u, f32& d) const {
+        u = ci[t];
+        d = w[t];
+    }
+};
+
+// cnt[v] = kept edges {u, v}: u < v, d(u, v) <= thr (one warp per row).
+template <typename Rows>
+__global__ void k_edge_count(Rows rows, u32 n, f32 thr, u64* __restrict__ cnt) {
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
-    for (u32 i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-        const f32* row = mat + u64(i) * n;
-        const u64 rbase = u64(i) * (i - 1) / 2;
-        for (u32 j0 = 0; j0 < i; j0 += 32) {
-            const u32 j = j0 + lane;
-            const f32 d = j < i ? row[j] : INFINITY;
-            const bool keep = j < i && d <= thr;
-            const u32 bal = __ballot_sync(0xffffffffu, keep);
-            if (!bal) continue;
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(bal));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (keep) {
-                const u64 idx = rbase + j;
-                keys[base + __popc(bal & ((1u << lane) - 1))] =
-                    (u64(__float_as_uint(d)) << kIdxBits) | (redzed ? idx : kIdxMask - idx);
+    for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        const u64 b = rows.begin(v), e = rows.end(v);
+        u32 c = 0;
+        for (u64 t0 = b; t0 < e; t0 += 32) {
+            bool keep = false;
+            if (t0 + lane < e) {
+                u32 u;
+                f32 d;
+                rows.at(v, t0 + lane, u, d);
+                keep = u < v && d <= thr;
             }
+            c += __popc(__ballot_sync(0xffffffffu, keep));
         }
+        if (lane == 0) cnt[v] = c;
+    }
+}
+
+// Kept edges in a fixed order: position p = off[v] + rank in row runs over
+// edge indices in increasing order (rows ascending, u ascending within a
+// row). Entry q (q = m - 1 - p for the Ripser order, idx descending; q = p
+// for the RedZeD order, idx ascending) gets sort key dbits << 32 | q and
+// idx. A stable sort on the dbits then yields (d, idx) in the filtration
+// order: the ties keep the order of q.
+template <typename Rows>
+__global__ void k_edge_fill(Rows rows, u32 n, f32 thr, const u64* __restrict__ off, u64 m, int redzed,
+                            u64* __restrict__ skey, u64* __restrict__ sidx) {
+    const int lane = threadIdx.x & 31;
+    const u32 warps = (gridDim.x * blockDim.x) >> 5;
+    for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        const u64 b = rows.begin(v), e = rows.end(v);
+        const u64 vbase = u64(v) * (v - 1) / 2;
+        u64 base = off[v];
+        for (u64 t0 = b; t0 < e; t0 += 32) {
+            bool keep = false;
+            u32 u = 0;
+            f32 d = 0.0f;
+            if (t0 + lane < e) {
+                rows.at(v, t0 + lane, u, d);
+                keep = u < v && d <= thr;
+            }
+            const u32 bal = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const u64 p = base + __popc(bal & ((1u << lane) - 1));
+                const u64 q = redzed ? p : m - 1 - p;
+                skey[q] = (u64(__float_as_uint(d)) << 32) | q;
+                sidx[q] = vbase + u;
+            }
+            base += __popc(bal);
+        }
+    }
+}
+
+// Sorted (dbits, q) pairs -> packed filtration keys.
+__global__ void k_edge_pack(const u64* __restrict__ skey, const u64* __restrict__ sidx, u64 m, int redzed,
+                            u64* __restrict__ keys) {
+    for (u64 r = u64(blockIdx.x) * blockDim.x + threadIdx.x; r < m; r += u64(gridDim.x) * blockDim.x) {
+        const u64 k = skey[r];
+        const u64 idx = sidx[u32(k)];
+        keys[r] = ((k >> 32) << kIdxBits) | (redzed ? idx : kIdxMask - idx);
     }
 }
 
@@ -162,38 +228,6 @@ struct CsrCx {
         return NOV;
     }
 };
-
-__global__ void k_edges_csr(const u64* __restrict__ rp, const u32* __restrict__ ci, const f32* __restrict__ w,
-                            u32 n, f32 thr, u64* __restrict__ keys, unsigned long long* __restrict__ count,
-                            int redzed) {
-    const int lane = threadIdx.x & 31;
-    const u32 warps = (gridDim.x * blockDim.x) >> 5;
-    for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
-        const u64 b = rp[v], e = rp[v + 1];
-        const u64 vbase = u64(v) * (v - 1) / 2;
-        for (u64 t0 = b; t0 < e; t0 += 32) {
-            const u64 t = t0 + lane;
-            bool keep = false;
-            u32 u = 0;
-            f32 d = 0.0f;
-            if (t < e) {
-                u = ci[t];
-                d = w[t];
-                keep = u < v && d <= thr;
-            }
-            const u32 bal = __ballot_sync(0xffffffffu, keep);
-            if (!bal) continue;
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(bal));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (keep) {
-                const u64 idx = vbase + u;
-                keys[base + __popc(bal & ((1u << lane) - 1))] =
-                    (u64(__float_as_uint(d)) << kIdxBits) | (redzed ? idx : kIdxMask - idx);
-            }
-        }
-    }
-}
 
 __global__ void k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, u64 m, u8* __restrict__ app,
                                u32* __restrict__ emw, u8* __restrict__ emf) {
@@ -338,31 +372,44 @@ inline u32 grid_for(u64 work, u32 per_block) {
 }  // namespace
 
 // Kept edges as sorted keys (Ripser or RedZeD order); returns the count.
+// The edges are written in index order (count, scan, fill), so one stable
+// sort on the distance bits alone gives the filtration order: 4 passes of 8
+// bits for distances within one binade pair, instead of a full 64-bit key
+// sort. Slots: S_EDGE_CNT, S_EDGE_SORT, S_EDGE_IDX, S_EDGE_KEYS (result),
+// and the sort's own (S_SORT_A, S_SORT_HIST, S_SCAN*, S_MISC3).
 static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys_out) {
-    const u64 cap = cx.mat ? u64(cx.n) * (cx.n ? cx.n - 1 : 0) / 2 : 0;
-    u64 capacity = cap;
-    if (!cx.mat) {
-        u64 nnz = 0;
-        TT_CUDA(cudaMemcpyAsync(&nnz, cx.rp + cx.n, sizeof(u64), cudaMemcpyDeviceToHost, c->stream));
-        TT_CUDA(cudaStreamSynchronize(c->stream));
-        capacity = nnz / 2 + 1;
-    }
-    u64* keys = c->arena.get<u64>(S_EDGE_KEYS, capacity + 1);
-    unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 4);
-    TT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream));
-    if (cx.n > 1) {
+    const u32 n = cx.n;
+    u64 m = 0;
+    u64* off = c->arena.get<u64>(S_EDGE_CNT, u64(n) + 2);
+    const u32 g = grid_for(u64(n) * 32, 256);
+    if (n > 1) {
         if (cx.mat)
-            k_edges_dense<<<grid_for(u64(cx.n) * 32, 256), 256, 0, c->stream>>>(cx.mat, cx.n, cx.thr, keys, cnt, redzed);
+            k_edge_count<<<g, 256, 0, c->stream>>>(DenseRows{cx.mat, n}, n, cx.thr, off);
         else
-            k_edges_csr<<<grid_for(u64(cx.n) * 32, 256), 256, 0, c->stream>>>(cx.rp, cx.ci, cx.w, cx.n, cx.thr, keys,
-                                                                              cnt, redzed);
-        TT_LAUNCH("k_edges");
+            k_edge_count<<<g, 256, 0, c->stream>>>(CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off);
+        TT_LAUNCH("k_edge_count");
         ++c->launches;
+        scan_exclusive<u64>(c, off, off, n, off + n);
+        TT_CUDA(cudaMemcpyAsync(&m, off + n, sizeof(m), cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaStreamSynchronize(c->stream));
     }
-    unsigned long long m = 0;
-    TT_CUDA(cudaMemcpyAsync(&m, cnt, sizeof(m), cudaMemcpyDeviceToHost, c->stream));
-    TT_CUDA(cudaStreamSynchronize(c->stream));
-    radix_sort_inplace<u32>(c, keys, nullptr, m);
+    if (m >= 0xffffffffull) invalid("gb300: more than 2^32 - 1 kept edges");
+    u64* keys = c->arena.get<u64>(S_EDGE_KEYS, m + 1);
+    if (m) {
+        u64* skey = c->arena.get<u64>(S_EDGE_SORT, m + 1);
+        u64* sidx = c->arena.get<u64>(S_EDGE_IDX, m + 1);
+        if (cx.mat)
+            k_edge_fill<<<g, 256, 0, c->stream>>>(DenseRows{cx.mat, n}, n, cx.thr, off, m, redzed, skey, sidx);
+        else
+            k_edge_fill<<<g, 256, 0, c->stream>>>(CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off, m, redzed, skey,
+                                                  sidx);
+        TT_LAUNCH("k_edge_fill");
+        u64* kb = c->arena.get<u64>(S_SORT_A, m);
+        const bool sw = radix_sort<u32>(c, skey, static_cast<u32*>(nullptr), m, kb, static_cast<u32*>(nullptr), 0, 32);
+        k_edge_pack<<<grid_for(m, 256), 256, 0, c->stream>>>(sw ? kb : skey, sidx, m, redzed, keys);
+        TT_LAUNCH("k_edge_pack");
+        c->launches += 2;
+    }
     *keys_out = keys;
     return m;
 }

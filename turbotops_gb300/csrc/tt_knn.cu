@@ -77,6 +77,105 @@ __global__ void k_row_ptr(const u32* __restrict__ rows, u64 nnz, u32 n, u64* __r
     }
 }
 
+// ---- symmetric kNN graph without a global sort ------------------------------
+// Every list entry (i, j, d) lands in row i and in row j (count, scan,
+// atomic fill); each row is then ordered by column with a warp-local rank
+// sort and its duplicates (mutual neighbours: same column, same distance
+// bits) dropped. Rows longer than kRowSortMax fall back to the global sort.
+constexpr u32 kRowSortMax = 2048;
+
+__global__ void k_graph_deg(const u32* __restrict__ ids, u32 n, u32 k, unsigned long long* __restrict__ deg) {
+    const u64 total = u64(n) * k;
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += u64(gridDim.x) * blockDim.x) {
+        atomicAdd(&deg[e / k], 1ull);
+        atomicAdd(&deg[ids[e]], 1ull);
+    }
+}
+
+__global__ void k_graph_fill(const u32* __restrict__ ids, const f32* __restrict__ d, u32 n, u32 k,
+                             const u64* __restrict__ off, u32* __restrict__ cur, u32* __restrict__ col,
+                             f32* __restrict__ w) {
+    const u64 total = u64(n) * k;
+    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += u64(gridDim.x) * blockDim.x) {
+        const u32 i = u32(e / k), j = ids[e];
+        const f32 de = d[e];
+        const u64 a = off[i] + atomicAdd(&cur[i], 1u);
+        col[a] = j;
+        w[a] = de;
+        const u64 b = off[j] + atomicAdd(&cur[j], 1u);
+        col[b] = i;
+        w[b] = de;
+    }
+}
+
+// One warp per row: rank of each entry by (column, position), scattered into
+// the sorted copy; ucnt[v] = distinct columns. Rows above kRowSortMax set
+// *overflow and are left to the global sort.
+__global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* __restrict__ col,
+                                const f32* __restrict__ w, u32* __restrict__ scol, f32* __restrict__ sw,
+                                unsigned long long* __restrict__ ucnt, u32* __restrict__ overflow) {
+    const int lane = threadIdx.x & 31;
+    const u32 warps = (gridDim.x * blockDim.x) >> 5;
+    for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        const u64 b = off[v];
+        const u32 L = u32(off[v + 1] - b);
+        if (L > kRowSortMax) {
+            if (lane == 0) atomicOr(overflow, 1u);
+            continue;
+        }
+        for (u32 a0 = 0; a0 < L; a0 += 32) {
+            const u32 a = a0 + lane;
+            const u32 ca = a < L ? col[b + a] : 0xffffffffu;
+            u32 rank = 0;
+            for (u32 t0 = 0; t0 < L; t0 += 32) {
+                const u32 ct = t0 + lane < L ? col[b + t0 + lane] : 0xffffffffu;
+                const u32 lim = min(32u, L - t0);
+                for (u32 s = 0; s < lim; ++s) {
+                    const u32 cs = __shfl_sync(0xffffffffu, ct, s);
+                    rank += (cs < ca) || (cs == ca && t0 + s < a);
+                }
+            }
+            if (a < L) {
+                scol[b + rank] = ca;
+                sw[b + rank] = w[b + a];
+            }
+        }
+        __syncwarp();
+        u32 uc = 0;
+        for (u32 r0 = 0; r0 < L; r0 += 32) {
+            const u32 r = r0 + lane;
+            const bool u = r < L && (r == 0 || scol[b + r - 1] != scol[b + r]);
+            uc += __popc(__ballot_sync(0xffffffffu, u));
+        }
+        if (lane == 0) ucnt[v] = uc;
+        __syncwarp();
+    }
+}
+
+// One warp per row: the distinct columns of the sorted row into the CSR.
+__global__ void k_graph_emit(const u64* __restrict__ off, u32 n, const u32* __restrict__ scol,
+                             const f32* __restrict__ sw, const u64* __restrict__ rp, u32* __restrict__ ci,
+                             f32* __restrict__ wout) {
+    const int lane = threadIdx.x & 31;
+    const u32 warps = (gridDim.x * blockDim.x) >> 5;
+    for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        const u64 b = off[v];
+        const u32 L = u32(off[v + 1] - b);
+        u64 o = rp[v];
+        for (u32 r0 = 0; r0 < L; r0 += 32) {
+            const u32 r = r0 + lane;
+            const bool u = r < L && (r == 0 || scol[b + r - 1] != scol[b + r]);
+            const u32 bal = __ballot_sync(0xffffffffu, u);
+            if (u) {
+                const u64 q = o + __popc(bal & ((1u << lane) - 1));
+                ci[q] = scol[b + r];
+                wout[q] = sw[b + r];
+            }
+            o += __popc(bal);
+        }
+    }
+}
+
 inline u32 grid_for(u64 work, u32 per_block) {
     const u64 g = (work + per_block - 1) / per_block;
     return u32(std::max<u64>(1, std::min<u64>(g, 64ull * kSMs)));
@@ -117,6 +216,49 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
     } else {
         invalid("gb300: knn_graph from external lists is not supported; pass ids = NULL");
     }
+    if (m) {
+        // row-local path: count, scan, fill, per-row sort + dedupe
+        const u32 gw = grid_for(u64(n) * 32, 256);
+        u64* off = c->arena.get<u64>(S_MISC0, 2 * (u64(n) + 2));
+        u64* ucnt = off + n + 2;
+        u32* cur = c->arena.get<u32>(S_MISC1, u64(n) + 4);
+        u32* ovf = cur + n;
+        TT_CUDA(cudaMemsetAsync(off, 0, (u64(n) + 1) * sizeof(u64), c->stream));
+        TT_CUDA(cudaMemsetAsync(cur, 0, (u64(n) + 1) * sizeof(u32), c->stream));
+        k_graph_deg<<<grid_for(u64(n) * k, 256), 256, 0, c->stream>>>(kid, n, k,
+                                                                        reinterpret_cast<unsigned long long*>(off));
+        TT_LAUNCH("k_graph_deg");
+        scan_exclusive<u64>(c, off, off, n, off + n);
+        u32* col = c->arena.get<u32>(S_GRAPH_KEYS, 2 * m + 2);
+        f32* cw = reinterpret_cast<f32*>(col + m + 1);
+        u32* scol = c->arena.get<u32>(S_GRAPH_TMP, 2 * m + 2);
+        f32* sw = reinterpret_cast<f32*>(scol + m + 1);
+        k_graph_fill<<<grid_for(u64(n) * k, 256), 256, 0, c->stream>>>(kid, kd, n, k, off, cur, col, cw);
+        TT_LAUNCH("k_graph_fill");
+        k_graph_rowsort<<<gw, 256, 0, c->stream>>>(off, n, col, cw, scol, sw,
+                                                    reinterpret_cast<unsigned long long*>(ucnt), ovf);
+        TT_LAUNCH("k_graph_rowsort");
+        c->launches += 3;
+        u32 overflow = 0;
+        TT_CUDA(cudaMemcpyAsync(&overflow, ovf, 4, cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+        if (!overflow) {
+            u64 nnz = 0;
+            scan_exclusive<u64>(c, ucnt, rp, n, rp + n);
+            TT_CUDA(cudaMemcpyAsync(&nnz, rp + n, 8, cudaMemcpyDeviceToHost, c->stream));
+            TT_CUDA(cudaStreamSynchronize(c->stream));
+            u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);
+            f32* w = c->arena.get<f32>(S_OUT2, nnz + 1);
+            k_graph_emit<<<gw, 256, 0, c->stream>>>(off, n, scol, sw, rp, ci, w);
+            TT_LAUNCH("k_graph_emit");
+            ++c->launches;
+            *ci_out = ci;
+            *w_out = w;
+            return nnz;
+        }
+    }
+    // a row longer than kRowSortMax (a hub): one global sort of all 2 n k
+    // directed entries by (row, column)
     u64* keys = c->arena.get<u64>(S_GRAPH_KEYS, m + 1);
     u32* vals = c->arena.get<u32>(S_GRAPH_TMP, m + 1);
     if (m) {

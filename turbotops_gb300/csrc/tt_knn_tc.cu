@@ -81,7 +81,7 @@ struct Shared {
     alignas(8) u64 bar_mma[2];
     u32 tmem_base;
     u32 block;
-    u32 stop;
+    u32 stop[2];
 };
 
 // Row r (0..127) of a 128-byte-swizzled tile: 16-byte chunk c of the row sits
@@ -386,7 +386,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         mbar_init(&S.bar_mma[0], 1);
         mbar_init(&S.bar_mma[1], 1);
         fence_mbar_init();
-        S.stop = 0;
+        S.stop[0] = S.stop[1] = 0;
     }
     tc_fence_before();
     __syncthreads();
@@ -641,9 +641,17 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 }
             }
             if (sb) ++um1; else ++um0;
+            // one reader of the error word; the flag is double-buffered by
+            // tile parity, so the write for tile it + 2 cannot overtake a read
+            // of this one
+            if (tid == 0) S.stop[it & 1] = *((volatile u32*)err);
             tc_fence_before();
             __syncthreads();   // TMEM buffer sb and shared stage st are free again
             if (st) ++ub1; else ++ub0;
+            if (S.stop[it & 1]) {   // block-uniform
+                failed = true;
+                break;
+            }
             u32 Tn;
             bool mn;
             if (next_tile(Tn, mn)) {   // block-uniform (may test a batch)
@@ -655,16 +663,10 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 nbits = (nbits & ~(1u << st)) | (u32(mn) << st);
                 ++nl;
             }
-            if (tid == 0) S.stop = *((volatile u32*)err);   // one reader: the decision is block-uniform
-            __syncthreads();
-            if (S.stop) {
-                failed = true;
-                break;
-            }
         }
         if (failed) {
-            // bounded drain of what is still in flight: the product for tile
-            // it + 1 and the copies of tiles (it, nl)
+            // bounded drain of what is still in flight: the product and the
+            // copy of tile it + 1 (no copy was issued after the failure showed)
             if (tid == 0) {
                 const u32 u1 = (it + 1) & 1;
                 if (it + 1 < nl) mbar_wait(&S.bar_mma[u1], (u1 ? um1 : um0) & 1, nullptr);

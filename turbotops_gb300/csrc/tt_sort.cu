@@ -231,7 +231,7 @@ template void scan_exclusive<u32>(tt_ctx*, const u32*, u32*, u64, u32*, int);
 // buffers that hold the result: the caller's (keys, vals) or the arena
 // scratch (kbuf, vbuf) — 'swapped' tells which.
 template <typename V>
-bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits) {
+bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits, int lo_bit) {
     if (n <= 1) return false;
     int bits = force_bits;
     if (bits <= 0) {
@@ -244,7 +244,7 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
         unsigned long long h[2];
         TT_CUDA(cudaMemcpyAsync(h, mm, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaStreamSynchronize(c->stream));
-        const u64 diff = h[0] ^ h[1];
+        const u64 diff = (h[0] ^ h[1]) >> lo_bit;
         bits = diff ? 64 - __builtin_clzll(diff) : 0;
     }
     const u32 tiles = div_up(n, RS_TILE);
@@ -252,7 +252,7 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
     u64 *ka = keys, *kb = kbuf;
     V *va = vals, *vb = vbuf;
     bool swapped = false;
-    for (int shift = 0; shift < bits; shift += 8) {
+    for (int shift = lo_bit; shift < lo_bit + bits; shift += 8) {
         k_rs_upsweep<<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, shift, hist, tiles);
         TT_LAUNCH("k_rs_upsweep");
         scan_exclusive<u32>(c, hist, hist, u64(tiles) * 256, nullptr, 0);
@@ -266,8 +266,8 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
     return swapped;
 }
 
-template bool radix_sort<u32>(tt_ctx*, u64*, u32*, u64, u64*, u32*, int);
-template bool radix_sort<u64>(tt_ctx*, u64*, u64*, u64, u64*, u64*, int);
+template bool radix_sort<u32>(tt_ctx*, u64*, u32*, u64, u64*, u32*, int, int);
+template bool radix_sort<u64>(tt_ctx*, u64*, u64*, u64, u64*, u64*, int, int);
 
 // Sort keys in place (result always back in `keys`, payload in `vals`).
 template <typename V>
