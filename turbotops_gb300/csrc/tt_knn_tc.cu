@@ -496,11 +496,15 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             const u32 w = sp == 0 ? u32(NSTAGE) : TC_TEST;
             u32 m = 0;
             if (active) {
+                // two tiles per step (independent loads and sums); sp < ntiles here
 #pragma unroll 1
-                for (u32 b = 0; b < w; ++b) {
-                    const u32 s = sp + b;
-                    if (s < ntiles && tile_needed(q, nqi, dk, stats + u64(spiral_tile(blk, s, ntiles)) * ST_STRIDE))
-                        m |= 1u << b;
+                for (u32 b = 0; b < w; b += 2) {
+                    const u32 s0 = sp + b, s1 = s0 + 1;
+                    const bool v0 = s0 < ntiles, v1 = b + 1 < w && s1 < ntiles;
+                    const f32* st0 = stats + u64(spiral_tile(blk, v0 ? s0 : sp, ntiles)) * ST_STRIDE;
+                    const f32* st1 = stats + u64(spiral_tile(blk, v1 ? s1 : sp, ntiles)) * ST_STRIDE;
+                    const bool n0 = tile_needed(q, nqi, dk, st0), n1 = tile_needed(q, nqi, dk, st1);
+                    m |= (u32(v0 && n0) << b) | (u32(v1 && n1) << (b + 1));
                 }
             }
             const u32 wm = __reduce_or_sync(0xffffffffu, m);
