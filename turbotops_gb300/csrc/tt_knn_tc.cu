@@ -18,21 +18,25 @@
 //    B-1, ...), tests them 16 at a time, and loads only the tiles some query
 //    of the block still needs; a warp skips a loaded tile that none of its
 //    queries needs.
-// 2. Gram filter. For a loaded tile,
-//      s~(q, c) = |q|^2 + |c|^2 - 2 G~(q, c),   G~ = TF32 tensor-core Gram, FP32 sum
-//    TF32 keeps 10 mantissa bits of each operand, so |G~ - q.c| <= 2^-9 |q||c|
-//    <= 2^-10 (|q|^2 + |c|^2); with the FP32 norms and the final fma the error
-//    of s~ stays below 2^-8 (|q|^2 + |c|^2). A candidate is evaluated exactly
-//    when
+// 2. Gram filter. For a loaded tile the tensor core produces
+//      D~(q, c) = G~(q, c) - |c|^2 (1 - 2^-7) / 2,   G~ = TF32 Gram, FP32 sum,
+//    the norm term entering as a fifth K-step (an exact TF32 head and its
+//    remainder), so that s~ - 2^-7 (|q|^2 + |c|^2) = |q|^2 (1 - 2^-7) - 2 D~
+//    with s~ = |q|^2 + |c|^2 - 2 G~. TF32 keeps 10 mantissa bits of each
+//    operand, so |G~ - q.c| <= 2^-9 |q||c| <= 2^-10 (|q|^2 + |c|^2); with the
+//    FP32 norms, the remainder's own TF32 rounding and the accumulation the
+//    error of s~ stays below 2^-8 (|q|^2 + |c|^2). A candidate is evaluated
+//    exactly when
 //      s~ - 2^-7 (|q|^2 + |c|^2) <= T_q,   T_q = sq_bound(d_k) (1 + 2^-16)
 //    so every candidate whose exact distance could enter the list passes
-//    (the 2^-16 covers the lane-ordered sum's own rounding).
+//    (the 2^-16 covers the lane-ordered sum's own rounding). The epilogue is
+//    a max over the accumulator row and one compare.
 //
 // Pipeline per CTA (128 threads = 4 warps, one query row per thread, 128
 // queries per block, persistent over query blocks):
 //   TMA (cp.async.bulk.tensor, 128-byte swizzle) loads the query tile once
 //   and the chosen candidate tiles into two shared-memory stages; thread 0
-//   issues tcgen05.mma.kind::tf32 (M = 128, N = 128, 4 x K = 8) into one of
+//   issues tcgen05.mma.kind::tf32 (M = 128, N = 128, 5 x K = 8) into one of
 //   two TMEM accumulators and commits to an mbarrier; while the tensor core
 //   works on the next tile the four warps read this tile's Gram rows
 //   (tcgen05.ld 32x32b.x32), run the filter and the exact path.
@@ -66,13 +70,24 @@ constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs pe
 static_assert(NSTAGE == 2, "the stage bookkeeping below assumes two stages");
 static_assert(TC_M == TC_N, "query blocks and candidate tiles share one tiling");
 
-constexpr u32 WC_BYTES = TC_N * 4;   // candidate norm terms per tile
-constexpr u32 ID_BYTES = TC_N * 4;   // original ids per tile
+constexpr u32 AUG_BYTES = TC_N * 16;  // augmentation rows per tile (one 16-byte core-matrix row each)
+constexpr u32 ID_BYTES = TC_N * 4;    // original ids per tile
 
+// The fifth K-step of every product adds the candidate's norm term: the
+// query side holds rows (1, 1, 0, 0 | 0, 0, 0, 0), the candidate side
+// (w_hi, w_lo, 0, 0 | 0, 0, 0, 0) with w = -|c|^2 (1 - 2^-7) / 2 split into an
+// exact TF32 head and its FP32 remainder, so the accumulator holds
+// D = G - |c|^2 (1 - 2^-7) / 2 and the filter is a compare against it.
+// Layout: no swizzle, K-major, 8-row core matrices of 16-byte rows; the
+// first K half of row r at r * 16 (so a tile's rows are one contiguous 2 KiB
+// copy), the second K half in a shared 2 KiB block of zeros.
+// The augmentation region sits at the start of shared memory.
 struct Shared {
+    alignas(1024) float4 aaug[TC_M];         // (1, 1, 0, 0) per query row
+    float4 baug[NSTAGE][TC_N];               // (w_hi, w_lo, 0, 0) per candidate row
+    float4 zeros[TC_N];                      // the second K half of both sides
     alignas(1024) unsigned char a[TILE_BYTES];
     alignas(1024) unsigned char b[NSTAGE][TILE_BYTES];
-    alignas(16) f32 wcs[NSTAGE][TC_N];   // |c|^2 (1 - 2^-7) of the tile's candidates
     alignas(16) u32 oid[NSTAGE][TC_N];   // original ids of the tile's candidates
     u32 buf[TC_BUF][TC_M];               // deferred survivors, entry-major (conflict-free)
     u32 need[2][4];                      // per-warp lookahead masks (double-buffered)
@@ -104,6 +119,14 @@ __device__ __forceinline__ u64 sw128_desc(u32 saddr) {
            (u64(2) << 61);
 }
 
+// UMMA shared-memory descriptor without swizzle, K-major: core matrices of
+// 8 rows x 16 bytes; lbo = byte offset between core matrices adjacent in K,
+// sbo = between core matrices adjacent in M / N.
+__device__ __forceinline__ u64 plain_desc(u32 saddr, u32 lbo, u32 sbo) {
+    return u64((saddr >> 4) & 0x3fff) | (u64((lbo >> 4) & 0x3fff) << 16) | (u64((sbo >> 4) & 0x3fff) << 32) |
+           (u64(1) << 46);
+}
+
 // Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, N, M.
 constexpr u32 kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (u32(TC_N >> 3) << 17) | (u32(TC_M >> 4) << 24);
 
@@ -115,18 +138,29 @@ __device__ __forceinline__ void tma_tile(void* dst, const CUtensorMap* map, int 
         : "memory");
 }
 
-__device__ __forceinline__ void mma_tile(u32 d_tmem, u32 a_saddr, u32 b_saddr) {
+__device__ __forceinline__ void mma_step(u32 d_tmem, u64 da, u64 db, u32 acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+        : "memory");
+}
+
+// D = A B^T over the 32 coordinates (4 K-steps on the swizzled tiles) plus
+// the augmentation step (a_aug, b_aug: starts of the first K halves; z: the
+// zero block holding both second halves).
+__device__ __forceinline__ void mma_tile(u32 d_tmem, u32 a_saddr, u32 b_saddr, u32 a_aug, u32 b_aug, u32 z) {
 #pragma unroll
-    for (int ks = 0; ks < TC_DIM / 8; ++ks) {   // K = 8 tf32 = 32 bytes per step
-        const u64 da = sw128_desc(a_saddr + 32 * ks);
-        const u64 db = sw128_desc(b_saddr + 32 * ks);
-        const u32 acc = ks > 0;
-        asm volatile(
-            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-            "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
-            : "memory");
-    }
+    for (int ks = 0; ks < TC_DIM / 8; ++ks)   // K = 8 tf32 = 32 bytes per step
+        mma_step(d_tmem, sw128_desc(a_saddr + 32 * ks), sw128_desc(b_saddr + 32 * ks), ks > 0);
+    mma_step(d_tmem, plain_desc(a_aug, z - a_aug, 128), plain_desc(b_aug, z - b_aug, 128), 1);
+}
+
+// max of three (one instruction on sm_100 and later)
+__device__ __forceinline__ f32 fmax3(f32 a, f32 b, f32 c) {
+    f32 r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
 }
 
 __device__ __forceinline__ void mma_commit(u64* bar) {
@@ -301,14 +335,16 @@ __global__ void k_tc_assign(const f32* __restrict__ x, u32 n, const f32* __restr
     val[i] = i;
 }
 
-// Regrouped copy: xp[r] = x[perm[r]], its norms and filter terms, the
-// original ids; rows [n, wpad) are padding (+inf terms, id ~0).
+// Regrouped copy: xp[r] = x[perm[r]], its norm, its augmentation row
+// (w_hi, w_lo, 0, 0), w = -|x|^2 (1 - 2^-7) / 2, and the original id; rows
+// [n, wpad) are padding (augmentation -3e38: never passes; id ~0).
 __global__ void k_tc_gather(const f32* __restrict__ x, u32 n, u32 wpad, const u32* __restrict__ perm,
-                            f32* __restrict__ xp, u32* __restrict__ ids, f32* __restrict__ nq, f32* __restrict__ wc) {
+                            f32* __restrict__ xp, u32* __restrict__ ids, f32* __restrict__ nq,
+                            float4* __restrict__ aug) {
     const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= wpad) return;
     if (r >= n) {
-        wc[r] = INFINITY;
+        aug[r] = make_float4(-3.0e38f, 0.0f, 0.0f, 0.0f);
         ids[r] = 0xffffffffu;
         return;
     }
@@ -326,7 +362,12 @@ __global__ void k_tc_gather(const f32* __restrict__ x, u32 n, u32 wpad, const u3
         s = fmaf(t4.w, t4.w, s);
     }
     nq[r] = s;
-    wc[r] = s * (1.0f - 1.0f / 128.0f);
+    const f32 w = -0.5f * (s * (1.0f - 1.0f / 128.0f));
+    // head: the 10 leading mantissa bits (exact in TF32); tail: the exact
+    // FP32 remainder. A non-finite w keeps its head and gets a zero tail.
+    const f32 hi = __uint_as_float(__float_as_uint(w) & 0xffffe000u);
+    const f32 lo = isfinite(w) ? w - hi : 0.0f;
+    aug[r] = make_float4(hi, lo, 0.0f, 0.0f);
     ids[r] = src;
 }
 
@@ -365,7 +406,7 @@ __global__ void k_tc_stats(const f32* __restrict__ xp, u32 n, u32 ntiles, f32* _
 
 __global__ void __launch_bounds__(128, 2)
 k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, const f32* __restrict__ xp,
-         const u32* __restrict__ oids, u32 n, u32 k, const f32* __restrict__ nq, const f32* __restrict__ wc,
+         const u32* __restrict__ oids, u32 n, u32 k, const f32* __restrict__ nq, const float4* __restrict__ aug,
          const f32* __restrict__ stats, u32* __restrict__ ids, f32* __restrict__ dists, u32* __restrict__ next_block,
          u32* __restrict__ err, unsigned long long* __restrict__ counters) {
     extern __shared__ unsigned char smem_raw[];
@@ -380,6 +421,9 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    S.aaug[tid] = make_float4(1.0f, 1.0f, 0.0f, 0.0f);
+    S.zeros[tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the tensor core
     if (tid == 0) {
         mbar_init(&S.bar_a, 1);
         for (int q = 0; q < NSTAGE; ++q) mbar_init(&S.bar_b[q], 1);
@@ -399,9 +443,9 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
 
     // stage s <- candidate tile T: the points (TMA, swizzled), their norm terms and ids
     auto load_stage = [&](int s, u32 T) {
-        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + WC_BYTES + ID_BYTES);
+        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + AUG_BYTES + ID_BYTES);
         tma_tile(S.b[s], &map, int(T * TC_N), &S.bar_b[s]);
-        bulk_g2s(S.wcs[s], wc + u64(T) * TC_N, WC_BYTES, &S.bar_b[s]);
+        bulk_g2s(S.baug[s], aug + u64(T) * TC_N, AUG_BYTES, &S.bar_b[s]);
         bulk_g2s(S.oid[s], oids + u64(T) * TC_N, ID_BYTES, &S.bar_b[s]);
     };
 
@@ -429,7 +473,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             ld[t] = INFINITY;
             lj[t] = 0xffffffffu;
         }
-        f32 rq = INFINITY;   // candidate passes iff fma(-2, G, wc) <= rq
+        f32 rq = INFINITY;   // candidate passes iff -2 D <= rq (D: the augmented product)
         f32 dk = INFINITY;   // current k-th distance
         u32 nbuf = 0;        // deferred survivors of this thread (S.buf[.][tid])
         // insert (d, j) into the sorted top-TC_K list; true if it entered
@@ -546,7 +590,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             mbar_wait(&S.bar_a, ph_a, err);
             mbar_wait(&S.bar_b[0], ub0 & 1, err);
             tc_fence_after();
-            mma_tile(tmem, smem_addr(S.a), smem_addr(S.b[0]));
+            mma_tile(tmem, smem_addr(S.a), smem_addr(S.b[0]), smem_addr(S.aaug), smem_addr(S.baug[0]),
+                     smem_addr(S.zeros));
             mma_commit(&S.bar_mma[0]);
         }
         // every thread reads the query tile below: acquire its TMA phase
@@ -562,7 +607,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 const int nb = sb ^ 1, ns = int((it + 1) % NSTAGE);
                 mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err);
                 tc_fence_after();
-                mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]));
+                mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]), smem_addr(S.aaug),
+                         smem_addr(S.baug[ns]), smem_addr(S.zeros));
                 mma_commit(&S.bar_mma[nb]);
             }
             // every thread acquires the stage's (complete) TMA phase before
@@ -573,41 +619,33 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             const u32 j0 = T * TC_N;
             if (__any_sync(0xffffffffu, mine)) {
                 const unsigned char* bt = S.b[st];
-                const f32* wcs = S.wcs[st];
                 const u32* oid = S.oid[st];
-                const f32 rqt = mine ? rq : -INFINITY;
+                // D = G - |c|^2 (1 - 2^-7) / 2 passes iff -2 D <= rq
+                const f32 t = mine ? -0.5f * rq : INFINITY;
                 // (A) filter the tile's 128 candidates, 32 per TMEM load. Survivors
-                // are rare, so the common case is a min-tree (32 independent fmas,
-                // depth-5 fminf) per chunk; the bit mask is built only by threads
-                // holding a survivor. Padding candidates carry +inf terms.
+                // are rare, so the common case is a max-tree (three-input max,
+                // depth 3) per chunk; the bit mask is built only by threads
+                // holding a survivor. Padding candidates carry -3e38.
                 u32 mk[TC_N / 32];
 #pragma unroll
                 for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
                     u32 v[32];
                     tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
-                    f32 e[32];
+                    f32 h1[11];
 #pragma unroll
-                    for (int g = 0; g < 8; ++g) {
-                        const float4 w4 = *reinterpret_cast<const float4*>(wcs + chunk * 32 + 4 * g);
-                        e[4 * g] = fmaf(-2.0f, __uint_as_float(v[4 * g]), w4.x);
-                        e[4 * g + 1] = fmaf(-2.0f, __uint_as_float(v[4 * g + 1]), w4.y);
-                        e[4 * g + 2] = fmaf(-2.0f, __uint_as_float(v[4 * g + 2]), w4.z);
-                        e[4 * g + 3] = fmaf(-2.0f, __uint_as_float(v[4 * g + 3]), w4.w);
-                    }
-                    f32 lo[16];
-#pragma unroll
-                    for (int h = 0; h < 16; ++h) lo[h] = fminf(e[h], e[h + 16]);
-#pragma unroll
-                    for (int h = 0; h < 8; ++h) lo[h] = fminf(lo[h], lo[h + 8]);
-#pragma unroll
-                    for (int h = 0; h < 4; ++h) lo[h] = fminf(lo[h], lo[h + 4]);
-                    const f32 emin = fminf(fminf(lo[0], lo[2]), fminf(lo[1], lo[3]));
+                    for (int h = 0; h < 10; ++h)
+                        h1[h] = fmax3(__uint_as_float(v[3 * h]), __uint_as_float(v[3 * h + 1]),
+                                      __uint_as_float(v[3 * h + 2]));
+                    h1[10] = fmaxf(__uint_as_float(v[30]), __uint_as_float(v[31]));
+                    const f32 h2a = fmax3(h1[0], h1[1], h1[2]), h2b = fmax3(h1[3], h1[4], h1[5]);
+                    const f32 h2c = fmax3(h1[6], h1[7], h1[8]), h2d = fmaxf(h1[9], h1[10]);
+                    const f32 dmax = fmaxf(fmax3(h2a, h2b, h2c), h2d);
                     u32 m = 0;
-                    if (active && emin <= rqt) {
+                    if (active && dmax >= t) {
 #pragma unroll
-                        for (int h = 0; h < 32; ++h) m |= u32(e[h] <= rqt) << h;
+                        for (int h = 0; h < 32; ++h) m |= u32(__uint_as_float(v[h]) >= t) << h;
                         const u32 cbase = j0 + u32(chunk * 32);
-                        // +inf terms still pass while rq is +inf (list not yet full)
+                        // padding still passes while rq is +inf (list not yet full)
                         if (cbase + 32 > n) m &= cbase < n ? (1u << (n - cbase)) - 1u : 0u;
                         if (i >= cbase && i < cbase + 32) m &= ~(1u << (i - cbase));
                     }
@@ -756,13 +794,13 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     f32* xp = c->arena.get<f32>(S_TC_X, u64(n) * TC_DIM);
     u32* oid = c->arena.get<u32>(S_TC_PERM, wpad);
     f32* nq = c->arena.get<f32>(S_MISC0, wpad);
-    f32* wc = c->arena.get<f32>(S_MISC3, wpad);
+    float4* aug = c->arena.get<float4>(S_MISC3, wpad);
     f32* stats = c->arena.get<f32>(S_TC_STATS, u64(ntiles) * ST_STRIDE);
     u32* ctl = c->arena.get<u32>(S_MISC1, 4);   // [0] next block, [1] error word
     unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 2);
     TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
     TT_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
-    k_tc_gather<<<div_up(wpad, 256), 256, 0, c->stream>>>(x, n, u32(wpad), perm, xp, oid, nq, wc);
+    k_tc_gather<<<div_up(wpad, 256), 256, 0, c->stream>>>(x, n, u32(wpad), perm, xp, oid, nq, aug);
     TT_LAUNCH("k_tc_gather");
     k_tc_stats<<<div_up(u64(ntiles) * 32, 256), 256, 0, c->stream>>>(xp, n, ntiles, stats);
     TT_LAUNCH("k_tc_stats");
@@ -777,7 +815,7 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     if (r != CUDA_SUCCESS) throw Error(TT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
     TT_CUDA(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)));
     const u32 grid = std::min<u32>(ntiles, 2 * u32(c->sms));
-    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, x, xp, oid, n, k, nq, wc, stats, ids, dists, ctl, ctl + 1, cnt);
+    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, x, xp, oid, n, k, nq, aug, stats, ids, dists, ctl, ctl + 1, cnt);
     TT_LAUNCH("k_knn_tc");
     c->launches += 3;
     u32 e = 0;
