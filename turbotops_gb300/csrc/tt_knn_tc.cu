@@ -61,10 +61,12 @@ constexpr int TC_M = 128;       // queries per block (TMEM lanes)
 constexpr int TC_N = 128;       // candidates per tile (accumulator columns)
 constexpr int TC_K = 16;        // register top-k capacity
 constexpr u32 TILE_BYTES = TC_M * TC_DIM * 4;   // 16 KiB (query and candidate tiles alike)
-constexpr int TC_BUF = 16;                      // deferred survivors per thread
+constexpr int TC_Q = 256;                       // survivor queue per warp (pairs)
 constexpr int NSTAGE = 2;                       // candidate tiles in flight (TMA ring)
 constexpr u32 TC_TEST = 16;                     // tiles tested per lookahead batch
 constexpr int ST_STRIDE = 36;                   // floats per tile record: centroid, R, |centroid|^2, pad
+constexpr u32 TST_F4 = TC_TEST * (ST_STRIDE / 4);   // float4 per lookahead batch of tile records
+static_assert(TST_F4 > 128 && TST_F4 <= 256, "two records' float4 per thread");
 constexpr int MAX_PIV = 256;
 constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
 static_assert(NSTAGE == 2, "the stage bookkeeping below assumes two stages");
@@ -89,14 +91,17 @@ struct Shared {
     alignas(1024) unsigned char a[TILE_BYTES];
     alignas(1024) unsigned char b[NSTAGE][TILE_BYTES];
     alignas(16) u32 oid[NSTAGE][TC_N];   // original ids of the tile's candidates
-    u32 buf[TC_BUF][TC_M];               // deferred survivors, entry-major (conflict-free)
+    u32 q[4][TC_Q];                      // per-warp survivor queue: owner lane << 7 | candidate row
+    f32 r[4][TC_Q];                      // their exact distances
     u32 need[2][4];                      // per-warp lookahead masks (double-buffered)
+    alignas(16) float4 tst[TST_F4];      // tile records of the current lookahead batch
     alignas(8) u64 bar_a;
     alignas(8) u64 bar_b[NSTAGE];
     alignas(8) u64 bar_mma[2];
     u32 tmem_base;
     u32 block;
     u32 stop[2];
+    volatile u32 fail;                   // a bounded wait of this CTA timed out
 };
 
 // Row r (0..127) of a 128-byte-swizzled tile: 16-byte chunk c of the row sits
@@ -218,13 +223,12 @@ __device__ __forceinline__ u32 spiral_tile(u32 B, u32 s, u32 ntiles) {
 // it can neither beat nor tie the k-th entry. dk below 2^-50 (where
 // underflow defeats relative bounds), any non-finite value and any NaN
 // keep the tile.
-__device__ __forceinline__ bool tile_needed(const f32 (&q)[TC_DIM], f32 nqi, f32 dk, const f32* __restrict__ st) {
+__device__ __forceinline__ bool tile_needed(const f32 (&q)[TC_DIM], f32 nqi, f32 dk, const float4* st) {
     if (!(dk >= 0x1p-50f) || !(dk < INFINITY)) return true;
-    const float4* c4 = reinterpret_cast<const float4*>(st);
     f32 g0 = 0.0f, g1 = 0.0f;
 #pragma unroll
     for (int ch = 0; ch < 8; ch += 2) {
-        const float4 a = __ldg(c4 + ch), b = __ldg(c4 + ch + 1);
+        const float4 a = st[ch], b = st[ch + 1];
         g0 = fmaf(q[4 * ch], a.x, g0);
         g1 = fmaf(q[4 * ch + 4], b.x, g1);
         g0 = fmaf(q[4 * ch + 1], a.y, g0);
@@ -234,7 +238,7 @@ __device__ __forceinline__ bool tile_needed(const f32 (&q)[TC_DIM], f32 nqi, f32
         g0 = fmaf(q[4 * ch + 3], a.w, g0);
         g1 = fmaf(q[4 * ch + 7], b.w, g1);
     }
-    const float2 rc = __ldg(reinterpret_cast<const float2*>(st + 32));   // R, |c|^2
+    const float4 rc = st[8];   // R, |c|^2, 0, 0
     const f32 s = nqi + rc.y;
     const f32 lower = fmaf(-2.0f, g0 + g1, s) - fmaf(s, 0x1p-16f, 0x1p-120f);
     const f32 t = dk + rc.x;
@@ -431,6 +435,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         mbar_init(&S.bar_mma[1], 1);
         fence_mbar_init();
         S.stop[0] = S.stop[1] = 0;
+        S.fail = 0;
     }
     tc_fence_before();
     __syncthreads();
@@ -456,6 +461,9 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         if (blk >= nblocks || failed) break;
         const u32 q0 = blk * TC_M;
         if (tid == 0) {
+            // the previous block's generic reads of the query tile (survivor
+            // queue) are ordered before this async-proxy overwrite
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_expect_tx(&S.bar_a, TILE_BYTES);
             tma_tile(S.a, &map, int(q0), &S.bar_a);
         }
@@ -475,7 +483,6 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         }
         f32 rq = INFINITY;   // candidate passes iff -2 D <= rq (D: the augmented product)
         f32 dk = INFINITY;   // current k-th distance
-        u32 nbuf = 0;        // deferred survivors of this thread (S.buf[.][tid])
         // insert (d, j) into the sorted top-TC_K list; true if it entered
         auto consider = [&](u32 j, f32 d) -> bool {
             ++exact_evals;
@@ -510,44 +517,40 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             const f32 tq = d < INFINITY ? sq_bound(d) * (1.0f + 1.0f / 65536.0f) : INFINITY;
             rq = tq - nqi * (1.0f - 1.0f / 128.0f);
         };
-        // evaluate the deferred survivors (original ids; coordinates from x, L2-resident)
-        auto flush = [&]() {
-            bool changed = false;
-#pragma unroll 1
-            for (u32 e = 0; e < nbuf; ++e) {
-                const u32 j = S.buf[e][tid];
-                const float4* xr = reinterpret_cast<const float4*>(x + u64(j) * TC_DIM);
-                f32 cb[TC_DIM];
-#pragma unroll
-                for (int ch = 0; ch < 8; ++ch) {
-                    const float4 t4 = __ldg(xr + ch);
-                    cb[4 * ch] = t4.x;
-                    cb[4 * ch + 1] = t4.y;
-                    cb[4 * ch + 2] = t4.z;
-                    cb[4 * ch + 3] = t4.w;
-                }
-                changed |= consider(j, __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM)));
-            }
-            nbuf = 0;
-            if (changed) update_rq();
-        };
-
         // Lookahead over the outward order (block-uniform state): `bmask`
         // holds the tiles of the current batch that some query of the block
         // needs, `mymask` the ones this thread's query needs.
         u32 sp = 0, bbase = 0, bmask = 0, mymask = 0;
+        // Tile records of a batch (TC_TEST positions from s0): float4 f of the
+        // batch is part f % 9 of the record at position s0 + f / 9. Thread t
+        // holds parts t and t + 128 in registers; they are loaded one batch
+        // ahead, so the L2 latency overlaps the tiles in between.
+        float4 pf0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), pf1 = pf0;
+        auto prefetch = [&](u32 s0) {
+            const u32 f0 = tid, f1 = tid + 128;
+            const u32 sa = s0 + f0 / 9, sb2 = s0 + f1 / 9;
+            if (sa < ntiles)
+                pf0 = __ldg(reinterpret_cast<const float4*>(stats + u64(spiral_tile(blk, sa, ntiles)) * ST_STRIDE) +
+                            f0 % 9);
+            if (f1 < TST_F4 && sb2 < ntiles)
+                pf1 = __ldg(reinterpret_cast<const float4*>(stats + u64(spiral_tile(blk, sb2, ntiles)) * ST_STRIDE) +
+                            f1 % 9);
+        };
         auto refill = [&]() {
             const u32 w = sp == 0 ? u32(NSTAGE) : TC_TEST;
+            if (sp == 0) prefetch(0);
+            S.tst[tid] = pf0;
+            if (tid + 128 < TST_F4) S.tst[tid + 128] = pf1;
+            __syncthreads();
+            if (sp + w < ntiles) prefetch(sp + w);   // the next batch starts at sp + w
             u32 m = 0;
             if (active) {
-                // two tiles per step (independent loads and sums); sp < ntiles here
+                // two tiles per step (independent sums); sp < ntiles here
 #pragma unroll 1
                 for (u32 b = 0; b < w; b += 2) {
-                    const u32 s0 = sp + b, s1 = s0 + 1;
-                    const bool v0 = s0 < ntiles, v1 = b + 1 < w && s1 < ntiles;
-                    const f32* st0 = stats + u64(spiral_tile(blk, v0 ? s0 : sp, ntiles)) * ST_STRIDE;
-                    const f32* st1 = stats + u64(spiral_tile(blk, v1 ? s1 : sp, ntiles)) * ST_STRIDE;
-                    const bool n0 = tile_needed(q, nqi, dk, st0), n1 = tile_needed(q, nqi, dk, st1);
+                    const bool v0 = sp + b < ntiles, v1 = b + 1 < w && sp + b + 1 < ntiles;
+                    const bool n0 = tile_needed(q, nqi, dk, S.tst + b * 9);
+                    const bool n1 = tile_needed(q, nqi, dk, S.tst + (b + 1) * 9);
                     m |= (u32(v0 && n0) << b) | (u32(v1 && n1) << (b + 1));
                 }
             }
@@ -587,25 +590,25 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             ++nl;
         }
         if (tid == 0) {
-            mbar_wait(&S.bar_a, ph_a, err);
-            mbar_wait(&S.bar_b[0], ub0 & 1, err);
+            mbar_wait(&S.bar_a, ph_a, err, &S.fail);
+            mbar_wait(&S.bar_b[0], ub0 & 1, err, &S.fail);
             tc_fence_after();
             mma_tile(tmem, smem_addr(S.a), smem_addr(S.b[0]), smem_addr(S.aaug), smem_addr(S.baug[0]),
                      smem_addr(S.zeros));
             mma_commit(&S.bar_mma[0]);
         }
         // every thread reads the query tile below: acquire its TMA phase
-        mbar_wait(&S.bar_a, ph_a, err);
+        mbar_wait(&S.bar_a, ph_a, err, &S.fail);
         ph_a ^= 1;
         u32 it = 0;
         for (; it < nl; ++it) {
             const int sb = int(it & 1);            // accumulator buffer
             const int st = int(it % NSTAGE);       // candidate stage
-            mbar_wait(&S.bar_mma[sb], (sb ? um1 : um0) & 1, err);
+            mbar_wait(&S.bar_mma[sb], (sb ? um1 : um0) & 1, err, &S.fail);
             tc_fence_after();
             if (tid == 0 && it + 1 < nl) {   // the tensor core works on the next tile during this epilogue
                 const int nb = sb ^ 1, ns = int((it + 1) % NSTAGE);
-                mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err);
+                mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err, &S.fail);
                 tc_fence_after();
                 mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]), smem_addr(S.aaug),
                          smem_addr(S.baug[ns]), smem_addr(S.zeros));
@@ -613,7 +616,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             }
             // every thread acquires the stage's (complete) TMA phase before
             // reading the candidate tile, its norm terms and ids
-            mbar_wait(&S.bar_b[st], (st ? ub1 : ub0) & 1, err);
+            mbar_wait(&S.bar_b[st], (st ? ub1 : ub0) & 1, err, &S.fail);
             const u32 T = st == 0 ? tl0 : tl1;
             const bool mine = (nbits >> st) & 1u;
             const u32 j0 = T * TC_N;
@@ -651,42 +654,68 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                     }
                     mk[chunk] = m;
                 }
-                // (B) survivors. Few per tile, and at different lanes: they are
-                // deferred into a per-thread buffer and evaluated in lockstep when
-                // some lane's buffer would overflow (exact distance from the
-                // L2-resident coordinates, then insertion). A tile with more
-                // survivors than a buffer holds (the first tile of a block, while
-                // the lists fill) is evaluated directly from the shared tile.
+                // (B) survivors. Few per tile (after the first), spread over the
+                // lanes: the warp queues its (query, candidate) pairs in shared
+                // memory, every lane computes exact distances for its share of
+                // the queue from the two resident tiles (query rows from the
+                // swizzled query tile, candidates from the stage), and each
+                // owner then inserts its own results. A queue longer than
+                // TC_Q (the first tile of a block, while the lists fill) is
+                // evaluated by the owners directly.
                 const u32 tcnt = __popc(mk[0]) + __popc(mk[1]) + __popc(mk[2]) + __popc(mk[3]);
-                if (__any_sync(0xffffffffu, tcnt != 0)) {
-                    if (__any_sync(0xffffffffu, tcnt > u32(TC_BUF))) {
-                        flush();
-                        bool changed = false;
+                u32 incl = tcnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const u32 y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= u32(o)) incl += y;
+                }
+                const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+                const u32 base = incl - tcnt;
+                if (total > u32(TC_Q)) {
+                    bool changed = false;
 #pragma unroll 1
-                        for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+                    for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
 #pragma unroll 1
-                            for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1) {
-                                const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
-                                f32 cb[TC_DIM];
-                                swz_row(bt, rr, cb);
-                                changed |= consider(oid[rr], __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM)));
-                            }
+                        for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1) {
+                            const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
+                            f32 cb[TC_DIM];
+                            swz_row(bt, rr, cb);
+                            changed |= consider(oid[rr], __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM)));
                         }
-                        if (changed) update_rq();
-                    } else {
-                        if (__any_sync(0xffffffffu, nbuf + tcnt > u32(TC_BUF))) flush();
-#pragma unroll 1
-                        for (int chunk = 0; chunk < TC_N / 32; ++chunk)
-                            for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1)
-                                S.buf[nbuf++][tid] = oid[chunk * 32 + __ffs(mm) - 1];
                     }
+                    if (changed) update_rq();
+                } else if (total) {
+                    u32* wq = S.q[warp];
+                    f32* wr = S.r[warp];
+                    u32 pos = base;
+#pragma unroll 1
+                    for (int chunk = 0; chunk < TC_N / 32; ++chunk)
+                        for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1)
+                            wq[pos++] = (lane << 7) | u32(chunk * 32 + __ffs(mm) - 1);
+                    __syncwarp();
+#pragma unroll 1
+                    for (u32 p = lane; p < total; p += 32) {
+                        const u32 e = wq[p];
+                        f32 qa[TC_DIM], cb[TC_DIM];
+                        swz_row(S.a, warp * 32 + (e >> 7), qa);
+                        swz_row(bt, e & 127u, cb);
+                        wr[p] = __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{qa}, RegVec<TC_DIM>{cb}, TC_DIM));
+                    }
+                    __syncwarp();
+                    bool changed = false;
+#pragma unroll 1
+                    for (u32 kk = 0; kk < tcnt; ++kk)
+                        changed |= consider(oid[wq[base + kk] & 127u], wr[base + kk]);
+                    if (changed) update_rq();
+                    __syncwarp();   // the queue is reused by the next tile
                 }
             }
             if (sb) ++um1; else ++um0;
-            // one reader of the error word; the flag is double-buffered by
-            // tile parity, so the write for tile it + 2 cannot overtake a read
-            // of this one
-            if (tid == 0) S.stop[it & 1] = *((volatile u32*)err);
+            // one reader of this CTA's timeout flag (shared memory: a global
+            // poll here would put an L2 round trip on every tile); the
+            // decision is double-buffered by tile parity, so the write for
+            // tile it + 2 cannot overtake a read of this one
+            if (tid == 0) S.stop[it & 1] = S.fail;
             tc_fence_before();
             __syncthreads();   // TMEM buffer sb and shared stage st are free again
             if (st) ++ub1; else ++ub0;
@@ -718,7 +747,6 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             break;
         }
         tiles_done += nl;
-        flush();
         if (active) {
             const u32 oi = oids[i];
 #pragma unroll

@@ -38,8 +38,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, u32 bytes, 
         : "memory");
 }
 
-// Wait for phase `parity` of `bar` to complete; bounded.
-__device__ __forceinline__ void mbar_wait(u64* bar, u32 parity, u32* err) {
+// Wait for phase `parity` of `bar` to complete; bounded. On a timeout the
+// error word gets TT_DEV_ERR_TIMEOUT and, if given, the CTA-local flag
+// `local` (shared memory) becomes 1, so the CTA can stop without polling
+// global memory.
+__device__ __forceinline__ void mbar_wait(u64* bar, u32 parity, u32* err, volatile u32* local = nullptr) {
     const u32 a = smem_addr(bar);
     for (u32 i = 0; i < kSpinLimit; ++i) {
         u32 done;
@@ -51,6 +54,7 @@ __device__ __forceinline__ void mbar_wait(u64* bar, u32 parity, u32* err) {
         if (done) return;
     }
     if (err) atomicOr(err, TT_DEV_ERR_TIMEOUT);
+    if (local) *local = 1u;
 }
 
 }  // namespace tt
