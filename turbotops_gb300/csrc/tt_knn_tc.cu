@@ -161,6 +161,32 @@ __device__ __forceinline__ void mma_tile(u32 d_tmem, u32 a_saddr, u32 b_saddr, u
     mma_step(d_tmem, plain_desc(a_aug, z - a_aug, 128), plain_desc(b_aug, z - b_aug, 128), 1);
 }
 
+// Ascending bitonic sort of N values held in registers (all indices are
+// compile-time constants once unrolled). NaN must not be present.
+template <int N>
+__device__ __forceinline__ void bitonic_sort(f32 (&a)[N]) {
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+        for (int stride = size / 2; stride > 0; stride >>= 1) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const f32 lo = fminf(a[i], a[j]), hi = fmaxf(a[i], a[j]);
+                    if ((i & size) == 0) {
+                        a[i] = lo;
+                        a[j] = hi;
+                    } else {
+                        a[i] = hi;
+                        a[j] = lo;
+                    }
+                }
+            }
+        }
+    }
+}
+
 // max of three (one instruction on sm_100 and later)
 __device__ __forceinline__ f32 fmax3(f32 a, f32 b, f32 c) {
     f32 r;
@@ -514,7 +540,9 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             for (int s = 0; s < TC_K; ++s)
                 if (s == int(k) - 1) d = ld[s];
             dk = d;
-            const f32 tq = d < INFINITY ? sq_bound(d) * (1.0f + 1.0f / 65536.0f) : INFINITY;
+            // the filter's relative error bounds need |q|^2 far above the
+            // subnormal range: below 2^-60 every candidate is evaluated
+            const f32 tq = d < INFINITY && nqi >= 0x1p-60f ? sq_bound(d) * (1.0f + 1.0f / 65536.0f) : INFINITY;
             rq = tq - nqi * (1.0f - 1.0f / 128.0f);
         };
         // Lookahead over the outward order (block-uniform state): `bmask`
@@ -672,6 +700,66 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 const u32 total = __shfl_sync(0xffffffffu, incl, 31);
                 const u32 base = incl - tcnt;
                 if (total > u32(TC_Q)) {
+                    // Mostly the first tile of a block: the lists are empty and
+                    // every candidate passed. The tile bounds its own k-th
+                    // distance: with L = |q|^2 (1 - 2^-7) - 2 D a lower bound of
+                    // the true squared distance s (the filter's), s <= L +
+                    // 3 2^-8 (|q|^2 + |c|^2) and |c|^2 <= 2 |q|^2 + 2 s give
+                    // U = (L + 9 2^-8 |q|^2) / (1 - 6 2^-8) >= s. The k-th
+                    // smallest of 32 group minima of U (4 candidates a group)
+                    // is U of k distinct candidates, so B >= the final k-th
+                    // squared distance; a candidate with L > B (1 + 2^-12) can
+                    // never enter (its lane-ordered distance exceeds the k-th).
+                    {
+                        f32 gm[32];
+#pragma unroll
+                        for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+                            u32 v[32];
+                            tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
+#pragma unroll
+                            for (int g = 0; g < 8; ++g) {
+                                f32 d4[4];
+#pragma unroll
+                                for (int e = 0; e < 4; ++e)
+                                    d4[e] = (mk[chunk] >> (4 * g + e)) & 1u ? __uint_as_float(v[4 * g + e]) : -INFINITY;
+                                gm[chunk * 8 + g] = fmaxf(fmax3(d4[0], d4[1], d4[2]), d4[3]);
+                            }
+                        }
+                        const f32 a = nqi * (1.0f - 1.0f / 128.0f);
+                        const f32 c1 = nqi * (1.0f + 0x1p-10f) * (9.0f / 256.0f);
+                        const f32 c2 = (1.0f + 0x1p-20f) / (1.0f - 6.0f / 256.0f);
+#pragma unroll
+                        for (int g = 0; g < 32; ++g) {
+                            const f32 u = (fmaf(-2.0f, gm[g], a) + c1) * c2 +
+                                          0x1p-20f * (fabsf(a) + 2.0f * fabsf(gm[g]) + c1);
+                            gm[g] = u == u ? u : INFINITY;   // no candidate (or NaN): no bound
+                        }
+                        bitonic_sort<32>(gm);
+                        f32 B = INFINITY;
+#pragma unroll
+                        for (int g = 0; g < TC_K; ++g)
+                            if (g == int(k) - 1) B = gm[g];
+                        const f32 Bp = B * (1.0f + 0x1p-12f);
+                        // (relative bounds: |q|^2 far above the subnormal range)
+                        const f32 t2 = B < INFINITY && nqi >= 0x1p-60f
+                                           ? 0.5f * (a - Bp) - 0x1p-20f * (fabsf(a) + fabsf(Bp))
+                                           : -INFINITY;
+                        if (__any_sync(0xffffffffu, t2 > t)) {
+                            const f32 tt = fmaxf(t, t2);
+#pragma unroll 1
+                            for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+                                u32 v[32];
+                                tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
+                                u32 m = 0;
+#pragma unroll
+                                for (int h = 0; h < 32; ++h) m |= u32(__uint_as_float(v[h]) >= tt) << h;
+                                mk[0] &= chunk == 0 ? m : ~0u;   // constant indices keep mk in registers
+                                mk[1] &= chunk == 1 ? m : ~0u;
+                                mk[2] &= chunk == 2 ? m : ~0u;
+                                mk[3] &= chunk == 3 ? m : ~0u;
+                            }
+                        }
+                    }
                     bool changed = false;
 #pragma unroll 1
                     for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
