@@ -513,21 +513,18 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         auto consider = [&](u32 j, f32 d) -> bool {
             ++exact_evals;
             if (!(d < ld[TC_K - 1] || (d == ld[TC_K - 1] && j < lj[TC_K - 1]))) return false;
-            bool placed = false;
+            // insertion index = entries ordered before (d, j): independent
+            // compares, then independent selects (no dependent chain)
+            u32 pos = 0;
+#pragma unroll
+            for (int s = 0; s < TC_K - 1; ++s) pos += u32(ld[s] < d || (ld[s] == d && lj[s] < j));
 #pragma unroll
             for (int s = TC_K - 1; s >= 1; --s) {
-                if (!placed) {
-                    if (d < ld[s - 1] || (d == ld[s - 1] && j < lj[s - 1])) {
-                        ld[s] = ld[s - 1];
-                        lj[s] = lj[s - 1];
-                    } else {
-                        ld[s] = d;
-                        lj[s] = j;
-                        placed = true;
-                    }
-                }
+                const bool shift = u32(s) > pos, here = u32(s) == pos;
+                ld[s] = shift ? ld[s - 1] : here ? d : ld[s];
+                lj[s] = shift ? lj[s - 1] : here ? j : lj[s];
             }
-            if (!placed) {
+            if (pos == 0) {
                 ld[0] = d;
                 lj[0] = j;
             }
