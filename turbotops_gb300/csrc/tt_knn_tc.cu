@@ -95,9 +95,11 @@ struct Shared {
     f32 r[4][TC_Q];                      // their exact distances
     u32 need[2][4];                      // per-warp lookahead masks (double-buffered)
     alignas(16) float4 tst[TST_F4];      // tile records of the current lookahead batch
+    alignas(1024) unsigned char cent[TC_TEST * 128];   // their centroids, 128-byte swizzled (MMA operand)
     alignas(8) u64 bar_a;
     alignas(8) u64 bar_b[NSTAGE];
     alignas(8) u64 bar_mma[2];
+    alignas(8) u64 bar_t;                // lookahead product done
     u32 tmem_base;
     u32 block;
     u32 stop[2];
@@ -135,6 +137,10 @@ __device__ __forceinline__ u64 plain_desc(u32 saddr, u32 lbo, u32 sbo) {
 // Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, N, M.
 constexpr u32 kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (u32(TC_N >> 3) << 17) | (u32(TC_M >> 4) << 24);
 
+// The lookahead product: M = 128 queries x N = TC_TEST centroids.
+constexpr u32 kIdescT = (1u << 4) | (2u << 7) | (2u << 10) | (u32(TC_TEST >> 3) << 17) | (u32(TC_M >> 4) << 24);
+static_assert(TC_TEST == 16, "the lookahead product reads 16 accumulator columns");
+
 __device__ __forceinline__ void tma_tile(void* dst, const CUtensorMap* map, int row, u64* bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
@@ -143,11 +149,11 @@ __device__ __forceinline__ void tma_tile(void* dst, const CUtensorMap* map, int 
         : "memory");
 }
 
-__device__ __forceinline__ void mma_step(u32 d_tmem, u64 da, u64 db, u32 acc) {
+__device__ __forceinline__ void mma_step(u32 d_tmem, u64 da, u64 db, u32 acc, u32 idesc = kIdesc) {
     asm volatile(
         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-        "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+        "l"(da), "l"(db), "r"(idesc), "r"(acc)
         : "memory");
 }
 
@@ -207,6 +213,15 @@ __device__ __forceinline__ void tmem_ld32(u32 taddr, u32 (&v)[32]) {
           "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
           "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
           "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(u32 taddr, u32 (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -459,6 +474,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         for (int q = 0; q < NSTAGE; ++q) mbar_init(&S.bar_b[q], 1);
         mbar_init(&S.bar_mma[0], 1);
         mbar_init(&S.bar_mma[1], 1);
+        mbar_init(&S.bar_t, 1);
         fence_mbar_init();
         S.stop[0] = S.stop[1] = 0;
         S.fail = 0;
@@ -468,6 +484,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
     tc_fence_after();
     const u32 tmem = S.tmem_base;
     u32 ph_a = 0, ub0 = 0, ub1 = 0, um0 = 0, um1 = 0;   // completed phases per stage / accumulator
+    u32 ut = 0;                                          // completed lookahead products
     unsigned long long exact_evals = 0, tiles_done = 0;
     u32 npar = 0;   // S.need buffer of the next lookahead
     bool failed = false;
@@ -561,23 +578,68 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 pf1 = __ldg(reinterpret_cast<const float4*>(stats + u64(spiral_tile(blk, sb2, ntiles)) * ST_STRIDE) +
                             f1 % 9);
         };
-        auto refill = [&]() {
+        // acc: TMEM address of an accumulator the tile loop does not use
+        // right now (its first TC_TEST columns take the lookahead product), or
+        // ~0u before the first tile (every k-th distance is still +inf then).
+        auto refill = [&](u32 acc) {
             const u32 w = sp == 0 ? u32(NSTAGE) : TC_TEST;
             if (sp == 0) prefetch(0);
-            S.tst[tid] = pf0;
-            if (tid + 128 < TST_F4) S.tst[tid + 128] = pf1;
+            {   // the batch's records; the centroids also as the MMA operand
+                const u32 f0 = tid, f1 = tid + 128;
+                S.tst[f0] = pf0;
+                if ((f0 % 9) < 8) {
+                    const u32 b = f0 / 9;
+                    *reinterpret_cast<float4*>(S.cent + b * 128 + (((f0 % 9) ^ (b & 7)) << 4)) = pf0;
+                }
+                if (f1 < TST_F4) {
+                    S.tst[f1] = pf1;
+                    if ((f1 % 9) < 8) {
+                        const u32 b = f1 / 9;
+                        *reinterpret_cast<float4*>(S.cent + b * 128 + (((f1 % 9) ^ (b & 7)) << 4)) = pf1;
+                    }
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // centroids -> tensor core
             __syncthreads();
             if (sp + w < ntiles) prefetch(sp + w);   // the next batch starts at sp + w
             u32 m = 0;
-            if (active) {
-                // two tiles per step (independent sums); sp < ntiles here
+            if (acc == ~0u) {
+                if (active) {
 #pragma unroll 1
-                for (u32 b = 0; b < w; b += 2) {
-                    const bool v0 = sp + b < ntiles, v1 = b + 1 < w && sp + b + 1 < ntiles;
-                    const bool n0 = tile_needed(q, nqi, dk, S.tst + b * 9);
-                    const bool n1 = tile_needed(q, nqi, dk, S.tst + (b + 1) * 9);
-                    m |= (u32(v0 && n0) << b) | (u32(v1 && n1) << (b + 1));
+                    for (u32 b = 0; b < w; ++b)
+                        if (sp + b < ntiles && tile_needed(q, nqi, dk, S.tst + b * 9)) m |= 1u << b;
                 }
+            } else {
+                // G = q . c for the 128 queries x 16 centroids on the tensor
+                // core. TF32 operands: |G~ - q.c| <= 2^-10 (|q|^2 + |c|^2), so
+                // |q|^2 + |c|^2 - 2 G~ - 2^-7 (|q|^2 + |c|^2) is a lower bound
+                // of |q - c|^2 with room for the FP32 roundings; the test is
+                // then tile_needed's (skip iff |q - c| > dk + R).
+                if (tid == 0) {
+                    tc_fence_after();
+#pragma unroll
+                    for (int ks = 0; ks < TC_DIM / 8; ++ks)
+                        mma_step(acc, sw128_desc(smem_addr(S.a) + 32 * ks), sw128_desc(smem_addr(S.cent) + 32 * ks),
+                                 ks > 0, kIdescT);
+                    mma_commit(&S.bar_t);
+                }
+                mbar_wait(&S.bar_t, ut & 1, err, &S.fail);
+                ++ut;
+                tc_fence_after();
+                u32 g[TC_TEST];
+                tmem_ld16(acc + ((warp * 32u) << 16), g);
+                const bool ok = active && dk >= 0x1p-50f && dk < INFINITY && nqi >= 0x1p-60f;
+#pragma unroll
+                for (int b = 0; b < int(TC_TEST); ++b) {
+                    const float4 rc = S.tst[b * 9 + 8];   // R, |c|^2, 0, 0
+                    const f32 s2 = nqi + rc.y;
+                    const f32 lower = fmaf(-2.0f, __uint_as_float(g[b]), s2) - fmaf(s2, 1.0f / 128.0f, 0x1p-120f);
+                    const f32 t2 = dk + rc.x;
+                    const f32 rhs = t2 * t2 * (1.0f + 0x1p-10f);
+                    const bool skip = ok && lower > rhs && lower <= 3.4e38f;
+                    if (active && sp + u32(b) < ntiles && !skip) m |= 1u << b;
+                }
+                tc_fence_before();
             }
             const u32 wm = __reduce_or_sync(0xffffffffu, m);
             if (lane == 0) S.need[npar][warp] = wm;
@@ -590,7 +652,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         };
         // next tile some query of the block needs (block-uniform); false when
         // the order is exhausted
-        auto next_tile = [&](u32& T, bool& mine) -> bool {
+        auto next_tile = [&](u32& T, bool& mine, u32 acc) -> bool {
             for (;;) {
                 if (bmask) {
                     const u32 b = u32(__ffs(bmask) - 1);
@@ -600,7 +662,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                     return true;
                 }
                 if (sp >= ntiles) return false;
-                refill();
+                refill(acc);
             }
         };
 
@@ -608,7 +670,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         for (int s = 0; s < NSTAGE; ++s) {
             u32 T;
             bool mine;
-            if (!next_tile(T, mine)) break;
+            if (!next_tile(T, mine, ~0u)) break;
             if (tid == 0) load_stage(s, T);
             if (s == 0) tl0 = T; else tl1 = T;
             nbits = (nbits & ~(1u << s)) | (u32(mine) << s);
@@ -810,7 +872,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             }
             u32 Tn;
             bool mn;
-            if (next_tile(Tn, mn)) {   // block-uniform (may test a batch)
+            if (next_tile(Tn, mn, tmem + u32(sb) * TC_N)) {   // block-uniform (may test a batch)
                 if (tid == 0) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     load_stage(st, Tn);
@@ -827,6 +889,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 const u32 u1 = (it + 1) & 1;
                 if (it + 1 < nl) mbar_wait(&S.bar_mma[u1], (u1 ? um1 : um0) & 1, nullptr);
                 for (u32 u = it + 1; u < nl; ++u) mbar_wait(&S.bar_b[u & 1], ((u & 1) ? ub1 : ub0) & 1, nullptr);
+                // the last lookahead product (returns at once if it completed)
+                if (ut) mbar_wait(&S.bar_t, (ut - 1) & 1, nullptr);
             }
             __syncthreads();
             break;
