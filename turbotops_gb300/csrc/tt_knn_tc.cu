@@ -424,7 +424,9 @@ __global__ void k_tc_stats(const f32* __restrict__ xp, u32 n, u32 ntiles, f32* _
     const u32 r0 = w * TC_N, r1 = min(r0 + TC_N, n);
     f32 sum = 0.0f;
     for (u32 r = r0; r < r1; ++r) sum += xp[u64(r) * TC_DIM + lane];
-    const f32 c = sum / f32(r1 - r0);
+    // the centroid is any point (the bound holds for every centre): rounded
+    // to a TF32-exact value, it enters the lookahead product without error
+    const f32 c = __uint_as_float(__float_as_uint(sum / f32(r1 - r0)) & 0xffffe000u);
     f32 cc = c * c;
 #pragma unroll
     for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(0xffffffffu, cc, o);
@@ -611,8 +613,10 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 }
             } else {
                 // G = q . c for the 128 queries x 16 centroids on the tensor
-                // core. TF32 operands: |G~ - q.c| <= 2^-10 (|q|^2 + |c|^2), so
-                // |q|^2 + |c|^2 - 2 G~ - 2^-7 (|q|^2 + |c|^2) is a lower bound
+                // core. The centroids are TF32-exact and the queries lose at
+                // most 2^-10 relative in TF32, so |G~ - q.c| <= 2^-10 |q||c|
+                // (FP32 accumulation included) <= 2^-11 (|q|^2 + |c|^2), and
+                // |q|^2 + |c|^2 - 2 G~ - 2^-8 (|q|^2 + |c|^2) is a lower bound
                 // of |q - c|^2 with room for the FP32 roundings; the test is
                 // then tile_needed's (skip iff |q - c| > dk + R).
                 if (tid == 0) {
@@ -633,7 +637,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 for (int b = 0; b < int(TC_TEST); ++b) {
                     const float4 rc = S.tst[b * 9 + 8];   // R, |c|^2, 0, 0
                     const f32 s2 = nqi + rc.y;
-                    const f32 lower = fmaf(-2.0f, __uint_as_float(g[b]), s2) - fmaf(s2, 1.0f / 128.0f, 0x1p-120f);
+                    const f32 lower = fmaf(-2.0f, __uint_as_float(g[b]), s2) - fmaf(s2, 1.0f / 256.0f, 0x1p-120f);
                     const f32 t2 = dk + rc.x;
                     const f32 rhs = t2 * t2 * (1.0f + 0x1p-10f);
                     const bool skip = ok && lower > rhs && lower <= 3.4e38f;
