@@ -83,6 +83,7 @@ __global__ void k_row_ptr(const u32* __restrict__ rows, u64 nnz, u32 n, u64* __r
 // sort and its duplicates (mutual neighbours: same column, same distance
 // bits) dropped. Rows longer than kRowSortMax fall back to the global sort.
 constexpr u32 kRowSortMax = 2048;
+constexpr u32 kWarpRowMax = 64;    // longer rows: one block each (k_graph_rowsort_long)
 
 __global__ void k_graph_deg(const u32* __restrict__ ids, u32 n, u32 k, unsigned long long* __restrict__ deg) {
     const u64 total = u64(n) * k;
@@ -123,6 +124,7 @@ __global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* _
             if (lane == 0) atomicOr(overflow, 1u);
             continue;
         }
+        if (L > kWarpRowMax) continue;   // k_graph_rowsort_long
         for (u32 a0 = 0; a0 < L; a0 += 32) {
             const u32 a = a0 + lane;
             const u32 ca = a < L ? col[b + a] : 0xffffffffu;
@@ -149,6 +151,57 @@ __global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* _
         }
         if (lane == 0) ucnt[v] = uc;
         __syncwarp();
+    }
+}
+
+// Rows of kWarpRowMax < L <= kRowSortMax entries (hubs: points in many
+// lists): one block per row, a bitonic sort of (column << 32 | distance
+// bits) in shared memory; duplicates are then identical and adjacent.
+constexpr u32 kLongThreads = 256;
+__global__ void __launch_bounds__(kLongThreads) k_graph_rowsort_long(const u64* __restrict__ off, u32 n,
+                                                                     const u32* __restrict__ col,
+                                                                     const f32* __restrict__ w, u32* __restrict__ scol,
+                                                                     f32* __restrict__ sw,
+                                                                     unsigned long long* __restrict__ ucnt) {
+    __shared__ unsigned long long key[kRowSortMax];
+    __shared__ u32 uc;
+    const u32 tid = threadIdx.x;
+    for (u32 v = blockIdx.x; v < n; v += gridDim.x) {
+        const u64 b = off[v];
+        const u32 L = u32(off[v + 1] - b);
+        if (L <= kWarpRowMax || L > kRowSortMax) continue;   // block-uniform
+        u32 P = 1;
+        while (P < L) P <<= 1;
+        for (u32 i = tid; i < P; i += kLongThreads)
+            key[i] = i < L ? (u64(col[b + i]) << 32) | __float_as_uint(w[b + i]) : ~0ull;
+        if (tid == 0) uc = 0;
+        __syncthreads();
+        for (u32 kk = 2; kk <= P; kk <<= 1) {
+            for (u32 j = kk >> 1; j > 0; j >>= 1) {
+                for (u32 i = tid; i < P; i += kLongThreads) {
+                    const u32 ij = i ^ j;
+                    if (ij > i) {
+                        const unsigned long long x0 = key[i], x1 = key[ij];
+                        if ((x0 > x1) == ((i & kk) == 0)) {
+                            key[i] = x1;
+                            key[ij] = x0;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        u32 c = 0;
+        for (u32 i = tid; i < L; i += kLongThreads) {
+            const unsigned long long x = key[i];
+            scol[b + i] = u32(x >> 32);
+            sw[b + i] = __uint_as_float(u32(x));
+            c += i == 0 || (key[i - 1] >> 32) != (x >> 32);
+        }
+        atomicAdd(&uc, c);
+        __syncthreads();
+        if (tid == 0) ucnt[v] = uc;
+        __syncthreads();
     }
 }
 
@@ -238,7 +291,10 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         k_graph_rowsort<<<gw, 256, 0, c->stream>>>(off, n, col, cw, scol, sw,
                                                     reinterpret_cast<unsigned long long*>(ucnt), ovf);
         TT_LAUNCH("k_graph_rowsort");
-        c->launches += 3;
+        k_graph_rowsort_long<<<std::min<u32>(n, 8 * u32(c->sms)), kLongThreads, 0, c->stream>>>(
+            off, n, col, cw, scol, sw, reinterpret_cast<unsigned long long*>(ucnt));
+        TT_LAUNCH("k_graph_rowsort_long");
+        c->launches += 4;
         u32 overflow = 0;
         TT_CUDA(cudaMemcpyAsync(&overflow, ovf, 4, cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaStreamSynchronize(c->stream));

@@ -292,13 +292,13 @@ __device__ __forceinline__ bool tile_needed(const f32 (&q)[TC_DIM], f32 nqi, f32
 // Pivots: rows floor(p n / P) of x; rank[p] = position of pivot p on a
 // nearest-first chain from pivot 0 (ties to the lower index), so that
 // pivots of one region of space sit next to each other in the order.
-__global__ void __launch_bounds__(256) k_tc_pivots(const f32* __restrict__ x, u32 n, u32 P, f32* __restrict__ piv,
-                                                   u32* __restrict__ rank) {
+// One warp: lane l owns pivots l, l + 32, ...; each chain step is a warp
+// argmin (no block barriers).
+__global__ void __launch_bounds__(32) k_tc_pivots(const f32* __restrict__ x, u32 n, u32 P, f32* __restrict__ piv,
+                                                  u32* __restrict__ rank) {
     __shared__ f32 pv[MAX_PIV][TC_DIM + 1];
-    __shared__ unsigned long long red[8];
-    __shared__ u32 cur_s;
-    const u32 p = threadIdx.x;
-    if (p < P) {
+    const u32 lane = threadIdx.x;
+    for (u32 p = lane; p < P; p += 32) {
         const u64 r = u64(p) * n / P;
 #pragma unroll 4
         for (int k = 0; k < TC_DIM; ++k) {
@@ -306,37 +306,27 @@ __global__ void __launch_bounds__(256) k_tc_pivots(const f32* __restrict__ x, u3
             piv[u64(p) * TC_DIM + k] = pv[p][k];
         }
     }
-    bool visited = p == 0;
-    if (p == 0) {
-        rank[0] = 0;
-        cur_s = 0;
-    }
-    __syncthreads();
+    u32 visited = lane == 0 ? 1u : 0u;   // bit i: pivot lane + 32 i is on the chain
+    if (lane == 0) rank[0] = 0;
+    __syncwarp();
+    u32 cur = 0;
     for (u32 step = 1; step < P; ++step) {
-        const u32 cur = cur_s;
         unsigned long long key = ~0ull;
-        if (p < P && !visited) {
+        for (u32 i = 0, p = lane; p < P; ++i, p += 32) {
+            if ((visited >> i) & 1u) continue;
             f32 d = 0.0f;
 #pragma unroll 8
             for (int k = 0; k < TC_DIM; ++k) {
                 const f32 t = pv[p][k] - pv[cur][k];
                 d = fmaf(t, t, d);
             }
-            key = (u64(fbits(d)) << 32) | p;
+            key = min(key, (unsigned long long)((u64(fbits(d)) << 32) | p));
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) key = min(key, (unsigned long long)__shfl_xor_sync(0xffffffffu, key, o));
-        if ((p & 31) == 0) red[p >> 5] = key;
-        __syncthreads();
-        if (p == 0) {
-            unsigned long long b = red[0];
-            for (int w = 1; w < 8; ++w) b = min(b, red[w]);
-            const u32 best = u32(b & 0xffffffffu);
-            rank[best] = step;
-            cur_s = best;
-        }
-        __syncthreads();
-        if (p == cur_s) visited = true;
+        cur = u32(key & 0xffffffffu);
+        if (lane == 0) rank[cur] = step;
+        if ((cur & 31u) == lane) visited |= 1u << (cur >> 5);
     }
 }
 
@@ -959,7 +949,7 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
         u32* rank = reinterpret_cast<u32*>(piv + u64(P) * TC_DIM);
         u64* key = c->arena.get<u64>(S_TC_KEYS, n);
         u32* val = c->arena.get<u32>(S_TC_VALS, n);
-        k_tc_pivots<<<1, 256, 0, c->stream>>>(x, n, P, piv, rank);
+        k_tc_pivots<<<1, 32, 0, c->stream>>>(x, n, P, piv, rank);
         TT_LAUNCH("k_tc_pivots");
         k_tc_assign<<<div_up(n, 256), 256, P * TC_DIM * sizeof(f32), c->stream>>>(x, n, piv, rank, P, key, val);
         TT_LAUNCH("k_tc_assign");
