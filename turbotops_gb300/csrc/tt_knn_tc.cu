@@ -12,9 +12,9 @@
 //    pivots strided samples chained nearest-first) so that a 128-point tile
 //    is compact; every tile keeps its centroid c and radius R = max |x - c|.
 //    A query q with current k-th distance d_k skips a tile when
-//    |q - c| > d_k + R (with margins for every rounding, tile_needed below):
-//    by the triangle inequality no point of the tile can then enter the
-//    list. A query block visits the tiles outward from its own (B, B+1,
+//    |q - c| > d_k + R (with margins for every rounding, see the lookahead
+//    product in the kernel): by the triangle inequality no point of the tile
+//    can then enter the list. A query block visits the tiles outward from its own (B, B+1,
 //    B-1, ...), tests them 16 at a time, and loads only the tiles some query
 //    of the block still needs; a warp skips a loaded tile that none of its
 //    queries needs.
@@ -105,6 +105,8 @@ struct Shared {
     u32 stop[2];
     volatile u32 fail;                   // a bounded wait of this CTA timed out
 };
+
+static_assert(sizeof(Shared) + 1024 <= TC_SMEM, "shared layout (plus alignment slack) exceeds the reservation");
 
 // Row r (0..127) of a 128-byte-swizzled tile: 16-byte chunk c of the row sits
 // at chunk position c ^ (r & 7) (the TMA / UMMA 128-byte swizzle).
@@ -248,43 +250,6 @@ __device__ __forceinline__ u32 spiral_tile(u32 B, u32 s, u32 ntiles) {
     if (s <= 2 * m) return s == 0 ? B : (s & 1) ? B + (s + 1) / 2 : B - s / 2;
     const u32 u = s - 2 * m;
     return right > left ? B + m + u : B - m - u;
-}
-
-// May a point of the tile with record `st` (centroid c, radius R, |c|^2)
-// still enter the list of a query q (|q|^2 = nqi) whose k-th distance is dk?
-// False only when |q - c| > dk + R with room for every rounding:
-//  * the Gram form |q|^2 + |c|^2 - 2 q.c of |q - c|^2 (FP32 sums of 32 terms
-//    and two additions) is within 2^-17 (|q|^2 + |c|^2) of the real value,
-//    so `lower` (2^-16 of it and 2^-120 absolute taken off) is a lower
-//    bound; the absolute part covers subnormal products;
-//  * rhs = (dk + R)^2 (1 + 2^-10) in FP32 exceeds (dk + R~)^2 (1 + 2^-11),
-//    and the computed radius R~ is within 2^-18 of the true max distance;
-// so every point x of the tile has |q - x| >= |q - c| - R > dk (1 + 2^-12.5)
-// and its lane-ordered FP32 distance (relative error < 2^-18) exceeds dk:
-// it can neither beat nor tie the k-th entry. dk below 2^-50 (where
-// underflow defeats relative bounds), any non-finite value and any NaN
-// keep the tile.
-__device__ __forceinline__ bool tile_needed(const f32 (&q)[TC_DIM], f32 nqi, f32 dk, const float4* st) {
-    if (!(dk >= 0x1p-50f) || !(dk < INFINITY)) return true;
-    f32 g0 = 0.0f, g1 = 0.0f;
-#pragma unroll
-    for (int ch = 0; ch < 8; ch += 2) {
-        const float4 a = st[ch], b = st[ch + 1];
-        g0 = fmaf(q[4 * ch], a.x, g0);
-        g1 = fmaf(q[4 * ch + 4], b.x, g1);
-        g0 = fmaf(q[4 * ch + 1], a.y, g0);
-        g1 = fmaf(q[4 * ch + 5], b.y, g1);
-        g0 = fmaf(q[4 * ch + 2], a.z, g0);
-        g1 = fmaf(q[4 * ch + 6], b.z, g1);
-        g0 = fmaf(q[4 * ch + 3], a.w, g0);
-        g1 = fmaf(q[4 * ch + 7], b.w, g1);
-    }
-    const float4 rc = st[8];   // R, |c|^2, 0, 0
-    const f32 s = nqi + rc.y;
-    const f32 lower = fmaf(-2.0f, g0 + g1, s) - fmaf(s, 0x1p-16f, 0x1p-120f);
-    const f32 t = dk + rc.x;
-    const f32 rhs = t * t * (1.0f + 0x1p-10f);
-    return !(lower > rhs && lower <= 3.4e38f);
 }
 
 // ---- tile order ------------------------------------------------------------
@@ -506,14 +471,14 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         const u32 i = q0 + row;   // regrouped index of this thread's query
         const bool active = i < n;
         const f32 nqi = active ? nq[i] : 0.0f;
-        f32 q[TC_DIM];
-#pragma unroll
-        for (int c = 0; c < TC_DIM; ++c) q[c] = active ? xp[u64(i) * TC_DIM + c] : 0.0f;
+        // Sorted list; its first TC_K - k slots hold -inf sentinels, so the
+        // k-th entry is always ld[TC_K - 1] (every index a compile-time
+        // constant: the list stays in registers).
         f32 ld[TC_K];
         u32 lj[TC_K];
 #pragma unroll
         for (int t = 0; t < TC_K; ++t) {
-            ld[t] = INFINITY;
+            ld[t] = u32(t) < TC_K - k ? -INFINITY : INFINITY;
             lj[t] = 0xffffffffu;
         }
         f32 rq = INFINITY;   // candidate passes iff -2 D <= rq (D: the augmented product)
@@ -541,10 +506,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         };
         // filter bound from the k-th entry; +inf until the list holds k
         auto update_rq = [&]() {
-            f32 d = INFINITY;
-#pragma unroll
-            for (int s = 0; s < TC_K; ++s)
-                if (s == int(k) - 1) d = ld[s];
+            const f32 d = ld[TC_K - 1];
             dk = d;
             // the filter's relative error bounds need |q|^2 far above the
             // subnormal range: below 2^-60 every candidate is evaluated
@@ -596,19 +558,26 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             if (sp + w < ntiles) prefetch(sp + w);   // the next batch starts at sp + w
             u32 m = 0;
             if (acc == ~0u) {
-                if (active) {
-#pragma unroll 1
-                    for (u32 b = 0; b < w; ++b)
-                        if (sp + b < ntiles && tile_needed(q, nqi, dk, S.tst + b * 9)) m |= 1u << b;
-                }
+                // before the first tile: every k-th distance is +inf, every
+                // tile is needed
+                if (active) m = (w >= 32 ? ~0u : (1u << w) - 1u) & (ntiles - sp >= 32 ? ~0u : (1u << (ntiles - sp)) - 1u);
             } else {
                 // G = q . c for the 128 queries x 16 centroids on the tensor
                 // core. The centroids are TF32-exact and the queries lose at
                 // most 2^-10 relative in TF32, so |G~ - q.c| <= 2^-10 |q||c|
                 // (FP32 accumulation included) <= 2^-11 (|q|^2 + |c|^2), and
-                // |q|^2 + |c|^2 - 2 G~ - 2^-8 (|q|^2 + |c|^2) is a lower bound
-                // of |q - c|^2 with room for the FP32 roundings; the test is
-                // then tile_needed's (skip iff |q - c| > dk + R).
+                // `lower` = |q|^2 + |c|^2 - 2 G~ - 2^-8 (|q|^2 + |c|^2) - 2^-120
+                // is a lower bound of |q - c|^2 with room for the FP32
+                // roundings (the absolute term covers subnormal products).
+                // A tile is skipped when lower > (dk + R)^2 (1 + 2^-10): that
+                // exceeds (dk + R~)^2 (1 + 2^-11), the computed radius R~ is
+                // within 2^-18 of the true maximum distance to the centre, so
+                // every point x of the tile has |q - x| >= |q - c| - R >
+                // dk (1 + 2^-12.5), and its lane-ordered FP32 distance
+                // (relative error < 2^-18) exceeds dk: it can neither beat nor
+                // tie the k-th entry. dk below 2^-50, |q|^2 below 2^-60 (where
+                // underflow defeats relative bounds), any non-finite value and
+                // any NaN keep the tile.
                 if (tid == 0) {
                     tc_fence_after();
 #pragma unroll
@@ -788,10 +757,13 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                             gm[g] = u == u ? u : INFINITY;   // no candidate (or NaN): no bound
                         }
                         bitonic_sort<32>(gm);
+                        // B = gm[k - 1] by a bit-mask select (an opaque mask, so the
+                        // compiler keeps gm in registers instead of indexing it)
+                        u32 ksel = 1u << (k - 1);
+                        asm volatile("" : "+r"(ksel));
                         f32 B = INFINITY;
 #pragma unroll
-                        for (int g = 0; g < TC_K; ++g)
-                            if (g == int(k) - 1) B = gm[g];
+                        for (int g = 0; g < TC_K; ++g) B = (ksel >> g) & 1u ? gm[g] : B;
                         const f32 Bp = B * (1.0f + 0x1p-12f);
                         // (relative bounds: |q|^2 far above the subnormal range)
                         const f32 t2 = B < INFINITY && nqi >= 0x1p-60f
@@ -814,6 +786,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                         }
                     }
                     bool changed = false;
+                    f32 qa[TC_DIM];   // this thread's query, from the query tile
+                    swz_row(S.a, row, qa);
 #pragma unroll 1
                     for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
 #pragma unroll 1
@@ -821,7 +795,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                             const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
                             f32 cb[TC_DIM];
                             swz_row(bt, rr, cb);
-                            changed |= consider(oid[rr], __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{q}, RegVec<TC_DIM>{cb}, TC_DIM)));
+                            changed |= consider(oid[rr], __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{qa}, RegVec<TC_DIM>{cb}, TC_DIM)));
                         }
                     }
                     if (changed) update_rq();
@@ -892,11 +866,12 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         tiles_done += nl;
         if (active) {
             const u32 oi = oids[i];
+            const u32 first = TC_K - k;   // entries [first, TC_K) are the k results
 #pragma unroll
             for (int s = 0; s < TC_K; ++s)
-                if (s < int(k)) {
-                    ids[u64(oi) * k + s] = lj[s];
-                    if (dists) dists[u64(oi) * k + s] = ld[s];
+                if (u32(s) >= first) {
+                    ids[u64(oi) * k + (s - first)] = lj[s];
+                    if (dists) dists[u64(oi) * k + (s - first)] = ld[s];
                 }
         }
         __syncthreads();
