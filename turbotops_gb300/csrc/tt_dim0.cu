@@ -146,13 +146,15 @@ __global__ void k_edge_fill(Rows rows, u32 n, f32 thr, const u64* __restrict__ o
     }
 }
 
-// Sorted (dbits, q) pairs -> packed filtration keys.
+// Sorted (dbits, q) pairs -> packed filtration keys; inv[q] = sorted
+// position of the edge that index order puts at q.
 __global__ void k_edge_pack(const u64* __restrict__ skey, const u64* __restrict__ sidx, u64 m, int redzed,
-                            u64* __restrict__ keys) {
+                            u64* __restrict__ keys, u32* __restrict__ inv) {
     for (u64 r = u64(blockIdx.x) * blockDim.x + threadIdx.x; r < m; r += u64(gridDim.x) * blockDim.x) {
         const u64 k = skey[r];
         const u64 idx = sidx[u32(k)];
         keys[r] = ((k >> 32) << kIdxBits) | (redzed ? idx : kIdxMask - idx);
+        inv[u32(k)] = u32(r);
     }
 }
 
@@ -229,9 +231,13 @@ struct CsrCx {
     }
 };
 
-__global__ void k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, u64 m, u8* __restrict__ app,
-                               u32* __restrict__ emw, u8* __restrict__ emf) {
-    for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
+// Edges are visited in index order (inv: index order -> sorted position), so
+// neighbouring threads share the larger vertex's row; results go to the
+// edge's sorted position.
+__global__ void k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, const u32* __restrict__ inv, u64 m,
+                               u8* __restrict__ app, u32* __restrict__ emw, u8* __restrict__ emf) {
+    for (u64 t = u64(blockIdx.x) * blockDim.x + threadIdx.x; t < m; t += u64(gridDim.x) * blockDim.x) {
+        const u64 e = inv[t];
         const u64 key = keys[e];
         const f32 d = key_d(key);
         const u64 idx = key_idx(key);
@@ -376,6 +382,7 @@ inline u32 grid_for(u64 work, u32 per_block) {
 // sort on the distance bits alone gives the filtration order: 4 passes of 8
 // bits for distances within one binade pair, instead of a full 64-bit key
 // sort. Slots: S_EDGE_CNT, S_EDGE_SORT, S_EDGE_IDX, S_EDGE_KEYS (result),
+// S_EDGE_INV (result: index order -> sorted position),
 // and the sort's own (S_SORT_A, S_SORT_HIST, S_SCAN*, S_MISC3).
 static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys_out) {
     const u32 n = cx.n;
@@ -406,7 +413,8 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
         TT_LAUNCH("k_edge_fill");
         u64* kb = c->arena.get<u64>(S_SORT_A, m);
         const bool sw = radix_sort<u32>(c, skey, static_cast<u32*>(nullptr), m, kb, static_cast<u32*>(nullptr), 0, 32);
-        k_edge_pack<<<grid_for(m, 256), 256, 0, c->stream>>>(sw ? kb : skey, sidx, m, redzed, keys);
+        u32* inv = c->arena.get<u32>(S_EDGE_INV, m + 1);
+        k_edge_pack<<<grid_for(m, 256), 256, 0, c->stream>>>(sw ? kb : skey, sidx, m, redzed, keys, inv);
         TT_LAUNCH("k_edge_pack");
         c->launches += 2;
     }
@@ -431,8 +439,9 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
         if (cx.mat)
             k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, c->stream>>>(cx.mat, n, out.keys, m, app, emw, emf);
         else
-            k_apparent_csr<<<grid_for(m, 256), 256, 0, c->stream>>>(CsrCx{cx.rp, cx.ci, cx.w}, out.keys, m, app, emw,
-                                                                     emf);
+            k_apparent_csr<<<grid_for(m, 256), 256, 0, c->stream>>>(CsrCx{cx.rp, cx.ci, cx.w}, out.keys,
+                                                                     c->arena.get<u32>(S_EDGE_INV, m + 1), m, app,
+                                                                     emw, emf);
         TT_LAUNCH("k_apparent");
         ++c->launches;
     }
