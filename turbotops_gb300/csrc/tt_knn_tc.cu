@@ -67,7 +67,7 @@ constexpr u32 TC_TEST = 16;                     // tiles tested per lookahead ba
 constexpr int ST_STRIDE = 36;                   // floats per tile record: centroid, R, |centroid|^2, pad
 constexpr u32 TST_F4 = TC_TEST * (ST_STRIDE / 4);   // float4 per lookahead batch of tile records
 static_assert(TST_F4 > 128 && TST_F4 <= 256, "two records' float4 per thread");
-constexpr int MAX_PIV = 256;
+constexpr int MAX_PIV = 128;
 constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
 static_assert(NSTAGE == 2, "the stage bookkeeping below assumes two stages");
 static_assert(TC_M == TC_N, "query blocks and candidate tiles share one tiling");
@@ -257,36 +257,41 @@ __device__ __forceinline__ u32 spiral_tile(u32 B, u32 s, u32 ntiles) {
 // Pivots: rows floor(p n / P) of x; rank[p] = position of pivot p on a
 // nearest-first chain from pivot 0 (ties to the lower index), so that
 // pivots of one region of space sit next to each other in the order.
-// One warp: lane l owns pivots l, l + 32, ...; each chain step is a warp
-// argmin (no block barriers).
-__global__ void __launch_bounds__(32) k_tc_pivots(const f32* __restrict__ x, u32 n, u32 P, f32* __restrict__ piv,
-                                                  u32* __restrict__ rank) {
-    __shared__ f32 pv[MAX_PIV][TC_DIM + 1];
-    const u32 lane = threadIdx.x;
-    for (u32 p = lane; p < P; p += 32) {
-        const u64 r = u64(p) * n / P;
-#pragma unroll 4
-        for (int k = 0; k < TC_DIM; ++k) {
-            pv[p][k] = x[r * TC_DIM + k];
-            piv[u64(p) * TC_DIM + k] = pv[p][k];
-        }
+// The block fills the P x P distance matrix in shared memory; one warp then
+// walks the chain (a warp argmin over one matrix row per step).
+__global__ void __launch_bounds__(256) k_tc_pivots(const f32* __restrict__ x, u32 n, u32 P, f32* __restrict__ piv,
+                                                   u32* __restrict__ rank) {
+    extern __shared__ f32 psm[];
+    f32* pv = psm;                       // P x (TC_DIM + 1)
+    f32* dm = psm + P * (TC_DIM + 1);    // P x P
+    for (u32 t = threadIdx.x; t < P * TC_DIM; t += blockDim.x) {
+        const u32 p = t / TC_DIM, k = t % TC_DIM;
+        const f32 v = x[(u64(p) * n / P) * TC_DIM + k];
+        pv[p * (TC_DIM + 1) + k] = v;
+        piv[u64(p) * TC_DIM + k] = v;
     }
+    __syncthreads();
+    for (u32 t = threadIdx.x; t < P * P; t += blockDim.x) {
+        const u32 p = t / P, r = t % P;
+        f32 d = 0.0f;
+#pragma unroll 8
+        for (int k = 0; k < TC_DIM; ++k) {
+            const f32 u = pv[p * (TC_DIM + 1) + k] - pv[r * (TC_DIM + 1) + k];
+            d = fmaf(u, u, d);
+        }
+        dm[t] = d;
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    const u32 lane = threadIdx.x;
     u32 visited = lane == 0 ? 1u : 0u;   // bit i: pivot lane + 32 i is on the chain
     if (lane == 0) rank[0] = 0;
-    __syncwarp();
     u32 cur = 0;
     for (u32 step = 1; step < P; ++step) {
         unsigned long long key = ~0ull;
-        for (u32 i = 0, p = lane; p < P; ++i, p += 32) {
-            if ((visited >> i) & 1u) continue;
-            f32 d = 0.0f;
-#pragma unroll 8
-            for (int k = 0; k < TC_DIM; ++k) {
-                const f32 t = pv[p][k] - pv[cur][k];
-                d = fmaf(t, t, d);
-            }
-            key = min(key, (unsigned long long)((u64(fbits(d)) << 32) | p));
-        }
+        for (u32 i = 0, p = lane; p < P; ++i, p += 32)
+            if (!((visited >> i) & 1u))
+                key = min(key, (unsigned long long)((u64(fbits(dm[cur * P + p])) << 32) | p));
 #pragma unroll
         for (int o = 16; o; o >>= 1) key = min(key, (unsigned long long)__shfl_xor_sync(0xffffffffu, key, o));
         cur = u32(key & 0xffffffffu);
@@ -924,7 +929,9 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
         u32* rank = reinterpret_cast<u32*>(piv + u64(P) * TC_DIM);
         u64* key = c->arena.get<u64>(S_TC_KEYS, n);
         u32* val = c->arena.get<u32>(S_TC_VALS, n);
-        k_tc_pivots<<<1, 32, 0, c->stream>>>(x, n, P, piv, rank);
+        const size_t psmem = (size_t(P) * (TC_DIM + 1) + size_t(P) * P) * sizeof(f32);
+        TT_CUDA(cudaFuncSetAttribute(k_tc_pivots, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psmem)));
+        k_tc_pivots<<<1, 256, psmem, c->stream>>>(x, n, P, piv, rank);
         TT_LAUNCH("k_tc_pivots");
         k_tc_assign<<<div_up(n, 256), 256, P * TC_DIM * sizeof(f32), c->stream>>>(x, n, piv, rank, P, key, val);
         TT_LAUNCH("k_tc_assign");
