@@ -303,12 +303,15 @@ def run_gpu(args, ws, rank, local):
     achieved = gram_flops / (knn_ms * 1e-3) / 1e12
     fp32_ops = N * N * (3.0 * DIM)            # sub + mul/fma + add per coordinate, exhaustive exact path
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "knn_tc_traffic.json")
+    tf = os.path.join(ROOT, "profiles", "knn_tc_l2_dim32.md")
     if tc_path and os.path.exists(tf):
+        # DRAM bytes of one k_knn_tc launch, from one ncu capture of this
+        # workload (the summary's "traffic:" line)
+        import re
         with open(tf) as f:
-            tj = json.load(f)
-        # DRAM bytes of one k_knn_tc launch (ncu) scaled by the tiles computed here
-        traffic = tj["dram_bytes"] * (tiles / tj["tiles"]) if tj.get("tiles") else tj["dram_bytes"]
+            mt = re.search(r"^traffic: dram_bytes_per_launch=(\d+) points=(\d+) dim=(\d+) k=(\d+)", f.read(), re.M)
+        if mt and (int(mt.group(2)), int(mt.group(3)), int(mt.group(4))) == (N, DIM, K):
+            traffic = int(mt.group(1))
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
