@@ -29,6 +29,29 @@ int guard(tt_ctx* c, F&& f) {
     }
 }
 
+// Any non-finite coordinate among count floats of a device buffer? (One
+// pass on the device instead of a scalar host loop over the caller's array.)
+__global__ void k_nonfinite(const f32* __restrict__ x, u64 count, u32* __restrict__ flag) {
+    u32 bad = 0;
+    for (u64 i = u64(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += u64(gridDim.x) * blockDim.x)
+        bad |= (__float_as_uint(x[i]) & 0x7f800000u) == 0x7f800000u;
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+void check_finite_dev(tt_ctx* c, const f32* x, u64 count) {
+    if (!count) return;
+    u32* flag = c->arena.get<u32>(S_MISC2, 4);
+    TT_CUDA(cudaMemsetAsync(flag, 0, sizeof(u32), c->stream));
+    const u32 grid = u32(std::min<u64>((count + 255) / 256, 4ull * u64(c->sms)));
+    k_nonfinite<<<grid, 256, 0, c->stream>>>(x, count, flag);
+    TT_LAUNCH("k_nonfinite");
+    ++c->launches;
+    u32 h = 0;
+    TT_CUDA(cudaMemcpyAsync(&h, flag, sizeof(u32), cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaStreamSynchronize(c->stream));
+    if (h) invalid("persistence: non-finite coordinate");
+}
+
 void check_metric(int kind, float p) {
     if (kind < TT_METRIC_L1 || kind > TT_METRIC_LP) invalid("metric: unknown kind");
     if (kind == TT_METRIC_LP && !(p >= 1.0f)) invalid("metric: p must be in [1, inf]");
@@ -302,10 +325,9 @@ int tt_knn_graph_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int ki
     return guard(c, [&] {
         check_metric(kind, p);
         if (k == 0) invalid("persistence: k must be >= 1");
-        for (u64 i = 0; i < u64(n) * dim; ++i)
-            if (!std::isfinite(x_h[i])) invalid("persistence: non-finite coordinate");
         f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
         if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
+        check_finite_dev(c, x, u64(n) * dim);
         const u32 kk = n ? std::min<u32>(k, n - 1) : 0;
         u64* rp = c->arena.get<u64>(S_OUT0, u64(n) + 1);
         u32* ci = nullptr;
@@ -350,10 +372,9 @@ int tt_knn_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int ki
     return guard(c, [&] {
         check_metric(kind, p);
         if (k == 0) invalid("persistence: k must be >= 1");
-        for (u64 i = 0; i < u64(n) * dim; ++i)
-            if (!std::isfinite(x_h[i])) invalid("persistence: non-finite coordinate");
         f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
         if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
+        check_finite_dev(c, x, u64(n) * dim);
         u64* rp = nullptr;
         u32* gci = nullptr;
         f32* gw = nullptr;
@@ -393,11 +414,10 @@ int tt_dense_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int 
         if (!thr_inout) invalid("gb300: null threshold");
         const float t = *thr_inout;
         if (std::isnan(t) || t < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
-        for (u64 i = 0; i < u64(n) * dim; ++i)
-            if (!std::isfinite(x_h[i])) invalid("persistence: non-finite coordinate");
         f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
-        f32* mat = c->arena.get<f32>(S_MAT, u64(n) * n + 1);
         if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
+        check_finite_dev(c, x, u64(n) * dim);
+        f32* mat = c->arena.get<f32>(S_MAT, u64(n) * n + 1);
         u32* rowmax = c->arena.get<u32>(S_ROWMAX, u64(n) + 1);
         dense_matrix(c, x, n, dim, kind, p, mat, std::isinf(t) ? rowmax : nullptr);
         float thr = t;
