@@ -20,14 +20,22 @@ def _ptr(a):
     return P(a.ctypes.data) if a is not None else None
 
 
-def _front_h(x, k, maxdim=1):
+def _front_h(x, k, maxdim=1, pinned=False):
     c = ctx()
     n, dim = x.shape
     kind, p = capi.metric_parse("l2")
     cap = 2 * n * k + 16
-    rp = np.zeros(n + 1, np.uint64)
-    col = np.zeros(cap, np.uint32)
-    w = np.zeros(cap, np.float32)
+    if pinned:
+        import torch
+        keep = [torch.zeros((n + 1) * 8 + cap * 8, dtype=torch.uint8).pin_memory()]
+        buf = keep[0].numpy()
+        rp = buf[:(n + 1) * 8].view(np.uint64)
+        col = buf[(n + 1) * 8:(n + 1) * 8 + cap * 4].view(np.uint32)
+        w = buf[(n + 1) * 8 + cap * 4:].view(np.float32)
+    else:
+        rp = np.zeros(n + 1, np.uint64)
+        col = np.zeros(cap, np.uint32)
+        w = np.zeros(cap, np.float32)
     h0 = np.zeros(max(n, 1), np.float32)
     cidx = np.zeros(cap, np.uint64)
     cd = np.zeros(cap, np.float32)
@@ -37,16 +45,17 @@ def _front_h(x, k, maxdim=1):
     st = c.L.tt_knn_front_h(c.h, _ptr(x), n, dim, kind, p, k, maxdim, _ptr(rp), _ptr(col), _ptr(w), cap,
                             C.byref(nnz), _ptr(h0), C.byref(nh0), C.byref(ess), _ptr(cidx), _ptr(cd), _ptr(cf),
                             _ptr(ca), cap, C.byref(ncols), C.byref(nedges))
-    return st, dict(rp=rp, col=col[:nnz.value], w=w[:nnz.value], h0=h0[:nh0.value], essential=ess.value,
-                    cidx=cidx[:ncols.value], cd=cd[:ncols.value], cf=cf[:ncols.value], ca=ca[:ncols.value],
-                    edges=nedges.value)
+    return st, dict(rp=rp.copy(), col=col[:nnz.value].copy(), w=w[:nnz.value].copy(), h0=h0[:nh0.value],
+                    essential=ess.value, cidx=cidx[:ncols.value], cd=cd[:ncols.value], cf=cf[:ncols.value],
+                    ca=ca[:ncols.value], edges=nedges.value)
 
 
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("kind,n,k", [("gmm", 3000, 15), ("gauss", 800, 7)])
-def test_knn_front_h_equals_device_path(kind, n, k):
+def test_knn_front_h_equals_device_path(kind, n, k, pinned):
     x = synth.gmm(n, 32, seed=n) if kind == "gmm" else synth.gauss(n, 5, n)
     x = np.ascontiguousarray(x, np.float32)
-    st, r = _front_h(x, k)
+    st, r = _front_h(x, k, pinned=pinned)
     assert st == capi.OK
     rp, ci, w = ops.knn_graph(ctx(), dev(x), k, "l2")
     assert np.array_equal(r["rp"], host(rp).view(np.uint64))

@@ -72,10 +72,31 @@ void fill_dim0(const Dim0Out& r, tt_dim0_out* out) {
     out->essential = r.essential;
 }
 
+// Is p page-locked host memory (so that copies into it are asynchronous)?
+bool pinned_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// The context's second stream, ordered after everything enqueued on its
+// main stream so far.
+cudaStream_t aux_after_main(tt_ctx* c) {
+    if (!c->aux) TT_CUDA(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    if (!c->aux_ev) TT_CUDA(cudaEventCreateWithFlags(&c->aux_ev, cudaEventDisableTiming));
+    TT_CUDA(cudaEventRecord(c->aux_ev, c->stream));
+    TT_CUDA(cudaStreamWaitEvent(c->aux, c->aux_ev, 0));
+    return c->aux;
+}
+
 // knn_lists_exact -> knn_graph -> dim0 on the device. The graph is moved into
 // slots that dim0 does not use, so both results stay valid together.
+template <typename AfterGraph>
 u64 knn_front_dev(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32 maxdim, u64** rp_out,
-                  u32** ci_out, f32** w_out, Dim0Out& r) {
+                  u32** ci_out, f32** w_out, Dim0Out& r, AfterGraph&& after_graph) {
     const u32 kk = n ? std::min<u32>(k, n - 1) : 0;
     u64* rp = c->arena.get<u64>(S_GRAPH_RP, u64(n) + 1);
     u32* ci = nullptr;
@@ -87,6 +108,7 @@ u64 knn_front_dev(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 
         TT_CUDA(cudaMemcpyAsync(gci, ci, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
         TT_CUDA(cudaMemcpyAsync(gw, w, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
     }
+    after_graph(nnz, rp, gci, gw);   // before dim0: the graph is final here
     Complex cx{nullptr, rp, gci, gw, n, INFINITY};
     dim0(c, cx, maxdim, r);
     *rp_out = rp;
@@ -134,6 +156,11 @@ void tt_ctx_destroy(tt_ctx* c) {
     c->arena.release();
     c->pinned.release();
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    if (c->aux) {
+        cudaStreamSynchronize(c->aux);
+        cudaStreamDestroy(c->aux);
+    }
+    if (c->aux_ev) cudaEventDestroy(c->aux_ev);
     delete c;
 }
 
@@ -354,7 +381,7 @@ int tt_knn_front(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, 
         u32* ci = nullptr;
         f32* w = nullptr;
         Dim0Out r;
-        const u64 nnz = knn_front_dev(c, x, n, dim, kind, p, k, maxdim, &rp, &ci, &w, r);
+        const u64 nnz = knn_front_dev(c, x, n, dim, kind, p, k, maxdim, &rp, &ci, &w, r, [](u64, u64*, u32*, f32*) {});
         out->graph.n = n;
         out->graph.nnz = nnz;
         out->graph.row_ptr_dev = rp;
@@ -379,14 +406,34 @@ int tt_knn_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int ki
         u32* gci = nullptr;
         f32* gw = nullptr;
         Dim0Out r;
-        const u64 nnz = knn_front_dev(c, x, n, dim, kind, p, k, maxdim, &rp, &gci, &gw, r);
-        if (nnz_out) *nnz_out = nnz;
-        if (nnz > cap) throw Error(TT_ERR_LENGTH, "gb300: graph exceeds the output capacity");
-        TT_CUDA(cudaMemcpyAsync(rp_h, rp, 8 * (u64(n) + 1), cudaMemcpyDeviceToHost, c->stream));
-        if (nnz) {
-            TT_CUDA(cudaMemcpyAsync(col_h, gci, 4 * nnz, cudaMemcpyDeviceToHost, c->stream));
-            TT_CUDA(cudaMemcpyAsync(w_h, gw, 4 * nnz, cudaMemcpyDeviceToHost, c->stream));
-        }
+        // The graph is final before dim0 starts: into page-locked buffers it
+        // is copied on the context's second stream while dim0 runs.
+        bool early = false;
+        auto copy_graph = [&](cudaStream_t s, u64 nnz, const u64* rpd, const u32* cid, const f32* wd) {
+            TT_CUDA(cudaMemcpyAsync(rp_h, rpd, 8 * (u64(n) + 1), cudaMemcpyDeviceToHost, s));
+            if (nnz) {
+                TT_CUDA(cudaMemcpyAsync(col_h, cid, 4 * nnz, cudaMemcpyDeviceToHost, s));
+                TT_CUDA(cudaMemcpyAsync(w_h, wd, 4 * nnz, cudaMemcpyDeviceToHost, s));
+            }
+        };
+        struct AuxDrain {   // no copy outlives the call, whatever path leaves it
+            tt_ctx* c;
+            bool& on;
+            ~AuxDrain() {
+                if (on) cudaStreamSynchronize(c->aux);
+            }
+        } drain{c, early};
+        const u64 nnz = knn_front_dev(c, x, n, dim, kind, p, k, maxdim, &rp, &gci, &gw, r,
+                                      [&](u64 m, u64* rpd, u32* cid, f32* wd) {
+                                          if (nnz_out) *nnz_out = m;
+                                          if (m > cap)
+                                              throw Error(TT_ERR_LENGTH, "gb300: graph exceeds the output capacity");
+                                          if (pinned_host(rp_h) && (!m || (pinned_host(col_h) && pinned_host(w_h)))) {
+                                              copy_graph(aux_after_main(c), m, rpd, cid, wd);
+                                              early = true;
+                                          }
+                                      });
+        if (!early) copy_graph(c->stream, nnz, rp, gci, gw);
         if (h0_h && r.nh0)
             TT_CUDA(cudaMemcpyAsync(h0_h, r.h0, sizeof(f32) * r.nh0, cudaMemcpyDeviceToHost, c->stream));
         if (nh0) *nh0 = r.nh0;
@@ -402,6 +449,10 @@ int tt_knn_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int ki
                 TT_CUDA(cudaMemcpyAsync(col_cf_app_h, r.emf, r.ncols, cudaMemcpyDeviceToHost, c->stream));
         }
         TT_CUDA(cudaStreamSynchronize(c->stream));
+        if (early) {
+            early = false;
+            TT_CUDA(cudaStreamSynchronize(c->aux));
+        }
     });
 }
 

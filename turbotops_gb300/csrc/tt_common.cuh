@@ -145,4 +145,6 @@ struct tt_ctx {
     int knn_mode = 0;               // 0 auto, 1 exhaustive scan, 2 tensor-core filter where applicable
     uint64_t filter_evals = 0;      // exact evaluations the last tensor-core kNN let through
     uint64_t filter_tiles = 0;      // 128 x 128 Gram tiles the last tensor-core kNN computed
+    cudaStream_t aux = nullptr;     // copies overlapped with compute (created on first use)
+    cudaEvent_t aux_ev = nullptr;
 };
