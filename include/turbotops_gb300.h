@@ -291,6 +291,16 @@ typedef struct tt_barcode {
  * GPU front end limits: maxdim <= 2 (dense) / <= 1 (graph input). */
 int tt_persistence_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t maxdim,
                      float threshold, int knn, uint32_t k, tt_barcode** out);
+/* tops::persistence(const CsrGraph&, maxdim, threshold, threads, mode)
+ * (turbotops.hpp:179-207): the flag complex of a weighted graph given as
+ * host CSR arrays (row_ptr n + 1 entries, 2m columns and weights). The graph
+ * must satisfy CsrGraph::valid() (core.hpp:137-148: row_ptr[0] = 0, even
+ * entry count, columns < n, no self loops, rows strictly ascending, the
+ * weight of (v, u) equal to that of (u, v)); otherwise TT_ERR_INVALID with
+ * the reference's message. Edges with weight <= threshold are kept. GPU
+ * front end limit: maxdim <= 1. */
+int tt_persistence_graph_h(tt_ctx* ctx, const uint64_t* row_ptr_h, const uint32_t* col_h, const float* weight_h,
+                           uint32_t n, uint32_t maxdim, float threshold, tt_barcode** out);
 void tt_barcode_free(tt_barcode* b);
 
 #ifdef __cplusplus

@@ -165,11 +165,19 @@ if __name__ == "__main__":
 
 def cli_cases() -> None:
     """Exact-text diagrams of the reference CLI on small hand-checkable inputs."""
-    inputs = {"sq": "0 0\n1 0\n1 1\n0 1\n", "tri": "0 0\n1 0\n0 1\n"}
+    inputs = {"sq": "0 0\n1 0\n1 1\n0 1\n", "tri": "0 0\n1 0\n0 1\n",
+              # weighted edge lists (--edges): a 4-cycle with one chord; repeated edges, a self
+              # loop, a comment and comma separators; a 6-cycle (one H1 bar that never dies)
+              "ecyc": "0 1 1\n1 2 1\n2 3 1\n3 0 1\n0 2 1.5\n",
+              "edup": "0 1 2\n1 0 1\n1 2 1\n2 0 3\n3 3 0\n# comment\n2,3,0.5\n0\t3\t2.5\n",
+              "ehex": "0 1 1\n1 2 1\n2 3 1\n3 4 1\n4 5 1\n5 0 1\n"}
     runs = [("sq", ["--maxdim", "1"]), ("sq", ["--maxdim", "1", "--metric", "l1"]),
             ("sq", ["--maxdim", "1", "--metric", "linf"]), ("sq", ["--maxdim", "1", "--metric", "lp:3"]),
             ("sq", ["--maxdim", "1", "--threshold", "1"]), ("tri", []),
-            ("sq", ["--graph", "knn", "-k", "2", "--maxdim", "1"]), ("sq", ["--maxdim", "2"])]
+            ("sq", ["--graph", "knn", "-k", "2", "--maxdim", "1"]), ("sq", ["--maxdim", "2"]),
+            ("ecyc", ["--edges", "--maxdim", "1"]), ("ecyc", ["--edges", "--maxdim", "1", "--threshold", "1"]),
+            ("edup", ["--edges", "--maxdim", "1"]), ("ehex", ["--edges", "--maxdim", "1"]),
+            ("ehex", ["--edges"])]
     out = []
     with tempfile.TemporaryDirectory() as td:
         for name, text in inputs.items():

@@ -75,3 +75,52 @@ def test_cli_rejects_bad_rows_metric_and_flags(tmp_path):
     assert r.returncode == 2 and "--graph must be full or knn" in r.stderr
     r = cli("run", str(q), "--mode", "sideways")
     assert r.returncode == 2 and "mode must be auto, boundary or coboundary" in r.stderr
+
+
+@pytest.mark.parametrize("text,msg", [
+    ("0 1\n", "in.txt:1: expected 'i j w'"),
+    ("0 1 1\n1 2 -1\n", "in.txt:2: bad weight"),
+    ("0 1 nan\n", "in.txt:1: bad weight"),
+    ("0 x 1\n", "bad vertex 'x'"),
+    ("0 1 w\n", "bad weight 'w'"),
+    ("0 4294967295 1\n", "vertex id too large"),
+    ("# nothing\n3 3 1\n", "in.txt: no vertices (empty edge list?)"),
+])
+def test_cli_edges_errors_exit_2(text, msg, tmp_path):
+    """Edge-list input errors (src/turbotops.cpp:173-205, :879-882), before any GPU work."""
+    p = tmp_path / "in.txt"
+    p.write_text(text)
+    r = cli("run", str(p), "--edges")
+    assert r.returncode == 2 and r.stderr.startswith("turbotops: ") and msg in r.stderr, r.stderr
+
+
+def test_symmetric_rows_matches_reference_ingestion():
+    """Both directions of every entry, self loops dropped, the smallest weight of a
+    repeated (row, column), rows sorted: checked against a direct restatement of
+    the reference's per-row vectors (python/turbotops_ext.cpp:82-98)."""
+    import numpy as np
+    from turbotops_gb300.api import symmetric_rows
+    rng = np.random.default_rng(5)
+    n = 60
+    i = rng.integers(0, n, 900)
+    j = rng.integers(0, n, 900)
+    w = rng.integers(0, 8, 900).astype(np.float32) * np.float32(0.5)
+    rp, ci, ww = symmetric_rows(i, j, w, n)
+    rows = [[] for _ in range(n)]
+    for a, b, d in zip(i, j, w):
+        if a == b:
+            continue
+        rows[a].append((int(b), float(d)))
+        rows[b].append((int(a), float(d)))
+    exp_rp, exp_ci, exp_w = [0], [], []
+    for r in rows:
+        r.sort()
+        seen = set()
+        for b, d in r:
+            if b in seen:
+                continue
+            seen.add(b)
+            exp_ci.append(b)
+            exp_w.append(d)
+        exp_rp.append(len(exp_ci))
+    assert rp.tolist() == exp_rp and ci.tolist() == exp_ci and ww.tolist() == exp_w

@@ -118,3 +118,51 @@ def test_persistence_validation_messages():
         tg.persistence(y)
     with pytest.raises(ValueError, match="unknown 'cosine'"):
         tg.persistence(x, metric="cosine")
+
+
+def test_graph_input_equals_point_knn_path():
+    """persistence(CsrGraph) on the kNN graph of a cloud is the same flag
+    complex as persistence(points, graph='knn'): identical diagrams."""
+    import numpy as np
+    from turbotops_gb300 import api, ops, synth
+    from gpu_util import ctx, dev, host
+    x = synth.gauss(700, 6, 31)
+    d1, i1 = api.persistence(x, maxdim=1, graph="knn", k=8)
+    rp, ci, w = ops.knn_graph(ctx(), dev(x), 8, "l2")
+    d2, i2 = api.persistence_graph(host(rp).view(np.uint64), host(ci).view(np.uint32), host(w), 700, maxdim=1)
+    assert np.array_equal(api.canonical(d1), api.canonical(d2))
+    assert i2["method"] == "sparse" and i2["edges"] == i1["edges"]
+    # a finite threshold keeps edges <= threshold
+    t = float(np.median(host(w)))
+    d3, _ = api.persistence_graph(host(rp).view(np.uint64), host(ci).view(np.uint32), host(w), 700, maxdim=1,
+                                  threshold=t)
+    assert all((b[:, 1][np.isfinite(b[:, 1])] <= t).all() for b in d3)
+
+
+def test_scipy_sparse_input_and_csr_validation():
+    import numpy as np
+    scipy_sparse = pytest.importorskip("scipy.sparse")
+    from turbotops_gb300 import api
+    # a one-directional, duplicated edge list: symmetrised, smallest weight kept
+    i = np.array([0, 1, 2, 3, 0, 1])
+    j = np.array([1, 2, 3, 0, 2, 0])
+    w = np.array([1, 1, 1, 1, 1.5, 0.5], np.float32)
+    g = scipy_sparse.coo_matrix((w, (i, j)), shape=(4, 4))
+    dg, info = api.persistence(g, maxdim=1)
+    rp, ci, ww = api.symmetric_rows(i, j, w, 4)
+    dg2, _ = api.persistence_graph(rp, ci, ww, 4, maxdim=1)
+    assert np.array_equal(api.canonical(dg), api.canonical(dg2))
+    assert sorted(dg[0][:, 1].tolist()) == [0.5, 1.0, 1.0, np.inf]
+    with pytest.raises(ValueError, match="weights must be finite and >= 0"):
+        api.persistence(scipy_sparse.coo_matrix((np.array([-1.0], np.float32), ([0], [1])), shape=(2, 2)))
+    # CsrGraph::valid(): asymmetric weights, unsorted rows, self loops
+    bad = [
+        (np.array([0, 1, 2], np.uint64), np.array([1, 0], np.uint32), np.array([1, 2], np.float32)),
+        (np.array([0, 2, 3, 4], np.uint64), np.array([2, 1, 0, 0], np.uint32), np.array([1, 1, 1, 1], np.float32)),
+        (np.array([0, 1, 1], np.uint64), np.array([0], np.uint32), np.array([1], np.float32)),
+    ]
+    for rp, ci, ww in bad:
+        with pytest.raises(ValueError, match="CsrGraph invariant violated"):
+            api.persistence_graph(rp, ci, ww, len(rp) - 1, maxdim=1)
+    with pytest.raises(ValueError, match="threshold must be non-negative"):
+        api.persistence_graph(rp, ci, ww, 4, maxdim=1, threshold=-1.0)

@@ -68,6 +68,7 @@ _SIGS = {
     "tt_assemble": (i32, [P, P, u32, f32, P, u64, P, u64, C.POINTER(u64), C.POINTER(P), C.POINTER(P),
                           C.POINTER(u64)]),
     "tt_persistence_h": (i32, [P, P, u32, u32, i32, f32, u32, f32, i32, u32, C.POINTER(C.POINTER(Barcode))]),
+    "tt_persistence_graph_h": (i32, [P, P, P, P, u32, u32, f32, C.POINTER(C.POINTER(Barcode))]),
     "tt_barcode_free": (None, [C.POINTER(Barcode)]),
     "tt_knn_front": (i32, [P, P, u32, u32, i32, f32, u32, u32, C.POINTER(KnnFrontOut)]),
     "tt_knn_front_h": (i32, [P, P, u32, u32, i32, f32, u32, u32, P, P, P, u64, C.POINTER(u64), P,

@@ -30,6 +30,7 @@ options:
   --graph full|knn    complex: all pairs, or the kNN graph (default full)
   -k N                neighbors for --graph knn (default 15)
   --dim D             coordinates per point for .bin input
+  --edges             input is a weighted edge list 'i j w' (0-based), one per line
   --mode M            boundary | coboundary | auto (diagrams never depend on it)
   --coboundary, --boundary, --no-coboundary, --engine E   accepted, as --mode
   --threads N         accepted (results never depend on it)
@@ -83,6 +84,53 @@ def read_text_points(path: str) -> np.ndarray:
     return np.asarray(rows, dtype=np.float32).reshape(len(rows), dim if rows else 0)
 
 
+def _parse_u64(tok: str, what: str) -> int:
+    """strtoull, base 10, whole token (src/turbotops.cpp:102-108): an optional
+    sign, '-' wrapping modulo 2^64; out of range is an error."""
+    body = tok[1:] if tok[:1] in "+-" else tok
+    if not body.isdigit():
+        raise CliError(f"bad {what} '{tok}'")
+    v = int(body)
+    if v > 0xFFFFFFFFFFFFFFFF:
+        raise CliError(f"bad {what} '{tok}'")
+    return (-v) % (1 << 64) if tok[:1] == "-" else v
+
+
+def read_edges(path: str):
+    """A weighted edge list 'i j w' (0-based), one per line (src/turbotops.cpp:173-205):
+    '#' comments, ',' and tabs as separators, self loops dropped, both
+    directions kept, the smallest weight of a repeated edge."""
+    from .api import symmetric_rows
+    try:
+        lines = open(path, "r", encoding="utf-8", errors="replace").read().split("\n")
+    except OSError:
+        raise CliError(f"cannot open {path}") from None
+    ii, jj, ww = [], [], []
+    n = 0
+    for lineno, line in enumerate(lines, 1):
+        line = line.split("#", 1)[0].replace(",", " ").replace("\t", " ")
+        toks = line.split()
+        if not toks:
+            continue
+        if len(toks) < 3:
+            raise CliError(f"{path}:{lineno}: expected 'i j w'")
+        i = _parse_u64(toks[0], "vertex")
+        j = _parse_u64(toks[1], "vertex")
+        d = _parse_f32(toks[2], "weight")
+        if i == j:
+            continue
+        if not (d >= 0) or not math.isfinite(d):
+            raise CliError(f"{path}:{lineno}: bad weight")
+        if max(i, j) >= 0xFFFFFFFF:
+            raise CliError("vertex id too large")
+        n = max(n, max(i, j) + 1)
+        ii.append(i)
+        jj.append(j)
+        ww.append(d)
+    rp, ci, w = symmetric_rows(np.array(ii, np.int64), np.array(jj, np.int64), np.array(ww, np.float32), n)
+    return rp, ci, w, n
+
+
 def read_bin_points(path: str, dim: int) -> np.ndarray:
     if not dim:
         raise CliError("--dim is required for .bin input")
@@ -101,7 +149,7 @@ def run(argv: list[str]) -> int:
         raise CliError("run: missing <input>\n" + USAGE)
     path = argv[0]
     o = {"maxdim": 1, "threshold": math.inf, "metric": "l2", "graph": "full", "k": 15, "dim": 0,
-         "output": None, "quiet": False}
+         "output": None, "quiet": False, "edges": False}
     it = iter(argv[1:])
     for a in it:
         def val():
@@ -138,7 +186,9 @@ def run(argv: list[str]) -> int:
             _parse_u32(val(), "threads")
         elif a == "--output":
             o["output"] = val()
-        elif a == "--edges" or a == "--approximate":
+        elif a == "--edges":
+            o["edges"] = True
+        elif a == "--approximate":
             raise CliError(f"{a} is not offered by the GPU front end")
         else:
             raise CliError(f"unknown option '{a}'")
@@ -148,10 +198,17 @@ def run(argv: list[str]) -> int:
             out_f = open(o["output"], "w")
         except OSError:
             raise CliError(f"cannot open {o['output']} for writing") from None
-    x = read_bin_points(path, o["dim"]) if path.endswith(".bin") else read_text_points(path)
     try:
-        dgms, info = api.persistence(x, maxdim=o["maxdim"], threshold=o["threshold"], metric=o["metric"],
-                                     graph=o["graph"], k=o["k"])
+        if o["edges"]:
+            rp, ci, w, nv = read_edges(path)
+            if not nv:
+                raise CliError(f"{path}: no vertices (empty edge list?)")
+            x = None
+            dgms, info = api.persistence_graph(rp, ci, w, nv, maxdim=o["maxdim"], threshold=o["threshold"])
+        else:
+            x = read_bin_points(path, o["dim"]) if path.endswith(".bin") else read_text_points(path)
+            dgms, info = api.persistence(x, maxdim=o["maxdim"], threshold=o["threshold"], metric=o["metric"],
+                                         graph=o["graph"], k=o["k"])
     except (ValueError, OverflowError, MemoryError) as e:
         raise CliError(str(e)) from None
     text = api.format_diagram(dgms)
@@ -159,9 +216,15 @@ def run(argv: list[str]) -> int:
     if out_f:
         out_f.close()
     if not o["quiet"]:
-        n, d = x.shape if x.size else (0, 0)
-        sys.stderr.write(f"turbotops: {n} points in R^{d}, method {info['method']}, threshold {info['threshold']:.9g}, "
-                         f"{info['edges']} edges, {info['seconds_total']:.3f} s\n")
+        if x is None:
+            sys.stderr.write(f"turbotops: graph with {nv} vertices, method {info['method']}, "
+                             f"threshold {info['threshold']:.9g}, {info['edges']} edges, "
+                             f"{info['seconds_total']:.3f} s\n")
+        else:
+            n, d = x.shape if x.size else (0, 0)
+            sys.stderr.write(f"turbotops: {n} points in R^{d}, method {info['method']}, "
+                             f"threshold {info['threshold']:.9g}, {info['edges']} edges, "
+                             f"{info['seconds_total']:.3f} s\n")
         for dd, g in enumerate(dgms):
             sys.stderr.write(f"  H{dd}: {len(g)} bars\n")
     return 0

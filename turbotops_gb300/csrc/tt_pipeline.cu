@@ -12,6 +12,7 @@
 // Engine choice (coboundary or RedZeD) never changes a diagram
 // (turbotops.hpp:19-25); this pipeline always reduces with the cohomology
 // reducer and reports the method it ran.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -80,6 +81,33 @@ std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim,
     out.columns.push_back(st.columns);
     out.emergent.push_back(st.emergent);
     return piv;
+}
+
+// Sparse front end on a device CSR graph (symmetric, rows sorted): dim0 on
+// the device, H0 bars, then compute_pairs(1) on the host over the host copy
+// of the graph (the caller's, or copied back here).
+void sparse_tail(tt_ctx* c, u64* rp, u32* gci, f32* gw, const u64* hrp_in, const u32* hci_in, const f32* hw_in, u32 n,
+                 u64 nnz, f32 thr, u32 maxdim, Result& out) {
+    Complex cx{nullptr, rp, gci, gw, n, thr};
+    Dim0Out r;
+    dim0(c, cx, maxdim, r);
+    out.edges = r.m;
+    h0_bars(c, r, out);
+    if (maxdim == 0) return;
+    if (maxdim >= 2) invalid("gb300: maxdim 2 on graph input is not supported by the GPU front end");
+    out.apparent.push_back(r.m - (n - r.essential) - r.ncols);
+    std::vector<u64> hrp;
+    std::vector<u32> hci;
+    std::vector<f32> hw;
+    if (!hrp_in) {
+        hrp = to_host(c, rp, u64(n) + 1);
+        hci = to_host(c, gci, nnz);
+        hw = to_host(c, gw, nnz);
+        sync(c);
+    }
+    host::HostComplex hc{nullptr, hrp_in ? hrp_in : hrp.data(), hci_in ? hci_in : hci.data(),
+                         hw_in ? hw_in : hw.data(), n, thr};
+    reduce_dim1(c, hc, maxdim, r, out);
 }
 
 void check_points(const f32* x, u32 n, u32 dim) {
@@ -181,20 +209,60 @@ void persistence_points(tt_ctx* c, const f32* x_h, u32 n, u32 dim, int kind, f32
         TT_CUDA(cudaMemcpyAsync(gw, w, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
     }
     if (n == 0) return;
-    Complex cx{nullptr, rp, gci, gw, n, thr};
-    Dim0Out r;
-    dim0(c, cx, maxdim, r);
-    out.edges = r.m;
-    h0_bars(c, r, out);
-    if (maxdim == 0) return;
-    if (maxdim >= 2) invalid("gb300: maxdim 2 on graph input is not supported by the GPU front end");
-    out.apparent.push_back(r.m - (n - r.essential) - r.ncols);
-    const auto hrp = to_host(c, rp, u64(n) + 1);
-    const auto hci = to_host(c, gci, nnz);
-    const auto hw = to_host(c, gw, nnz);
-    sync(c);
-    host::HostComplex hc{nullptr, hrp.data(), hci.data(), hw.data(), n, thr};
-    reduce_dim1(c, hc, maxdim, r, out);
+    sparse_tail(c, rp, gci, gw, nullptr, nullptr, nullptr, n, nnz, thr, maxdim, out);
+}
+
+// tops::persistence(const CsrGraph&, maxdim, threshold) (turbotops.hpp:179-207):
+// the caller's graph, checked as CsrGraph::valid() (core.hpp:137-148) does,
+// uploaded, then the sparse front end.
+void persistence_graph(tt_ctx* c, const u64* rp_h, const u32* ci_h, const f32* w_h, u32 n, u32 maxdim, f32 thr,
+                       Result& out) {
+    if (std::isnan(thr) || thr < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+    if (maxdim + 2 > 32) invalid("rips: maxdim must be <= 30");
+    if (!rp_h) invalid("gb300: null row_ptr");
+    const u64 nnz = rp_h[n];
+    bool ok = rp_h[0] == 0 && nnz % 2 == 0 && (!nnz || (ci_h && w_h));
+    for (u32 v = 0; ok && v < n; ++v) {
+        const u64 b = rp_h[v], e = rp_h[v + 1];
+        if (e < b || e > nnz) {
+            ok = false;
+            break;
+        }
+        for (u64 t = b; t < e; ++t) {
+            const u32 u = ci_h[t];
+            if (u >= n || u == v || (t > b && ci_h[t - 1] >= u)) {
+                ok = false;
+                break;
+            }
+            // weight(u, v): binary search of v in row u (core.hpp:104-109)
+            const u64 ub = rp_h[u], ue = rp_h[u + 1];
+            if (ue < ub || ue > nnz) {
+                ok = false;
+                break;
+            }
+            const u32* it = std::lower_bound(ci_h + ub, ci_h + ue, v);
+            const f32 wuv = (it != ci_h + ue && *it == v) ? w_h[it - ci_h] : INFINITY;
+            if (wuv != w_h[t]) {
+                ok = false;
+                break;
+            }
+        }
+    }
+    if (!ok) invalid("persistence: CsrGraph invariant violated (see CsrGraph::valid)");
+    if (maxdim > 2) invalid("gb300: the GPU front end supports maxdim <= 2");
+    out.ensure(maxdim);
+    out.method = "sparse";
+    out.threshold = thr;
+    if (n == 0) return;
+    u64* rp = c->arena.get<u64>(S_GRAPH_RP, u64(n) + 1);
+    u32* gci = c->arena.get<u32>(S_GRAPH_TMP, nnz + 1);
+    f32* gw = c->arena.get<f32>(S_KNN_D, nnz + 1);
+    TT_CUDA(cudaMemcpyAsync(rp, rp_h, 8 * (u64(n) + 1), cudaMemcpyHostToDevice, c->stream));
+    if (nnz) {
+        TT_CUDA(cudaMemcpyAsync(gci, ci_h, 4 * nnz, cudaMemcpyHostToDevice, c->stream));
+        TT_CUDA(cudaMemcpyAsync(gw, w_h, 4 * nnz, cudaMemcpyHostToDevice, c->stream));
+    }
+    sparse_tail(c, rp, gci, gw, rp_h, ci_h, w_h, n, nnz, thr, maxdim, out);
 }
 
 }  // namespace
@@ -255,6 +323,18 @@ extern "C" int tt_persistence_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_
         if (kind == TT_METRIC_LP && !(p >= 1.0f)) invalid("metric: p must be in [1, inf]");
         Result r;
         persistence_points(c, x_h, n, dim, kind, p, maxdim, threshold, knn, k, r);
+        *out = pack(r);
+    });
+}
+
+extern "C" int tt_persistence_graph_h(tt_ctx* c, const uint64_t* row_ptr_h, const uint32_t* col_h,
+                                      const float* weight_h, uint32_t n, uint32_t maxdim, float threshold,
+                                      tt_barcode** out) {
+    return guarded(c, [&] {
+        if (!out) invalid("gb300: null output");
+        *out = nullptr;
+        Result r;
+        persistence_graph(c, row_ptr_h, col_h, weight_h, n, maxdim, threshold, r);
         *out = pack(r);
     });
 }
