@@ -63,10 +63,8 @@ constexpr int TC_K = 16;        // register top-k capacity
 constexpr u32 TILE_BYTES = TC_M * TC_DIM * 4;   // 16 KiB (query and candidate tiles alike)
 constexpr int TC_Q = 256;                       // survivor queue per warp (pairs)
 constexpr int NSTAGE = 2;                       // candidate tiles in flight (TMA ring)
-constexpr u32 TC_TEST = 16;                     // tiles tested per lookahead batch
+constexpr u32 TC_TEST = 128;                    // most positions tested per lookahead batch (one N = 128 product)
 constexpr int ST_STRIDE = 36;                   // floats per tile record: centroid, R, |centroid|^2, pad
-constexpr u32 TST_F4 = TC_TEST * (ST_STRIDE / 4);   // float4 per lookahead batch of tile records
-static_assert(TST_F4 > 128 && TST_F4 <= 256, "two records' float4 per thread");
 constexpr int MAX_PIV = 128;
 constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
 static_assert(NSTAGE == 2, "the stage bookkeeping below assumes two stages");
@@ -93,9 +91,9 @@ struct Shared {
     alignas(16) u32 oid[NSTAGE][TC_N];   // original ids of the tile's candidates
     u32 q[4][TC_Q];                      // per-warp survivor queue: owner lane << 7 | candidate row
     f32 r[4][TC_Q];                      // their exact distances
-    u32 need[2][4];                      // per-warp lookahead masks (double-buffered)
-    alignas(16) float4 tst[TST_F4];      // tile records of the current lookahead batch
-    alignas(1024) unsigned char cent[TC_TEST * 128];   // their centroids, 128-byte swizzled (MMA operand)
+    u32 need[2][4][TC_TEST / 32];        // per-warp lookahead masks (double-buffered)
+    alignas(1024) unsigned char cent[TC_TEST * 128];   // lookahead batch centroids, 128-byte swizzled (MMA operand)
+    alignas(16) float2 trc[TC_TEST];     // their radius and |centroid|^2
     alignas(8) u64 bar_a;
     alignas(8) u64 bar_b[NSTAGE];
     alignas(8) u64 bar_mma[2];
@@ -139,9 +137,9 @@ __device__ __forceinline__ u64 plain_desc(u32 saddr, u32 lbo, u32 sbo) {
 // Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, N, M.
 constexpr u32 kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (u32(TC_N >> 3) << 17) | (u32(TC_M >> 4) << 24);
 
-// The lookahead product: M = 128 queries x N = TC_TEST centroids.
-constexpr u32 kIdescT = (1u << 4) | (2u << 7) | (2u << 10) | (u32(TC_TEST >> 3) << 17) | (u32(TC_M >> 4) << 24);
-static_assert(TC_TEST == 16, "the lookahead product reads 16 accumulator columns");
+// The lookahead product: M = 128 queries x N = TC_TEST centroids (the same
+// shape as a tile product).
+static_assert(TC_TEST == TC_N, "the lookahead product fills one accumulator");
 
 __device__ __forceinline__ void tma_tile(void* dst, const CUtensorMap* map, int row, u64* bar) {
     asm volatile(
@@ -215,15 +213,6 @@ __device__ __forceinline__ void tmem_ld32(u32 taddr, u32 (&v)[32]) {
           "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
           "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
           "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(u32 taddr, u32 (&v)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -338,6 +327,68 @@ __global__ void k_tc_assign(const f32* __restrict__ x, u32 n, const f32* __restr
     }
     key[i] = rank[best];
     val[i] = i;
+}
+
+// First position of each cell (chain rank) in the rank-sorted keys; cell P
+// ends the array.
+__global__ void k_tc_cells(const u64* __restrict__ skey, u32 n, u32 P, u32* __restrict__ cell_off) {
+    for (u32 p = blockIdx.x * blockDim.x + threadIdx.x; p <= P; p += gridDim.x * blockDim.x) {
+        u32 lo = 0, hi = n;
+        while (lo < hi) {
+            const u32 mid = (lo + hi) >> 1;
+            if (skey[mid] < p) lo = mid + 1;
+            else hi = mid;
+        }
+        cell_off[p] = lo;
+    }
+}
+
+// Second level: every point of a cell (s points) joins the nearest of
+// min(16, max(1, s / 128)) sub-pivots (the cell's points at strided
+// positions, ties to the lower one); key = cell << 4 | sub-pivot, so that
+// the tiles of a cell follow its sub-cells.
+__global__ void k_tc_assign2(const f32* __restrict__ x, u32 n, const u64* __restrict__ skey,
+                             const u32* __restrict__ perm, const u32* __restrict__ cell_off, u64* __restrict__ key2,
+                             u32* __restrict__ val2) {
+    const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const u32 cell = u32(skey[r]);
+    const u32 o = cell_off[cell], s = cell_off[cell + 1] - o;
+    const u32 S = min(16u, max(1u, s / 128u));
+    const u32 self = perm[r];
+    f32 q[TC_DIM];
+    const float4* xr = reinterpret_cast<const float4*>(x + u64(self) * TC_DIM);
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+        const float4 t4 = __ldg(xr + ch);
+        q[4 * ch] = t4.x;
+        q[4 * ch + 1] = t4.y;
+        q[4 * ch + 2] = t4.z;
+        q[4 * ch + 3] = t4.w;
+    }
+    u32 best = 0;
+    f32 bd = INFINITY;
+    for (u32 j = 0; j < S; ++j) {
+        const float4* pr = reinterpret_cast<const float4*>(x + u64(perm[o + u32(u64(j) * s / S)]) * TC_DIM);
+        f32 d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+        for (int ch = 0; ch < 8; ++ch) {
+            const float4 t4 = __ldg(pr + ch);
+            const f32 a0 = q[4 * ch] - t4.x, a1 = q[4 * ch + 1] - t4.y;
+            const f32 a2 = q[4 * ch + 2] - t4.z, a3 = q[4 * ch + 3] - t4.w;
+            d0 = fmaf(a0, a0, d0);
+            d1 = fmaf(a1, a1, d1);
+            d0 = fmaf(a2, a2, d0);
+            d1 = fmaf(a3, a3, d1);
+        }
+        const f32 d = d0 + d1;
+        if (d < bd) {
+            bd = d;
+            best = j;
+        }
+    }
+    key2[r] = (u64(cell) << 4) | best;
+    val2[r] = self;
 }
 
 // Regrouped copy: xp[r] = x[perm[r]], its norm, its augmentation row
@@ -518,58 +569,42 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             const f32 tq = d < INFINITY && nqi >= 0x1p-60f ? sq_bound(d) * (1.0f + 1.0f / 65536.0f) : INFINITY;
             rq = tq - nqi * (1.0f - 1.0f / 128.0f);
         };
-        // Lookahead over the outward order (block-uniform state): `bmask`
-        // holds the tiles of the current batch that some query of the block
-        // needs, `mymask` the ones this thread's query needs.
-        u32 sp = 0, bbase = 0, bmask = 0, mymask = 0;
-        // Tile records of a batch (TC_TEST positions from s0): float4 f of the
-        // batch is part f % 9 of the record at position s0 + f / 9. Thread t
-        // holds parts t and t + 128 in registers; they are loaded one batch
-        // ahead, so the L2 latency overlaps the tiles in between.
-        float4 pf0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), pf1 = pf0;
-        auto prefetch = [&](u32 s0) {
-            const u32 f0 = tid, f1 = tid + 128;
-            const u32 sa = s0 + f0 / 9, sb2 = s0 + f1 / 9;
-            if (sa < ntiles)
-                pf0 = __ldg(reinterpret_cast<const float4*>(stats + u64(spiral_tile(blk, sa, ntiles)) * ST_STRIDE) +
-                            f0 % 9);
-            if (f1 < TST_F4 && sb2 < ntiles)
-                pf1 = __ldg(reinterpret_cast<const float4*>(stats + u64(spiral_tile(blk, sb2, ntiles)) * ST_STRIDE) +
-                            f1 % 9);
-        };
-        // acc: TMEM address of an accumulator the tile loop does not use
-        // right now (its first TC_TEST columns take the lookahead product), or
-        // ~0u before the first tile (every k-th distance is still +inf then).
+        // Lookahead over the outward order (block-uniform state): bm holds the
+        // positions of the current batch that some query of the block needs,
+        // my the ones this thread's query needs (bit b of word c: position
+        // bbase + 32 c + b).
+        u32 sp = 0, bbase = 0;
+        u32 bm0 = 0, bm1 = 0, bm2 = 0, bm3 = 0, my0 = 0, my1 = 0, my2 = 0, my3 = 0;
+        static_assert(TC_TEST == 128, "four mask words");
+        // acc: TMEM address of an accumulator the tile loop does not use right
+        // now (the lookahead product fills it), or ~0u before the first tile
+        // (every k-th distance is still +inf then). Batches grow with the
+        // distance from the block's own tile (2, 8, 10, 20, 40, ..., 128
+        // positions) so that the first ones are tested with fresh distances.
         auto refill = [&](u32 acc) {
-            const u32 w = sp == 0 ? u32(NSTAGE) : TC_TEST;
-            if (sp == 0) prefetch(0);
-            {   // the batch's records; the centroids also as the MMA operand
-                const u32 f0 = tid, f1 = tid + 128;
-                S.tst[f0] = pf0;
-                if ((f0 % 9) < 8) {
-                    const u32 b = f0 / 9;
-                    *reinterpret_cast<float4*>(S.cent + b * 128 + (((f0 % 9) ^ (b & 7)) << 4)) = pf0;
-                }
-                if (f1 < TST_F4) {
-                    S.tst[f1] = pf1;
-                    if ((f1 % 9) < 8) {
-                        const u32 b = f1 / 9;
-                        *reinterpret_cast<float4*>(S.cent + b * 128 + (((f1 % 9) ^ (b & 7)) << 4)) = pf1;
+            const u32 w = sp == 0 ? u32(NSTAGE) : min(TC_TEST, max(8u, sp));
+            u32 m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+            if (acc == ~0u) {
+                if (active)
+                    m0 = (w >= 32 ? ~0u : (1u << w) - 1u) & (ntiles - sp >= 32 ? ~0u : (1u << (ntiles - sp)) - 1u);
+            } else {
+                {   // the batch's records: centroid (MMA operand, row = position), radius, |centroid|^2
+                    const u32 pos = sp + tid;
+                    if (tid < w && pos < ntiles) {
+                        const float4* rec =
+                            reinterpret_cast<const float4*>(stats + u64(spiral_tile(blk, pos, ntiles)) * ST_STRIDE);
+#pragma unroll
+                        for (int ch = 0; ch < 8; ++ch)
+                            *reinterpret_cast<float4*>(S.cent + tid * 128 + ((ch ^ (tid & 7)) << 4)) = __ldg(rec + ch);
+                        const float4 rc = __ldg(rec + 8);
+                        S.trc[tid] = make_float2(rc.x, rc.y);
                     }
                 }
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // centroids -> tensor core
-            __syncthreads();
-            if (sp + w < ntiles) prefetch(sp + w);   // the next batch starts at sp + w
-            u32 m = 0;
-            if (acc == ~0u) {
-                // before the first tile: every k-th distance is +inf, every
-                // tile is needed
-                if (active) m = (w >= 32 ? ~0u : (1u << w) - 1u) & (ntiles - sp >= 32 ? ~0u : (1u << (ntiles - sp)) - 1u);
-            } else {
-                // G = q . c for the 128 queries x 16 centroids on the tensor
-                // core. The centroids are TF32-exact and the queries lose at
-                // most 2^-10 relative in TF32, so |G~ - q.c| <= 2^-10 |q||c|
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // centroids -> tensor core
+                __syncthreads();
+                // G = q . c for the 128 queries x the batch's centroids on the
+                // tensor core. The centroids are TF32-exact and the queries lose
+                // at most 2^-10 relative in TF32, so |G~ - q.c| <= 2^-10 |q||c|
                 // (FP32 accumulation included) <= 2^-11 (|q|^2 + |c|^2), and
                 // `lower` = |q|^2 + |c|^2 - 2 G~ - 2^-8 (|q|^2 + |c|^2) - 2^-120
                 // is a lower bound of |q - c|^2 with room for the FP32
@@ -588,45 +623,81 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
 #pragma unroll
                     for (int ks = 0; ks < TC_DIM / 8; ++ks)
                         mma_step(acc, sw128_desc(smem_addr(S.a) + 32 * ks), sw128_desc(smem_addr(S.cent) + 32 * ks),
-                                 ks > 0, kIdescT);
+                                 ks > 0);
                     mma_commit(&S.bar_t);
                 }
                 mbar_wait(&S.bar_t, ut & 1, err, &S.fail);
                 ++ut;
                 tc_fence_after();
-                u32 g[TC_TEST];
-                tmem_ld16(acc + ((warp * 32u) << 16), g);
                 const bool ok = active && dk >= 0x1p-50f && dk < INFINITY && nqi >= 0x1p-60f;
 #pragma unroll
-                for (int b = 0; b < int(TC_TEST); ++b) {
-                    const float4 rc = S.tst[b * 9 + 8];   // R, |c|^2, 0, 0
-                    const f32 s2 = nqi + rc.y;
-                    const f32 lower = fmaf(-2.0f, __uint_as_float(g[b]), s2) - fmaf(s2, 1.0f / 256.0f, 0x1p-120f);
-                    const f32 t2 = dk + rc.x;
-                    const f32 rhs = t2 * t2 * (1.0f + 0x1p-10f);
-                    const bool skip = ok && lower > rhs && lower <= 3.4e38f;
-                    if (active && sp + u32(b) < ntiles && !skip) m |= 1u << b;
+                for (int c = 0; c < int(TC_TEST / 32); ++c) {
+                    if (u32(c) * 32 >= w) break;   // block-uniform
+                    u32 g[32];
+                    tmem_ld32(acc + ((warp * 32u) << 16) + u32(c * 32), g);
+                    u32 mc = 0;
+#pragma unroll
+                    for (int h = 0; h < 32; ++h) {
+                        const u32 b = u32(c * 32 + h);
+                        const float2 rc = S.trc[b];   // R, |c|^2
+                        const f32 s2 = nqi + rc.y;
+                        const f32 lower = fmaf(-2.0f, __uint_as_float(g[h]), s2) - fmaf(s2, 1.0f / 256.0f, 0x1p-120f);
+                        const f32 t2 = dk + rc.x;
+                        const f32 rhs = t2 * t2 * (1.0f + 0x1p-10f);
+                        const bool skip = ok && lower > rhs && lower <= 3.4e38f;
+                        mc |= u32(active && b < w && sp + b < ntiles && !skip) << h;
+                    }
+                    if (c == 0) m0 = mc;
+                    else if (c == 1) m1 = mc;
+                    else if (c == 2) m2 = mc;
+                    else m3 = mc;
                 }
                 tc_fence_before();
             }
-            const u32 wm = __reduce_or_sync(0xffffffffu, m);
-            if (lane == 0) S.need[npar][warp] = wm;
+            {
+                const u32 w0 = __reduce_or_sync(0xffffffffu, m0), w1 = __reduce_or_sync(0xffffffffu, m1);
+                const u32 w2 = __reduce_or_sync(0xffffffffu, m2), w3 = __reduce_or_sync(0xffffffffu, m3);
+                if (lane == 0) {
+                    S.need[npar][warp][0] = w0;
+                    S.need[npar][warp][1] = w1;
+                    S.need[npar][warp][2] = w2;
+                    S.need[npar][warp][3] = w3;
+                }
+            }
             __syncthreads();
-            bmask = S.need[npar][0] | S.need[npar][1] | S.need[npar][2] | S.need[npar][3];
+            {
+                const u32(&nd)[4][TC_TEST / 32] = S.need[npar];
+                bm0 = nd[0][0] | nd[1][0] | nd[2][0] | nd[3][0];
+                bm1 = nd[0][1] | nd[1][1] | nd[2][1] | nd[3][1];
+                bm2 = nd[0][2] | nd[1][2] | nd[2][2] | nd[3][2];
+                bm3 = nd[0][3] | nd[1][3] | nd[2][3] | nd[3][3];
+                my0 = m0;
+                my1 = m1;
+                my2 = m2;
+                my3 = m3;
+            }
             npar ^= 1;
             bbase = sp;
-            mymask = m;
             sp += w;
         };
         // next tile some query of the block needs (block-uniform); false when
         // the order is exhausted
         auto next_tile = [&](u32& T, bool& mine, u32 acc) -> bool {
             for (;;) {
-                if (bmask) {
-                    const u32 b = u32(__ffs(bmask) - 1);
-                    bmask &= bmask - 1;
-                    T = spiral_tile(blk, bbase + b, ntiles);
-                    mine = (mymask >> b) & 1u;
+                // lowest set position over the four words (no references to
+                // the words: they stay in registers)
+                if (bm0 | bm1 | bm2 | bm3) {
+                    const u32 c = bm0 ? 0u : bm1 ? 1u : bm2 ? 2u : 3u;
+                    const u32 bw = c == 0 ? bm0 : c == 1 ? bm1 : c == 2 ? bm2 : bm3;
+                    const u32 myw = c == 0 ? my0 : c == 1 ? my1 : c == 2 ? my2 : my3;
+                    const u32 b = u32(__ffs(bw) - 1);
+                    const u32 rest = bw & (bw - 1);
+                    if (c == 0) bm0 = rest;
+                    else if (c == 1) bm1 = rest;
+                    else if (c == 2) bm2 = rest;
+                    else bm3 = rest;
+                    T = spiral_tile(blk, bbase + c * 32 + b, ntiles);
+                    mine = (myw >> b) & 1u;
                     return true;
                 }
                 if (sp >= ntiles) return false;
@@ -937,11 +1008,25 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
         TT_LAUNCH("k_tc_assign");
         c->launches += 2;
         perm = val;
-        if (P > 1) {
-            u64* kb = c->arena.get<u64>(S_SORT_A, n);
-            u32* vb = c->arena.get<u32>(S_SORT_VA, n);
-            const int bits = 32 - __builtin_clz(P - 1);
-            if (radix_sort<u32>(c, key, val, n, kb, vb, bits)) perm = vb;
+        u64* skey = key;
+        u64* kb = c->arena.get<u64>(S_SORT_A, n);
+        u32* vb = c->arena.get<u32>(S_SORT_VA, n);
+        const int bits = P > 1 ? 32 - __builtin_clz(P - 1) : 0;
+        if (P > 1 && radix_sort<u32>(c, key, val, n, kb, vb, bits)) {
+            perm = vb;
+            skey = kb;
+        }
+        // second level: sub-cells within every cell (tiles then follow them)
+        if (n >= 2 * TC_N) {
+            u32* cell_off = c->arena.get<u32>(S_TC_CELL, u64(P) + 2);
+            u64* key2 = c->arena.get<u64>(S_TC_KEY2, n);
+            u32* val2 = c->arena.get<u32>(S_TC_VAL2, n);
+            k_tc_cells<<<1, 256, 0, c->stream>>>(skey, n, P, cell_off);
+            TT_LAUNCH("k_tc_cells");
+            k_tc_assign2<<<div_up(n, 256), 256, 0, c->stream>>>(x, n, skey, perm, cell_off, key2, val2);
+            TT_LAUNCH("k_tc_assign2");
+            c->launches += 2;
+            perm = radix_sort<u32>(c, key2, val2, n, kb, vb, bits + 4) ? vb : val2;
         }
     }
     f32* xp = c->arena.get<f32>(S_TC_X, u64(n) * TC_DIM);
