@@ -75,6 +75,13 @@ def _cases_tile_order():
         "tiny": (synth.gauss(5000, 32, 9) * np.float32(1e-21), 7),
         # well separated clusters, k = 1
         "far_clusters": (synth.gmm(12000, 32, centres=4, seed=2) * np.float32(50.0), 1),
+        # point scales from 1e-3 to 1e3 side by side: the per-tile TF32 error
+        # terms differ by six orders of magnitude
+        "wide_range": (synth.gauss(9000, 32, 4) * (10.0 ** rng.uniform(-3, 3, (9000, 1))).astype(np.float32), 9),
+        # clusters of near-duplicates (spread 1e-4 around points far from the
+        # origin): the neighbours sit inside the filter's rounding band
+        "near_duplicates": (np.repeat(synth.gauss(400, 32, 6) * np.float32(30.0), 25, axis=0)
+                            + rng.normal(0, 1e-4, (10000, 32)).astype(np.float32), 15),
     }
     return out
 

@@ -125,7 +125,7 @@ enum Slot : int {
     S_KNN_D, S_KNN_I, S_GRAPH_KEYS, S_GRAPH_TMP, S_PIV,           // kNN / graph / pivots
     S_SCAN2, S_SCAN3, S_MISC0, S_MISC1, S_MISC2, S_MISC3, S_ROWMAX, S_GRAPH_RP, S_ASM0, S_ASM1, S_ASM2, S_ASM3, S_ASM4,
     S_TC_X, S_TC_PERM, S_TC_STATS, S_TC_KEYS, S_TC_VALS, S_TC_PIV,   // tensor-core kNN (tile order)
-    S_TC_KEY2, S_TC_VAL2, S_TC_CELL,
+    S_TC_KEY2, S_TC_VAL2, S_TC_CELL, S_TC_LO, S_TC_ERR,
     S_EDGE_CNT, S_EDGE_SORT, S_EDGE_IDX, S_EDGE_INV,               // ordered edge generation
     S_NSLOTS
 };

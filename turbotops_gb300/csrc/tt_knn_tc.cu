@@ -14,28 +14,35 @@
 //    A query q with current k-th distance d_k skips a tile when
 //    |q - c| > d_k + R (with margins for every rounding, see the lookahead
 //    product in the kernel): by the triangle inequality no point of the tile
-//    can then enter the list. A query block visits the tiles outward from its own (B, B+1,
-//    B-1, ...), tests them 16 at a time, and loads only the tiles some query
-//    of the block still needs; a warp skips a loaded tile that none of its
-//    queries needs.
-// 2. Gram filter. For a loaded tile the tensor core produces
-//      D~(q, c) = G~(q, c) - |c|^2 (1 - 2^-7) / 2,   G~ = TF32 Gram, FP32 sum,
-//    the norm term entering as a fifth K-step (an exact TF32 head and its
-//    remainder), so that s~ - 2^-7 (|q|^2 + |c|^2) = |q|^2 (1 - 2^-7) - 2 D~
-//    with s~ = |q|^2 + |c|^2 - 2 G~. TF32 keeps 10 mantissa bits of each
-//    operand, so |G~ - q.c| <= 2^-9 |q||c| <= 2^-10 (|q|^2 + |c|^2); with the
-//    FP32 norms, the remainder's own TF32 rounding and the accumulation the
-//    error of s~ stays below 2^-8 (|q|^2 + |c|^2). A candidate is evaluated
-//    exactly when
-//      s~ - 2^-7 (|q|^2 + |c|^2) <= T_q,   T_q = sq_bound(d_k) (1 + 2^-16)
-//    so every candidate whose exact distance could enter the list passes
-//    (the 2^-16 covers the lane-ordered sum's own rounding). The epilogue is
-//    a max over the accumulator row and one compare.
+//    can then enter the list. A query block visits the tiles outward from
+//    its own (B, B+1, B-1, ...), tests them in batches (one tensor-core
+//    product of the queries with up to 128 centroids each), and loads only
+//    the tiles some query of the block still needs; a warp skips a loaded
+//    tile that none of its queries needs.
+// 2. Gram filter. The regrouped copy keeps every coordinate as a TF32-exact
+//    head x~ (13 low mantissa bits cleared) plus those bits in a side array,
+//    so the tensor core multiplies exact values and the exact path
+//    reassembles x bit for bit. For a loaded tile the tensor core produces
+//      D(q, c) = q~ . c~ - W(c),   W(c) <= |c~|^2 (1 - 2^-16) / 2,
+//    the norm term entering as a fifth K-step (two TF32-exact parts). Only
+//    the FP32 accumulation rounds (<= 2^-19 (|q~|^2 + |c~|^2)), so
+//      L = |q~|^2 (1 - 2^-16) - 2 D <= |q~ - c~|^2,
+//    and with e_x >= |x - x~| (per point, rounded up) the true distance is
+//    at least sqrt(L) - e_q - e_c. A candidate is evaluated exactly when
+//      L <= (sqrt(T_q) + e_q + e_T)^2,   T_q = sq_bound(d_k) (1 + 2^-16),
+//    e_T the tile's largest e_c, so every candidate whose lane-ordered
+//    distance could enter the list passes (the 2^-16 in T_q covers the
+//    lane-ordered sum's own rounding). The margins are absolute (of the
+//    order of the TF32 rounding of the points, times d_k), not relative to
+//    |q|^2 + |c|^2: points far from the origin filter as tightly as points
+//    near it. The epilogue is a max over the accumulator row and one
+//    compare.
 //
 // Pipeline per CTA (128 threads = 4 warps, one query row per thread, 128
 // queries per block, persistent over query blocks):
 //   TMA (cp.async.bulk.tensor, 128-byte swizzle) loads the query tile once
-//   and the chosen candidate tiles into two shared-memory stages; thread 0
+//   and the chosen candidate tiles into two shared-memory stages (bulk
+//   copies bring their low bits, norm terms and ids alongside); thread 0
 //   issues tcgen05.mma.kind::tf32 (M = 128, N = 128, 5 x K = 8) into one of
 //   two TMEM accumulators and commits to an mbarrier; while the tensor core
 //   works on the next tile the four warps read this tile's Gram rows
@@ -66,12 +73,13 @@ constexpr int NSTAGE = 2;                       // candidate tiles in flight (TM
 constexpr u32 TC_TEST = 128;                    // most positions tested per lookahead batch (one N = 128 product)
 constexpr int ST_STRIDE = 36;                   // floats per tile record: centroid, R, |centroid|^2, pad
 constexpr int MAX_PIV = 128;
-constexpr size_t TC_SMEM = 100 * 1024;          // caps residency at two CTAs per SM
+constexpr size_t TC_SMEM = 110 * 1024;          // two CTAs per SM (2 x (110 + 1) KiB of 228)
 static_assert(NSTAGE == 2, "the stage bookkeeping below assumes two stages");
 static_assert(TC_M == TC_N, "query blocks and candidate tiles share one tiling");
 
 constexpr u32 AUG_BYTES = TC_N * 16;  // augmentation rows per tile (one 16-byte core-matrix row each)
 constexpr u32 ID_BYTES = TC_N * 4;    // original ids per tile
+constexpr u32 LO_BYTES = TC_N * TC_DIM * 2;   // low mantissa bits per tile (u16 per coordinate)
 
 // The fifth K-step of every product adds the candidate's norm term: the
 // query side holds rows (1, 1, 0, 0 | 0, 0, 0, 0), the candidate side
@@ -88,6 +96,8 @@ struct Shared {
     float4 zeros[TC_N];                      // the second K half of both sides
     alignas(1024) unsigned char a[TILE_BYTES];
     alignas(1024) unsigned char b[NSTAGE][TILE_BYTES];
+    alignas(16) u16 alo[TC_M * TC_DIM];  // the query tile's low mantissa bits
+    alignas(16) u16 blo[NSTAGE][TC_N * TC_DIM];   // the stages' low mantissa bits
     alignas(16) u32 oid[NSTAGE][TC_N];   // original ids of the tile's candidates
     u32 q[4][TC_Q];                      // per-warp survivor queue: owner lane << 7 | candidate row
     f32 r[4][TC_Q];                      // their exact distances
@@ -116,6 +126,21 @@ __device__ __forceinline__ void swz_row(const unsigned char* tile, u32 r, f32 (&
         o[4 * ch + 1] = t4.y;
         o[4 * ch + 2] = t4.z;
         o[4 * ch + 3] = t4.w;
+    }
+}
+
+// Row r of a tile reassembled: the TF32-exact head from the swizzled tile,
+// the 13 low mantissa bits from the low-bits array (lo_index layout).
+__device__ __forceinline__ void raw_row(const unsigned char* tile, const u16* lo, u32 r, f32 (&o)[TC_DIM]) {
+    swz_row(tile, r, o);
+    const uint4* lr = reinterpret_cast<const uint4*>(lo + r * TC_DIM);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const uint4 t = lr[c ^ ((r >> 1) & 3u)];
+        const u32 w[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+            o[8 * c + e] = __uint_as_float(__float_as_uint(o[8 * c + e]) | ((w[e >> 1] >> (16 * (e & 1))) & 0xffffu));
     }
 }
 
@@ -215,6 +240,25 @@ __device__ __forceinline__ void tmem_ld32(u32 taddr, u32 (&v)[32]) {
           "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Two 32-column loads in flight at once: tmem_ld32_start issues one, and
+// tmem_wait2 waits for both (every register tied to the wait, so that no
+// use of a loaded value can be scheduled before it).
+__device__ __forceinline__ void tmem_ld32_start(u32 taddr, u32 (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait2(u32 (&v)[32], u32 (&w)[32]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]), "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15]), "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]), "+r"(v[22]), "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]), "+r"(v[29]), "+r"(v[30]), "+r"(v[31])
+                 :
+                 : "memory");
+    asm volatile(""
+                 : "+r"(w[0]), "+r"(w[1]), "+r"(w[2]), "+r"(w[3]), "+r"(w[4]), "+r"(w[5]), "+r"(w[6]), "+r"(w[7]), "+r"(w[8]), "+r"(w[9]), "+r"(w[10]), "+r"(w[11]), "+r"(w[12]), "+r"(w[13]), "+r"(w[14]), "+r"(w[15]), "+r"(w[16]), "+r"(w[17]), "+r"(w[18]), "+r"(w[19]), "+r"(w[20]), "+r"(w[21]), "+r"(w[22]), "+r"(w[23]), "+r"(w[24]), "+r"(w[25]), "+r"(w[26]), "+r"(w[27]), "+r"(w[28]), "+r"(w[29]), "+r"(w[30]), "+r"(w[31]));
 }
 
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -391,50 +435,89 @@ __global__ void k_tc_assign2(const f32* __restrict__ x, u32 n, const u64* __rest
     val2[r] = self;
 }
 
-// Regrouped copy: xp[r] = x[perm[r]], its norm, its augmentation row
-// (w_hi, w_lo, 0, 0), w = -|x|^2 (1 - 2^-7) / 2, and the original id; rows
-// [n, wpad) are padding (augmentation -3e38: never passes; id ~0).
+// Index of coordinate k of row r in the low-bits array: u16 per coordinate,
+// 64 bytes per row, 16-byte chunk c (coordinates 8c..8c+7) stored at chunk
+// position c ^ ((r >> 1) & 3), so that eight consecutive rows read by one
+// quarter-warp hit distinct banks.
+__host__ __device__ __forceinline__ u32 lo_index(u32 r, u32 k) {
+    return r * TC_DIM + ((((k >> 3) ^ ((r >> 1) & 3u)) << 3) | (k & 7u));
+}
+
+// Regrouped copy in two parts. xh[r]: the coordinates of x[perm[r]] with
+// their 13 low mantissa bits cleared (TF32-exact: the tensor core multiplies
+// them without rounding). lo[r]: those 13 bits, u16 per coordinate, so that
+// xh | lo is the point again, bit for bit (the exact path's input). Per row:
+// nq = |xh|^2 rounded down; e >= |x - xh| (rounded up; a coordinate below
+// 2^-126 counts in full, in case the tensor core flushes it); the
+// augmentation row (w_hi, w_lo, 0, 0) with
+// -w_hi - w_lo in [W (1 - 2^-20), W], W = nq (1 - 2^-16) / 2 (two TF32-exact
+// parts, both truncated toward zero); the original id. Rows [n, wpad) are
+// padding (augmentation -3e38: never passes; id ~0).
 __global__ void k_tc_gather(const f32* __restrict__ x, u32 n, u32 wpad, const u32* __restrict__ perm,
-                            f32* __restrict__ xp, u32* __restrict__ ids, f32* __restrict__ nq,
-                            float4* __restrict__ aug) {
+                            f32* __restrict__ xh, u16* __restrict__ lo, u32* __restrict__ ids,
+                            f32* __restrict__ nq, f32* __restrict__ eq, float4* __restrict__ aug) {
     const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= wpad) return;
+    uint4* lr = reinterpret_cast<uint4*>(lo + u64(r) * TC_DIM);
     if (r >= n) {
         aug[r] = make_float4(-3.0e38f, 0.0f, 0.0f, 0.0f);
         ids[r] = 0xffffffffu;
+        nq[r] = 0.0f;
+        eq[r] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) lr[c] = make_uint4(0u, 0u, 0u, 0u);
         return;
     }
     const u32 src = perm[r];
     const float4* xr = reinterpret_cast<const float4*>(x + u64(src) * TC_DIM);
-    float4* xo = reinterpret_cast<float4*>(xp + u64(r) * TC_DIM);
-    f32 s = 0.0f;
+    float4* xo = reinterpret_cast<float4*>(xh + u64(r) * TC_DIM);
+    f32 s = 0.0f, e2 = 0.0f;
+    u32 lw[16];   // the low bits, two coordinates per word
 #pragma unroll
     for (int ch = 0; ch < 8; ++ch) {
         const float4 t4 = __ldg(xr + ch);
-        xo[ch] = t4;
-        s = fmaf(t4.x, t4.x, s);
-        s = fmaf(t4.y, t4.y, s);
-        s = fmaf(t4.z, t4.z, s);
-        s = fmaf(t4.w, t4.w, s);
+        const f32 v[4] = {t4.x, t4.y, t4.z, t4.w};
+        f32 h[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const u32 u = __float_as_uint(v[e]);
+            h[e] = __uint_as_float(u & 0xffffe000u);
+            s = __fmaf_rd(h[e], h[e], s);   // exact products (11-bit significands), sum rounded down
+            const f32 b = fabsf(v[e]) < 0x1p-126f ? fabsf(v[e]) : fabsf(v[e] - h[e]);
+            e2 = __fmaf_ru(b, b, e2);
+            const u32 l = u & 0x1fffu;
+            if (e & 1) lw[2 * ch + (e >> 1)] |= l << 16;
+            else lw[2 * ch + (e >> 1)] = l;
+        }
+        xo[ch] = make_float4(h[0], h[1], h[2], h[3]);
     }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        lr[c ^ ((r >> 1) & 3u)] = make_uint4(lw[4 * c], lw[4 * c + 1], lw[4 * c + 2], lw[4 * c + 3]);
     nq[r] = s;
-    const f32 w = -0.5f * (s * (1.0f - 1.0f / 128.0f));
-    // head: the 10 leading mantissa bits (exact in TF32); tail: the exact
-    // FP32 remainder. A non-finite w keeps its head and gets a zero tail.
+    eq[r] = __fsqrt_ru(e2);
+    const f32 w = -__fmul_rd(s, 0.5f * (1.0f - 0x1p-16f));
+    // head and remainder, both truncated toward zero; a non-finite w keeps
+    // its head and gets a zero tail
     const f32 hi = __uint_as_float(__float_as_uint(w) & 0xffffe000u);
-    const f32 lo = isfinite(w) ? w - hi : 0.0f;
-    aug[r] = make_float4(hi, lo, 0.0f, 0.0f);
+    const f32 rem = isfinite(w) ? w - hi : 0.0f;   // exact
+    aug[r] = make_float4(hi, __uint_as_float(__float_as_uint(rem) & 0xffffe000u), 0.0f, 0.0f);
     ids[r] = src;
 }
 
-// One warp per tile: centroid (lane k holds coordinate k), |centroid|^2,
-// radius = sqrt(max_x |x - c|^2).
-__global__ void k_tc_stats(const f32* __restrict__ xp, u32 n, u32 ntiles, f32* __restrict__ stats) {
+// One warp per tile, lane k on coordinate k of the reassembled points
+// (xh | lo): centroid, |centroid|^2, radius = sqrt(max_x |x - c|^2), and the
+// tile's largest e and nq (the Gram filter's per-tile error terms).
+__global__ void k_tc_stats(const f32* __restrict__ xh, const u16* __restrict__ lo, const f32* __restrict__ nq,
+                           const f32* __restrict__ eq, u32 n, u32 ntiles, f32* __restrict__ stats) {
     const u32 w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= ntiles) return;
     const u32 r0 = w * TC_N, r1 = min(r0 + TC_N, n);
+    auto coord = [&](u32 r) {
+        return __uint_as_float(__float_as_uint(xh[u64(r) * TC_DIM + lane]) | u32(lo[lo_index(r, lane)]));
+    };
     f32 sum = 0.0f;
-    for (u32 r = r0; r < r1; ++r) sum += xp[u64(r) * TC_DIM + lane];
+    for (u32 r = r0; r < r1; ++r) sum += coord(r);
     // the centroid is any point (the bound holds for every centre): rounded
     // to a TF32-exact value, it enters the lookahead product without error
     const f32 c = __uint_as_float(__float_as_uint(sum / f32(r1 - r0)) & 0xffffe000u);
@@ -443,27 +526,37 @@ __global__ void k_tc_stats(const f32* __restrict__ xp, u32 n, u32 ntiles, f32* _
     for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(0xffffffffu, cc, o);
     f32 r2 = 0.0f;
     for (u32 r = r0; r < r1; ++r) {
-        const f32 t = xp[u64(r) * TC_DIM + lane] - c;
+        const f32 t = coord(r) - c;
         f32 d = t * t;
 #pragma unroll
         for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
         // a NaN coordinate makes the radius NaN (sticky): the tile is then never skipped
         r2 = (d != d || r2 != r2) ? d + r2 : fmaxf(r2, d);
     }
+    f32 em = 0.0f, nm = 0.0f;
+    for (u32 r = r0 + lane; r < r1; r += 32) {
+        em = fmaxf(em, eq[r]);
+        nm = fmaxf(nm, nq[r]);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        em = fmaxf(em, __shfl_xor_sync(0xffffffffu, em, o));
+        nm = fmaxf(nm, __shfl_xor_sync(0xffffffffu, nm, o));
+    }
     f32* o = stats + u64(w) * ST_STRIDE;
     o[lane] = c;
     if (lane == 0) {
         o[32] = sqrtf(r2);
         o[33] = cc;
-        o[34] = 0.0f;
-        o[35] = 0.0f;
+        o[34] = em;
+        o[35] = nm;
     }
 }
 
 // ---- the kNN kernel ---------------------------------------------------------
 
 __global__ void __launch_bounds__(128, 2)
-k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, const f32* __restrict__ xp,
+k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, const f32* __restrict__ eq,
          const u32* __restrict__ oids, u32 n, u32 k, const f32* __restrict__ nq, const float4* __restrict__ aug,
          const f32* __restrict__ stats, u32* __restrict__ ids, f32* __restrict__ dists, u32* __restrict__ next_block,
          u32* __restrict__ err, unsigned long long* __restrict__ counters) {
@@ -504,8 +597,9 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
 
     // stage s <- candidate tile T: the points (TMA, swizzled), their norm terms and ids
     auto load_stage = [&](int s, u32 T) {
-        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + AUG_BYTES + ID_BYTES);
+        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + LO_BYTES + AUG_BYTES + ID_BYTES);
         tma_tile(S.b[s], &map, int(T * TC_N), &S.bar_b[s]);
+        bulk_g2s(S.blo[s], lo + u64(T) * TC_N * TC_DIM, LO_BYTES, &S.bar_b[s]);
         bulk_g2s(S.baug[s], aug + u64(T) * TC_N, AUG_BYTES, &S.bar_b[s]);
         bulk_g2s(S.oid[s], oids + u64(T) * TC_N, ID_BYTES, &S.bar_b[s]);
     };
@@ -520,13 +614,16 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             // the previous block's generic reads of the query tile (survivor
             // queue) are ordered before this async-proxy overwrite
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(&S.bar_a, TILE_BYTES);
+            mbar_expect_tx(&S.bar_a, TILE_BYTES + LO_BYTES);
             tma_tile(S.a, &map, int(q0), &S.bar_a);
+            bulk_g2s(S.alo, lo + u64(q0) * TC_DIM, LO_BYTES, &S.bar_a);
         }
         const u32 row = warp * 32 + lane;
         const u32 i = q0 + row;   // regrouped index of this thread's query
         const bool active = i < n;
-        const f32 nqi = active ? nq[i] : 0.0f;
+        const f32 nqi = active ? nq[i] : 0.0f;            // |q~|^2 (rounded down), q~ the TF32 head
+        const f32 eqi = active ? eq[i] : 0.0f;            // >= |q - q~|
+        const f32 nql = __fmul_rd(nqi, 1.0f - 0x1p-16f);
         // Sorted list; its first TC_K - k slots hold -inf sentinels, so the
         // k-th entry is always ld[TC_K - 1] (every index a compile-time
         // constant: the list stays in registers).
@@ -537,7 +634,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             ld[t] = u32(t) < TC_K - k ? -INFINITY : INFINITY;
             lj[t] = 0xffffffffu;
         }
-        f32 rq = INFINITY;   // candidate passes iff -2 D <= rq (D: the augmented product)
+        f32 sq = INFINITY;   // >= the true distance of any candidate that can still enter, plus |q - q~|
         f32 dk = INFINITY;   // current k-th distance
         // insert (d, j) into the sorted top-TC_K list; true if it entered
         auto consider = [&](u32 j, f32 d) -> bool {
@@ -560,14 +657,16 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             }
             return true;
         };
-        // filter bound from the k-th entry; +inf until the list holds k
-        auto update_rq = [&]() {
+        // filter bound from the k-th entry; +inf until the list holds k. A
+        // candidate whose lane-ordered distance can tie or beat d has true
+        // squared distance <= sq_bound(d) (1 + 2^-16) (the sum's own rounding).
+        auto update_bound = [&]() {
             const f32 d = ld[TC_K - 1];
             dk = d;
             // the filter's relative error bounds need |q|^2 far above the
             // subnormal range: below 2^-60 every candidate is evaluated
-            const f32 tq = d < INFINITY && nqi >= 0x1p-60f ? sq_bound(d) * (1.0f + 1.0f / 65536.0f) : INFINITY;
-            rq = tq - nqi * (1.0f - 1.0f / 128.0f);
+            sq = d < INFINITY && nqi >= 0x1p-60f ? __fadd_ru(__fsqrt_ru(__fmul_ru(sq_bound(d), 1.0f + 0x1p-16f)), eqi)
+                                                 : INFINITY;
         };
         // Lookahead over the outward order (block-uniform state): bm holds the
         // positions of the current batch that some query of the block needs,
@@ -588,7 +687,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 if (active)
                     m0 = (w >= 32 ? ~0u : (1u << w) - 1u) & (ntiles - sp >= 32 ? ~0u : (1u << (ntiles - sp)) - 1u);
             } else {
-                {   // the batch's records: centroid (MMA operand, row = position), radius, |centroid|^2
+                {   // the batch's records: centroid (MMA operand, row = position); R (1 + 2^-16)
+                    // and |centroid|^2 (1 - 2^-16) - 2^-120, each rounded outward
                     const u32 pos = sp + tid;
                     if (tid < w && pos < ntiles) {
                         const float4* rec =
@@ -597,27 +697,30 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                         for (int ch = 0; ch < 8; ++ch)
                             *reinterpret_cast<float4*>(S.cent + tid * 128 + ((ch ^ (tid & 7)) << 4)) = __ldg(rec + ch);
                         const float4 rc = __ldg(rec + 8);
-                        S.trc[tid] = make_float2(rc.x, rc.y);
+                        S.trc[tid] = make_float2(__fmul_ru(rc.x, 1.0f + 0x1p-16f),
+                                                 __fsub_rd(__fmul_rd(rc.y, 1.0f - 0x1p-16f), 0x1p-120f));
                     }
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // centroids -> tensor core
                 __syncthreads();
-                // G = q . c for the 128 queries x the batch's centroids on the
-                // tensor core. The centroids are TF32-exact and the queries lose
-                // at most 2^-10 relative in TF32, so |G~ - q.c| <= 2^-10 |q||c|
-                // (FP32 accumulation included) <= 2^-11 (|q|^2 + |c|^2), and
-                // `lower` = |q|^2 + |c|^2 - 2 G~ - 2^-8 (|q|^2 + |c|^2) - 2^-120
-                // is a lower bound of |q - c|^2 with room for the FP32
-                // roundings (the absolute term covers subnormal products).
-                // A tile is skipped when lower > (dk + R)^2 (1 + 2^-10): that
-                // exceeds (dk + R~)^2 (1 + 2^-11), the computed radius R~ is
-                // within 2^-18 of the true maximum distance to the centre, so
-                // every point x of the tile has |q - x| >= |q - c| - R >
-                // dk (1 + 2^-12.5), and its lane-ordered FP32 distance
-                // (relative error < 2^-18) exceeds dk: it can neither beat nor
-                // tie the k-th entry. dk below 2^-50, |q|^2 below 2^-60 (where
-                // underflow defeats relative bounds), any non-finite value and
-                // any NaN keep the tile.
+                // G = q~ . c for the 128 queries x the batch's centroids on the
+                // tensor core. Both operands are TF32-exact (q~: the query's
+                // head; c: rounded when the record was made), so the products
+                // are exact and only the FP32 accumulation rounds:
+                // |G - q~.c| <= 2^-19 (|q~|^2 + |c|^2). With s2 = nq + |c|^2
+                // (nq rounded down, |c|^2 within 2^-19),
+                //   lower = s2 (1 - 2^-16) - 2 G - 2^-120 <= |q~ - c|^2
+                // (rounded down; the absolute term covers products in the
+                // subnormal range),
+                // and |q - c| >= |q~ - c| - e_q. A tile is skipped when
+                // lower > (sq + R (1 + 2^-16))^2, sq = sqrt(T) + e_q (T the
+                // squared-distance bound of an entering candidate, rounded
+                // up): then every point x of the tile has |q - x| >=
+                // |q - c| - R > sqrt(T) (R is within 2^-18 of the tile's
+                // largest distance to c), so it can neither beat nor tie the
+                // k-th entry. dk below 2^-50, |q|^2 below 2^-60 (where
+                // underflow defeats relative bounds), any non-finite value
+                // and any NaN keep the tile.
                 if (tid == 0) {
                     tc_fence_after();
 #pragma unroll
@@ -630,27 +733,36 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 ++ut;
                 tc_fence_after();
                 const bool ok = active && dk >= 0x1p-50f && dk < INFINITY && nqi >= 0x1p-60f;
+                const u32 lim = min(w, ntiles - sp);   // positions in this batch
+                auto valid = [&](int c) -> u32 {
+                    return lim <= u32(32 * c) ? 0u : lim - u32(32 * c) >= 32 ? ~0u : (1u << (lim - u32(32 * c))) - 1u;
+                };
 #pragma unroll
-                for (int c = 0; c < int(TC_TEST / 32); ++c) {
-                    if (u32(c) * 32 >= w) break;   // block-uniform
-                    u32 g[32];
-                    tmem_ld32(acc + ((warp * 32u) << 16) + u32(c * 32), g);
-                    u32 mc = 0;
+                for (int c2 = 0; c2 < int(TC_TEST / 64); ++c2) {
+                    if (u32(c2) * 64 >= w) break;   // block-uniform
+                    u32 g0[32], g1[32];
+                    tmem_ld32_start(acc + ((warp * 32u) << 16) + u32(c2 * 64), g0);
+                    tmem_ld32_start(acc + ((warp * 32u) << 16) + u32(c2 * 64 + 32), g1);
+                    tmem_wait2(g0, g1);
+                    u32 sk0 = 0, sk1 = 0;   // positions this query can skip
 #pragma unroll
                     for (int h = 0; h < 32; ++h) {
-                        const u32 b = u32(c * 32 + h);
-                        const float2 rc = S.trc[b];   // R, |c|^2
-                        const f32 s2 = nqi + rc.y;
-                        const f32 lower = fmaf(-2.0f, __uint_as_float(g[h]), s2) - fmaf(s2, 1.0f / 256.0f, 0x1p-120f);
-                        const f32 t2 = dk + rc.x;
-                        const f32 rhs = t2 * t2 * (1.0f + 0x1p-10f);
-                        const bool skip = ok && lower > rhs && lower <= 3.4e38f;
-                        mc |= u32(active && b < w && sp + b < ntiles && !skip) << h;
+                        const float2 ra = S.trc[c2 * 64 + h], rb = S.trc[c2 * 64 + 32 + h];
+                        const f32 la = __fmaf_rd(-2.0f, __uint_as_float(g0[h]), __fadd_rd(nql, ra.y));
+                        const f32 lb = __fmaf_rd(-2.0f, __uint_as_float(g1[h]), __fadd_rd(nql, rb.y));
+                        const f32 ta = __fadd_ru(sq, ra.x), tb = __fadd_ru(sq, rb.x);
+                        sk0 |= u32(la > __fmul_ru(ta, ta) && la <= 3.4e38f) << h;
+                        sk1 |= u32(lb > __fmul_ru(tb, tb) && lb <= 3.4e38f) << h;
                     }
-                    if (c == 0) m0 = mc;
-                    else if (c == 1) m1 = mc;
-                    else if (c == 2) m2 = mc;
-                    else m3 = mc;
+                    const u32 mc0 = active ? valid(2 * c2) & (ok ? ~sk0 : ~0u) : 0u;
+                    const u32 mc1 = active ? valid(2 * c2 + 1) & (ok ? ~sk1 : ~0u) : 0u;
+                    if (c2 == 0) {
+                        m0 = mc0;
+                        m1 = mc1;
+                    } else {
+                        m2 = mc0;
+                        m3 = mc1;
+                    }
                 }
                 tc_fence_before();
             }
@@ -706,12 +818,14 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
         };
 
         u32 tl0 = 0, tl1 = 0, nbits = 0, nl = 0;   // stage tiles, this thread's need bits, tiles loaded
+        f32 et0 = 0.0f, et1 = 0.0f;                 // the stage tiles' largest |x - x~|
         for (int s = 0; s < NSTAGE; ++s) {
             u32 T;
             bool mine;
             if (!next_tile(T, mine, ~0u)) break;
             if (tid == 0) load_stage(s, T);
-            if (s == 0) tl0 = T; else tl1 = T;
+            const f32 et = __ldg(stats + u64(T) * ST_STRIDE + 34);
+            if (s == 0) tl0 = T, et0 = et; else tl1 = T, et1 = et;
             nbits = (nbits & ~(1u << s)) | (u32(mine) << s);
             ++nl;
         }
@@ -748,18 +862,25 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
             const u32 j0 = T * TC_N;
             if (__any_sync(0xffffffffu, mine)) {
                 const unsigned char* bt = S.b[st];
+                const u16* blo = S.blo[st];
                 const u32* oid = S.oid[st];
-                // D = G - |c|^2 (1 - 2^-7) / 2 passes iff -2 D <= rq
-                const f32 t = mine ? -0.5f * rq : INFINITY;
-                // (A) filter the tile's 128 candidates, 32 per TMEM load. Survivors
-                // are rare, so the common case is a max-tree (three-input max,
-                // depth 3) per chunk; the bit mask is built only by threads
-                // holding a survivor. Padding candidates carry -3e38.
-                u32 mk[TC_N / 32];
-#pragma unroll
-                for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
-                    u32 v[32];
-                    tmem_ld32(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(chunk * 32), v);
+                // Gram filter. D = G + w_hi + w_lo with G = q~ . c~ (TF32-exact
+                // heads: exact products, FP32 accumulation, |G - q~.c~| <=
+                // 2^-19 (|q~|^2 + |c~|^2)) and -w_hi - w_lo <= |c~|^2 (1 - 2^-16) / 2,
+                // so L = nq (1 - 2^-16) - 2 D <= |q~ - c~|^2. A candidate that can
+                // enter has |q - c| <= sqrt(T), and |q - c| >= |q~ - c~| - e_q - e_c
+                // with e_c <= e_T (the tile's largest), so its L <= (sq + e_T)^2:
+                // it passes iff D >= t = (nq (1 - 2^-16) - (sq + e_T)^2) / 2
+                // (every step rounded toward passing).
+                const f32 eT = st == 0 ? et0 : et1;
+                const f32 sT = __fadd_ru(sq, eT);
+                const f32 t = mine ? 0.5f * __fsub_rd(nql, __fmul_ru(sT, sT)) : INFINITY;
+                // (A) filter the tile's 128 candidates, two 32-column TMEM loads
+                // in flight at a time. Survivors are rare, so the common case is
+                // a max-tree (three-input max, depth 3) per chunk; the bit mask
+                // is built only by threads holding a survivor. Padding
+                // candidates carry -3e38.
+                auto filt = [&](const u32 (&v)[32], int chunk) -> u32 {
                     f32 h1[11];
 #pragma unroll
                     for (int h = 0; h < 10; ++h)
@@ -774,11 +895,21 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
 #pragma unroll
                         for (int h = 0; h < 32; ++h) m |= u32(__uint_as_float(v[h]) >= t) << h;
                         const u32 cbase = j0 + u32(chunk * 32);
-                        // padding still passes while rq is +inf (list not yet full)
+                        // padding still passes while sq is +inf (list not yet full)
                         if (cbase + 32 > n) m &= cbase < n ? (1u << (n - cbase)) - 1u : 0u;
                         if (i >= cbase && i < cbase + 32) m &= ~(1u << (i - cbase));
                     }
-                    mk[chunk] = m;
+                    return m;
+                };
+                u32 mk[TC_N / 32];
+#pragma unroll
+                for (int c2 = 0; c2 < TC_N / 64; ++c2) {
+                    u32 v0[32], v1[32];
+                    tmem_ld32_start(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(c2 * 64), v0);
+                    tmem_ld32_start(tmem + u32(sb) * TC_N + ((warp * 32u) << 16) + u32(c2 * 64 + 32), v1);
+                    tmem_wait2(v0, v1);
+                    mk[2 * c2] = filt(v0, 2 * c2);
+                    mk[2 * c2 + 1] = filt(v1, 2 * c2 + 1);
                 }
                 // (B) survivors. Few per tile (after the first), spread over the
                 // lanes: the warp queues its (query, candidate) pairs in shared
@@ -800,14 +931,17 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                 if (total > u32(TC_Q)) {
                     // Mostly the first tile of a block: the lists are empty and
                     // every candidate passed. The tile bounds its own k-th
-                    // distance: with L = |q|^2 (1 - 2^-7) - 2 D a lower bound of
-                    // the true squared distance s (the filter's), s <= L +
-                    // 3 2^-8 (|q|^2 + |c|^2) and |c|^2 <= 2 |q|^2 + 2 s give
-                    // U = (L + 9 2^-8 |q|^2) / (1 - 6 2^-8) >= s. The k-th
-                    // smallest of 32 group minima of U (4 candidates a group)
-                    // is U of k distinct candidates, so B >= the final k-th
-                    // squared distance; a candidate with L > B (1 + 2^-12) can
-                    // never enter (its lane-ordered distance exceeds the k-th).
+                    // distance. For a candidate |q~ - c~|^2 <= (|q~|^2 + |c~|^2)
+                    // (1 + 2^-18) - 2 (D + w_hi + w_lo) and |c~|^2 <= -2 (w_hi + w_lo)
+                    // (1 + 2^-15), so with N_T the tile's largest |c~|^2,
+                    // u = nq (1 + 2^-16) - 2 D + 2^-14 N_T >= |q~ - c~|^2 (rounded
+                    // up; a negative or NaN u, which only overflow can make, is
+                    // no bound). The k-th smallest of 32 group minima of u (4
+                    // candidates a group) is u of k distinct candidates, whose
+                    // true distances are then <= sqrt(u_k) + e_q + e_T; with the
+                    // lane-ordered sums' rounding, no candidate farther than
+                    // s_B = (sqrt(u_k) + e_q + e_T) (1 + 2^-14) can enter, so one
+                    // with L > (s_B + e_q + e_T)^2 is dropped.
                     {
                         f32 gm[32];
 #pragma unroll
@@ -823,14 +957,12 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                                 gm[chunk * 8 + g] = fmaxf(fmax3(d4[0], d4[1], d4[2]), d4[3]);
                             }
                         }
-                        const f32 a = nqi * (1.0f - 1.0f / 128.0f);
-                        const f32 c1 = nqi * (1.0f + 0x1p-10f) * (9.0f / 256.0f);
-                        const f32 c2 = (1.0f + 0x1p-20f) / (1.0f - 6.0f / 256.0f);
+                        const f32 NT = __ldg(stats + u64(T) * ST_STRIDE + 35);
+                        const f32 au = __fmaf_ru(NT, 0x1p-14f, __fmul_ru(nqi, 1.0f + 0x1p-16f));
 #pragma unroll
                         for (int g = 0; g < 32; ++g) {
-                            const f32 u = (fmaf(-2.0f, gm[g], a) + c1) * c2 +
-                                          0x1p-20f * (fabsf(a) + 2.0f * fabsf(gm[g]) + c1);
-                            gm[g] = u == u ? u : INFINITY;   // no candidate (or NaN): no bound
+                            const f32 u = __fmaf_ru(-2.0f, gm[g], au);
+                            gm[g] = u >= 0.0f ? u : INFINITY;   // no candidate in the group: +inf
                         }
                         bitonic_sort<32>(gm);
                         // B = gm[k - 1] by a bit-mask select (an opaque mask, so the
@@ -840,11 +972,11 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                         f32 B = INFINITY;
 #pragma unroll
                         for (int g = 0; g < TC_K; ++g) B = (ksel >> g) & 1u ? gm[g] : B;
-                        const f32 Bp = B * (1.0f + 0x1p-12f);
+                        const f32 sB = __fmul_ru(__fadd_ru(__fadd_ru(__fsqrt_ru(B), eqi), eT), 1.0f + 0x1p-14f);
+                        const f32 sB2 = __fadd_ru(__fadd_ru(sB, eqi), eT);
                         // (relative bounds: |q|^2 far above the subnormal range)
-                        const f32 t2 = B < INFINITY && nqi >= 0x1p-60f
-                                           ? 0.5f * (a - Bp) - 0x1p-20f * (fabsf(a) + fabsf(Bp))
-                                           : -INFINITY;
+                        const f32 t2 = B < INFINITY && nqi >= 0x1p-60f ? 0.5f * __fsub_rd(nql, __fmul_ru(sB2, sB2))
+                                                                      : -INFINITY;
                         if (__any_sync(0xffffffffu, t2 > t)) {
                             const f32 tt = fmaxf(t, t2);
 #pragma unroll 1
@@ -863,18 +995,18 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                     }
                     bool changed = false;
                     f32 qa[TC_DIM];   // this thread's query, from the query tile
-                    swz_row(S.a, row, qa);
+                    raw_row(S.a, S.alo, row, qa);
 #pragma unroll 1
                     for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
 #pragma unroll 1
                         for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1) {
                             const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
                             f32 cb[TC_DIM];
-                            swz_row(bt, rr, cb);
+                            raw_row(bt, blo, rr, cb);
                             changed |= consider(oid[rr], __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{qa}, RegVec<TC_DIM>{cb}, TC_DIM)));
                         }
                     }
-                    if (changed) update_rq();
+                    if (changed) update_bound();
                 } else if (total) {
                     u32* wq = S.q[warp];
                     f32* wr = S.r[warp];
@@ -888,8 +1020,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                     for (u32 p = lane; p < total; p += 32) {
                         const u32 e = wq[p];
                         f32 qa[TC_DIM], cb[TC_DIM];
-                        swz_row(S.a, warp * 32 + (e >> 7), qa);
-                        swz_row(bt, e & 127u, cb);
+                        raw_row(S.a, S.alo, warp * 32 + (e >> 7), qa);
+                        raw_row(bt, blo, e & 127u, cb);
                         wr[p] = __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{qa}, RegVec<TC_DIM>{cb}, TC_DIM));
                     }
                     __syncwarp();
@@ -897,7 +1029,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
 #pragma unroll 1
                     for (u32 kk = 0; kk < tcnt; ++kk)
                         changed |= consider(oid[wq[base + kk] & 127u], wr[base + kk]);
-                    if (changed) update_rq();
+                    if (changed) update_bound();
                     __syncwarp();   // the queue is reused by the next tile
                 }
             }
@@ -921,7 +1053,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const f32* __restrict__ x, con
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     load_stage(st, Tn);
                 }
-                if (st == 0) tl0 = Tn; else tl1 = Tn;
+                const f32 et = __ldg(stats + u64(Tn) * ST_STRIDE + 34);
+                if (st == 0) tl0 = Tn, et0 = et; else tl1 = Tn, et1 = et;
                 nbits = (nbits & ~(1u << st)) | (u32(mn) << st);
                 ++nl;
             }
@@ -987,7 +1120,7 @@ bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x) {
 
 // Exact kNN lists through the tile order and the tensor-core filter; sets
 // the context's counts of exact evaluations and computed Gram tiles.
-// Slots: S_TC_* (regrouped copy and tile records), S_MISC0/1/3, S_COUNT, and
+// Slots: S_TC_* (regrouped copy, its low bits and error terms, tile records), S_MISC0/1/3, S_COUNT, and
 // the radix sort's own (S_SORT_*, S_SCAN*).
 void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     const u32 ntiles = div_up(n, TC_N);
@@ -1029,7 +1162,9 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
             perm = radix_sort<u32>(c, key2, val2, n, kb, vb, bits + 4) ? vb : val2;
         }
     }
-    f32* xp = c->arena.get<f32>(S_TC_X, u64(n) * TC_DIM);
+    f32* xh = c->arena.get<f32>(S_TC_X, u64(n) * TC_DIM);
+    u16* lo = c->arena.get<u16>(S_TC_LO, wpad * TC_DIM);
+    f32* eq = c->arena.get<f32>(S_TC_ERR, wpad);
     u32* oid = c->arena.get<u32>(S_TC_PERM, wpad);
     f32* nq = c->arena.get<f32>(S_MISC0, wpad);
     float4* aug = c->arena.get<float4>(S_MISC3, wpad);
@@ -1038,22 +1173,22 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 2);
     TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
     TT_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
-    k_tc_gather<<<div_up(wpad, 256), 256, 0, c->stream>>>(x, n, u32(wpad), perm, xp, oid, nq, aug);
+    k_tc_gather<<<div_up(wpad, 256), 256, 0, c->stream>>>(x, n, u32(wpad), perm, xh, lo, oid, nq, eq, aug);
     TT_LAUNCH("k_tc_gather");
-    k_tc_stats<<<div_up(u64(ntiles) * 32, 256), 256, 0, c->stream>>>(xp, n, ntiles, stats);
+    k_tc_stats<<<div_up(u64(ntiles) * 32, 256), 256, 0, c->stream>>>(xh, lo, nq, eq, n, ntiles, stats);
     TT_LAUNCH("k_tc_stats");
     CUtensorMap map;
     const cuuint64_t gdim[2] = {cuuint64_t(TC_DIM), cuuint64_t(n)};
     const cuuint64_t gstride[1] = {cuuint64_t(TC_DIM) * 4};
     const cuuint32_t box[2] = {cuuint32_t(TC_DIM), cuuint32_t(TC_M)};
     const cuuint32_t estride[2] = {1, 1};
-    const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, xp, gdim, gstride, box, estride,
+    const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, xh, gdim, gstride, box, estride,
                                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(TT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
     TT_CUDA(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)));
     const u32 grid = std::min<u32>(ntiles, 2 * u32(c->sms));
-    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, x, xp, oid, n, k, nq, aug, stats, ids, dists, ctl, ctl + 1, cnt);
+    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, lo, eq, oid, n, k, nq, aug, stats, ids, dists, ctl, ctl + 1, cnt);
     TT_LAUNCH("k_knn_tc");
     c->launches += 3;
     u32 e = 0;
