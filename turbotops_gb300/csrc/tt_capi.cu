@@ -161,6 +161,12 @@ void tt_ctx_destroy(tt_ctx* c) {
         cudaStreamDestroy(c->aux);
     }
     if (c->aux_ev) cudaEventDestroy(c->aux_ev);
+    if (c->side) {
+        cudaStreamSynchronize(c->side);
+        cudaStreamDestroy(c->side);
+    }
+    for (auto e : c->side_ev)
+        if (e) cudaEventDestroy(e);
     delete c;
 }
 

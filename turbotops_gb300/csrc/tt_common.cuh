@@ -125,7 +125,7 @@ enum Slot : int {
     S_KNN_D, S_KNN_I, S_GRAPH_KEYS, S_GRAPH_TMP, S_PIV,           // kNN / graph / pivots
     S_SCAN2, S_SCAN3, S_MISC0, S_MISC1, S_MISC2, S_MISC3, S_ROWMAX, S_GRAPH_RP, S_ASM0, S_ASM1, S_ASM2, S_ASM3, S_ASM4,
     S_TC_X, S_TC_PERM, S_TC_STATS, S_TC_KEYS, S_TC_VALS, S_TC_PIV,   // tensor-core kNN (tile order)
-    S_TC_KEY2, S_TC_VAL2, S_TC_CELL, S_TC_LO, S_TC_ERR,
+    S_TC_KEY2, S_TC_VAL2, S_TC_CELL, S_TC_LO, S_TC_ERR, S_TC_SPV,
     S_EDGE_CNT, S_EDGE_SORT, S_EDGE_IDX, S_EDGE_INV,               // ordered edge generation
     S_NSLOTS
 };
@@ -148,4 +148,44 @@ struct tt_ctx {
     uint64_t filter_tiles = 0;      // 128 x 128 Gram tiles the last tensor-core kNN computed
     cudaStream_t aux = nullptr;     // copies overlapped with compute (created on first use)
     cudaEvent_t aux_ev = nullptr;
+    cudaStream_t side = nullptr;    // kernels overlapped with the main stream's (created on first use)
+    cudaEvent_t side_ev[2] = {nullptr, nullptr};
 };
+
+namespace tt {
+// The context's side stream (non-blocking, so it also runs beside a legacy
+// default main stream), ordered after everything issued so far on the main
+// stream. Whoever forks work onto it joins it back (side_join) before the
+// main stream reads the results.
+inline cudaStream_t side_after_main(tt_ctx* c) {
+    if (!c->side) TT_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    for (auto& e : c->side_ev)
+        if (!e) TT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    TT_CUDA(cudaEventRecord(c->side_ev[0], c->stream));
+    TT_CUDA(cudaStreamWaitEvent(c->side, c->side_ev[0], 0));
+    return c->side;
+}
+// The main stream waits for everything issued so far on the side stream.
+inline void side_join(tt_ctx* c) {
+    TT_CUDA(cudaEventRecord(c->side_ev[1], c->side));
+    TT_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[1], 0));
+}
+// Joins on scope exit unless released; on an exception the side stream is
+// drained instead, so no side kernel outlives the call that launched it.
+struct SideScope {
+    tt_ctx* c;
+    bool open = false;
+    explicit SideScope(tt_ctx* ctx) : c(ctx) {}
+    cudaStream_t fork() {
+        open = true;
+        return side_after_main(c);
+    }
+    void join() {
+        if (open) side_join(c);
+        open = false;
+    }
+    ~SideScope() {
+        if (open) cudaStreamSynchronize(c->side);
+    }
+};
+}  // namespace tt

@@ -435,13 +435,18 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
     u32* emw = c->arena.get<u32>(S_EDGE_TMP, m + 1);
     u8* emf = c->arena.get<u8>(S_MISC2, m + 1);
     TT_CUDA(cudaMemsetAsync(tree, 0, m + 1, c->stream));
+    // The apparent/emergent scan and the spanning forest read the same sorted
+    // edges and write disjoint flags: the scan runs on the side stream while
+    // the forest's rounds (and their host round trips) run on the main one.
+    SideScope side(c);
     if (maxdim >= 1 && m) {
+        u32* inv = c->arena.get<u32>(S_EDGE_INV, m + 1);
+        cudaStream_t s = side.fork();
         if (cx.mat)
-            k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, c->stream>>>(cx.mat, n, out.keys, m, app, emw, emf);
+            k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, s>>>(cx.mat, n, out.keys, m, app, emw, emf);
         else
-            k_apparent_csr<<<grid_for(m, 256), 256, 0, c->stream>>>(CsrCx{cx.rp, cx.ci, cx.w}, out.keys,
-                                                                     c->arena.get<u32>(S_EDGE_INV, m + 1), m, app,
-                                                                     emw, emf);
+            k_apparent_csr<<<grid_for(m, 256), 256, 0, s>>>(CsrCx{cx.rp, cx.ci, cx.w}, out.keys, inv, m, app, emw,
+                                                            emf);
         TT_LAUNCH("k_apparent");
         ++c->launches;
     }
@@ -480,6 +485,7 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
             if (h[1] == 0) break;
         }
     }
+    side.join();   // the flags of the scan
     // ordered compaction of H0 deaths and columns
     const int want_cols = maxdim >= 1;
     u64* fh = c->arena.get<u64>(S_MISC0, 4 * m + 8);

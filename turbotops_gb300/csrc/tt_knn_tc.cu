@@ -130,7 +130,7 @@ __device__ __forceinline__ void swz_row(const unsigned char* tile, u32 r, f32 (&
 }
 
 // Row r of a tile reassembled: the TF32-exact head from the swizzled tile,
-// the 13 low mantissa bits from the low-bits array (lo_index layout).
+// the 13 low mantissa bits from the low-bits array (layout at k_tc_tiles).
 __device__ __forceinline__ void raw_row(const unsigned char* tile, const u16* lo, u32 r, f32 (&o)[TC_DIM]) {
     swz_row(tile, r, o);
     const uint4* lr = reinterpret_cast<const uint4*>(lo + r * TC_DIM);
@@ -291,15 +291,18 @@ __device__ __forceinline__ u32 spiral_tile(u32 B, u32 s, u32 ntiles) {
 // nearest-first chain from pivot 0 (ties to the lower index), so that
 // pivots of one region of space sit next to each other in the order.
 // The block fills the P x P distance matrix in shared memory; one warp then
-// walks the chain (a warp argmin over one matrix row per step).
-__global__ void __launch_bounds__(256) k_tc_pivots(const f32* __restrict__ x, u32 n, u32 P, f32* __restrict__ piv,
-                                                   u32* __restrict__ rank) {
+// walks the chain (two warp reductions per step: the smallest distance,
+// then the lowest pivot index holding it; non-negative float bits order
+// like the floats).
+constexpr int PIV_THREADS = 1024;
+__global__ void __launch_bounds__(PIV_THREADS) k_tc_pivots(const f32* __restrict__ x, u32 n, u32 P,
+                                                          f32* __restrict__ piv, u32* __restrict__ rank) {
     extern __shared__ f32 psm[];
     f32* pv = psm;                       // P x (TC_DIM + 1)
     f32* dm = psm + P * (TC_DIM + 1);    // P x P
     for (u32 t = threadIdx.x; t < P * TC_DIM; t += blockDim.x) {
         const u32 p = t / TC_DIM, k = t % TC_DIM;
-        const f32 v = x[(u64(p) * n / P) * TC_DIM + k];
+        const f32 v = __ldg(x + (u64(p) * n / P) * TC_DIM + k);
         pv[p * (TC_DIM + 1) + k] = v;
         piv[u64(p) * TC_DIM + k] = v;
     }
@@ -321,56 +324,72 @@ __global__ void __launch_bounds__(256) k_tc_pivots(const f32* __restrict__ x, u3
     if (lane == 0) rank[0] = 0;
     u32 cur = 0;
     for (u32 step = 1; step < P; ++step) {
-        unsigned long long key = ~0ull;
-        for (u32 i = 0, p = lane; p < P; ++i, p += 32)
-            if (!((visited >> i) & 1u))
-                key = min(key, (unsigned long long)((u64(fbits(dm[cur * P + p])) << 32) | p));
-#pragma unroll
-        for (int o = 16; o; o >>= 1) key = min(key, (unsigned long long)__shfl_xor_sync(0xffffffffu, key, o));
-        cur = u32(key & 0xffffffffu);
+        u32 bd = 0xffffffffu, bp = 0xffffffffu;   // this lane's nearest unvisited pivot
+        for (u32 i = 0, p = lane; p < P; ++i, p += 32) {
+            const u32 db = fbits(dm[cur * P + p]);
+            if (!((visited >> i) & 1u) && (bp == 0xffffffffu || db < bd)) {
+                bd = db;
+                bp = p;
+            }
+        }
+        const u32 md = __reduce_min_sync(0xffffffffu, bd);
+        cur = __reduce_min_sync(0xffffffffu, bp != 0xffffffffu && bd == md ? bp : 0xffffffffu);
         if (lane == 0) rank[cur] = step;
         if ((cur & 31u) == lane) visited |= 1u << (cur >> 5);
     }
 }
 
 // key[i] = chain rank of the nearest pivot of point i (ties to the lower
-// pivot index), val[i] = i.
+// pivot index), val[i] = i. Two points a thread; the distance order comes
+// from |p|^2 - 2 x.p (the assignment only shapes the tile order: any
+// nearest-pivot choice leaves the lists unchanged).
 __global__ void k_tc_assign(const f32* __restrict__ x, u32 n, const f32* __restrict__ piv, const u32* __restrict__ rank,
                             u32 P, u64* __restrict__ key, u32* __restrict__ val) {
-    extern __shared__ f32 sp[];
-    for (u32 t = threadIdx.x; t < P * TC_DIM; t += blockDim.x) sp[t] = piv[t];
+    extern __shared__ float4 sp4[];      // P x 8 float4, then P norms
+    f32* pn = reinterpret_cast<f32*>(sp4 + P * 8);
+    for (u32 t = threadIdx.x; t < P * 8; t += blockDim.x) sp4[t] = reinterpret_cast<const float4*>(piv)[t];
     __syncthreads();
-    const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    f32 q[TC_DIM];
-    const float4* xr = reinterpret_cast<const float4*>(x + u64(i) * TC_DIM);
+    for (u32 p = threadIdx.x; p < P; p += blockDim.x) {
+        f32 s = 0.0f;
+#pragma unroll
+        for (int ch = 0; ch < 8; ++ch) {
+            const float4 c = sp4[p * 8 + ch];
+            s = fmaf(c.x, c.x, fmaf(c.y, c.y, fmaf(c.z, c.z, fmaf(c.w, c.w, s))));
+        }
+        pn[p] = s;
+    }
+    __syncthreads();
+    const u32 i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i0 >= n) return;
+    const u32 i1 = min(i0 + 1, n - 1);
+    f32 q0[TC_DIM], q1[TC_DIM];
 #pragma unroll
     for (int ch = 0; ch < 8; ++ch) {
-        const float4 t4 = __ldg(xr + ch);
-        q[4 * ch] = t4.x;
-        q[4 * ch + 1] = t4.y;
-        q[4 * ch + 2] = t4.z;
-        q[4 * ch + 3] = t4.w;
+        const float4 a = __ldg(reinterpret_cast<const float4*>(x + u64(i0) * TC_DIM) + ch);
+        const float4 b = __ldg(reinterpret_cast<const float4*>(x + u64(i1) * TC_DIM) + ch);
+        q0[4 * ch] = a.x, q0[4 * ch + 1] = a.y, q0[4 * ch + 2] = a.z, q0[4 * ch + 3] = a.w;
+        q1[4 * ch] = b.x, q1[4 * ch + 1] = b.y, q1[4 * ch + 2] = b.z, q1[4 * ch + 3] = b.w;
     }
-    u32 best = 0;
-    f32 bd = INFINITY;
+    u32 b0 = 0, b1 = 0;
+    f32 d0 = INFINITY, d1 = INFINITY;
     for (u32 p = 0; p < P; ++p) {
-        const f32* c = sp + p * TC_DIM;
-        f32 d0 = 0.0f, d1 = 0.0f;
+        f32 s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
-        for (int k = 0; k < TC_DIM; k += 2) {
-            const f32 t0 = q[k] - c[k], t1 = q[k + 1] - c[k + 1];
-            d0 = fmaf(t0, t0, d0);
-            d1 = fmaf(t1, t1, d1);
+        for (int ch = 0; ch < 8; ++ch) {
+            const float4 c = sp4[p * 8 + ch];
+            s0 = fmaf(q0[4 * ch], c.x, fmaf(q0[4 * ch + 1], c.y, fmaf(q0[4 * ch + 2], c.z, fmaf(q0[4 * ch + 3], c.w, s0))));
+            s1 = fmaf(q1[4 * ch], c.x, fmaf(q1[4 * ch + 1], c.y, fmaf(q1[4 * ch + 2], c.z, fmaf(q1[4 * ch + 3], c.w, s1))));
         }
-        const f32 d = d0 + d1;
-        if (d < bd) {
-            bd = d;
-            best = p;
-        }
+        const f32 e0 = fmaf(-2.0f, s0, pn[p]), e1 = fmaf(-2.0f, s1, pn[p]);
+        if (e0 < d0) d0 = e0, b0 = p;
+        if (e1 < d1) d1 = e1, b1 = p;
     }
-    key[i] = rank[best];
-    val[i] = i;
+    key[i0] = rank[b0];
+    val[i0] = i0;
+    if (i0 + 1 < n) {
+        key[i0 + 1] = rank[b1];
+        val[i0 + 1] = i0 + 1;
+    }
 }
 
 // First position of each cell (chain rank) in the rank-sorted keys; cell P
@@ -390,15 +409,33 @@ __global__ void k_tc_cells(const u64* __restrict__ skey, u32 n, u32 P, u32* __re
 // Second level: every point of a cell (s points) joins the nearest of
 // min(16, max(1, s / 128)) sub-pivots (the cell's points at strided
 // positions, ties to the lower one); key = cell << 4 | sub-pivot, so that
-// the tiles of a cell follow its sub-cells.
+// the tiles of a cell follow its sub-cells. k_tc_subpiv gathers the
+// sub-pivots into a table (row cell * 16 + j, then |.|^2), one warp a row.
+__host__ __device__ __forceinline__ u32 sub_count(u32 s) { return s / 128u < 1u ? 1u : s / 128u > 16u ? 16u : s / 128u; }
+
+__global__ void k_tc_subpiv(const f32* __restrict__ x, const u32* __restrict__ perm, const u32* __restrict__ cell_off,
+                            u32 P, f32* __restrict__ spv, f32* __restrict__ spn) {
+    const u32 wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (wid >= P * 16) return;
+    const u32 cell = wid >> 4, j = wid & 15u;
+    const u32 o = cell_off[cell], s = cell_off[cell + 1] - o;
+    if (s == 0 || j >= sub_count(s)) return;
+    const f32 v = __ldg(x + u64(perm[o + u32(u64(j) * s / sub_count(s))]) * TC_DIM + lane);
+    spv[u64(wid) * TC_DIM + lane] = v;
+    f32 q = v * v;
+#pragma unroll
+    for (int off = 16; off; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
+    if (lane == 0) spn[wid] = q;
+}
+
 __global__ void k_tc_assign2(const f32* __restrict__ x, u32 n, const u64* __restrict__ skey,
-                             const u32* __restrict__ perm, const u32* __restrict__ cell_off, u64* __restrict__ key2,
+                             const u32* __restrict__ perm, const u32* __restrict__ cell_off,
+                             const f32* __restrict__ spv, const f32* __restrict__ spn, u64* __restrict__ key2,
                              u32* __restrict__ val2) {
     const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const u32 cell = u32(skey[r]);
-    const u32 o = cell_off[cell], s = cell_off[cell + 1] - o;
-    const u32 S = min(16u, max(1u, s / 128u));
+    const u32 S = sub_count(cell_off[cell + 1] - cell_off[cell]);
     const u32 self = perm[r];
     f32 q[TC_DIM];
     const float4* xr = reinterpret_cast<const float4*>(x + u64(self) * TC_DIM);
@@ -413,21 +450,16 @@ __global__ void k_tc_assign2(const f32* __restrict__ x, u32 n, const u64* __rest
     u32 best = 0;
     f32 bd = INFINITY;
     for (u32 j = 0; j < S; ++j) {
-        const float4* pr = reinterpret_cast<const float4*>(x + u64(perm[o + u32(u64(j) * s / S)]) * TC_DIM);
-        f32 d0 = 0.0f, d1 = 0.0f;
+        const float4* pr = reinterpret_cast<const float4*>(spv + u64(cell * 16 + j) * TC_DIM);
+        f32 d = 0.0f;
 #pragma unroll
         for (int ch = 0; ch < 8; ++ch) {
-            const float4 t4 = __ldg(pr + ch);
-            const f32 a0 = q[4 * ch] - t4.x, a1 = q[4 * ch + 1] - t4.y;
-            const f32 a2 = q[4 * ch + 2] - t4.z, a3 = q[4 * ch + 3] - t4.w;
-            d0 = fmaf(a0, a0, d0);
-            d1 = fmaf(a1, a1, d1);
-            d0 = fmaf(a2, a2, d0);
-            d1 = fmaf(a3, a3, d1);
+            const float4 c = __ldg(pr + ch);
+            d = fmaf(q[4 * ch], c.x, fmaf(q[4 * ch + 1], c.y, fmaf(q[4 * ch + 2], c.z, fmaf(q[4 * ch + 3], c.w, d))));
         }
-        const f32 d = d0 + d1;
-        if (d < bd) {
-            bd = d;
+        const f32 e = fmaf(-2.0f, d, __ldg(spn + cell * 16 + j));
+        if (e < bd) {
+            bd = e;
             best = j;
         }
     }
@@ -435,121 +467,140 @@ __global__ void k_tc_assign2(const f32* __restrict__ x, u32 n, const u64* __rest
     val2[r] = self;
 }
 
-// Index of coordinate k of row r in the low-bits array: u16 per coordinate,
-// 64 bytes per row, 16-byte chunk c (coordinates 8c..8c+7) stored at chunk
-// position c ^ ((r >> 1) & 3), so that eight consecutive rows read by one
-// quarter-warp hit distinct banks.
-__host__ __device__ __forceinline__ u32 lo_index(u32 r, u32 k) {
-    return r * TC_DIM + ((((k >> 3) ^ ((r >> 1) & 3u)) << 3) | (k & 7u));
-}
-
-// Regrouped copy in two parts. xh[r]: the coordinates of x[perm[r]] with
-// their 13 low mantissa bits cleared (TF32-exact: the tensor core multiplies
-// them without rounding). lo[r]: those 13 bits, u16 per coordinate, so that
+// The low-bits array: u16 per coordinate, 64 bytes per row, 16-byte chunk
+// c (coordinates 8c..8c+7) of row r stored at chunk position c ^ ((r >> 1)
+// & 3), so that eight consecutive rows read by one quarter-warp hit
+// distinct banks.
+// Regrouped copy in two parts, one block (128 threads) per tile, thread r
+// on row T * 128 + r. xh[row]: the coordinates of x[perm[row]] with their
+// 13 low mantissa bits cleared (TF32-exact: the tensor core multiplies them
+// without rounding). lo[row]: those 13 bits, u16 per coordinate, so that
 // xh | lo is the point again, bit for bit (the exact path's input). Per row:
 // nq = |xh|^2 rounded down; e >= |x - xh| (rounded up; a coordinate below
 // 2^-126 counts in full, in case the tensor core flushes it); the
 // augmentation row (w_hi, w_lo, 0, 0) with
 // -w_hi - w_lo in [W (1 - 2^-20), W], W = nq (1 - 2^-16) / 2 (two TF32-exact
 // parts, both truncated toward zero); the original id. Rows [n, wpad) are
-// padding (augmentation -3e38: never passes; id ~0).
-__global__ void k_tc_gather(const f32* __restrict__ x, u32 n, u32 wpad, const u32* __restrict__ perm,
-                            f32* __restrict__ xh, u16* __restrict__ lo, u32* __restrict__ ids,
-                            f32* __restrict__ nq, f32* __restrict__ eq, float4* __restrict__ aug) {
-    const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= wpad) return;
+// padding (augmentation -3e38: never passes; id ~0). Then the tile record:
+// centroid (the mean of the rows, rounded to TF32 so that it enters the
+// lookahead product exactly; the bound holds for every centre), radius
+// sqrt(max |x - c|^2) (a NaN coordinate makes it NaN: the tile is then never
+// skipped), |c|^2, and the tile's largest e and nq (the Gram filter's
+// per-tile error terms).
+__global__ void __launch_bounds__(TC_N) k_tc_tiles(const f32* __restrict__ x, u32 n, const u32* __restrict__ perm,
+                                                  f32* __restrict__ xh, u16* __restrict__ lo, u32* __restrict__ ids,
+                                                  f32* __restrict__ nq, f32* __restrict__ eq,
+                                                  float4* __restrict__ aug, f32* __restrict__ stats) {
+    __shared__ f32 rows[TC_N][TC_DIM + 1];
+    __shared__ f32 part[4][TC_DIM];
+    __shared__ f32 cent[TC_DIM];
+    __shared__ f32 red[3][4];
+    const u32 T = blockIdx.x, t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const u32 r = T * TC_N + t;
+    const bool live = r < n;
+    f32 v[TC_DIM];
+    f32 s = 0.0f, e2 = 0.0f;
     uint4* lr = reinterpret_cast<uint4*>(lo + u64(r) * TC_DIM);
-    if (r >= n) {
+    if (live) {
+        const u32 src = perm[r];
+        const float4* xr = reinterpret_cast<const float4*>(x + u64(src) * TC_DIM);
+        float4* xo = reinterpret_cast<float4*>(xh + u64(r) * TC_DIM);
+        u32 lw[16];   // the low bits, two coordinates per word
+#pragma unroll
+        for (int ch = 0; ch < 8; ++ch) {
+            const float4 t4 = __ldg(xr + ch);
+            v[4 * ch] = t4.x, v[4 * ch + 1] = t4.y, v[4 * ch + 2] = t4.z, v[4 * ch + 3] = t4.w;
+            f32 h[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const f32 ve = v[4 * ch + e];
+                const u32 u = __float_as_uint(ve);
+                h[e] = __uint_as_float(u & 0xffffe000u);
+                s = __fmaf_rd(h[e], h[e], s);   // exact products (11-bit significands), sum rounded down
+                const f32 b = fabsf(ve) < 0x1p-126f ? fabsf(ve) : fabsf(ve - h[e]);
+                e2 = __fmaf_ru(b, b, e2);
+                const u32 l = u & 0x1fffu;
+                if (e & 1) lw[2 * ch + (e >> 1)] |= l << 16;
+                else lw[2 * ch + (e >> 1)] = l;
+            }
+            xo[ch] = make_float4(h[0], h[1], h[2], h[3]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            lr[c ^ ((r >> 1) & 3u)] = make_uint4(lw[4 * c], lw[4 * c + 1], lw[4 * c + 2], lw[4 * c + 3]);
+        const f32 w = -__fmul_rd(s, 0.5f * (1.0f - 0x1p-16f));
+        // head and remainder, both truncated toward zero; a non-finite w keeps
+        // its head and gets a zero tail
+        const f32 hi = __uint_as_float(__float_as_uint(w) & 0xffffe000u);
+        const f32 rem = isfinite(w) ? w - hi : 0.0f;   // exact
+        aug[r] = make_float4(hi, __uint_as_float(__float_as_uint(rem) & 0xffffe000u), 0.0f, 0.0f);
+        ids[r] = src;
+        e2 = __fsqrt_ru(e2);
+    } else {
+#pragma unroll
+        for (int k = 0; k < TC_DIM; ++k) v[k] = 0.0f;
         aug[r] = make_float4(-3.0e38f, 0.0f, 0.0f, 0.0f);
         ids[r] = 0xffffffffu;
-        nq[r] = 0.0f;
-        eq[r] = 0.0f;
 #pragma unroll
         for (int c = 0; c < 4; ++c) lr[c] = make_uint4(0u, 0u, 0u, 0u);
-        return;
     }
-    const u32 src = perm[r];
-    const float4* xr = reinterpret_cast<const float4*>(x + u64(src) * TC_DIM);
-    float4* xo = reinterpret_cast<float4*>(xh + u64(r) * TC_DIM);
-    f32 s = 0.0f, e2 = 0.0f;
-    u32 lw[16];   // the low bits, two coordinates per word
-#pragma unroll
-    for (int ch = 0; ch < 8; ++ch) {
-        const float4 t4 = __ldg(xr + ch);
-        const f32 v[4] = {t4.x, t4.y, t4.z, t4.w};
-        f32 h[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const u32 u = __float_as_uint(v[e]);
-            h[e] = __uint_as_float(u & 0xffffe000u);
-            s = __fmaf_rd(h[e], h[e], s);   // exact products (11-bit significands), sum rounded down
-            const f32 b = fabsf(v[e]) < 0x1p-126f ? fabsf(v[e]) : fabsf(v[e] - h[e]);
-            e2 = __fmaf_ru(b, b, e2);
-            const u32 l = u & 0x1fffu;
-            if (e & 1) lw[2 * ch + (e >> 1)] |= l << 16;
-            else lw[2 * ch + (e >> 1)] = l;
-        }
-        xo[ch] = make_float4(h[0], h[1], h[2], h[3]);
-    }
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-        lr[c ^ ((r >> 1) & 3u)] = make_uint4(lw[4 * c], lw[4 * c + 1], lw[4 * c + 2], lw[4 * c + 3]);
     nq[r] = s;
-    eq[r] = __fsqrt_ru(e2);
-    const f32 w = -__fmul_rd(s, 0.5f * (1.0f - 0x1p-16f));
-    // head and remainder, both truncated toward zero; a non-finite w keeps
-    // its head and gets a zero tail
-    const f32 hi = __uint_as_float(__float_as_uint(w) & 0xffffe000u);
-    const f32 rem = isfinite(w) ? w - hi : 0.0f;   // exact
-    aug[r] = make_float4(hi, __uint_as_float(__float_as_uint(rem) & 0xffffe000u), 0.0f, 0.0f);
-    ids[r] = src;
-}
-
-// One warp per tile, lane k on coordinate k of the reassembled points
-// (xh | lo): centroid, |centroid|^2, radius = sqrt(max_x |x - c|^2), and the
-// tile's largest e and nq (the Gram filter's per-tile error terms).
-__global__ void k_tc_stats(const f32* __restrict__ xh, const u16* __restrict__ lo, const f32* __restrict__ nq,
-                           const f32* __restrict__ eq, u32 n, u32 ntiles, f32* __restrict__ stats) {
-    const u32 w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= ntiles) return;
-    const u32 r0 = w * TC_N, r1 = min(r0 + TC_N, n);
-    auto coord = [&](u32 r) {
-        return __uint_as_float(__float_as_uint(xh[u64(r) * TC_DIM + lane]) | u32(lo[lo_index(r, lane)]));
-    };
-    f32 sum = 0.0f;
-    for (u32 r = r0; r < r1; ++r) sum += coord(r);
-    // the centroid is any point (the bound holds for every centre): rounded
-    // to a TF32-exact value, it enters the lookahead product without error
-    const f32 c = __uint_as_float(__float_as_uint(sum / f32(r1 - r0)) & 0xffffe000u);
-    f32 cc = c * c;
+    eq[r] = e2;
+    // centroid: column sums through shared memory (rows of 33 floats: no bank conflicts)
 #pragma unroll
-    for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(0xffffffffu, cc, o);
-    f32 r2 = 0.0f;
-    for (u32 r = r0; r < r1; ++r) {
-        const f32 t = coord(r) - c;
-        f32 d = t * t;
+    for (int k = 0; k < TC_DIM; ++k) rows[t][k] = v[k];
+    __syncthreads();
+    {
+        f32 cs = 0.0f;
+        for (u32 q = warp * 32; q < warp * 32 + 32; ++q) cs += rows[q][lane];
+        part[warp][lane] = cs;
+    }
+    __syncthreads();
+    const u32 cnt = min(u32(TC_N), n - T * TC_N);
+    if (t < 32) {
+        const f32 sum = (part[0][t] + part[1][t]) + (part[2][t] + part[3][t]);
+        const f32 c = __uint_as_float(__float_as_uint(sum / f32(cnt)) & 0xffffe000u);
+        cent[t] = c;
+        f32 cc = c * c;
 #pragma unroll
-        for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-        // a NaN coordinate makes the radius NaN (sticky): the tile is then never skipped
-        r2 = (d != d || r2 != r2) ? d + r2 : fmaxf(r2, d);
+        for (int o = 16; o; o >>= 1) cc += __shfl_xor_sync(0xffffffffu, cc, o);
+        if (t == 0) stats[u64(T) * ST_STRIDE + 33] = cc;
+        stats[u64(T) * ST_STRIDE + t] = c;
     }
-    f32 em = 0.0f, nm = 0.0f;
-    for (u32 r = r0 + lane; r < r1; r += 32) {
-        em = fmaxf(em, eq[r]);
-        nm = fmaxf(nm, nq[r]);
+    __syncthreads();
+    f32 d = 0.0f;
+    if (live) {
+#pragma unroll
+        for (int k = 0; k < TC_DIM; ++k) {
+            const f32 u = v[k] - cent[k];
+            d = fmaf(u, u, d);
+        }
     }
+    f32 em = e2, nm = s;
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
+        const f32 od = __shfl_xor_sync(0xffffffffu, d, o);
+        d = (d != d || od != od) ? d + od : fmaxf(d, od);   // NaN is sticky
         em = fmaxf(em, __shfl_xor_sync(0xffffffffu, em, o));
         nm = fmaxf(nm, __shfl_xor_sync(0xffffffffu, nm, o));
     }
-    f32* o = stats + u64(w) * ST_STRIDE;
-    o[lane] = c;
     if (lane == 0) {
+        red[0][warp] = d;
+        red[1][warp] = em;
+        red[2][warp] = nm;
+    }
+    __syncthreads();
+    if (t == 0) {
+        f32 r2 = red[0][0], e = red[1][0], nmax = red[2][0];
+        for (int q = 1; q < 4; ++q) {
+            r2 = (r2 != r2 || red[0][q] != red[0][q]) ? r2 + red[0][q] : fmaxf(r2, red[0][q]);
+            e = fmaxf(e, red[1][q]);
+            nmax = fmaxf(nmax, red[2][q]);
+        }
+        f32* o = stats + u64(T) * ST_STRIDE;
         o[32] = sqrtf(r2);
-        o[33] = cc;
-        o[34] = em;
-        o[35] = nm;
+        o[34] = e;
+        o[35] = nmax;
     }
 }
 
@@ -1135,9 +1186,10 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
         u32* val = c->arena.get<u32>(S_TC_VALS, n);
         const size_t psmem = (size_t(P) * (TC_DIM + 1) + size_t(P) * P) * sizeof(f32);
         TT_CUDA(cudaFuncSetAttribute(k_tc_pivots, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psmem)));
-        k_tc_pivots<<<1, 256, psmem, c->stream>>>(x, n, P, piv, rank);
+        k_tc_pivots<<<1, PIV_THREADS, psmem, c->stream>>>(x, n, P, piv, rank);
         TT_LAUNCH("k_tc_pivots");
-        k_tc_assign<<<div_up(n, 256), 256, P * TC_DIM * sizeof(f32), c->stream>>>(x, n, piv, rank, P, key, val);
+        k_tc_assign<<<div_up(div_up(n, 2), 256), 256, P * (TC_DIM + 1) * sizeof(f32), c->stream>>>(x, n, piv, rank,
+                                                                                                     P, key, val);
         TT_LAUNCH("k_tc_assign");
         c->launches += 2;
         perm = val;
@@ -1156,9 +1208,13 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
             u32* val2 = c->arena.get<u32>(S_TC_VAL2, n);
             k_tc_cells<<<1, 256, 0, c->stream>>>(skey, n, P, cell_off);
             TT_LAUNCH("k_tc_cells");
-            k_tc_assign2<<<div_up(n, 256), 256, 0, c->stream>>>(x, n, skey, perm, cell_off, key2, val2);
+            f32* spv = c->arena.get<f32>(S_TC_SPV, u64(P) * 16 * (TC_DIM + 1));
+            f32* spn = spv + u64(P) * 16 * TC_DIM;
+            k_tc_subpiv<<<div_up(u64(P) * 16 * 32, 256), 256, 0, c->stream>>>(x, perm, cell_off, P, spv, spn);
+            TT_LAUNCH("k_tc_subpiv");
+            k_tc_assign2<<<div_up(n, 256), 256, 0, c->stream>>>(x, n, skey, perm, cell_off, spv, spn, key2, val2);
             TT_LAUNCH("k_tc_assign2");
-            c->launches += 2;
+            c->launches += 3;
             perm = radix_sort<u32>(c, key2, val2, n, kb, vb, bits + 4) ? vb : val2;
         }
     }
@@ -1173,10 +1229,8 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 2);
     TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
     TT_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
-    k_tc_gather<<<div_up(wpad, 256), 256, 0, c->stream>>>(x, n, u32(wpad), perm, xh, lo, oid, nq, eq, aug);
-    TT_LAUNCH("k_tc_gather");
-    k_tc_stats<<<div_up(u64(ntiles) * 32, 256), 256, 0, c->stream>>>(xh, lo, nq, eq, n, ntiles, stats);
-    TT_LAUNCH("k_tc_stats");
+    k_tc_tiles<<<ntiles, TC_N, 0, c->stream>>>(x, n, perm, xh, lo, oid, nq, eq, aug, stats);
+    TT_LAUNCH("k_tc_tiles");
     CUtensorMap map;
     const cuuint64_t gdim[2] = {cuuint64_t(TC_DIM), cuuint64_t(n)};
     const cuuint64_t gstride[1] = {cuuint64_t(TC_DIM) * 4};
@@ -1190,7 +1244,7 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     const u32 grid = std::min<u32>(ntiles, 2 * u32(c->sms));
     k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, lo, eq, oid, n, k, nq, aug, stats, ids, dists, ctl, ctl + 1, cnt);
     TT_LAUNCH("k_knn_tc");
-    c->launches += 3;
+    c->launches += 2;
     u32 e = 0;
     unsigned long long h[2] = {0, 0};
     TT_CUDA(cudaMemcpyAsync(&e, ctl + 1, 4, cudaMemcpyDeviceToHost, c->stream));
