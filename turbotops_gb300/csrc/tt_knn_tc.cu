@@ -71,7 +71,7 @@ constexpr u32 TILE_BYTES = TC_M * TC_DIM * 4;   // 16 KiB (query and candidate t
 constexpr int TC_Q = 256;                       // survivor queue per warp (pairs)
 constexpr int NSTAGE = 2;                       // candidate tiles in flight (TMA ring)
 constexpr u32 TC_TEST = 128;                    // most positions tested per lookahead batch (one N = 128 product)
-constexpr int ST_STRIDE = 36;                   // floats per tile record: centroid, R, |centroid|^2, pad
+constexpr int ST_STRIDE = 36;                   // floats per tile record: centroid, R, |centroid|^2, largest e, largest nq
 constexpr int MAX_PIV = 128;
 constexpr size_t TC_SMEM = 110 * 1024;          // two CTAs per SM (2 x (110 + 1) KiB of 228)
 static_assert(NSTAGE == 2, "the stage bookkeeping below assumes two stages");
@@ -99,6 +99,7 @@ struct Shared {
     alignas(16) u16 alo[TC_M * TC_DIM];  // the query tile's low mantissa bits
     alignas(16) u16 blo[NSTAGE][TC_N * TC_DIM];   // the stages' low mantissa bits
     alignas(16) u32 oid[NSTAGE][TC_N];   // original ids of the tile's candidates
+    float4 trec[NSTAGE];                 // the stage tile's record tail: R, |c|^2, largest e, largest nq
     u32 q[4][TC_Q];                      // per-warp survivor queue: owner lane << 7 | candidate row
     f32 r[4][TC_Q];                      // their exact distances
     u32 need[2][4][TC_TEST / 32];        // per-warp lookahead masks (double-buffered)
@@ -648,11 +649,12 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
 
     // stage s <- candidate tile T: the points (TMA, swizzled), their norm terms and ids
     auto load_stage = [&](int s, u32 T) {
-        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + LO_BYTES + AUG_BYTES + ID_BYTES);
+        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + LO_BYTES + AUG_BYTES + ID_BYTES + 16);
         tma_tile(S.b[s], &map, int(T * TC_N), &S.bar_b[s]);
         bulk_g2s(S.blo[s], lo + u64(T) * TC_N * TC_DIM, LO_BYTES, &S.bar_b[s]);
         bulk_g2s(S.baug[s], aug + u64(T) * TC_N, AUG_BYTES, &S.bar_b[s]);
         bulk_g2s(S.oid[s], oids + u64(T) * TC_N, ID_BYTES, &S.bar_b[s]);
+        bulk_g2s(&S.trec[s], stats + u64(T) * ST_STRIDE + 32, 16, &S.bar_b[s]);
     };
 
     for (;;) {
@@ -675,44 +677,41 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
         const f32 nqi = active ? nq[i] : 0.0f;            // |q~|^2 (rounded down), q~ the TF32 head
         const f32 eqi = active ? eq[i] : 0.0f;            // >= |q - q~|
         const f32 nql = __fmul_rd(nqi, 1.0f - 0x1p-16f);
-        // Sorted list; its first TC_K - k slots hold -inf sentinels, so the
-        // k-th entry is always ld[TC_K - 1] (every index a compile-time
-        // constant: the list stays in registers).
-        f32 ld[TC_K];
-        u32 lj[TC_K];
+        // Sorted list of keys (distance bits << 32 | original id): distances
+        // are >= +0, so unsigned key order is the (distance, id) order of the
+        // lists, ties to the smaller id. Its first TC_K - k slots hold the
+        // sentinel 0 (no key is below it and none moves past it), so the
+        // k-th entry is always lk[TC_K - 1] (every index a compile-time
+        // constant: the list stays in registers); empty slots hold (+inf, ~0).
+        u64 lk[TC_K];
 #pragma unroll
-        for (int t = 0; t < TC_K; ++t) {
-            ld[t] = u32(t) < TC_K - k ? -INFINITY : INFINITY;
-            lj[t] = 0xffffffffu;
-        }
+        for (int t = 0; t < TC_K; ++t) lk[t] = u32(t) < TC_K - k ? 0ull : 0x7f800000ffffffffull;
         f32 sq = INFINITY;   // >= the true distance of any candidate that can still enter, plus |q - q~|
         f32 dk = INFINITY;   // current k-th distance
-        // insert (d, j) into the sorted top-TC_K list; true if it entered
+        // insert (d, j) into the sorted top-TC_K list; true if it entered.
+        // c_s = (lk[s - 1] > key) is monotone in s, so slot s takes lk[s - 1]
+        // where c_s holds, the key where c_s fails but c_{s + 1} holds, and
+        // keeps its entry otherwise: independent compares and selects (a
+        // NaN distance orders above +inf and never enters).
         auto consider = [&](u32 j, f32 d) -> bool {
             ++exact_evals;
-            if (!(d < ld[TC_K - 1] || (d == ld[TC_K - 1] && j < lj[TC_K - 1]))) return false;
-            // insertion index = entries ordered before (d, j): independent
-            // compares, then independent selects (no dependent chain)
-            u32 pos = 0;
-#pragma unroll
-            for (int s = 0; s < TC_K - 1; ++s) pos += u32(ld[s] < d || (ld[s] == d && lj[s] < j));
+            const u64 key = (u64(__float_as_uint(d)) << 32) | j;
+            if (!(key < lk[TC_K - 1])) return false;
+            bool above = true;   // c_{s + 1}
 #pragma unroll
             for (int s = TC_K - 1; s >= 1; --s) {
-                const bool shift = u32(s) > pos, here = u32(s) == pos;
-                ld[s] = shift ? ld[s - 1] : here ? d : ld[s];
-                lj[s] = shift ? lj[s - 1] : here ? j : lj[s];
+                const bool c = lk[s - 1] > key;
+                lk[s] = c ? lk[s - 1] : above ? key : lk[s];
+                above = c;
             }
-            if (pos == 0) {
-                ld[0] = d;
-                lj[0] = j;
-            }
+            if (above) lk[0] = key;
             return true;
         };
         // filter bound from the k-th entry; +inf until the list holds k. A
         // candidate whose lane-ordered distance can tie or beat d has true
         // squared distance <= sq_bound(d) (1 + 2^-16) (the sum's own rounding).
         auto update_bound = [&]() {
-            const f32 d = ld[TC_K - 1];
+            const f32 d = __uint_as_float(u32(lk[TC_K - 1] >> 32));
             dk = d;
             // the filter's relative error bounds need |q|^2 far above the
             // subnormal range: below 2^-60 every candidate is evaluated
@@ -869,14 +868,12 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
         };
 
         u32 tl0 = 0, tl1 = 0, nbits = 0, nl = 0;   // stage tiles, this thread's need bits, tiles loaded
-        f32 et0 = 0.0f, et1 = 0.0f;                 // the stage tiles' largest |x - x~|
         for (int s = 0; s < NSTAGE; ++s) {
             u32 T;
             bool mine;
             if (!next_tile(T, mine, ~0u)) break;
             if (tid == 0) load_stage(s, T);
-            const f32 et = __ldg(stats + u64(T) * ST_STRIDE + 34);
-            if (s == 0) tl0 = T, et0 = et; else tl1 = T, et1 = et;
+            if (s == 0) tl0 = T; else tl1 = T;
             nbits = (nbits & ~(1u << s)) | (u32(mine) << s);
             ++nl;
         }
@@ -923,7 +920,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
                 // with e_c <= e_T (the tile's largest), so its L <= (sq + e_T)^2:
                 // it passes iff D >= t = (nq (1 - 2^-16) - (sq + e_T)^2) / 2
                 // (every step rounded toward passing).
-                const f32 eT = st == 0 ? et0 : et1;
+                const float4 trec = S.trec[st];
+                const f32 eT = trec.z;
                 const f32 sT = __fadd_ru(sq, eT);
                 const f32 t = mine ? 0.5f * __fsub_rd(nql, __fmul_ru(sT, sT)) : INFINITY;
                 // (A) filter the tile's 128 candidates, two 32-column TMEM loads
@@ -971,14 +969,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
                 // TC_Q (the first tile of a block, while the lists fill) is
                 // evaluated by the owners directly.
                 const u32 tcnt = __popc(mk[0]) + __popc(mk[1]) + __popc(mk[2]) + __popc(mk[3]);
-                u32 incl = tcnt;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const u32 y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= u32(o)) incl += y;
-                }
-                const u32 total = __shfl_sync(0xffffffffu, incl, 31);
-                const u32 base = incl - tcnt;
+                const u32 total = __reduce_add_sync(0xffffffffu, tcnt);
                 if (total > u32(TC_Q)) {
                     // Mostly the first tile of a block: the lists are empty and
                     // every candidate passed. The tile bounds its own k-th
@@ -1008,7 +999,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
                                 gm[chunk * 8 + g] = fmaxf(fmax3(d4[0], d4[1], d4[2]), d4[3]);
                             }
                         }
-                        const f32 NT = __ldg(stats + u64(T) * ST_STRIDE + 35);
+                        const f32 NT = trec.w;
                         const f32 au = __fmaf_ru(NT, 0x1p-14f, __fmul_ru(nqi, 1.0f + 0x1p-16f));
 #pragma unroll
                         for (int g = 0; g < 32; ++g) {
@@ -1059,6 +1050,13 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
                     }
                     if (changed) update_bound();
                 } else if (total) {
+                    u32 incl = tcnt;   // queue positions: an inclusive scan of the counts
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const u32 y = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= u32(o)) incl += y;
+                    }
+                    const u32 base = incl - tcnt;
                     u32* wq = S.q[warp];
                     f32* wr = S.r[warp];
                     u32 pos = base;
@@ -1104,8 +1102,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     load_stage(st, Tn);
                 }
-                const f32 et = __ldg(stats + u64(Tn) * ST_STRIDE + 34);
-                if (st == 0) tl0 = Tn, et0 = et; else tl1 = Tn, et1 = et;
+                if (st == 0) tl0 = Tn; else tl1 = Tn;
                 nbits = (nbits & ~(1u << st)) | (u32(mn) << st);
                 ++nl;
             }
@@ -1130,8 +1127,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
 #pragma unroll
             for (int s = 0; s < TC_K; ++s)
                 if (u32(s) >= first) {
-                    ids[u64(oi) * k + (s - first)] = lj[s];
-                    if (dists) dists[u64(oi) * k + (s - first)] = ld[s];
+                    ids[u64(oi) * k + (s - first)] = u32(lk[s]);
+                    if (dists) dists[u64(oi) * k + (s - first)] = __uint_as_float(u32(lk[s] >> 32));
                 }
         }
         __syncthreads();
