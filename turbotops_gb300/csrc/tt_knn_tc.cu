@@ -80,26 +80,31 @@ static_assert(TC_M == TC_N, "query blocks and candidate tiles share one tiling")
 constexpr u32 AUG_BYTES = TC_N * 16;  // augmentation rows per tile (one 16-byte core-matrix row each)
 constexpr u32 ID_BYTES = TC_N * 4;    // original ids per tile
 constexpr u32 LO_BYTES = TC_N * TC_DIM * 2;   // low mantissa bits per tile (u16 per coordinate)
+// A tile's pack: everything but the TF32 heads, one bulk copy: the low bits,
+// the augmentation rows, the original ids and the record tail (R, |c|^2,
+// largest e, largest nq).
+constexpr u32 PK_AUG = LO_BYTES;
+constexpr u32 PK_ID = PK_AUG + AUG_BYTES;
+constexpr u32 PK_TAIL = PK_ID + ID_BYTES;
+constexpr u32 PACK_BYTES = PK_TAIL + 16;
+static_assert(PACK_BYTES % 16 == 0, "bulk copies move multiples of 16 bytes");
 
 // The fifth K-step of every product adds the candidate's norm term: the
 // query side holds rows (1, 1, 0, 0 | 0, 0, 0, 0), the candidate side
-// (w_hi, w_lo, 0, 0 | 0, 0, 0, 0) with w = -|c|^2 (1 - 2^-7) / 2 split into an
-// exact TF32 head and its FP32 remainder, so the accumulator holds
-// D = G - |c|^2 (1 - 2^-7) / 2 and the filter is a compare against it.
+// (w_hi, w_lo, 0, 0 | 0, 0, 0, 0) with -w_hi - w_lo <= |c~|^2 (1 - 2^-16) / 2
+// (two TF32-exact parts), so the accumulator holds D = G + w_hi + w_lo and
+// the filter is a compare against it.
 // Layout: no swizzle, K-major, 8-row core matrices of 16-byte rows; the
 // first K half of row r at r * 16 (so a tile's rows are one contiguous 2 KiB
-// copy), the second K half in a shared 2 KiB block of zeros.
-// The augmentation region sits at the start of shared memory.
+// copy), the second K half in a shared 2 KiB block of zeros placed above
+// both first halves (the descriptors' leading offsets are positive).
 struct Shared {
     alignas(1024) float4 aaug[TC_M];         // (1, 1, 0, 0) per query row
-    float4 baug[NSTAGE][TC_N];               // (w_hi, w_lo, 0, 0) per candidate row
-    float4 zeros[TC_N];                      // the second K half of both sides
     alignas(1024) unsigned char a[TILE_BYTES];
     alignas(1024) unsigned char b[NSTAGE][TILE_BYTES];
     alignas(16) u16 alo[TC_M * TC_DIM];  // the query tile's low mantissa bits
-    alignas(16) u16 blo[NSTAGE][TC_N * TC_DIM];   // the stages' low mantissa bits
-    alignas(16) u32 oid[NSTAGE][TC_N];   // original ids of the tile's candidates
-    float4 trec[NSTAGE];                 // the stage tile's record tail: R, |c|^2, largest e, largest nq
+    alignas(16) unsigned char pk[NSTAGE][PACK_BYTES];   // the stage tiles' packs
+    float4 zeros[TC_N];                  // the second K half of both augmentation sides
     u32 q[4][TC_Q];                      // per-warp survivor queue: owner lane << 7 | candidate row
     f32 r[4][TC_Q];                      // their exact distances
     u32 need[2][4][TC_TEST / 32];        // per-warp lookahead masks (double-buffered)
@@ -489,9 +494,8 @@ __global__ void k_tc_assign2(const f32* __restrict__ x, u32 n, const u64* __rest
 // skipped), |c|^2, and the tile's largest e and nq (the Gram filter's
 // per-tile error terms).
 __global__ void __launch_bounds__(TC_N) k_tc_tiles(const f32* __restrict__ x, u32 n, const u32* __restrict__ perm,
-                                                  f32* __restrict__ xh, u16* __restrict__ lo, u32* __restrict__ ids,
-                                                  f32* __restrict__ nq, f32* __restrict__ eq,
-                                                  float4* __restrict__ aug, f32* __restrict__ stats) {
+                                                  f32* __restrict__ xh, unsigned char* __restrict__ pack,
+                                                  f32* __restrict__ nq, f32* __restrict__ eq, f32* __restrict__ stats) {
     __shared__ f32 rows[TC_N][TC_DIM + 1];
     __shared__ f32 part[4][TC_DIM];
     __shared__ f32 cent[TC_DIM];
@@ -501,7 +505,10 @@ __global__ void __launch_bounds__(TC_N) k_tc_tiles(const f32* __restrict__ x, u3
     const bool live = r < n;
     f32 v[TC_DIM];
     f32 s = 0.0f, e2 = 0.0f;
-    uint4* lr = reinterpret_cast<uint4*>(lo + u64(r) * TC_DIM);
+    unsigned char* pt = pack + u64(T) * PACK_BYTES;
+    uint4* lr = reinterpret_cast<uint4*>(pt) + 4 * t;
+    float4* aug = reinterpret_cast<float4*>(pt + PK_AUG);
+    u32* ids = reinterpret_cast<u32*>(pt + PK_ID);
     if (live) {
         const u32 src = perm[r];
         const float4* xr = reinterpret_cast<const float4*>(x + u64(src) * TC_DIM);
@@ -534,14 +541,14 @@ __global__ void __launch_bounds__(TC_N) k_tc_tiles(const f32* __restrict__ x, u3
         // its head and gets a zero tail
         const f32 hi = __uint_as_float(__float_as_uint(w) & 0xffffe000u);
         const f32 rem = isfinite(w) ? w - hi : 0.0f;   // exact
-        aug[r] = make_float4(hi, __uint_as_float(__float_as_uint(rem) & 0xffffe000u), 0.0f, 0.0f);
-        ids[r] = src;
+        aug[t] = make_float4(hi, __uint_as_float(__float_as_uint(rem) & 0xffffe000u), 0.0f, 0.0f);
+        ids[t] = src;
         e2 = __fsqrt_ru(e2);
     } else {
 #pragma unroll
         for (int k = 0; k < TC_DIM; ++k) v[k] = 0.0f;
-        aug[r] = make_float4(-3.0e38f, 0.0f, 0.0f, 0.0f);
-        ids[r] = 0xffffffffu;
+        aug[t] = make_float4(-3.0e38f, 0.0f, 0.0f, 0.0f);
+        ids[t] = 0xffffffffu;
 #pragma unroll
         for (int c = 0; c < 4; ++c) lr[c] = make_uint4(0u, 0u, 0u, 0u);
     }
@@ -602,14 +609,15 @@ __global__ void __launch_bounds__(TC_N) k_tc_tiles(const f32* __restrict__ x, u3
         o[32] = sqrtf(r2);
         o[34] = e;
         o[35] = nmax;
+        reinterpret_cast<float4*>(pt + PK_TAIL)[0] = make_float4(o[32], o[33], e, nmax);
     }
 }
 
 // ---- the kNN kernel ---------------------------------------------------------
 
 __global__ void __launch_bounds__(128, 2)
-k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, const f32* __restrict__ eq,
-         const u32* __restrict__ oids, u32 n, u32 k, const f32* __restrict__ nq, const float4* __restrict__ aug,
+k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restrict__ pack, const f32* __restrict__ eq,
+         u32 n, u32 k, const f32* __restrict__ nq,
          const f32* __restrict__ stats, u32* __restrict__ ids, f32* __restrict__ dists, u32* __restrict__ next_block,
          u32* __restrict__ err, unsigned long long* __restrict__ counters) {
     extern __shared__ unsigned char smem_raw[];
@@ -647,14 +655,11 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
     u32 npar = 0;   // S.need buffer of the next lookahead
     bool failed = false;
 
-    // stage s <- candidate tile T: the points (TMA, swizzled), their norm terms and ids
+    // stage s <- candidate tile T: the TF32 heads (TMA, swizzled) and the pack
     auto load_stage = [&](int s, u32 T) {
-        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + LO_BYTES + AUG_BYTES + ID_BYTES + 16);
+        mbar_expect_tx(&S.bar_b[s], TILE_BYTES + PACK_BYTES);
         tma_tile(S.b[s], &map, int(T * TC_N), &S.bar_b[s]);
-        bulk_g2s(S.blo[s], lo + u64(T) * TC_N * TC_DIM, LO_BYTES, &S.bar_b[s]);
-        bulk_g2s(S.baug[s], aug + u64(T) * TC_N, AUG_BYTES, &S.bar_b[s]);
-        bulk_g2s(S.oid[s], oids + u64(T) * TC_N, ID_BYTES, &S.bar_b[s]);
-        bulk_g2s(&S.trec[s], stats + u64(T) * ST_STRIDE + 32, 16, &S.bar_b[s]);
+        bulk_g2s(S.pk[s], pack + u64(T) * PACK_BYTES, PACK_BYTES, &S.bar_b[s]);
     };
 
     for (;;) {
@@ -669,7 +674,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_expect_tx(&S.bar_a, TILE_BYTES + LO_BYTES);
             tma_tile(S.a, &map, int(q0), &S.bar_a);
-            bulk_g2s(S.alo, lo + u64(q0) * TC_DIM, LO_BYTES, &S.bar_a);
+            bulk_g2s(S.alo, pack + u64(blk) * PACK_BYTES, LO_BYTES, &S.bar_a);
         }
         const u32 row = warp * 32 + lane;
         const u32 i = q0 + row;   // regrouped index of this thread's query
@@ -881,7 +886,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
             mbar_wait(&S.bar_a, ph_a, err, &S.fail);
             mbar_wait(&S.bar_b[0], ub0 & 1, err, &S.fail);
             tc_fence_after();
-            mma_tile(tmem, smem_addr(S.a), smem_addr(S.b[0]), smem_addr(S.aaug), smem_addr(S.baug[0]),
+            mma_tile(tmem, smem_addr(S.a), smem_addr(S.b[0]), smem_addr(S.aaug), smem_addr(S.pk[0] + PK_AUG),
                      smem_addr(S.zeros));
             mma_commit(&S.bar_mma[0]);
         }
@@ -899,7 +904,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
                 mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err, &S.fail);
                 tc_fence_after();
                 mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]), smem_addr(S.aaug),
-                         smem_addr(S.baug[ns]), smem_addr(S.zeros));
+                         smem_addr(S.pk[ns] + PK_AUG), smem_addr(S.zeros));
                 mma_commit(&S.bar_mma[nb]);
             }
             // every thread acquires the stage's (complete) TMA phase before
@@ -910,8 +915,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
             const u32 j0 = T * TC_N;
             if (__any_sync(0xffffffffu, mine)) {
                 const unsigned char* bt = S.b[st];
-                const u16* blo = S.blo[st];
-                const u32* oid = S.oid[st];
+                const u16* blo = reinterpret_cast<const u16*>(S.pk[st]);
+                const u32* oid = reinterpret_cast<const u32*>(S.pk[st] + PK_ID);
                 // Gram filter. D = G + w_hi + w_lo with G = q~ . c~ (TF32-exact
                 // heads: exact products, FP32 accumulation, |G - q~.c~| <=
                 // 2^-19 (|q~|^2 + |c~|^2)) and -w_hi - w_lo <= |c~|^2 (1 - 2^-16) / 2,
@@ -920,7 +925,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
                 // with e_c <= e_T (the tile's largest), so its L <= (sq + e_T)^2:
                 // it passes iff D >= t = (nq (1 - 2^-16) - (sq + e_T)^2) / 2
                 // (every step rounded toward passing).
-                const float4 trec = S.trec[st];
+                const float4 trec = *reinterpret_cast<const float4*>(S.pk[st] + PK_TAIL);
                 const f32 eT = trec.z;
                 const f32 sT = __fadd_ru(sq, eT);
                 const f32 t = mine ? 0.5f * __fsub_rd(nql, __fmul_ru(sT, sT)) : INFINITY;
@@ -1098,7 +1103,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
             u32 Tn;
             bool mn;
             if (next_tile(Tn, mn, tmem + u32(sb) * TC_N)) {   // block-uniform (may test a batch)
-                if (tid == 0) {
+                if (tid == 32) {   // warp 1 issues the copies, warp 0 the products
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     load_stage(st, Tn);
                 }
@@ -1122,7 +1127,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const u16* __restrict__ lo, co
         }
         tiles_done += nl;
         if (active) {
-            const u32 oi = oids[i];
+            const u32 oi = reinterpret_cast<const u32*>(pack + u64(blk) * PACK_BYTES + PK_ID)[row];
             const u32 first = TC_K - k;   // entries [first, TC_K) are the k results
 #pragma unroll
             for (int s = 0; s < TC_K; ++s)
@@ -1168,7 +1173,7 @@ bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x) {
 
 // Exact kNN lists through the tile order and the tensor-core filter; sets
 // the context's counts of exact evaluations and computed Gram tiles.
-// Slots: S_TC_* (regrouped copy, its low bits and error terms, tile records), S_MISC0/1/3, S_COUNT, and
+// Slots: S_TC_* (regrouped heads, tile packs, error terms, tile records), S_MISC0/1, S_COUNT, and
 // the radix sort's own (S_SORT_*, S_SCAN*).
 void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     const u32 ntiles = div_up(n, TC_N);
@@ -1216,17 +1221,15 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
         }
     }
     f32* xh = c->arena.get<f32>(S_TC_X, u64(n) * TC_DIM);
-    u16* lo = c->arena.get<u16>(S_TC_LO, wpad * TC_DIM);
+    unsigned char* pack = c->arena.get<unsigned char>(S_TC_LO, u64(ntiles) * PACK_BYTES);
     f32* eq = c->arena.get<f32>(S_TC_ERR, wpad);
-    u32* oid = c->arena.get<u32>(S_TC_PERM, wpad);
     f32* nq = c->arena.get<f32>(S_MISC0, wpad);
-    float4* aug = c->arena.get<float4>(S_MISC3, wpad);
     f32* stats = c->arena.get<f32>(S_TC_STATS, u64(ntiles) * ST_STRIDE);
     u32* ctl = c->arena.get<u32>(S_MISC1, 4);   // [0] next block, [1] error word
     unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 2);
     TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
     TT_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
-    k_tc_tiles<<<ntiles, TC_N, 0, c->stream>>>(x, n, perm, xh, lo, oid, nq, eq, aug, stats);
+    k_tc_tiles<<<ntiles, TC_N, 0, c->stream>>>(x, n, perm, xh, pack, nq, eq, stats);
     TT_LAUNCH("k_tc_tiles");
     CUtensorMap map;
     const cuuint64_t gdim[2] = {cuuint64_t(TC_DIM), cuuint64_t(n)};
@@ -1239,7 +1242,7 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     if (r != CUDA_SUCCESS) throw Error(TT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
     TT_CUDA(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)));
     const u32 grid = std::min<u32>(ntiles, 2 * u32(c->sms));
-    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, lo, eq, oid, n, k, nq, aug, stats, ids, dists, ctl, ctl + 1, cnt);
+    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, pack, eq, n, k, nq, stats, ids, dists, ctl, ctl + 1, cnt);
     TT_LAUNCH("k_knn_tc");
     c->launches += 2;
     u32 e = 0;
