@@ -899,14 +899,6 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
             const int st = int(it % NSTAGE);       // candidate stage
             mbar_wait(&S.bar_mma[sb], (sb ? um1 : um0) & 1, err, &S.fail);
             tc_fence_after();
-            if (tid == 0 && it + 1 < nl) {   // the tensor core works on the next tile during this epilogue
-                const int nb = sb ^ 1, ns = int((it + 1) % NSTAGE);
-                mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err, &S.fail);
-                tc_fence_after();
-                mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]), smem_addr(S.aaug),
-                         smem_addr(S.pk[ns] + PK_AUG), smem_addr(S.zeros));
-                mma_commit(&S.bar_mma[nb]);
-            }
             // every thread acquires the stage's (complete) TMA phase before
             // reading the candidate tile, its norm terms and ids
             mbar_wait(&S.bar_b[st], (st ? ub1 : ub0) & 1, err, &S.fail);
@@ -1086,6 +1078,17 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
                     if (changed) update_bound();
                     __syncwarp();   // the queue is reused by the next tile
                 }
+            }
+            if (tid == 0 && it + 1 < nl) {
+                // the next tile's product, issued once this warp's epilogue is
+                // done (its copy has had the whole epilogue to land); the tensor
+                // core runs it while the other warps finish this tile
+                const int nb = sb ^ 1, ns = int((it + 1) % NSTAGE);
+                mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err, &S.fail);
+                tc_fence_after();
+                mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]), smem_addr(S.aaug),
+                         smem_addr(S.pk[ns] + PK_AUG), smem_addr(S.zeros));
+                mma_commit(&S.bar_mma[nb]);
             }
             if (sb) ++um1; else ++um0;
             // one reader of this CTA's timeout flag (shared memory: a global
