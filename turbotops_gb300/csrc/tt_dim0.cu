@@ -275,25 +275,41 @@ __global__ void k_iota(u32* __restrict__ p, u32 n) {
 
 // For each live edge with endpoints in different components, offer its rank
 // to both components; edges inside a component are dropped from the list.
+// (The survivors' list grows by one atomic per warp: ranks from a ballot.)
 __global__ void k_bv_offer(const u64* __restrict__ keys, const u32* __restrict__ live, u32 nlive, int all,
                            const u32* __restrict__ comp, u32* __restrict__ best, u32* __restrict__ live_out,
                            u32* __restrict__ nlive_out) {
-    for (u32 t = blockIdx.x * blockDim.x + threadIdx.x; t < nlive; t += gridDim.x * blockDim.x) {
-        const u32 r = all ? t : live[t];
-        u32 a, b;
-        decode_edge(key_idx(keys[r]), a, b);
-        const u32 ca = comp[a], cb = comp[b];
-        if (ca == cb) continue;
-        atomicMin(&best[ca], r);
-        atomicMin(&best[cb], r);
-        live_out[atomicAdd(nlive_out, 1u)] = r;
+    const u32 lane = threadIdx.x & 31;
+    for (u32 base = blockIdx.x * blockDim.x; base < nlive; base += gridDim.x * blockDim.x) {
+        const u32 t = base + threadIdx.x;   // whole warps iterate together
+        bool keep = false;
+        u32 r = 0;
+        if (t < nlive) {
+            r = all ? t : live[t];
+            u32 a, b;
+            decode_edge(key_idx(keys[r]), a, b);
+            const u32 ca = comp[a], cb = comp[b];
+            if (ca != cb) {
+                atomicMin(&best[ca], r);
+                atomicMin(&best[cb], r);
+                keep = true;
+            }
+        }
+        const u32 m = __ballot_sync(0xffffffffu, keep);
+        if (!m) continue;
+        u32 pos = 0;
+        if (lane == u32(__ffs(m) - 1)) pos = atomicAdd(nlive_out, u32(__popc(m)));
+        pos = __shfl_sync(0xffffffffu, pos, __ffs(m) - 1);
+        if (keep) live_out[pos + __popc(m & ((1u << lane) - 1u))] = r;
     }
 }
 
 // Every component root with an offered edge takes it into the forest and
 // hooks onto the other side; of a mutual pair only the larger root hooks.
+// (The hook count is summed per warp: one atomic a warp.)
 __global__ void k_bv_hook(const u64* __restrict__ keys, const u32* __restrict__ comp, const u32* __restrict__ best,
                           u32* __restrict__ parent, u8* __restrict__ tree, u32 n, u32* __restrict__ hooks) {
+    u32 mine = 0;
     for (u32 c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         if (comp[c] != c) continue;
         const u32 r = best[c];
@@ -304,8 +320,10 @@ __global__ void k_bv_hook(const u64* __restrict__ keys, const u32* __restrict__ 
         tree[r] = 1;
         if (best[o] == r && c < o) continue;   // mutual: o hooks onto c
         parent[c] = o;
-        atomicAdd(hooks, 1u);
+        ++mine;
     }
+    mine = __reduce_add_sync(0xffffffffu, mine);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(hooks, mine);
 }
 
 __global__ void k_bv_flatten(const u32* __restrict__ parent, u32* __restrict__ comp, u32* __restrict__ best, u32 n) {
