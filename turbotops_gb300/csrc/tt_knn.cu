@@ -111,10 +111,12 @@ __global__ void k_graph_fill(const u32* __restrict__ ids, const f32* __restrict_
 
 // One warp per row: rank of each entry by (column, position), scattered into
 // the sorted copy; ucnt[v] = distinct columns. Rows above kRowSortMax set
-// *overflow and are left to the global sort.
+// *overflow and are left to the global sort; rows above kWarpRowMax are
+// listed (longs[0] = count, then the rows) for k_graph_rowsort_long.
 __global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* __restrict__ col,
                                 const f32* __restrict__ w, u32* __restrict__ scol, f32* __restrict__ sw,
-                                unsigned long long* __restrict__ ucnt, u32* __restrict__ overflow) {
+                                unsigned long long* __restrict__ ucnt, u32* __restrict__ overflow,
+                                u32* __restrict__ longs) {
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
     for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
@@ -124,7 +126,10 @@ __global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* _
             if (lane == 0) atomicOr(overflow, 1u);
             continue;
         }
-        if (L > kWarpRowMax) continue;   // k_graph_rowsort_long
+        if (L > kWarpRowMax) {   // k_graph_rowsort_long
+            if (lane == 0) longs[1 + atomicAdd(longs, 1u)] = v;
+            continue;
+        }
         for (u32 a0 = 0; a0 < L; a0 += 32) {
             const u32 a = a0 + lane;
             const u32 ca = a < L ? col[b + a] : 0xffffffffu;
@@ -158,7 +163,8 @@ __global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* _
 // lists): one block per row, a bitonic sort of (column << 32 | distance
 // bits) in shared memory; duplicates are then identical and adjacent.
 constexpr u32 kLongThreads = 256;
-__global__ void __launch_bounds__(kLongThreads) k_graph_rowsort_long(const u64* __restrict__ off, u32 n,
+__global__ void __launch_bounds__(kLongThreads) k_graph_rowsort_long(const u64* __restrict__ off,
+                                                                     const u32* __restrict__ longs,
                                                                      const u32* __restrict__ col,
                                                                      const f32* __restrict__ w, u32* __restrict__ scol,
                                                                      f32* __restrict__ sw,
@@ -166,10 +172,11 @@ __global__ void __launch_bounds__(kLongThreads) k_graph_rowsort_long(const u64* 
     __shared__ unsigned long long key[kRowSortMax];
     __shared__ u32 uc;
     const u32 tid = threadIdx.x;
-    for (u32 v = blockIdx.x; v < n; v += gridDim.x) {
+    const u32 nl = longs[0];
+    for (u32 li = blockIdx.x; li < nl; li += gridDim.x) {
+        const u32 v = longs[1 + li];
         const u64 b = off[v];
         const u32 L = u32(off[v + 1] - b);
-        if (L <= kWarpRowMax || L > kRowSortMax) continue;   // block-uniform
         u32 P = 1;
         while (P < L) P <<= 1;
         for (u32 i = tid; i < P; i += kLongThreads)
@@ -288,11 +295,13 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         f32* sw = reinterpret_cast<f32*>(scol + m + 1);
         k_graph_fill<<<grid_for(u64(n) * k, 256), 256, 0, c->stream>>>(kid, kd, n, k, off, cur, col, cw);
         TT_LAUNCH("k_graph_fill");
+        u32* longs = c->arena.get<u32>(S_GRAPH_LONG, u64(n) + 1);
+        TT_CUDA(cudaMemsetAsync(longs, 0, sizeof(u32), c->stream));
         k_graph_rowsort<<<gw, 256, 0, c->stream>>>(off, n, col, cw, scol, sw,
-                                                    reinterpret_cast<unsigned long long*>(ucnt), ovf);
+                                                    reinterpret_cast<unsigned long long*>(ucnt), ovf, longs);
         TT_LAUNCH("k_graph_rowsort");
         k_graph_rowsort_long<<<std::min<u32>(n, 8 * u32(c->sms)), kLongThreads, 0, c->stream>>>(
-            off, n, col, cw, scol, sw, reinterpret_cast<unsigned long long*>(ucnt));
+            off, longs, col, cw, scol, sw, reinterpret_cast<unsigned long long*>(ucnt));
         TT_LAUNCH("k_graph_rowsort_long");
         c->launches += 4;
         u32 overflow = 0;
