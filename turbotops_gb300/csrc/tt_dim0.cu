@@ -89,11 +89,14 @@ struct CsrRows {
     }
 };
 
-// cnt[v] = kept edges {u, v}: u < v, d(u, v) <= thr (one warp per row).
+// cnt[v] = kept edges {u, v}: u < v, d(u, v) <= thr (one warp per row);
+// dmm[0] / dmm[1] = the smallest / largest distance bits kept (the sort's
+// bit range, known with the count).
 template <typename Rows>
-__global__ void k_edge_count(Rows rows, u32 n, f32 thr, u64* __restrict__ cnt) {
+__global__ void k_edge_count(Rows rows, u32 n, f32 thr, u64* __restrict__ cnt, u32* __restrict__ dmm) {
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
+    u32 lo = 0xffffffffu, hi = 0;
     for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
         const u64 b = rows.begin(v), e = rows.end(v);
         u32 c = 0;
@@ -104,10 +107,32 @@ __global__ void k_edge_count(Rows rows, u32 n, f32 thr, u64* __restrict__ cnt) {
                 f32 d;
                 rows.at(v, t0 + lane, u, d);
                 keep = u < v && d <= thr;
+                if (keep) {
+                    lo = min(lo, __float_as_uint(d));
+                    hi = max(hi, __float_as_uint(d));
+                }
             }
             c += __popc(__ballot_sync(0xffffffffu, keep));
         }
         if (lane == 0) cnt[v] = c;
+    }
+    // one atomic pair per block
+    __shared__ u32 blo, bhi;
+    if (threadIdx.x == 0) {
+        blo = 0xffffffffu;
+        bhi = 0;
+    }
+    __syncthreads();
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (lane == 0 && lo <= hi) {
+        atomicMin(&blo, lo);
+        atomicMax(&bhi, hi);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && blo <= bhi) {
+        atomicMin(&dmm[0], blo);
+        atomicMax(&dmm[1], bhi);
     }
 }
 
@@ -406,17 +431,26 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
     const u32 n = cx.n;
     u64 m = 0;
     u64* off = c->arena.get<u64>(S_EDGE_CNT, u64(n) + 2);
+    u32* dmm = reinterpret_cast<u32*>(off + n + 1);   // beside the total: one copy brings both
     const u32 g = grid_for(u64(n) * 32, 256);
+    int dbits = 0;   // distance bits the sort must see
     if (n > 1) {
+        TT_CUDA(cudaMemsetAsync(dmm, 0xff, sizeof(u32), c->stream));
+        TT_CUDA(cudaMemsetAsync(dmm + 1, 0, sizeof(u32), c->stream));
         if (cx.mat)
-            k_edge_count<<<g, 256, 0, c->stream>>>(DenseRows{cx.mat, n}, n, cx.thr, off);
+            k_edge_count<<<g, 256, 0, c->stream>>>(DenseRows{cx.mat, n}, n, cx.thr, off, dmm);
         else
-            k_edge_count<<<g, 256, 0, c->stream>>>(CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off);
+            k_edge_count<<<g, 256, 0, c->stream>>>(CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off, dmm);
         TT_LAUNCH("k_edge_count");
         ++c->launches;
         scan_exclusive<u64>(c, off, off, n, off + n);
-        TT_CUDA(cudaMemcpyAsync(&m, off + n, sizeof(m), cudaMemcpyDeviceToHost, c->stream));
+        u64 h[2];
+        TT_CUDA(cudaMemcpyAsync(h, off + n, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaStreamSynchronize(c->stream));
+        m = h[0];
+        const u32 lo = u32(h[1]), hi = u32(h[1] >> 32);
+        const u32 diff = m ? lo ^ hi : 0u;
+        dbits = diff ? 32 - __builtin_clz(diff) : 0;
     }
     if (m >= 0xffffffffull) invalid("gb300: more than 2^32 - 1 kept edges");
     u64* keys = c->arena.get<u64>(S_EDGE_KEYS, m + 1);
@@ -430,7 +464,9 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
                                                   sidx);
         TT_LAUNCH("k_edge_fill");
         u64* kb = c->arena.get<u64>(S_SORT_A, m);
-        const bool sw = radix_sort<u32>(c, skey, static_cast<u32*>(nullptr), m, kb, static_cast<u32*>(nullptr), 0, 32);
+        // a stable sort on the distance bits that differ (none: already in order)
+        const bool sw = dbits > 0 && radix_sort<u32>(c, skey, static_cast<u32*>(nullptr), m, kb,
+                                                     static_cast<u32*>(nullptr), dbits, 32);
         u32* inv = c->arena.get<u32>(S_EDGE_INV, m + 1);
         k_edge_pack<<<grid_for(m, 256), 256, 0, c->stream>>>(sw ? kb : skey, sidx, m, redzed, keys, inv);
         TT_LAUNCH("k_edge_pack");

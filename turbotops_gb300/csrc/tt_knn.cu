@@ -304,14 +304,15 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
             off, longs, col, cw, scol, sw, reinterpret_cast<unsigned long long*>(ucnt));
         TT_LAUNCH("k_graph_rowsort_long");
         c->launches += 4;
+        // the row pointers from the distinct counts (meaningful only without
+        // overflow), read back with the overflow flag in one round trip
+        scan_exclusive<u64>(c, ucnt, rp, n, rp + n);
         u32 overflow = 0;
+        u64 nnz = 0;
         TT_CUDA(cudaMemcpyAsync(&overflow, ovf, 4, cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaMemcpyAsync(&nnz, rp + n, 8, cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaStreamSynchronize(c->stream));
         if (!overflow) {
-            u64 nnz = 0;
-            scan_exclusive<u64>(c, ucnt, rp, n, rp + n);
-            TT_CUDA(cudaMemcpyAsync(&nnz, rp + n, 8, cudaMemcpyDeviceToHost, c->stream));
-            TT_CUDA(cudaStreamSynchronize(c->stream));
             u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);
             f32* w = c->arena.get<f32>(S_OUT2, nnz + 1);
             k_graph_emit<<<gw, 256, 0, c->stream>>>(off, n, scol, sw, rp, ci, w);
