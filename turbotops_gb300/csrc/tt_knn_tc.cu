@@ -1141,8 +1141,11 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
         }
         __syncthreads();
     }
-    if (counters) {
-        if (exact_evals) atomicAdd(&counters[0], exact_evals);
+    if (counters) {   // one atomic a warp
+        unsigned long long ev = exact_evals;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) ev += __shfl_xor_sync(0xffffffffu, ev, o);
+        if (lane == 0 && ev) atomicAdd(&counters[0], ev);
         if (tid == 0 && tiles_done) atomicAdd(&counters[1], tiles_done);
     }
     tc_fence_before();
