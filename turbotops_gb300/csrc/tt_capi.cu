@@ -161,6 +161,7 @@ void tt_ctx_destroy(tt_ctx* c) {
         cudaStreamDestroy(c->aux);
     }
     if (c->aux_ev) cudaEventDestroy(c->aux_ev);
+    if (c->tc_host) cudaFreeHost(c->tc_host);
     if (c->side) {
         cudaStreamSynchronize(c->side);
         cudaStreamDestroy(c->side);

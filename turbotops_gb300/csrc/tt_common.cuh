@@ -149,6 +149,8 @@ struct tt_ctx {
     uint64_t filter_tiles = 0;      // 128 x 128 Gram tiles the last tensor-core kNN computed
     cudaStream_t aux = nullptr;     // copies overlapped with compute (created on first use)
     cudaEvent_t aux_ev = nullptr;
+    unsigned long long* tc_host = nullptr;   // page-locked: the tensor-core kNN's error word and counters
+    bool tc_pending = false;                 // ... copied there, not yet read (deferred to a later sync)
     cudaStream_t side = nullptr;    // kernels overlapped with the main stream's (created on first use)
     cudaEvent_t side_ev[2] = {nullptr, nullptr};
 };

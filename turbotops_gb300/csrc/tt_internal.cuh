@@ -91,7 +91,8 @@ u64 assemble2(tt_ctx* c, const Complex& cx, const u64* keys, u64 m, const u64* p
               u64** cidx, f32** cd, u64* napp);
 
 // ---- tt_knn.cu
-void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists);
+void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists,
+               bool defer = false);
 u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* ids, u32 k,
               u64* rp, u32** ci, f32** w);
 u64 radius_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32 tau, u64* rp,

@@ -244,14 +244,15 @@ inline u32 grid_for(u64 work, u32 per_block) {
 }  // namespace
 
 bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x);
-void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists);
+void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists, bool defer);
+void knn_tc_settle(tt_ctx* c);
 
-void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists) {
+void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists, bool defer) {
     if (k == 0 || n < 2) return;
     // L2 in R^32: the tensor-core Gram filter (tt_knn_tc.cu) unless the
     // context asks for the exhaustive scan; both give the same lists
     if (c->knn_mode != 1 && knn_tc_applicable(n, dim, kind, k, x) && (c->knn_mode == 2 || n >= 1024)) {
-        knn_tc(c, x, n, k, ids, dists);
+        knn_tc(c, x, n, k, ids, dists, defer);
         return;
     }
     u32* err = error_word(c);
@@ -272,7 +273,7 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
     f32* kd = c->arena.get<f32>(S_KNN_D, u64(n) * k + 1);
     if (!ids) {
         kid = c->arena.get<u32>(S_KNN_I, u64(n) * k + 1);
-        knn_exact(c, x, n, dim, kind, p, k, kid, kd);
+        knn_exact(c, x, n, dim, kind, p, k, kid, kd, true);   // its status is read at the next round trip
     } else {
         invalid("gb300: knn_graph from external lists is not supported; pass ids = NULL");
     }
@@ -312,6 +313,7 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         TT_CUDA(cudaMemcpyAsync(&overflow, ovf, 4, cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaMemcpyAsync(&nnz, rp + n, 8, cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaStreamSynchronize(c->stream));
+        knn_tc_settle(c);
         if (!overflow) {
             u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);
             f32* w = c->arena.get<f32>(S_OUT2, nnz + 1);
@@ -342,6 +344,7 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         scan_exclusive<u64>(c, f, pos, m, tot);
         TT_CUDA(cudaMemcpyAsync(&nnz, tot, 8, cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaStreamSynchronize(c->stream));
+        knn_tc_settle(c);
         ++c->launches;
     }
     u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);

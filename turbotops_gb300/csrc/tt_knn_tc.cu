@@ -1177,11 +1177,23 @@ bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x) {
            (reinterpret_cast<uintptr_t>(x) & 15) == 0;
 }
 
+// The deferred status of the last knn_tc (error word, counters), once the
+// stream has been synchronised: throws on a device timeout.
+void knn_tc_settle(tt_ctx* c) {
+    if (!c->tc_pending) return;
+    c->tc_pending = false;
+    if (c->tc_host[0]) throw Error(TT_ERR_TIMEOUT, "gb300: a bounded device wait timed out in the tensor-core kNN");
+    c->filter_evals = c->tc_host[1];
+    c->filter_tiles = c->tc_host[2];
+}
+
 // Exact kNN lists through the tile order and the tensor-core filter; sets
-// the context's counts of exact evaluations and computed Gram tiles.
+// the context's counts of exact evaluations and computed Gram tiles. With
+// defer, the status is only copied back: the caller synchronises later and
+// then calls knn_tc_settle before it relies on the lists.
 // Slots: S_TC_* (regrouped heads, tile packs, error terms, tile records), S_MISC0/1, S_COUNT, and
 // the radix sort's own (S_SORT_*, S_SCAN*).
-void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
+void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists, bool defer) {
     const u32 ntiles = div_up(n, TC_N);
     const u64 wpad = u64(ntiles) * TC_N;
     // about 12 tiles per pivot region
@@ -1251,14 +1263,15 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists) {
     k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, pack, eq, n, k, nq, stats, ids, dists, ctl, ctl + 1, cnt);
     TT_LAUNCH("k_knn_tc");
     c->launches += 2;
-    u32 e = 0;
-    unsigned long long h[2] = {0, 0};
-    TT_CUDA(cudaMemcpyAsync(&e, ctl + 1, 4, cudaMemcpyDeviceToHost, c->stream));
-    TT_CUDA(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
-    TT_CUDA(cudaStreamSynchronize(c->stream));
-    if (e) throw Error(TT_ERR_TIMEOUT, "gb300: a bounded device wait timed out in the tensor-core kNN");
-    c->filter_evals = h[0];
-    c->filter_tiles = h[1];
+    if (!c->tc_host) TT_CUDA(cudaMallocHost(&c->tc_host, 4 * sizeof(unsigned long long)));
+    c->tc_host[0] = 0;
+    TT_CUDA(cudaMemcpyAsync(c->tc_host, ctl + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaMemcpyAsync(c->tc_host + 1, cnt, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+    c->tc_pending = true;
+    if (!defer) {
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+        knn_tc_settle(c);
+    }
 }
 
 }  // namespace tt
