@@ -229,26 +229,22 @@ struct CsrCx {
     const u64* rp;
     const u32* ci;
     const f32* w;
-    __device__ __forceinline__ f32 d(u32 i, u32 j) const {
-        if (i == j) return 0.0f;
-        u64 lo = rp[i], hi = rp[i + 1];
-        while (lo < hi) {
-            const u64 mid = (lo + hi) >> 1;
-            if (ci[mid] < j) lo = mid + 1;
-            else hi = mid;
-        }
-        return (lo < rp[i + 1] && ci[lo] == j) ? w[lo] : INFINITY;
-    }
     // Largest common neighbour x of a and b with both weights <= cap (the
-    // k-way intersection walked from the top, rips.hpp:429-471).
-    __device__ __forceinline__ u32 top_cofacet2(u32 a, u32 b, f32 cap) const {
+    // k-way intersection walked from the top, rips.hpp:429-471), and its two
+    // weights w(a, x), w(b, x).
+    __device__ __forceinline__ u32 top_cofacet2(u32 a, u32 b, f32 cap, f32& wax, f32& wbx) const {
         u64 pa = rp[a + 1], pb = rp[b + 1];
         const u64 la = rp[a], lb = rp[b];
         while (pa > la && pb > lb) {
             const u32 xa = ci[pa - 1], xb = ci[pb - 1];
             if (xa > xb) { --pa; continue; }
             if (xb > xa) { --pb; continue; }
-            if (w[pa - 1] <= cap && w[pb - 1] <= cap) return xa;
+            const f32 x1 = w[pa - 1], x2 = w[pb - 1];
+            if (x1 <= cap && x2 <= cap) {
+                wax = x1;
+                wbx = x2;
+                return xa;
+            }
             --pa;
             --pb;
         }
@@ -268,16 +264,26 @@ __global__ void k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, const u32
         const u64 idx = key_idx(key);
         u32 a, b;
         decode_edge(idx, a, b);
-        const u32 w = cx.top_cofacet2(a, b, d);
+        f32 wax = 0.0f, wbx = 0.0f;
+        const u32 w = cx.top_cofacet2(a, b, d, wax, wbx);
         bool apparent = false, em = false;
         if (w != NOV) {
             u32 c0 = a, c1 = b, c2 = w;
             sort3(c0, c1, c2);
-            u32 f0 = 0, f1 = 0;
-            const u64 f = tri_zero_facet(cx, c0, c1, c2, d, f0, f1);
-            apparent = f == idx;
+            // the zero facet (tri_zero_facet's order) from the three known
+            // edge lengths: (a, b) = d, (a, w) = wax, (b, w) = wbx
+            auto len = [&](u32 u, u32 v) -> f32 {
+                if ((u == a && v == b) || (u == b && v == a)) return d;
+                return u == a || v == a ? wax : wbx;
+            };
+            u32 f0, f1;
+            if (len(c1, c2) == d) f0 = c1, f1 = c2;
+            else if (len(c0, c2) == d) f0 = c0, f1 = c2;
+            else f0 = c0, f1 = c1;   // (a, b) is one of the three pairs: one length equals d
+            apparent = edge_idx(f0, f1) == idx;
             if (!apparent) {
-                const u32 w2 = cx.top_cofacet2(f0, f1, d);
+                f32 t1, t2;
+                const u32 w2 = cx.top_cofacet2(f0, f1, d, t1, t2);
                 if (w2 != NOV) {
                     u32 g0 = f0, g1 = f1, g2 = w2;
                     sort3(g0, g1, g2);
