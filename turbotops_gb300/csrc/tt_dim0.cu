@@ -306,11 +306,15 @@ __global__ void k_iota(u32* __restrict__ p, u32 n) {
 
 // For each live edge with endpoints in different components, offer its rank
 // to both components; edges inside a component are dropped from the list.
-// (The survivors' list grows by one atomic per warp: ranks from a ballot.)
-__global__ void k_bv_offer(const u64* __restrict__ keys, const u32* __restrict__ live, u32 nlive, int all,
-                           const u32* __restrict__ comp, u32* __restrict__ best, u32* __restrict__ live_out,
-                           u32* __restrict__ nlive_out) {
+// (The survivors' list grows by one atomic per warp: ranks from a ballot.
+// The first round offers all m edges; later rounds read their count from
+// the previous round's counter, so rounds run without a host round trip.)
+__global__ void k_bv_offer(const u64* __restrict__ keys, const u32* __restrict__ live,
+                           const u32* __restrict__ nlive_in, u32 m, const u32* __restrict__ comp,
+                           u32* __restrict__ best, u32* __restrict__ live_out, u32* __restrict__ nlive_out) {
     const u32 lane = threadIdx.x & 31;
+    const bool all = nlive_in == nullptr;
+    const u32 nlive = all ? m : *nlive_in;
     for (u32 base = blockIdx.x * blockDim.x; base < nlive; base += gridDim.x * blockDim.x) {
         const u32 t = base + threadIdx.x;   // whole warps iterate together
         bool keep = false;
@@ -518,31 +522,39 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
     u32* best = c->arena.get<u32>(S_UF_BEST, n + 1);
     u32* live0 = c->arena.get<u32>(S_UF_WORK, m + 1);
     u32* live1 = c->arena.get<u32>(S_UF_WORK2, m + 1);
-    u32* ctr = c->arena.get<u32>(S_MISC1, 4);   // [0] live count, [1] hooks
+    constexpr int kRounds = 64;
+    u32* ctr = c->arena.get<u32>(S_MISC1, 2 * kRounds);   // per round: live count, hooks
     u64 total_hooks = 0;
     if (n) {
         k_iota<<<grid_for(n, 256), 256, 0, c->stream>>>(comp, n);
         k_iota<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, n);
         TT_CUDA(cudaMemsetAsync(best, 0xff, sizeof(u32) * n, c->stream));
         c->launches += 2;
-        u32 nlive = u32(m);
-        bool all = true;
-        for (int round = 0; nlive && round < 64; ++round) {
-            TT_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(u32), c->stream));
-            k_bv_offer<<<grid_for(nlive, 256), 256, 0, c->stream>>>(out.keys, live0, nlive, all, comp, best, live1,
-                                                                     ctr);
-            k_bv_hook<<<grid_for(n, 256), 256, 0, c->stream>>>(out.keys, comp, best, parent, tree, n, ctr + 1);
-            k_bv_flatten<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, comp, best, n);
-            TT_LAUNCH("boruvka");
-            c->launches += 3;
-            u32 h[2];
-            TT_CUDA(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaMemsetAsync(ctr, 0, 2 * kRounds * sizeof(u32), c->stream));
+        // Two rounds a host round trip (a round after convergence finds no
+        // edge between components and changes nothing); the grid covers the
+        // last live count the host knows (counts only shrink).
+        u32 known = u32(m);
+        for (int round = 0; known && round < kRounds;) {
+            const int first = round;
+            for (int q = 0; q < 2 && round < kRounds; ++q, ++round) {
+                k_bv_offer<<<grid_for(known, 256), 256, 0, c->stream>>>(
+                    out.keys, live0, round ? ctr + 2 * (round - 1) : nullptr, u32(m), comp, best, live1, ctr + 2 * round);
+                k_bv_hook<<<grid_for(n, 256), 256, 0, c->stream>>>(out.keys, comp, best, parent, tree, n,
+                                                                   ctr + 2 * round + 1);
+                k_bv_flatten<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, comp, best, n);
+                TT_LAUNCH("boruvka");
+                c->launches += 3;
+                std::swap(live0, live1);
+            }
+            u32 h[4] = {0, 0, 0, 0};
+            TT_CUDA(cudaMemcpyAsync(h, ctr + 2 * first, sizeof(u32) * 2 * (round - first), cudaMemcpyDeviceToHost,
+                                    c->stream));
             TT_CUDA(cudaStreamSynchronize(c->stream));
-            total_hooks += h[1];
-            std::swap(live0, live1);
-            all = false;
-            nlive = h[0];
-            if (h[1] == 0) break;
+            const int last = round - first - 1;
+            total_hooks += h[1] + (last ? h[3] : 0);
+            known = h[2 * last];
+            if (h[2 * last + 1] == 0) break;
         }
     }
     side.join();   // the flags of the scan
