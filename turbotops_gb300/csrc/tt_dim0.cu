@@ -522,7 +522,7 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
     u32* best = c->arena.get<u32>(S_UF_BEST, n + 1);
     u32* live0 = c->arena.get<u32>(S_UF_WORK, m + 1);
     u32* live1 = c->arena.get<u32>(S_UF_WORK2, m + 1);
-    constexpr int kRounds = 64;
+    constexpr int kRounds = 64, kPerTrip = 3;
     u32* ctr = c->arena.get<u32>(S_MISC1, 2 * kRounds);   // per round: live count, hooks
     u64 total_hooks = 0;
     if (n) {
@@ -531,13 +531,13 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
         TT_CUDA(cudaMemsetAsync(best, 0xff, sizeof(u32) * n, c->stream));
         c->launches += 2;
         TT_CUDA(cudaMemsetAsync(ctr, 0, 2 * kRounds * sizeof(u32), c->stream));
-        // Two rounds a host round trip (a round after convergence finds no
+        // Three rounds a host round trip (a round after convergence finds no
         // edge between components and changes nothing); the grid covers the
         // last live count the host knows (counts only shrink).
         u32 known = u32(m);
         for (int round = 0; known && round < kRounds;) {
             const int first = round;
-            for (int q = 0; q < 2 && round < kRounds; ++q, ++round) {
+            for (int q = 0; q < kPerTrip && round < kRounds; ++q, ++round) {
                 k_bv_offer<<<grid_for(known, 256), 256, 0, c->stream>>>(
                     out.keys, live0, round ? ctr + 2 * (round - 1) : nullptr, u32(m), comp, best, live1, ctr + 2 * round);
                 k_bv_hook<<<grid_for(n, 256), 256, 0, c->stream>>>(out.keys, comp, best, parent, tree, n,
@@ -547,12 +547,12 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
                 c->launches += 3;
                 std::swap(live0, live1);
             }
-            u32 h[4] = {0, 0, 0, 0};
+            u32 h[2 * kPerTrip] = {};
             TT_CUDA(cudaMemcpyAsync(h, ctr + 2 * first, sizeof(u32) * 2 * (round - first), cudaMemcpyDeviceToHost,
                                     c->stream));
             TT_CUDA(cudaStreamSynchronize(c->stream));
             const int last = round - first - 1;
-            total_hooks += h[1] + (last ? h[3] : 0);
+            for (int q = 0; q <= last; ++q) total_hooks += h[2 * q + 1];
             known = h[2 * last];
             if (h[2 * last + 1] == 0) break;
         }
