@@ -1056,11 +1056,21 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
                     const u32 base = incl - tcnt;
                     u32* wq = S.q[warp];
                     f32* wr = S.r[warp];
-                    u32 pos = base;
+                    {   // this lane's survivors into the queue: one pass over the set bits
+                        u32 m0 = mk[0], m1 = mk[1], m2 = mk[2], m3 = mk[3];
+                        u32 pos = base;
 #pragma unroll 1
-                    for (int chunk = 0; chunk < TC_N / 32; ++chunk)
-                        for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1)
-                            wq[pos++] = (lane << 7) | u32(chunk * 32 + __ffs(mm) - 1);
+                        while (m0 | m1 | m2 | m3) {
+                            const u32 c = m0 ? 0u : m1 ? 32u : m2 ? 64u : 96u;
+                            const u32 wd = m0 ? m0 : m1 ? m1 : m2 ? m2 : m3;
+                            wq[pos++] = (lane << 7) | (c + u32(__ffs(wd) - 1));
+                            const u32 rest = wd & (wd - 1);
+                            if (m0) m0 = rest;
+                            else if (m1) m1 = rest;
+                            else if (m2) m2 = rest;
+                            else m3 = rest;
+                        }
+                    }
                     __syncwarp();
 #pragma unroll 1
                     for (u32 p = lane; p < total; p += 32) {
