@@ -270,10 +270,6 @@ __device__ __forceinline__ void tmem_wait2(u32 (&v)[32], u32 (&w)[32]) {
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 
-// m[c] for a run-time c without dynamic register indexing (keeps m in registers)
-__device__ __forceinline__ u32 pick4(const u32 (&m)[4], int c) {
-    return c == 0 ? m[0] : c == 1 ? m[1] : c == 2 ? m[2] : m[3];
-}
 
 template <int DIM>
 struct RegVec {
@@ -1035,15 +1031,20 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
                     bool changed = false;
                     f32 qa[TC_DIM];   // this thread's query, from the query tile
                     raw_row(S.a, S.alo, row, qa);
+                    u32 m0 = mk[0], m1 = mk[1], m2 = mk[2], m3 = mk[3];
 #pragma unroll 1
-                    for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
-#pragma unroll 1
-                        for (u32 mm = pick4(mk, chunk); mm; mm &= mm - 1) {
-                            const u32 rr = u32(chunk * 32 + __ffs(mm) - 1);
-                            f32 cb[TC_DIM];
-                            raw_row(bt, blo, rr, cb);
-                            changed |= consider(oid[rr], __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{qa}, RegVec<TC_DIM>{cb}, TC_DIM)));
-                        }
+                    while (m0 | m1 | m2 | m3) {   // one pass over the set bits
+                        const u32 c = m0 ? 0u : m1 ? 32u : m2 ? 64u : 96u;
+                        const u32 wd = m0 ? m0 : m1 ? m1 : m2 ? m2 : m3;
+                        const u32 rr = c + u32(__ffs(wd) - 1);
+                        const u32 rest = wd & (wd - 1);
+                        if (m0) m0 = rest;
+                        else if (m1) m1 = rest;
+                        else if (m2) m2 = rest;
+                        else m3 = rest;
+                        f32 cb[TC_DIM];
+                        raw_row(bt, blo, rr, cb);
+                        changed |= consider(oid[rr], __fsqrt_rn(l2_sq_acc(RegVec<TC_DIM>{qa}, RegVec<TC_DIM>{cb}, TC_DIM)));
                     }
                     if (changed) update_bound();
                 } else if (total) {
