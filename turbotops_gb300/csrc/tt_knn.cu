@@ -85,10 +85,12 @@ __global__ void k_row_ptr(const u32* __restrict__ rows, u64 nnz, u32 n, u64* __r
 constexpr u32 kRowSortMax = 2048;
 constexpr u32 kWarpRowMax = 64;    // longer rows: one block each (k_graph_rowsort_long)
 
+// Row i holds its own list (k entries, slots off[i] .. off[i] + k - 1 in
+// list order) and the entries naming i (after them, atomic cursor).
 __global__ void k_graph_deg(const u32* __restrict__ ids, u32 n, u32 k, unsigned long long* __restrict__ deg) {
     const u64 total = u64(n) * k;
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += u64(gridDim.x) * blockDim.x) {
-        atomicAdd(&deg[e / k], 1ull);
+        if (e % k == 0) atomicAdd(&deg[e / k], (unsigned long long)k);
         atomicAdd(&deg[ids[e]], 1ull);
     }
 }
@@ -100,10 +102,10 @@ __global__ void k_graph_fill(const u32* __restrict__ ids, const f32* __restrict_
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += u64(gridDim.x) * blockDim.x) {
         const u32 i = u32(e / k), j = ids[e];
         const f32 de = d[e];
-        const u64 a = off[i] + atomicAdd(&cur[i], 1u);
+        const u64 a = off[i] + e % k;
         col[a] = j;
         w[a] = de;
-        const u64 b = off[j] + atomicAdd(&cur[j], 1u);
+        const u64 b = off[j] + k + atomicAdd(&cur[j], 1u);
         col[b] = i;
         w[b] = de;
     }
