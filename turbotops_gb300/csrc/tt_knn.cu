@@ -132,30 +132,40 @@ __global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* _
             if (lane == 0) longs[1 + atomicAdd(longs, 1u)] = v;
             continue;
         }
-        for (u32 a0 = 0; a0 < L; a0 += 32) {
-            const u32 a = a0 + lane;
-            const u32 ca = a < L ? col[b + a] : 0xffffffffu;
-            u32 rank = 0;
-            for (u32 t0 = 0; t0 < L; t0 += 32) {
-                const u32 ct = t0 + lane < L ? col[b + t0 + lane] : 0xffffffffu;
-                const u32 lim = min(32u, L - t0);
-                for (u32 s = 0; s < lim; ++s) {
-                    const u32 cs = __shfl_sync(0xffffffffu, ct, s);
-                    rank += (cs < ca) || (cs == ca && t0 + s < a);
-                }
-            }
-            if (a < L) {
-                scol[b + rank] = ca;
-                sw[b + rank] = w[b + a];
-            }
+        // at most two entries a lane (L <= 64): their rank by (column,
+        // position) and whether an equal column comes earlier, in one pass
+        // of shuffles; the distinct count needs no second read of the row
+        const u32 c0 = lane < L ? col[b + lane] : 0xffffffffu;
+        const u32 c1 = lane + 32 < L ? col[b + 32 + lane] : 0xffffffffu;
+        const f32 w0 = lane < L ? w[b + lane] : 0.0f;
+        const f32 w1 = lane + 32 < L ? w[b + 32 + lane] : 0.0f;
+        u32 r0 = 0, r1 = 0, e0 = 0, e1 = 0;
+        const u32 l0 = L < 32 ? L : 32u;
+        for (u32 s = 0; s < l0; ++s) {
+            const u32 cs = __shfl_sync(0xffffffffu, c0, s);
+            const bool before = s < lane;
+            r0 += cs < c0 || (cs == c0 && before);
+            e0 += cs == c0 && before;
+            r1 += cs <= c1;   // position s precedes position 32 + lane
+            e1 += cs == c1;
         }
-        __syncwarp();
-        u32 uc = 0;
-        for (u32 r0 = 0; r0 < L; r0 += 32) {
-            const u32 r = r0 + lane;
-            const bool u = r < L && (r == 0 || scol[b + r - 1] != scol[b + r]);
-            uc += __popc(__ballot_sync(0xffffffffu, u));
+        for (u32 s = 0; s + 32 < L; ++s) {
+            const u32 cs = __shfl_sync(0xffffffffu, c1, s);
+            const bool before = s < lane;
+            r0 += cs < c0;    // position 32 + s follows position lane
+            r1 += cs < c1 || (cs == c1 && before);
+            e1 += cs == c1 && before;
         }
+        if (lane < L) {
+            scol[b + r0] = c0;
+            sw[b + r0] = w0;
+        }
+        if (lane + 32 < L) {
+            scol[b + r1] = c1;
+            sw[b + r1] = w1;
+        }
+        const u32 uc = __popc(__ballot_sync(0xffffffffu, lane < L && e0 == 0)) +
+                       __popc(__ballot_sync(0xffffffffu, lane + 32 < L && e1 == 0));
         if (lane == 0) ucnt[v] = uc;
         __syncwarp();
     }
