@@ -101,13 +101,9 @@ u64 knn_front_dev(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 
     u64* rp = c->arena.get<u64>(S_GRAPH_RP, u64(n) + 1);
     u32* ci = nullptr;
     f32* w = nullptr;
-    const u64 nnz = knn_graph(c, x, n, dim, kind, p, nullptr, kk, rp, &ci, &w);
-    u32* gci = c->arena.get<u32>(S_GRAPH_TMP, nnz + 1);
-    f32* gw = c->arena.get<f32>(S_KNN_D, nnz + 1);
-    if (nnz) {
-        TT_CUDA(cudaMemcpyAsync(gci, ci, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
-        TT_CUDA(cudaMemcpyAsync(gw, w, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
-    }
+    const u64 nnz = knn_graph(c, x, n, dim, kind, p, nullptr, kk, rp, &ci, &w);   // its own slots: dim0 keeps them
+    u32* gci = ci;
+    f32* gw = w;
     after_graph(nnz, rp, gci, gw);   // before dim0: the graph is final here
     Complex cx{nullptr, rp, gci, gw, n, INFINITY};
     dim0(c, cx, maxdim, r);

@@ -127,7 +127,7 @@ enum Slot : int {
     S_TC_X, S_TC_PERM, S_TC_STATS, S_TC_KEYS, S_TC_VALS, S_TC_PIV,   // tensor-core kNN (tile order)
     S_TC_KEY2, S_TC_VAL2, S_TC_CELL, S_TC_LO, S_TC_ERR, S_TC_SPV,
     S_EDGE_CNT, S_EDGE_SORT, S_EDGE_IDX, S_EDGE_INV,               // ordered edge generation
-    S_GRAPH_LONG,                                                  // kNN graph: rows above the warp sort
+    S_GRAPH_LONG, S_GRAPH_CI, S_GRAPH_W,                           // kNN graph: long rows; its columns and weights
     S_NSLOTS
 };
 

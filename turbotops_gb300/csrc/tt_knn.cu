@@ -327,8 +327,8 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         TT_CUDA(cudaStreamSynchronize(c->stream));
         knn_tc_settle(c);
         if (!overflow) {
-            u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);
-            f32* w = c->arena.get<f32>(S_OUT2, nnz + 1);
+            u32* ci = c->arena.get<u32>(S_GRAPH_CI, nnz + 1);
+            f32* w = c->arena.get<f32>(S_GRAPH_W, nnz + 1);
             k_graph_emit<<<gw, 256, 0, c->stream>>>(off, n, scol, sw, rp, ci, w);
             TT_LAUNCH("k_graph_emit");
             ++c->launches;
@@ -359,8 +359,8 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         knn_tc_settle(c);
         ++c->launches;
     }
-    u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);
-    f32* w = c->arena.get<f32>(S_OUT2, nnz + 1);
+    u32* ci = c->arena.get<u32>(S_GRAPH_CI, nnz + 1);
+    f32* w = c->arena.get<f32>(S_GRAPH_W, nnz + 1);
     u32* rows = c->arena.get<u32>(S_OUT3, nnz + 1);
     if (m) {
         k_unique_emit<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, vals, m, f, pos, ci, w, rows);

@@ -202,11 +202,17 @@ void persistence_points(tt_ctx* c, const f32* x_h, u32 n, u32 dim, int kind, f32
     u64 nnz = 0;
     if (knn) nnz = knn_graph(c, x, n, dim, kind, p, nullptr, n ? std::min<u32>(k, n - 1) : 0, rp, &ci, &w);
     else nnz = radius_graph(c, x, n, dim, kind, p, thr, rp, &ci, &w);
-    u32* gci = c->arena.get<u32>(S_GRAPH_TMP, nnz + 1);
-    f32* gw = c->arena.get<f32>(S_KNN_D, nnz + 1);
-    if (nnz) {
-        TT_CUDA(cudaMemcpyAsync(gci, ci, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
-        TT_CUDA(cudaMemcpyAsync(gw, w, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
+    // the kNN graph has its own slots; the radius graph's (S_OUT*) are
+    // moved out of the way of the later stages
+    u32* gci = ci;
+    f32* gw = w;
+    if (!knn) {
+        gci = c->arena.get<u32>(S_GRAPH_TMP, nnz + 1);
+        gw = c->arena.get<f32>(S_KNN_D, nnz + 1);
+        if (nnz) {
+            TT_CUDA(cudaMemcpyAsync(gci, ci, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
+            TT_CUDA(cudaMemcpyAsync(gw, w, 4 * nnz, cudaMemcpyDeviceToDevice, c->stream));
+        }
     }
     if (n == 0) return;
     sparse_tail(c, rp, gci, gw, nullptr, nullptr, nullptr, n, nnz, thr, maxdim, out);
