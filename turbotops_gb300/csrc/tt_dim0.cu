@@ -373,31 +373,33 @@ __global__ void k_bv_flatten(const u32* __restrict__ parent, u32* __restrict__ c
 // --------------------------------------------------------------------------
 // Ordered compaction of H0 bars and columns.
 // --------------------------------------------------------------------------
+// One flag word per edge: finite H0 bar << 32 | column (m < 2^32, so one
+// scan counts both without a carry between the halves).
 __global__ void k_flags_dim0(const u64* __restrict__ keys, const u8* __restrict__ tree, const u8* __restrict__ app,
-                             u64 m, int want_cols, u64* __restrict__ fh, u64* __restrict__ fc) {
+                             u64 m, int want_cols, u64* __restrict__ f) {
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
         const bool t = tree[e];
-        fh[e] = t && key_d(keys[e]) > 0.0f;
-        fc[e] = want_cols && !t && !(app && app[e]);
+        f[e] = (u64(t && key_d(keys[e]) > 0.0f) << 32) | u64(want_cols && !t && !(app && app[e]));
     }
 }
 
 __global__ void k_emit_dim0(const u64* __restrict__ keys, const u8* __restrict__ tree, const u8* __restrict__ app,
                             const u32* __restrict__ emw, const u8* __restrict__ emf, u64 m, int want_cols,
-                            const u64* __restrict__ oh, const u64* __restrict__ oc, const u64* __restrict__ tot,
+                            const u64* __restrict__ o2, const u64* __restrict__ tot,
                             f32* __restrict__ h0, u64* __restrict__ h0_edge, u64* __restrict__ cidx,
                             f32* __restrict__ cd, u64* __restrict__ emi, u8* __restrict__ emf_out) {
-    const u64 ncols = tot[1];
+    const u64 ncols = tot[0] & 0xffffffffull;
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
         const u64 key = keys[e];
         const f32 d = key_d(key);
         const bool t = tree[e];
+        const u64 oe = o2[e];   // exclusive counts: H0 bars << 32 | columns
         if (t && d > 0.0f) {
-            h0[oh[e]] = d;
-            h0_edge[oh[e]] = key_idx(key);   // the bar's critical (death) edge
+            h0[oe >> 32] = d;
+            h0_edge[oe >> 32] = key_idx(key);   // the bar's critical (death) edge
         }
         if (want_cols && !t && !(app && app[e])) {
-            const u64 o = ncols - 1 - oc[e];   // descending order (rips.hpp:867)
+            const u64 o = ncols - 1 - (oe & 0xffffffffull);   // descending order (rips.hpp:867)
             const u64 idx = key_idx(key);
             cidx[o] = idx;
             cd[o] = d;
@@ -417,11 +419,6 @@ __global__ void k_emit_dim0(const u64* __restrict__ keys, const u8* __restrict__
     }
 }
 
-__global__ void k_pair_totals(const u64* __restrict__ oh, const u64* __restrict__ oc, const u64* __restrict__ fh,
-                              const u64* __restrict__ fc, u64 m, u64* __restrict__ tot) {
-    tot[0] = m ? oh[m - 1] + fh[m - 1] : 0;
-    tot[1] = m ? oc[m - 1] + fc[m - 1] : 0;
-}
 
 inline u32 grid_for(u64 work, u32 per_block) {
     const u64 g = (work + per_block - 1) / per_block;
@@ -560,24 +557,21 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
     side.join();   // the flags of the scan
     // ordered compaction of H0 deaths and columns
     const int want_cols = maxdim >= 1;
-    u64* fh = c->arena.get<u64>(S_MISC0, 4 * m + 8);
-    u64* fc = fh + m + 2;
-    u64* oh = fc + m + 2;
-    u64* oc = oh + m + 2;
+    u64* f2 = c->arena.get<u64>(S_MISC0, 2 * m + 4);
+    u64* o2 = f2 + m + 2;
     u64* tot = c->arena.get<u64>(S_COUNT, 4);
     if (m) {
-        k_flags_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, m, want_cols, fh, fc);
+        k_flags_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, m, want_cols, f2);
         TT_LAUNCH("k_flags_dim0");
-        scan_exclusive<u64>(c, fh, oh, m, nullptr);
-        scan_exclusive<u64>(c, fc, oc, m, nullptr);
-        k_pair_totals<<<1, 1, 0, c->stream>>>(oh, oc, fh, fc, m, tot);
-        c->launches += 2;
+        scan_exclusive<u64>(c, f2, o2, m, tot);
+        c->launches += 1;
     } else {
-        TT_CUDA(cudaMemsetAsync(tot, 0, 2 * sizeof(u64), c->stream));
+        TT_CUDA(cudaMemsetAsync(tot, 0, sizeof(u64), c->stream));
     }
-    u64 h[2];
-    TT_CUDA(cudaMemcpyAsync(h, tot, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    u64 hp = 0;
+    TT_CUDA(cudaMemcpyAsync(&hp, tot, sizeof(hp), cudaMemcpyDeviceToHost, c->stream));
     TT_CUDA(cudaStreamSynchronize(c->stream));
+    const u64 h[2] = {hp >> 32, hp & 0xffffffffull};
     out.nh0 = h[0];
     out.ncols = h[1];
     out.h0 = c->arena.get<f32>(S_OUT0, h[0] + 1);
@@ -587,9 +581,8 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
     out.emf = c->arena.get<u8>(S_OUT4, h[1] + 1);
     out.h0_edge = c->arena.get<u64>(S_OUT5, h[0] + 1);
     if (m) {
-        k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, emw, emf, m, want_cols, oh, oc,
-                                                             tot, out.h0, out.h0_edge, out.cidx, out.cd, out.emi,
-                                                             out.emf);
+        k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, emw, emf, m, want_cols, o2, tot,
+                                                             out.h0, out.h0_edge, out.cidx, out.cd, out.emi, out.emf);
         TT_LAUNCH("k_emit_dim0");
         ++c->launches;
     }
