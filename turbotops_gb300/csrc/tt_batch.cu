@@ -310,11 +310,7 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         TT_CUDA(cudaMemcpyAsync(b->row_cloud, row_cloud.data(), 4 * row_cloud.size(), cudaMemcpyHostToDevice, s));
         // size the sort's scratch outside any capture: the same calls, no graph
         b->sctx.arena.get<u64>(S_SORT_A, b->total_pairs);
-        const u32 rs_tiles = div_up(b->total_pairs, 4096);
-        b->sctx.arena.get<u32>(S_SORT_HIST, u64(rs_tiles) * 256 + 1);
-        const u64 scan1 = (u64(rs_tiles) * 256 + 4095) / 4096, scan2 = (scan1 + 4095) / 4096;
-        b->sctx.arena.get<u32>(S_SCAN, 2 * scan1 + 2);
-        b->sctx.arena.get<u32>(S_SCAN2, 2 * scan2 + 2);
+        radix_reserve(&b->sctx, b->total_pairs);
         TT_CUDA(cudaStreamSynchronize(s));
     } catch (...) {
         b->release();

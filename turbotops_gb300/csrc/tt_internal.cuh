@@ -56,6 +56,7 @@ template <typename V>
 bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits = 0, int lo_bit = 0);
 template <typename V>
 void radix_sort_inplace(tt_ctx* c, u64* keys, V* vals, u64 n, int force_bits = 0);
+void radix_reserve(tt_ctx* c, u64 n);   // every slot radix_sort of n keys may grow
 
 // ---- tt_dim0.cu
 struct Dim0Out {

@@ -20,6 +20,7 @@ namespace {
 
 constexpr int RS_THREADS = 256, RS_ITEMS = 16, RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_MAXBITS = 9, RS_BINS = 1 << RS_MAXBITS;   // digit width and bins per pass (at most)
 constexpr int SCAN_THREADS = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 // ---------------------------------------------------------------------------
@@ -94,20 +95,22 @@ __global__ void k_tile_scan(const T* __restrict__ in, u64 n, const T* __restrict
 // ---------------------------------------------------------------------------
 // Radix sort kernels.
 // ---------------------------------------------------------------------------
+// Digits of up to RS_MAXBITS bits (a pass sorts `width` bits from `shift`).
 __global__ void __launch_bounds__(RS_THREADS)
-k_rs_upsweep(const u64* __restrict__ keys, u64 n, int shift, u32* __restrict__ hist, u32 tiles) {
-    __shared__ u32 h[RS_WARPS][256];
-    for (int t = threadIdx.x; t < RS_WARPS * 256; t += RS_THREADS) (&h[0][0])[t] = 0;
+k_rs_upsweep(const u64* __restrict__ keys, u64 n, int shift, u32 width, u32* __restrict__ hist, u32 tiles) {
+    __shared__ u32 h[RS_WARPS][RS_BINS];
+    const u32 nd = 1u << width, mask = nd - 1u;
+    for (int t = threadIdx.x; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&h[0][0])[t] = 0;
     __syncthreads();
     const int w = threadIdx.x >> 5;
     const u64 base = u64(blockIdx.x) * RS_TILE;
 #pragma unroll 4
     for (int i = 0; i < RS_ITEMS; ++i) {
         const u64 k = base + u64(i) * RS_THREADS + threadIdx.x;
-        if (k < n) atomicAdd(&h[w][(keys[k] >> shift) & 0xff], 1u);
+        if (k < n) atomicAdd(&h[w][u32(keys[k] >> shift) & mask], 1u);
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
+    for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) {
         u32 s = 0;
 #pragma unroll
         for (int q = 0; q < RS_WARPS; ++q) s += h[q][d];
@@ -118,11 +121,12 @@ k_rs_upsweep(const u64* __restrict__ keys, u64 n, int shift, u32* __restrict__ h
 template <typename V>
 __global__ void __launch_bounds__(RS_THREADS)
 k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __restrict__ vin,
-             V* __restrict__ vout, u64 n, int shift, const u32* __restrict__ offs, u32 tiles) {
-    __shared__ u32 cnt[RS_WARPS][256];   // per-warp running count, then warp prefix
-    __shared__ u32 gbase[256];
-    for (int t = threadIdx.x; t < RS_WARPS * 256; t += RS_THREADS) (&cnt[0][0])[t] = 0;
-    for (int d = threadIdx.x; d < 256; d += RS_THREADS) gbase[d] = offs[u64(d) * tiles + blockIdx.x];
+             V* __restrict__ vout, u64 n, int shift, u32 width, const u32* __restrict__ offs, u32 tiles) {
+    __shared__ u32 cnt[RS_WARPS][RS_BINS];   // per-warp running count, then warp prefix
+    __shared__ u32 gbase[RS_BINS];
+    const u32 nd = 1u << width, mask = nd - 1u;
+    for (int t = threadIdx.x; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&cnt[0][0])[t] = 0;
+    for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) gbase[d] = offs[u64(d) * tiles + blockIdx.x];
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const u32 lt = (1u << lane) - 1u;
@@ -136,12 +140,12 @@ k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __res
         const u64 k = base + u64(i) * 32 + lane;
         const bool ok = k < n;
         key[i] = ok ? kin[k] : ~0ull;
-        const u32 dg = ok ? u32(key[i] >> shift) & 0xffu : 0x100u;   // 0x100: no key
+        const u32 dg = ok ? u32(key[i] >> shift) & mask : RS_BINS;   // RS_BINS: no key
         const u32 peers = __match_any_sync(0xffffffffu, dg);
         const u32 before = __popc(peers & lt);
         const int leader = __ffs(peers) - 1;
         u32 prev = 0;
-        if (lane == leader && dg < 256) {
+        if (lane == leader && dg < RS_BINS) {
             prev = cnt[w][dg];
             cnt[w][dg] = prev + __popc(peers);
         }
@@ -151,7 +155,7 @@ k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __res
     }
     __syncthreads();
     // exclusive prefix over warps, per digit
-    for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
+    for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) {
         u32 s = 0;
 #pragma unroll
         for (int q = 0; q < RS_WARPS; ++q) {
@@ -165,7 +169,7 @@ k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __res
     for (int i = 0; i < RS_ITEMS; ++i) {
         const u64 k = base + u64(i) * 32 + lane;
         if (k < n) {
-            const u32 dg = u32(key[i] >> shift) & 0xffu;
+            const u32 dg = u32(key[i] >> shift) & mask;
             const u32 pos = gbase[dg] + cnt[w][dg] + rank[i];
             kout[pos] = key[i];
             if (vin) vout[pos] = vin[k];
@@ -248,20 +252,26 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
         bits = diff ? 64 - __builtin_clzll(diff) : 0;
     }
     const u32 tiles = div_up(n, RS_TILE);
-    u32* hist = c->arena.get<u32>(S_SORT_HIST, u64(tiles) * 256 + 1);
+    u32* hist = c->arena.get<u32>(S_SORT_HIST, u64(tiles) * RS_BINS + 1);
     u64 *ka = keys, *kb = kbuf;
     V *va = vals, *vb = vbuf;
     bool swapped = false;
-    for (int shift = lo_bit; shift < lo_bit + bits; shift += 8) {
-        k_rs_upsweep<<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, shift, hist, tiles);
+    // as few passes as digits of up to RS_MAXBITS bits allow, the bits
+    // spread evenly over them (25 bits: 9 + 8 + 8)
+    const int passes = (bits + RS_MAXBITS - 1) / RS_MAXBITS;
+    int shift = lo_bit;
+    for (int q = 0; q < passes; ++q) {
+        const int width = (lo_bit + bits - shift + (passes - q) - 1) / (passes - q);
+        k_rs_upsweep<<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, shift, u32(width), hist, tiles);
         TT_LAUNCH("k_rs_upsweep");
-        scan_exclusive<u32>(c, hist, hist, u64(tiles) * 256, nullptr, 0);
-        k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, shift, hist, tiles);
+        scan_exclusive<u32>(c, hist, hist, u64(tiles) << width, nullptr, 0);
+        k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, shift, u32(width), hist, tiles);
         TT_LAUNCH("k_rs_scatter");
         c->launches += 2;
         std::swap(ka, kb);
         std::swap(va, vb);
         swapped = !swapped;
+        shift += width;
     }
     return swapped;
 }
@@ -278,6 +288,20 @@ void radix_sort_inplace(tt_ctx* c, u64* keys, V* vals, u64 n, int force_bits) {
     if (radix_sort<V>(c, keys, vals, n, kb, vb, force_bits)) {
         TT_CUDA(cudaMemcpyAsync(keys, kb, n * sizeof(u64), cudaMemcpyDeviceToDevice, c->stream));
         if (vals) TT_CUDA(cudaMemcpyAsync(vals, vb, n * sizeof(V), cudaMemcpyDeviceToDevice, c->stream));
+    }
+}
+
+// Every scratch slot radix_sort of n keys may grow (for callers that record
+// their work into a CUDA graph, where no allocation may happen).
+void radix_reserve(tt_ctx* c, u64 n) {
+    const u64 tiles = div_up(n, RS_TILE);
+    c->arena.get<u32>(S_SORT_HIST, tiles * RS_BINS + 1);
+    u64 e = tiles * RS_BINS;   // histogram entries, scanned level by level
+    const int slots[3] = {S_SCAN, S_SCAN2, S_SCAN3};
+    for (int d = 0; d < 3 && e > u64(SCAN_TILE); ++d) {
+        const u64 t = (e + SCAN_TILE - 1) / SCAN_TILE;
+        c->arena.get<u32>(slots[d], 2 * t + 2);
+        e = t;
     }
 }
 
