@@ -20,7 +20,7 @@ namespace {
 
 constexpr int RS_THREADS = 256, RS_ITEMS = 16, RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_MAXBITS = 9, RS_BINS = 1 << RS_MAXBITS;   // digit width and bins per pass (at most)
+constexpr int RS_MAXBITS = 11, RS_BINS = 1 << RS_MAXBITS;   // digit width and bins per pass (at most)
 constexpr int SCAN_THREADS = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 // ---------------------------------------------------------------------------
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(RS_THREADS)
 k_rs_upsweep(const u64* __restrict__ keys, u64 n, int shift, u32 width, u32* __restrict__ hist, u32 tiles) {
     __shared__ u32 h[RS_WARPS][RS_BINS];
     const u32 nd = 1u << width, mask = nd - 1u;
-    for (int t = threadIdx.x; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&h[0][0])[t] = 0;
+    for (u32 t = threadIdx.x; t < RS_WARPS * nd; t += RS_THREADS) h[t / nd][t % nd] = 0;
     __syncthreads();
     const int w = threadIdx.x >> 5;
     const u64 base = u64(blockIdx.x) * RS_TILE;
@@ -125,7 +125,7 @@ k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __res
     __shared__ u32 cnt[RS_WARPS][RS_BINS];   // per-warp running count, then warp prefix
     __shared__ u32 gbase[RS_BINS];
     const u32 nd = 1u << width, mask = nd - 1u;
-    for (int t = threadIdx.x; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&cnt[0][0])[t] = 0;
+    for (u32 t = threadIdx.x; t < RS_WARPS * nd; t += RS_THREADS) cnt[t / nd][t % nd] = 0;
     for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) gbase[d] = offs[u64(d) * tiles + blockIdx.x];
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -257,7 +257,7 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
     V *va = vals, *vb = vbuf;
     bool swapped = false;
     // as few passes as digits of up to RS_MAXBITS bits allow, the bits
-    // spread evenly over them (25 bits: 9 + 8 + 8)
+    // spread evenly over them (25 bits: 9 + 8 + 8; 11 bits: one pass)
     const int passes = (bits + RS_MAXBITS - 1) / RS_MAXBITS;
     int shift = lo_bit;
     for (int q = 0; q < passes; ++q) {
