@@ -83,7 +83,52 @@ __global__ void k_row_ptr(const u32* __restrict__ rows, u64 nnz, u32 n, u64* __r
 // sort and its duplicates (mutual neighbours: same column, same distance
 // bits) dropped. Rows longer than kRowSortMax fall back to the global sort.
 constexpr u32 kRowSortMax = 2048;
-constexpr u32 kWarpRowMax = 64;    // longer rows: one block each (k_graph_rowsort_long)
+constexpr u32 kWarpRowMax = 128;   // longer rows: one block each (k_graph_rowsort_long)
+
+// Rank of each of a row's L <= 32 * SLOTS entries (slot j of lane l holds
+// position 32 j + l) by (column, position), and whether an equal column
+// comes earlier, in one pass of shuffles; scattered into the sorted copy.
+// Returns the row's distinct columns.
+template <int SLOTS>
+__device__ __forceinline__ u32 warp_rank_row(const u32* __restrict__ col, const f32* __restrict__ w, u64 b, u32 L,
+                                             u32* __restrict__ scol, f32* __restrict__ sw, u32 lane) {
+    u32 x[SLOTS], r[SLOTS], e[SLOTS];
+    f32 wv[SLOTS];
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j) {
+        const u32 p = 32u * j + lane;
+        x[j] = p < L ? col[b + p] : 0xffffffffu;
+        wv[j] = p < L ? w[b + p] : 0.0f;
+        r[j] = 0;
+        e[j] = 0;
+    }
+#pragma unroll
+    for (int c = 0; c < SLOTS; ++c) {
+        if (32u * c >= L) break;   // warp-uniform
+        const u32 lim = L - 32u * c < 32u ? L - 32u * c : 32u;
+        for (u32 s = 0; s < lim; ++s) {
+            const u32 cs = __shfl_sync(0xffffffffu, x[c], s);
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j) {
+                // position 32 c + s precedes position 32 j + lane?
+                const bool before = c < j || (c == j && s < lane);
+                r[j] += cs < x[j] || (cs == x[j] && before);
+                e[j] += cs == x[j] && before;
+            }
+        }
+    }
+    u32 uc = 0;
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j) {
+        const u32 p = 32u * j + lane;
+        if (p < L) {
+            scol[b + r[j]] = x[j];
+            sw[b + r[j]] = wv[j];
+        }
+        uc += __popc(__ballot_sync(0xffffffffu, p < L && e[j] == 0));
+    }
+    return uc;
+}
 
 // Row i holds its own list (k entries, slots off[i] .. off[i] + k - 1 in
 // list order) and the entries naming i (after them, atomic cursor).
@@ -132,40 +177,9 @@ __global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* _
             if (lane == 0) longs[1 + atomicAdd(longs, 1u)] = v;
             continue;
         }
-        // at most two entries a lane (L <= 64): their rank by (column,
-        // position) and whether an equal column comes earlier, in one pass
-        // of shuffles; the distinct count needs no second read of the row
-        const u32 c0 = lane < L ? col[b + lane] : 0xffffffffu;
-        const u32 c1 = lane + 32 < L ? col[b + 32 + lane] : 0xffffffffu;
-        const f32 w0 = lane < L ? w[b + lane] : 0.0f;
-        const f32 w1 = lane + 32 < L ? w[b + 32 + lane] : 0.0f;
-        u32 r0 = 0, r1 = 0, e0 = 0, e1 = 0;
-        const u32 l0 = L < 32 ? L : 32u;
-        for (u32 s = 0; s < l0; ++s) {
-            const u32 cs = __shfl_sync(0xffffffffu, c0, s);
-            const bool before = s < lane;
-            r0 += cs < c0 || (cs == c0 && before);
-            e0 += cs == c0 && before;
-            r1 += cs <= c1;   // position s precedes position 32 + lane
-            e1 += cs == c1;
-        }
-        for (u32 s = 0; s + 32 < L; ++s) {
-            const u32 cs = __shfl_sync(0xffffffffu, c1, s);
-            const bool before = s < lane;
-            r0 += cs < c0;    // position 32 + s follows position lane
-            r1 += cs < c1 || (cs == c1 && before);
-            e1 += cs == c1 && before;
-        }
-        if (lane < L) {
-            scol[b + r0] = c0;
-            sw[b + r0] = w0;
-        }
-        if (lane + 32 < L) {
-            scol[b + r1] = c1;
-            sw[b + r1] = w1;
-        }
-        const u32 uc = __popc(__ballot_sync(0xffffffffu, lane < L && e0 == 0)) +
-                       __popc(__ballot_sync(0xffffffffu, lane + 32 < L && e1 == 0));
+        const u32 uc = L <= 32 ? warp_rank_row<1>(col, w, b, L, scol, sw, lane)
+                       : L <= 64 ? warp_rank_row<2>(col, w, b, L, scol, sw, lane)
+                                 : warp_rank_row<4>(col, w, b, L, scol, sw, lane);
         if (lane == 0) ucnt[v] = uc;
         __syncwarp();
     }
