@@ -341,9 +341,12 @@ __global__ void k_bv_offer(const u64* __restrict__ keys, const u32* __restrict__
 
 // Every component root with an offered edge takes it into the forest and
 // hooks onto the other side; of a mutual pair only the larger root hooks.
-// (The hook count is summed per warp: one atomic a warp.)
+// (The hook count is summed per warp: one atomic a warp. A round whose offer
+// found no edge between components has nothing to hook: live == 0.)
 __global__ void k_bv_hook(const u64* __restrict__ keys, const u32* __restrict__ comp, const u32* __restrict__ best,
-                          u32* __restrict__ parent, u8* __restrict__ tree, u32 n, u32* __restrict__ hooks) {
+                          u32* __restrict__ parent, u8* __restrict__ tree, u32 n, u32* __restrict__ hooks,
+                          const u32* __restrict__ live) {
+    if (*live == 0) return;
     u32 mine = 0;
     for (u32 c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         if (comp[c] != c) continue;
@@ -361,7 +364,9 @@ __global__ void k_bv_hook(const u64* __restrict__ keys, const u32* __restrict__ 
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(hooks, mine);
 }
 
-__global__ void k_bv_flatten(const u32* __restrict__ parent, u32* __restrict__ comp, u32* __restrict__ best, u32 n) {
+__global__ void k_bv_flatten(const u32* __restrict__ parent, u32* __restrict__ comp, u32* __restrict__ best, u32 n,
+                             const u32* __restrict__ live) {
+    if (*live == 0) return;   // no hook this round: parents, components and offers unchanged
     for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         u32 r = parent[v];
         for (u32 s = 0; parent[r] != r && s < n; ++s) r = parent[r];
@@ -538,8 +543,8 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
                 k_bv_offer<<<grid_for(known, 256), 256, 0, c->stream>>>(
                     out.keys, live0, round ? ctr + 2 * (round - 1) : nullptr, u32(m), comp, best, live1, ctr + 2 * round);
                 k_bv_hook<<<grid_for(n, 256), 256, 0, c->stream>>>(out.keys, comp, best, parent, tree, n,
-                                                                   ctr + 2 * round + 1);
-                k_bv_flatten<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, comp, best, n);
+                                                                   ctr + 2 * round + 1, ctr + 2 * round);
+                k_bv_flatten<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, comp, best, n, ctr + 2 * round);
                 TT_LAUNCH("boruvka");
                 c->launches += 3;
                 std::swap(live0, live1);
