@@ -1,8 +1,8 @@
 """Seeded synthetic point clouds for the five benchmark workloads.
 
 No public dataset is involved: every workload is generated here with numpy's
-``default_rng`` so that the GPU machine, the tests and the CPU baseline all see the
-same float32 bits.
+``default_rng`` so that the bench, the tests and the CPU baseline all see the
+same float32 bits on every machine.
 
 * ``torus(n=1000)``            seed 1 — torus R=2, r=1, angles U[0, 2pi), + N(0, 0.05^2)
 * ``lattice(n=3000)``          seed 2 — distinct points of {0..15}^4, exact float32
