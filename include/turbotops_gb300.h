@@ -60,6 +60,12 @@ uint64_t tt_ctx_filter_evals(const tt_ctx* ctx);
 /* Candidate tiles (128 x 128 Gram blocks) the last filtered kNN computed;
  * the exhaustive product is ceil(n / 128)^2. */
 uint64_t tt_ctx_filter_tiles(const tt_ctx* ctx);
+/* Diagnostic, no reference counterpart: the tensor-core Gram filter's one
+ * hardware assumption, measured. Runs `products` seeded 128 x 128 TF32
+ * products (TF32-exact operands, the filter's augmentation step) and stores
+ * the largest |D - exact| / (|a|^2 + |b|^2); the filter's margins hold while
+ * it stays below 2^-19. */
+int tt_tc_gram_check(tt_ctx* ctx, uint32_t products, uint64_t seed, double* max_rel);
 /* Stream-ordered copy of bytes between any two device or host addresses
  * (lets bindings move context-owned results into their own buffers). */
 int tt_copy_async(tt_ctx* ctx, void* dst, const void* src, size_t bytes);

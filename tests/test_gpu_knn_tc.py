@@ -112,3 +112,15 @@ def test_tile_order_prunes_and_matches_at_scale():
     assert np.array_equal(i1, i2)
     assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
     assert 0 < tiles < 0.5 * nt * nt, (tiles, nt * nt)
+
+
+def test_tensor_core_accumulation_bound():
+    """The Gram filter assumes that kind::tf32 with FP32 accumulation errs by at
+    most 2^-19 (|a|^2 + |b|^2) on TF32-exact operands (the filter's margins are
+    2^-16 of the norms). Measured on 304 seeded 128 x 128 products, issued as
+    the kNN kernel issues them: mixed exponents and signs, and rows near a
+    common offset where the sum cancels."""
+    c = ctx()
+    r = C.c_double()
+    c.check(c.L.tt_tc_gram_check(c.h, 304, 12345, C.byref(r)))
+    assert 0.0 <= r.value < 2.0 ** -19, r.value

@@ -185,6 +185,13 @@ int tt_ctx_set_knn_mode(tt_ctx* c, int mode) {
 uint64_t tt_ctx_filter_evals(const tt_ctx* c) { return c ? c->filter_evals : 0; }
 uint64_t tt_ctx_filter_tiles(const tt_ctx* c) { return c ? c->filter_tiles : 0; }
 
+int tt_tc_gram_check(tt_ctx* c, uint32_t products, uint64_t seed, double* max_rel) {
+    return guard(c, [&] {
+        if (!max_rel) invalid("gb300: null output");
+        *max_rel = tc_gram_check(c, products, seed);
+    });
+}
+
 int tt_copy_async(tt_ctx* c, void* dst, const void* src, size_t bytes) {
     return guard(c, [&] {
         if (bytes) TT_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));

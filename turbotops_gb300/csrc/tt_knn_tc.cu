@@ -25,7 +25,8 @@
 //    reassembles x bit for bit. For a loaded tile the tensor core produces
 //      D(q, c) = q~ . c~ - W(c),   W(c) <= |c~|^2 (1 - 2^-16) / 2,
 //    the norm term entering as a fifth K-step (two TF32-exact parts). Only
-//    the FP32 accumulation rounds (<= 2^-19 (|q~|^2 + |c~|^2)), so
+//    the FP32 accumulation rounds (<= 2^-19 (|q~|^2 + |c~|^2); measured on
+//    the device by k_tc_gram_check below: under 2^-22 on GB300), so
 //      L = |q~|^2 (1 - 2^-16) - 2 D <= |q~ - c~|^2,
 //    and with e_x >= |x - x~| (per point, rounded up) the true distance is
 //    at least sqrt(L) - e_q - e_c. A candidate is evaluated exactly when
@@ -1165,6 +1166,134 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_N) : "memory");
 }
 
+// ---- a check of the tensor core's accumulation bound ------------------------
+//
+// The Gram filter's margins rest on one property of kind::tf32 with FP32
+// accumulation: for TF32-exact operands (exact products) the accumulated
+// result D of the five K-steps (32 coordinates and the augmentation) errs
+// by at most 2^-19 (|a|^2 + |b|^2) from the exact sum. This kernel measures
+// that error on the device: one 128 x 128 product per CTA of seeded
+// TF32-exact rows (mixed exponents 2^-8 .. 2^8 and signs, and rows near a
+// common offset, where the sum cancels), issued exactly as the kNN kernel
+// issues it, against an FP64 sum of the same products. out: the largest
+// |D - exact| / (|a|^2 + |b|^2), as the bits of a non-negative double.
+struct GramCheckSmem {
+    alignas(1024) float4 aaug[TC_M];
+    float4 baug[TC_N];
+    float4 zeros[TC_N];
+    alignas(1024) unsigned char a[TILE_BYTES];
+    alignas(1024) unsigned char b[TILE_BYTES];
+    alignas(8) u64 bar;
+    u32 tmem_base;
+};
+constexpr size_t GC_SMEM = 72 * 1024;   // at most three CTAs an SM: 3 x 128 TMEM columns
+static_assert(sizeof(GramCheckSmem) + 1024 <= GC_SMEM, "check layout exceeds its reservation");
+
+__device__ __forceinline__ u32 gc_hash(u64 x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return u32(x);
+}
+
+// coordinate k of row r of operand side (0 = queries, 1 = candidates) in product t
+__device__ __forceinline__ f32 gc_value(u64 seed, u32 t, u32 side, u32 r, u32 k) {
+    const u32 h = gc_hash(seed ^ (u64(t) << 40) ^ (u64(side) << 39) ^ (u64(r) << 8) ^ k);
+    const u32 rowkind = gc_hash(seed ^ (u64(t) << 40) ^ (u64(side) << 39) ^ (u64(r) << 8) ^ 0xffu) & 3u;
+    if (rowkind == 0) {   // near a common offset of 100: the Gram sum cancels against the norms
+        const f32 off = 100.0f + f32(int(h & 1023u) - 512) * 0x1p-10f;
+        return __uint_as_float(__float_as_uint(off) & 0xffffe000u);
+    }
+    const int e = int((h >> 10) % 17u) - 8;               // 2^-8 .. 2^8
+    const f32 mant = 1.0f + f32(h & 1023u) * 0x1p-10f;    // 11 significant bits: TF32-exact
+    const f32 v = ldexpf(mant, e);
+    return (h >> 31) ? -v : v;
+}
+
+__global__ void __launch_bounds__(128) k_tc_gram_check(u64 seed, unsigned long long* __restrict__ out,
+                                                      u32* __restrict__ err) {
+    extern __shared__ unsigned char gc_raw[];
+    GramCheckSmem& S = *reinterpret_cast<GramCheckSmem*>((reinterpret_cast<uintptr_t>(gc_raw) + 1023) & ~uintptr_t(1023));
+    const u32 tid = threadIdx.x, warp = tid >> 5, t = blockIdx.x;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem_base)),
+                     "r"(TC_N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // this thread's query row and candidate row, swizzled as the TMA writes them
+    f32 qa[TC_DIM], cb[TC_DIM];
+    f32 nb = 0.0f;
+#pragma unroll
+    for (int k = 0; k < TC_DIM; ++k) {
+        qa[k] = gc_value(seed, t, 0, tid, u32(k));
+        cb[k] = gc_value(seed, t, 1, tid, u32(k));
+        nb = __fmaf_rd(cb[k], cb[k], nb);
+    }
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+        *reinterpret_cast<float4*>(S.a + tid * 128 + ((ch ^ (tid & 7)) << 4)) =
+            make_float4(qa[4 * ch], qa[4 * ch + 1], qa[4 * ch + 2], qa[4 * ch + 3]);
+        *reinterpret_cast<float4*>(S.b + tid * 128 + ((ch ^ (tid & 7)) << 4)) =
+            make_float4(cb[4 * ch], cb[4 * ch + 1], cb[4 * ch + 2], cb[4 * ch + 3]);
+    }
+    {   // the augmentation rows, made as the regrouping makes them
+        const f32 w = -__fmul_rd(nb, 0.5f * (1.0f - 0x1p-16f));
+        const f32 hi = __uint_as_float(__float_as_uint(w) & 0xffffe000u);
+        const f32 lo = __uint_as_float(__float_as_uint(w - hi) & 0xffffe000u);
+        S.aaug[tid] = make_float4(1.0f, 1.0f, 0.0f, 0.0f);
+        S.baug[tid] = make_float4(hi, lo, 0.0f, 0.0f);
+        S.zeros[tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (tid == 0) {
+        mbar_init(&S.bar, 1);
+        fence_mbar_init();
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const u32 tmem = S.tmem_base;
+    if (tid == 0) {
+        mma_tile(tmem, smem_addr(S.a), smem_addr(S.b), smem_addr(S.aaug), smem_addr(S.baug), smem_addr(S.zeros));
+        mma_commit(&S.bar);
+    }
+    mbar_wait(&S.bar, 0, err);
+    tc_fence_after();
+    double na = 0.0;
+#pragma unroll
+    for (int k = 0; k < TC_DIM; ++k) na += double(qa[k]) * double(qa[k]);
+    double worst = 0.0;
+#pragma unroll 1
+    for (int chunk = 0; chunk < TC_N / 32; ++chunk) {
+        u32 v[32];
+        tmem_ld32(tmem + ((warp * 32u) << 16) + u32(chunk * 32), v);
+#pragma unroll 1
+        for (int h = 0; h < 32; ++h) {
+            const u32 c = u32(chunk * 32 + h);
+            f32 cr[TC_DIM];
+            swz_row(S.b, c, cr);
+            double dot = 0.0, ncr = 0.0;
+#pragma unroll
+            for (int k = 0; k < TC_DIM; ++k) {
+                dot += double(qa[k]) * double(cr[k]);
+                ncr += double(cr[k]) * double(cr[k]);
+            }
+            const float4 au = S.baug[c];
+            const double exact = dot + double(au.x) + double(au.y);
+            const double r = fabs(double(__uint_as_float(v[h])) - exact) / (na + ncr);
+            worst = r > worst ? r : worst;
+        }
+    }
+    atomicMax(out, (unsigned long long)__double_as_longlong(worst));
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N) : "memory");
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -1182,6 +1311,27 @@ EncodeTiledFn encode_fn() {
 }
 
 }  // namespace
+
+// The largest measured |D - exact| / (|a|^2 + |b|^2) over `products` seeded
+// 128 x 128 tensor-core products (see k_tc_gram_check).
+double tc_gram_check(tt_ctx* c, u32 products, u64 seed) {
+    unsigned long long* out = c->arena.get<unsigned long long>(S_MISC1, 2);
+    u32* err = reinterpret_cast<u32*>(out + 1);
+    TT_CUDA(cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), c->stream));
+    TT_CUDA(cudaFuncSetAttribute(k_tc_gram_check, cudaFuncAttributeMaxDynamicSharedMemorySize, int(GC_SMEM)));
+    if (products) {
+        k_tc_gram_check<<<products, 128, GC_SMEM, c->stream>>>(seed, out, err);
+        TT_LAUNCH("k_tc_gram_check");
+        ++c->launches;
+    }
+    unsigned long long h[2] = {0, 0};
+    TT_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaStreamSynchronize(c->stream));
+    if (u32(h[1])) throw Error(TT_ERR_TIMEOUT, "gb300: a bounded device wait timed out in the Gram check");
+    double r;
+    __builtin_memcpy(&r, &h[0], sizeof(r));
+    return r;
+}
 
 bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x) {
     return kind == M_L2 && dim == u32(TC_DIM) && k >= 1 && k <= u32(TC_K) && n >= 2 &&
