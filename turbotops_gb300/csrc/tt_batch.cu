@@ -80,10 +80,13 @@ __global__ void k_batch_radius(const u32* __restrict__ rowmax, const u32* __rest
 }
 
 // One warp per row of one cloud (rows listed globally).
+// Every pair (c, i, j), j < i, owns key slot pair_off[c] + i (i - 1) / 2 + j:
+// a kept pair writes its key there (coalesced, no shared counter), the rest
+// keep the all-ones fill and sort last.
 __global__ void k_batch_edges(const f32* __restrict__ mats, const u64* __restrict__ mat_off,
-                              const u32* __restrict__ sizes, const u64* __restrict__ pt_off,
-                              const u32* __restrict__ row_cloud, u64 rows, const u32* __restrict__ radius, int ib,
-                              u64* __restrict__ keys, unsigned long long* __restrict__ count,
+                              const u64* __restrict__ pair_off, const u32* __restrict__ sizes,
+                              const u64* __restrict__ pt_off, const u32* __restrict__ row_cloud, u64 rows,
+                              const u32* __restrict__ radius, int ib, u64* __restrict__ keys,
                               u64* __restrict__ per_cloud) {
     const int lane = threadIdx.x & 31;
     const u64 warps = (u64(gridDim.x) * blockDim.x) >> 5;
@@ -94,27 +97,23 @@ __global__ void k_batch_edges(const f32* __restrict__ mats, const u64* __restric
         const f32 thr = __uint_as_float(radius[c]);
         const f32* row = mats + mat_off[c] + u64(i) * n;
         const u64 rbase = u64(i) * (i - 1) / 2;
+        u64* slots = keys + pair_off[c] + rbase;
         u64 kept = 0;
         for (u32 j0 = 0; j0 < i; j0 += 32) {
             const u32 j = j0 + lane;
             const f32 d = j < i ? row[j] : INFINITY;
             const bool keep = j < i && d <= thr;
-            const u32 bal = __ballot_sync(0xffffffffu, keep);
-            if (!bal) continue;
-            kept += __popc(bal);
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(bal));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (keep)
-                keys[base + __popc(bal & ((1u << lane) - 1))] =
-                    (u64(c) << (31 + ib)) | (u64(__float_as_uint(d)) << ib) | (rbase + j);
+            kept += __popc(__ballot_sync(0xffffffffu, keep));
+            if (keep) slots[j] = (u64(c) << (31 + ib)) | (u64(__float_as_uint(d)) << ib) | (rbase + j);
         }
         if (lane == 0 && kept) atomicAdd((unsigned long long*)&per_cloud[c], (unsigned long long)kept);
     }
 }
 
-// Exclusive scan of the per-cloud edge counts (one CTA; clouds <= 65536).
-__global__ void k_batch_offsets(const u64* __restrict__ per_cloud, u32 clouds, u64* __restrict__ off) {
+// Exclusive scan of the per-cloud edge counts (one CTA; clouds <= 65536);
+// *count = all kept edges.
+__global__ void k_batch_offsets(const u64* __restrict__ per_cloud, u32 clouds, u64* __restrict__ off,
+                                unsigned long long* __restrict__ count) {
     __shared__ u64 part[1024];
     const u32 t = threadIdx.x;
     const u32 per = (clouds + blockDim.x - 1) / blockDim.x;
@@ -136,7 +135,10 @@ __global__ void k_batch_offsets(const u64* __restrict__ per_cloud, u32 clouds, u
         off[c] = run;
         run += per_cloud[c];
     }
-    if (t == blockDim.x - 1) off[clouds] = run;
+    if (t == blockDim.x - 1) {
+        off[clouds] = run;
+        *count = run;
+    }
 }
 
 __global__ void k_batch_emit(const u64* __restrict__ keys, const unsigned long long* __restrict__ count, int ib,
@@ -171,6 +173,7 @@ struct Batch {
     u32* radius = nullptr;
     u64* pt_off = nullptr;
     u64* mat_off = nullptr;
+    u64* pair_off = nullptr;   // first key slot of every cloud's pairs
     u32* sizes = nullptr;
     Tile* tiles = nullptr;
     u32* row_cloud = nullptr;
@@ -219,10 +222,10 @@ struct Batch {
         k_batch_radius<<<g2, 256, 0, s>>>(rowmax, row_cloud, total_pts, radius);
         TT_LAUNCH("k_batch_radius");
         const u32 g3 = u32(std::min<u64>((total_pts * 32 + 255) / 256, u64(owner->sms) * 32));
-        k_batch_edges<<<g3, 256, 0, s>>>(mats, mat_off, sizes, pt_off, row_cloud, total_pts, radius, ib, keys, count,
-                                         per_cloud);
+        k_batch_edges<<<g3, 256, 0, s>>>(mats, mat_off, pair_off, sizes, pt_off, row_cloud, total_pts, radius, ib,
+                                         keys, per_cloud);
         TT_LAUNCH("k_batch_edges");
-        k_batch_offsets<<<1, 1024, 0, s>>>(per_cloud, clouds, edge_off);
+        k_batch_offsets<<<1, 1024, 0, s>>>(per_cloud, clouds, edge_off, count);
         TT_LAUNCH("k_batch_offsets");
         radix_sort_inplace<u32>(&sctx, keys, nullptr, total_pairs, 31 + ib + bits_for(clouds));
         const u32 g4 = u32(std::min<u64>((total_pairs + 255) / 256, u64(owner->sms) * 32));
@@ -264,7 +267,7 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         b->sctx.device = c->device;
         b->sctx.sms = c->sms;
         TT_CUDA(cudaStreamCreateWithFlags(&b->sctx.stream, cudaStreamNonBlocking));
-        std::vector<u64> pt_off(clouds + 1, 0), mat_off(clouds + 1, 0);
+        std::vector<u64> pt_off(clouds + 1, 0), mat_off(clouds + 1, 0), pair_off(clouds + 1, 0);
         std::vector<Tile> tiles;
         std::vector<u32> row_cloud;
         u64 pairs = 0;
@@ -275,6 +278,7 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
             pt_off[q + 1] = pt_off[q] + n;
             mat_off[q + 1] = mat_off[q] + u64(n) * n;
             pairs += u64(n) * (n - 1) / 2;
+            pair_off[q + 1] = pairs;
             for (u32 i0 = 0; i0 < n; i0 += BT_R)
                 for (u32 j0 = 0; j0 < n; j0 += BT_C) tiles.push_back(Tile{q, i0, j0});
             for (u32 i = 0; i < n; ++i) row_cloud.push_back(q);
@@ -292,6 +296,7 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         b->radius = b->alloc<u32>(clouds);
         b->pt_off = b->alloc<u64>(clouds + 1);
         b->mat_off = b->alloc<u64>(clouds + 1);
+        b->pair_off = b->alloc<u64>(clouds + 1);
         b->sizes = b->alloc<u32>(clouds);
         b->tiles = b->alloc<Tile>(tiles.size());
         b->row_cloud = b->alloc<u32>(row_cloud.size());
@@ -305,6 +310,7 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         cudaStream_t s = b->sctx.stream;
         TT_CUDA(cudaMemcpyAsync(b->pt_off, pt_off.data(), 8 * (clouds + 1), cudaMemcpyHostToDevice, s));
         TT_CUDA(cudaMemcpyAsync(b->mat_off, mat_off.data(), 8 * (clouds + 1), cudaMemcpyHostToDevice, s));
+        TT_CUDA(cudaMemcpyAsync(b->pair_off, pair_off.data(), 8 * (clouds + 1), cudaMemcpyHostToDevice, s));
         TT_CUDA(cudaMemcpyAsync(b->sizes, sizes_h, 4 * clouds, cudaMemcpyHostToDevice, s));
         TT_CUDA(cudaMemcpyAsync(b->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, s));
         TT_CUDA(cudaMemcpyAsync(b->row_cloud, row_cloud.data(), 4 * row_cloud.size(), cudaMemcpyHostToDevice, s));
