@@ -73,10 +73,25 @@ k_batch_dense(const f32* __restrict__ x, const u64* __restrict__ pt_off, const u
     }
 }
 
+// (A cloud's rows are contiguous: a warp whose 32 rows share one cloud takes
+// their minimum first and issues one atomic.)
 __global__ void k_batch_radius(const u32* __restrict__ rowmax, const u32* __restrict__ row_cloud, u64 rows,
                                u32* __restrict__ radius) {
-    for (u64 r = u64(blockIdx.x) * blockDim.x + threadIdx.x; r < rows; r += u64(gridDim.x) * blockDim.x)
-        atomicMin(&radius[row_cloud[r]], rowmax[r]);
+    const u32 lane = threadIdx.x & 31;
+    const u64 stride = u64(gridDim.x) * blockDim.x;
+    for (u64 base = u64(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < rows; base += stride) {
+        const u64 r = base + lane;   // whole warps iterate together
+        const bool ok = r < rows;
+        const u32 c = ok ? row_cloud[r] : 0xffffffffu;
+        u32 v = ok ? rowmax[r] : 0xffffffffu;
+        const u32 c0 = __shfl_sync(0xffffffffu, c, 0);
+        if (__all_sync(0xffffffffu, !ok || c == c0)) {
+            v = __reduce_min_sync(0xffffffffu, v);
+            if (lane == 0) atomicMin(&radius[c0], v);
+        } else if (ok) {
+            atomicMin(&radius[c], v);
+        }
+    }
 }
 
 // One warp per row of one cloud (rows listed globally).
