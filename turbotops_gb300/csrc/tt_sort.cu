@@ -5,13 +5,15 @@
 // orders on (diameter, index) and are reproduced exactly by sorting a packed
 // 64-bit key, so ties never depend on sort stability or thread count.
 //
-// Radix sort: 8-bit digits, 4096-key tiles (256 threads x 16 keys). Per pass:
+// Radix sort: digits of up to 11 bits, 4096-key tiles (256 threads x 16
+// keys). Per pass:
 //   k_rs_upsweep   per-tile digit histogram -> hist[digit * tiles + tile]
 //   scan           exclusive scan of hist (digit-major gives global offsets)
 //   k_rs_scatter   stable in-tile ranking (warp match + per-warp counters,
 //                  warp-major order), scatter to offsets
 // Only the bits in which min key and max key differ are sorted (keys share
-// every bit above the highest differing one), which is usually 4-6 passes.
+// every bit above the highest differing one), spread evenly over the fewest
+// passes (25 bits: 9 + 8 + 8).
 #include "tt_internal.cuh"
 
 namespace tt {
