@@ -436,7 +436,7 @@ inline u32 grid_for(u64 work, u32 per_block) {
 // The edges are written in index order (count, scan, fill), so one stable
 // sort on the distance bits alone gives the filtration order: only the bits
 // in which the kept distances differ (their range comes back with the count),
-// three passes for the bench's 25 bits, instead of a full 64-bit key sort.
+// three passes when 25 bits differ, instead of a full 64-bit key sort.
 // Slots: S_EDGE_CNT, S_EDGE_SORT, S_EDGE_IDX, S_EDGE_KEYS (result),
 // S_EDGE_INV (result: index order -> sorted position),
 // and the sort's own (S_SORT_A, S_SORT_HIST, S_SCAN*, S_MISC3).
