@@ -255,8 +255,10 @@ struct CsrCx {
 // Edges are visited in index order (inv: index order -> sorted position), so
 // neighbouring threads share the larger vertex's row; results go to the
 // edge's sorted position.
-__global__ void k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, const u32* __restrict__ inv, u64 m,
-                               u8* __restrict__ app, u32* __restrict__ emw, u8* __restrict__ emf) {
+// (32 registers: 64 warps an SM to hide the walk's load latency.)
+__global__ void __launch_bounds__(256, 8)
+    k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, const u32* __restrict__ inv, u64 m, u8* __restrict__ app,
+                   u32* __restrict__ emw, u8* __restrict__ emf) {
     for (u64 t = u64(blockIdx.x) * blockDim.x + threadIdx.x; t < m; t += u64(gridDim.x) * blockDim.x) {
         const u64 e = inv[t];
         const u64 key = keys[e];
