@@ -42,12 +42,15 @@
 // Pipeline per CTA (128 threads = 4 warps, one query row per thread, 128
 // queries per block, persistent over query blocks):
 //   TMA (cp.async.bulk.tensor, 128-byte swizzle) loads the query tile once
-//   and the chosen candidate tiles into two shared-memory stages (bulk
-//   copies bring their low bits, norm terms and ids alongside); thread 0
-//   issues tcgen05.mma.kind::tf32 (M = 128, N = 128, 5 x K = 8) into one of
-//   two TMEM accumulators and commits to an mbarrier; while the tensor core
-//   works on the next tile the four warps read this tile's Gram rows
-//   (tcgen05.ld 32x32b.x32), run the filter and the exact path.
+//   and the chosen candidate tiles into two shared-memory stages, each with
+//   one bulk copy of the tile's pack (low bits, augmentation rows, ids,
+//   record tail); warp 1 issues a stage's copies as soon as the stage is
+//   free. Thread 0 issues tcgen05.mma.kind::tf32 (M = 128, N = 128,
+//   5 x K = 8) for the next tile into the free one of two TMEM accumulators
+//   once its own epilogue is done and commits to an mbarrier; the tensor core
+//   runs it while the other warps finish the current tile, reading its Gram
+//   rows (tcgen05.ld 32x32b.x32, two loads in flight), filtering and running
+//   the exact path. One barrier a tile.
 // TMEM: 2 x 128 columns per CTA; shared memory is padded so that at most two
 // CTAs share an SM, so tcgen05.alloc never waits. Every mbarrier wait is
 // bounded (tt_tma.cuh); on a timeout the kernel records the error, waits
