@@ -1,0 +1,47 @@
+// host_reduce_shim.cpp — test harness only: the product's host reduction
+// (turbotops_gb300/csrc/tt_reduce.cpp, compute_pairs) behind one C entry
+// point, compiled with the host compiler so the CPU tests can check it
+// against the reference's diagrams without a GPU. The columns it reduces come
+// from the oracle's dim0 / emergent / assemble restatements.
+#include <stdint.h>
+
+#include <exception>
+#include <vector>
+
+#include "../turbotops_gb300/csrc/tt_reduce.h"
+
+// Reduces `ncols` dimension-`dim` columns (descending filtration order) over a
+// dense full matrix (rp == NULL) or a CSR graph. em_idx / em_app may be NULL
+// (the emergent test then runs on the host). Bars go to birth/death (at most
+// ncols each), pivots (ascending) to piv (at most ncols). Returns 0, or -1 on
+// an exception.
+extern "C" int hr_compute_pairs(const float* mat, const uint64_t* rp, const uint32_t* ci, const float* w, uint32_t n,
+                                float thr, uint32_t dim, uint32_t maxdim, const uint64_t* cidx, const float* cd,
+                                uint64_t ncols, const uint64_t* em_idx, const uint8_t* em_app, float* birth,
+                                float* death, uint64_t* nbars, uint64_t* piv, uint64_t* npiv, uint64_t* emergent) {
+    try {
+        tt::host::HostComplex hc;
+        hc.mat = mat;
+        hc.rp = rp;
+        hc.ci = ci;
+        hc.w = w;
+        hc.n = n;
+        hc.thr = thr;
+        std::vector<tt::host::Entry> cols(ncols);
+        for (uint64_t i = 0; i < ncols; ++i) cols[i] = tt::host::Entry{cidx[i], cd[i]};
+        std::vector<uint64_t> pv;
+        tt::host::ReduceStats st;
+        const tt::host::Bars b = tt::host::compute_pairs(hc, dim, maxdim, cols, em_idx, em_app, pv, st);
+        for (size_t i = 0; i < b.birth.size(); ++i) {
+            birth[i] = b.birth[i];
+            death[i] = b.death[i];
+        }
+        *nbars = b.birth.size();
+        for (size_t i = 0; i < pv.size(); ++i) piv[i] = pv[i];
+        *npiv = pv.size();
+        *emergent = st.emergent;
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}

@@ -1,0 +1,119 @@
+"""The host reduction (turbotops_gb300/csrc/tt_reduce.cpp, the reference's
+Reducer::compute_pairs, rips.hpp:874-978) on the CPU, against the reference's
+own outputs: whole diagrams (dim0 H0 + reduced H1/H2), and the dimension-1
+pivot sets the reference dumped. The columns come from the oracle's dim0,
+emergent and assemble restatements (themselves pinned to the reference by
+test_oracle_golden.py); the reduction is the product's source, compiled here
+with the host compiler through tests/host_reduce_shim.cpp."""
+import ctypes as C
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from golden_io import GOLDEN, canonical, cases, ids, thr_of
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BARS = cases("bars")
+ASM = cases("asm")
+
+
+@pytest.fixture(scope="module")
+def shim(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("hr") / "libhostreduce.so")
+    src = [os.path.join(ROOT, "tests", "host_reduce_shim.cpp"),
+           os.path.join(ROOT, "turbotops_gb300", "csrc", "tt_reduce.cpp")]
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", so] + src, check=True)
+    L = C.CDLL(so)
+    P = C.c_void_p
+    L.hr_compute_pairs.restype = C.c_int
+    L.hr_compute_pairs.argtypes = [P, P, P, P, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, P, P, C.c_uint64,
+                                   P, P, P, P, P, P, P, P]
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def reduce(L, mat, thr, dim, maxdim, cidx, cd, emi=None, emf=None):
+    cidx = np.ascontiguousarray(cidx, np.uint64)
+    cd = np.ascontiguousarray(cd, np.float32)
+    k = cidx.size
+    birth = np.empty(k + 1, np.float32)
+    death = np.empty(k + 1, np.float32)
+    piv = np.empty(k + 1, np.uint64)
+    nb, npv, em = (np.zeros(1, np.uint64) for _ in range(3))
+    mat = np.ascontiguousarray(mat, np.float32)
+    rc = L.hr_compute_pairs(_p(mat), None, None, None, mat.shape[0], float(thr), dim, maxdim, _p(cidx), _p(cd), k,
+                            _p(emi), _p(emf), _p(birth), _p(death), _p(nb), _p(piv), _p(npv), _p(em))
+    assert rc == 0
+    b = int(nb[0])
+    return birth[:b], death[:b], piv[: int(npv[0])], int(em[0])
+
+
+def diagram(L, x, metric, maxdim, host_emergent=False):
+    """tops::persistence on a dense cloud: threshold = enclosing radius,
+    dim0 H0, compute_pairs(1), assemble(1) + compute_pairs(2)."""
+    mat = O.dense(x, metric)
+    thr = O.enclosing_radius(mat)
+    r = O.dim0(mat=mat, thr=thr, maxdim=maxdim)
+    h0 = r["h0"].reshape(-1, 2)
+    rows = [np.column_stack([np.zeros(len(h0), np.float32), h0])]
+    if maxdim >= 1:
+        if host_emergent:
+            emi = emf = None
+        else:
+            e = O.emergent(mat=mat, cidx=r["cidx"], cd=r["cd"])
+            emi, emf = e["emi"], e["emf"]
+        b, d, piv, _ = reduce(L, mat, thr, 1, maxdim, r["cidx"], r["cd"], emi, emf)
+        rows.append(np.column_stack([np.ones(len(b), np.float32), b, d]))
+        if maxdim >= 2:
+            a = O.assemble(mat, thr, r["eidx"], r["ed"], piv)
+            b2, d2, _, _ = reduce(L, mat, thr, 2, maxdim, a["c2idx"], a["c2d"])
+            rows.append(np.column_stack([np.full(len(b2), 2, np.float32), b2, d2]))
+    return canonical(np.concatenate(rows).astype(np.float32))
+
+
+@pytest.mark.parametrize("c", BARS, ids=ids(BARS))
+def test_diagram_vs_reference(shim, c):
+    got = diagram(shim, c["x"], c["metric"], c["params"]["maxdim"])
+    ref = canonical(c["bars"])
+    assert got.shape == ref.shape
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("c", [b for b in BARS if b["params"]["maxdim"] >= 1], ids=ids([b for b in BARS if b["params"]["maxdim"] >= 1]))
+def test_host_emergent_test_equals_precomputed(shim, c):
+    """The emergent-pair test evaluated by the reducer itself (the path of
+    dimension >= 2) gives the dimension-1 diagram the precomputed one gives."""
+    a = diagram(shim, c["x"], c["metric"], 1)
+    b = diagram(shim, c["x"], c["metric"], 1, host_emergent=True)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("c", ASM, ids=ids(ASM))
+def test_dim1_pivots_vs_reference(shim, c):
+    """The set of dimension-1 pivots (death triangles, the input of assemble)
+    equals the reference's, with its threshold and columns."""
+    thr = np.float32(c["thr"][0])
+    b, d, piv, _ = reduce(shim, O.dense(c["x"], c["metric"]), thr, 1, 2, c["cidx"], c["cd"], c["emi"], c["emf"])
+    assert np.array_equal(np.sort(piv), np.sort(c["piv"]))
+
+
+def test_torus_config_pivots_vs_reference(shim):
+    """Configuration 1 (torus, 1000 points, L2, enclosing radius): the
+    reference's 393,249 edges reduce to its dimension-1 pivot set."""
+    from turbotops_gb300 import synth
+    cfg = json.load(open(os.path.join(GOLDEN, "configs.json")))["torus1000_l2"]
+    ref = np.load(os.path.join(GOLDEN, "cfg_torus1000_piv.npz"))["piv"]
+    mat = O.dense(synth.torus(), "l2")
+    thr = O.enclosing_radius(mat)
+    assert float(thr) == cfg["thr"]
+    r = O.dim0(mat=mat, thr=thr, maxdim=2)
+    e = O.emergent(mat=mat, cidx=r["cidx"], cd=r["cd"])
+    _, _, piv, _ = reduce(shim, mat, thr, 1, 2, r["cidx"], r["cd"], e["emi"], e["emf"])
+    assert np.array_equal(np.sort(piv), np.sort(ref))

@@ -4,7 +4,7 @@
 //
 // The algorithm is Ripser's (U. Bauer, J. Appl. Comput. Topol. 2021) as the
 // reference runs it: columns in descending filtration order (d desc, index
-// asc); each column's coboundary in a binary heap ordered by (d asc, index
+// asc); each column's coboundary in a priority queue ordered by (d asc, index
 // desc) with mod-2 cancellation at the top; a pivot already owned by an
 // earlier column adds that column's stored reduction; a pivot with a
 // zero-apparent facet adds that facet's coboundary; otherwise the pivot pairs
@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <limits>
 #include <stdexcept>
 #include <string>
@@ -47,11 +48,13 @@ struct Binom {
     }
     uint64_t& at(uint32_t v, uint32_t k) { return t[uint64_t(k) * (n + 1) + v]; }
     uint64_t operator()(uint32_t v, uint32_t k) const { return k > K ? 0 : t[uint64_t(k) * (n + 1) + v]; }
+    const uint64_t* row(uint32_t k) const { return t.data() + uint64_t(k) * (n + 1); }   // k <= K
 };
 
 struct Cx {
     const HostComplex& c;
     const Binom& B;
+    mutable std::vector<float> cdw;   // dense: diameter of the cofacet through each vertex
 
     float dist(uint32_t i, uint32_t j) const {
         if (i == j) return 0.0f;
@@ -136,6 +139,45 @@ struct Cx {
             for (uint32_t i = 0; i < nv; ++i) cd = std::max(cd, c.w[p[i] - 1]);
             if (cd <= cap && !fn(Entry{A[t] + B(x, nv + 1 - t) + S[t], cd}, x, t)) return;
             if (--p[0] == lo[0]) return;
+        }
+    }
+
+    // Every cofacet with diameter <= cap, in the order of cofacets(): fn(Entry).
+    // Dense: the diameters through all vertices are taken row by row first,
+    // then emitted per range of vertices between the simplex's own, where the
+    // index is one binomial row plus a constant.
+    template <typename F>
+    void all_cofacets(const uint32_t* vd, uint32_t nv, float diam, float cap, F&& fn) const {
+        if (!c.mat) {
+            cofacets(vd, nv, diam, cap, [&](const Entry& e, uint32_t, uint32_t) {
+                fn(e);
+                return true;
+            });
+            return;
+        }
+        const uint32_t n = c.n;
+        cdw.resize(n);
+        float* cd = cdw.data();
+        const float* r0 = c.mat + uint64_t(vd[0]) * n;
+        for (uint32_t w = 0; w < n; ++w) cd[w] = std::max(diam, r0[w]);
+        for (uint32_t i = 1; i < nv; ++i) {
+            const float* r = c.mat + uint64_t(vd[i]) * n;
+            for (uint32_t w = 0; w < n; ++w) cd[w] = std::max(cd[w], r[w]);
+        }
+        uint64_t A = 0, S[34];
+        S[nv] = 0;
+        for (uint32_t i = nv; i-- > 0;) S[i] = S[i + 1] + B(vd[i], nv - i);
+        uint32_t hi = n;   // w in [lo, hi): the vertices above vd[t] and below vd[t - 1]
+        for (uint32_t t = 0; t <= nv; ++t) {
+            const uint32_t lo = t < nv ? vd[t] + 1 : 0;
+            const uint64_t base = A + S[t];
+            const uint64_t* Bk = B.row(nv + 1 - t);
+            for (uint32_t w = hi; w-- > lo;)
+                if (cd[w] <= cap) fn(Entry{base + Bk[w], cd[w]});
+            if (t < nv) {
+                A += B(vd[t], nv + 1 - t);
+                hi = vd[t];
+            }
         }
     }
 
@@ -230,29 +272,91 @@ struct PivotMap {
     }
 };
 
-// Min-heap in filtration order with pairwise cancellation of equal indices.
-struct Heap {
-    std::vector<Entry> h;
+// The working coboundary: a priority queue in filtration order (smallest
+// diameter first, larger index first among equal diameters) with pairwise
+// cancellation of equal indices at the top. Entries go into buckets by the
+// order-preserving bits of their diameter between the column's birth (no
+// entry is earlier) and the largest diameter of the complex; only the lowest
+// non-empty bucket is kept as a binary heap, and a bitmap finds the next one.
+// A push is an append and a pop works in a small heap, where one heap over the
+// whole column (the long reductions of noisy circles hold a million entries,
+// and two in five of them surface to cancel) paid a walk through memory for
+// both. Buckets are monotone in the diameter and equal keys share a bucket, so
+// the entries surface in exactly the order of a single heap.
+struct BucketQueue {
+    static constexpr uint32_t kBits = 14, kBuckets = 1u << kBits;
+    std::vector<std::vector<Entry>> bk = std::vector<std::vector<Entry>>(kBuckets);
+    std::vector<uint64_t> live = std::vector<uint64_t>(kBuckets / 64, 0);   // non-empty buckets
+    uint32_t cur = kBuckets;   // buckets below cur are empty; bk[cur] is a heap
+    uint32_t lo = 0, shift = 0;
+    uint64_t count = 0;
+
     static bool later(const Entry& a, const Entry& b) { return precedes(b, a); }
-    void clear() { h.clear(); }
-    void push(const Entry& e) {
-        h.push_back(e);
-        std::push_heap(h.begin(), h.end(), later);
+    static uint32_t ord(float d) {
+        uint32_t u;
+        std::memcpy(&u, &d, 4);
+        return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
     }
-    void heapify(std::vector<Entry>& v) {
-        std::make_heap(v.begin(), v.end(), later);
-        h.swap(v);
+    // Empties the queue; entries of the next column are expected in [a, b]
+    // (outside it they only share the end buckets).
+    void reset(float a, float b) {
+        for (uint32_t w = 0; w < kBuckets / 64; ++w) {
+            for (uint64_t m = live[w]; m; m &= m - 1) bk[(w << 6) + uint32_t(__builtin_ctzll(m))].clear();
+            live[w] = 0;
+        }
+        lo = ord(a);
+        const uint32_t span = ord(b) > lo ? ord(b) - lo : 0;
+        shift = 0;
+        while ((span >> shift) >= kBuckets) ++shift;
+        cur = kBuckets;
+        count = 0;
+    }
+    uint32_t bucket(float d) const {
+        const uint32_t u = ord(d);
+        if (u <= lo) return 0;
+        const uint32_t x = (u - lo) >> shift;
+        return x < kBuckets ? x : kBuckets - 1;
+    }
+    void push(const Entry& e) {
+        const uint32_t x = bucket(e.d);
+        std::vector<Entry>& v = bk[x];
+        live[x >> 6] |= 1ull << (x & 63);
+        v.push_back(e);
+        ++count;
+        if (x == cur) std::push_heap(v.begin(), v.end(), later);
+        else if (x < cur) cur = x;   // the bucket was empty: one entry is a heap
+    }
+    bool empty() const { return count == 0; }
+    // the lowest non-empty bucket as the current heap (count > 0, so a push
+    // has set cur below kBuckets)
+    void settle() {
+        if (!bk[cur].empty()) return;
+        uint32_t w = cur >> 6;
+        uint64_t m = live[w] & (~0ull << (cur & 63));
+        while (!m) m = live[++w];
+        cur = (w << 6) + uint32_t(__builtin_ctzll(m));
+        std::make_heap(bk[cur].begin(), bk[cur].end(), later);
+    }
+    const Entry& front() {
+        settle();
+        return bk[cur].front();
+    }
+    void pop() {
+        std::vector<Entry>& v = bk[cur];
+        std::pop_heap(v.begin(), v.end(), later);
+        v.pop_back();
+        --count;
+        if (v.empty()) live[cur >> 6] &= ~(1ull << (cur & 63));
     }
     Entry pop_pivot() {
         Entry piv{kNone, 0};
-        while (!h.empty()) {
+        while (!empty()) {
+            const Entry f = front();
             if (piv.idx == kNone) {
-                piv = h.front();
-                std::pop_heap(h.begin(), h.end(), later);
-                h.pop_back();
-            } else if (h.front().idx == piv.idx) {
-                std::pop_heap(h.begin(), h.end(), later);
-                h.pop_back();
+                piv = f;
+                pop();
+            } else if (f.idx == piv.idx) {
+                pop();
                 piv.idx = kNone;
             } else {
                 break;
@@ -273,25 +377,32 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
                    const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
                    ReduceStats& st) {
     const Binom B(hc.n, maxdim + 2);
-    const Cx cx{hc, B};
+    const Cx cx{hc, B, {}};
     const uint32_t nv = dim + 1;
     Bars bars;
     PivotMap pivots(cols.size() + 16);
     std::vector<uint64_t> off{0};
-    std::vector<Entry> red, wr, buf;
-    Heap wc;
+    std::vector<Entry> red, wr;
+    BucketQueue wc;
+    // the largest diameter an entry can have: the threshold, else the largest
+    // distance of the complex
+    float dmax = hc.thr;
+    if (!(dmax < INFINITY)) {
+        dmax = 0;
+        const float* v = hc.mat ? hc.mat : hc.w;
+        const uint64_t m = hc.mat ? uint64_t(hc.n) * hc.n : (hc.n ? hc.rp[hc.n] : 0);
+        for (uint64_t i = 0; i < m; ++i)
+            if (v[i] < INFINITY) dmax = std::max(dmax, v[i]);
+    }
     uint32_t vd[34];
     auto push_coboundary = [&](const Entry& s) {
         cx.decode(s.idx, nv, vd);
-        cx.cofacets(vd, nv, s.d, hc.thr, [&](const Entry& e, uint32_t, uint32_t) {
-            wc.push(e);
-            return true;
-        });
+        cx.all_cofacets(vd, nv, s.d, hc.thr, [&](const Entry& e) { wc.push(e); });
     };
     for (uint64_t c = 0; c < cols.size(); ++c) {
         const Entry col = cols[c];
         const float birth = col.d;
-        wc.clear();
+        wc.reset(col.d, dmax);
         wr.clear();
         Entry pivot{kNone, 0};
         bool emergent = false;
@@ -301,17 +412,9 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
                 pivot = Entry{em_idx[c], col.d};
                 emergent = true;
             }
-            if (!emergent) {
-                buf.clear();
-                cx.decode(col.idx, nv, vd);
-                cx.cofacets(vd, nv, col.d, hc.thr, [&](const Entry& e, uint32_t, uint32_t) {
-                    buf.push_back(e);
-                    return true;
-                });
-            }
+            if (!emergent) push_coboundary(col);
         } else {
             bool check = true;
-            buf.clear();
             cx.decode(col.idx, nv, vd);
             cx.cofacets(vd, nv, col.d, hc.thr, [&](const Entry& cf, uint32_t, uint32_t) {
                 if (check && cf.d == col.d) {
@@ -322,14 +425,13 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
                     }
                     check = false;
                 }
-                buf.push_back(cf);
+                wc.push(cf);
                 return true;
             });
         }
         if (emergent) {
             ++st.emergent;
         } else {
-            wc.heapify(buf);
             pivot = wc.get_pivot();
         }
         bool fresh = emergent;
