@@ -109,3 +109,20 @@ def test_forward_bars_equal_persistence():
         ref = dg[1]
         key = lambda a: a[np.lexsort((a[:, 1], a[:, 0]))]  # noqa: E731
         assert np.array_equal(key(got), key(ref))
+
+
+def test_forward_independent_of_reduction_threads():
+    """The host reductions run on threads that take clouds as their device
+    front end finishes; bars, critical edges and offsets must not depend on
+    that schedule (all host threads vs one), an empty cloud included."""
+    clouds = _clouds(count=16, n=200, seed=17)
+    clouds.insert(5, np.zeros((0, 3), np.float32))
+    sizes = [c.shape[0] for c in clouds]
+    x = torch.from_numpy(np.concatenate(clouds)).cuda()
+    a = topo.diagrams(x, sizes, threads=0)
+    b = topo.diagrams(x, sizes, threads=1)
+    for f in ["h0_offset", "h0_death", "h0_edge", "h1_offset", "h1_birth", "h1_death", "h1_birth_edge",
+              "h1_death_edge"]:
+        u, v = getattr(a, f), getattr(b, f)
+        assert torch.equal(torch.as_tensor(u), torch.as_tensor(v)), f
+    assert int(a.h1_offset[6]) == int(a.h1_offset[5])   # the empty cloud has no bars

@@ -3,8 +3,9 @@
 //
 // No counterpart in the reference (its Barcode keeps values only,
 // rips.hpp:52-67). Forward: for every cloud the GPU runs the dense front end
-// (distances, enclosing radius, dim0); the host runs compute_pairs(1) for all
-// clouds in parallel on a thread pool, recording each bar's critical
+// (distances, enclosing radius, dim0); host threads run compute_pairs(1) for
+// the clouds whose front end is done while the GPU works on the next ones,
+// recording each bar's critical
 // simplices; each bar value is then the length of one edge:
 //   H0 death   the spanning-tree edge that merged two components
 //   H1 birth   the column's edge
@@ -19,7 +20,9 @@
 // one thread per edge, float atomics into the gradient.
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdlib>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -99,6 +102,41 @@ struct Cloud {
     host::Bars bars;
 };
 
+// Hands clouds from the thread that runs their device front end to the
+// threads that reduce them: a cloud is published once its outputs are on the
+// host, and reducers take published clouds in order, so the reductions of the
+// first clouds overlap the front end of the later ones and a thread that
+// finishes early takes the next cloud. Each cloud's reduction is independent
+// of the others, so the bars do not depend on the schedule.
+struct CloudQueue {
+    std::mutex m;
+    std::condition_variable cv;
+    u32 count, ready = 0, next = 0;
+    bool stop = false;
+    explicit CloudQueue(u32 c) : count(c) {}
+    // the next cloud to reduce; count when none is left (or after stop)
+    u32 take() {
+        std::unique_lock<std::mutex> lk(m);
+        cv.wait(lk, [&] { return stop || next < ready || next >= count; });
+        if (stop || next >= count) return count;
+        return next++;
+    }
+    void publish(u32 q) {
+        {
+            std::lock_guard<std::mutex> lk(m);
+            ready = q + 1;
+        }
+        cv.notify_all();
+    }
+    void halt() {
+        {
+            std::lock_guard<std::mutex> lk(m);
+            stop = true;
+        }
+        cv.notify_all();
+    }
+};
+
 }  // namespace
 
 struct TopoResult {
@@ -121,53 +159,14 @@ extern "C" int tt_topo_forward(tt_ctx* c, const float* x, const uint32_t* sizes,
         if (kind < TT_METRIC_L1 || kind > TT_METRIC_LP) invalid("metric: unknown kind");
         if (kind == TT_METRIC_LP && !(p >= 1.0f)) invalid("metric: p must be in [1, inf]");
         std::vector<Cloud> cl(count);
-        u64 off = 0;
-        // device front end, cloud by cloud
-        for (u32 q = 0; q < count; ++q) {
-            Cloud& C = cl[q];
-            C.n = sizes[q];
-            C.off = off;
-            off += C.n;
-            if (C.n == 0) continue;
-            const u32 n = C.n;
-            f32* mat = c->arena.get<f32>(S_MAT, u64(n) * n + 1);
-            u32* rowmax = c->arena.get<u32>(S_ROWMAX, u64(n) + 1);
-            dense_matrix(c, x + C.off * dim, n, dim, kind, p, mat, rowmax);
-            min_bits(c, rowmax, n, rowmax + n);
-            u32 b = 0;
-            TT_CUDA(cudaMemcpyAsync(&b, rowmax + n, 4, cudaMemcpyDeviceToHost, c->stream));
-            TT_CUDA(cudaStreamSynchronize(c->stream));
-            C.thr = bitsf(b);
-            Complex cx{mat, nullptr, nullptr, nullptr, n, C.thr};
-            Dim0Out r;
-            dim0(c, cx, 1, r);
-            C.mat.resize(u64(n) * n);
-            C.h0d.resize(r.nh0);
-            C.h0e.resize(r.nh0);
-            C.ci.resize(r.ncols);
-            C.cd.resize(r.ncols);
-            C.emi.resize(r.ncols);
-            C.emf.resize(r.ncols);
-            TT_CUDA(cudaMemcpyAsync(C.mat.data(), mat, 4 * u64(n) * n, cudaMemcpyDeviceToHost, c->stream));
-            if (r.nh0) {
-                TT_CUDA(cudaMemcpyAsync(C.h0d.data(), r.h0, 4 * r.nh0, cudaMemcpyDeviceToHost, c->stream));
-                TT_CUDA(cudaMemcpyAsync(C.h0e.data(), r.h0_edge, 8 * r.nh0, cudaMemcpyDeviceToHost, c->stream));
-            }
-            if (r.ncols) {
-                TT_CUDA(cudaMemcpyAsync(C.ci.data(), r.cidx, 8 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
-                TT_CUDA(cudaMemcpyAsync(C.cd.data(), r.cd, 4 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
-                TT_CUDA(cudaMemcpyAsync(C.emi.data(), r.emi, 8 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
-                TT_CUDA(cudaMemcpyAsync(C.emf.data(), r.emf, r.ncols, cudaMemcpyDeviceToHost, c->stream));
-            }
-            TT_CUDA(cudaStreamSynchronize(c->stream));
-        }
-        // host reductions, clouds in parallel
+        // host reducers (the calling thread joins them after the front end)
         u32 nt = threads > 0 ? u32(threads) : std::max(1u, std::thread::hardware_concurrency());
         nt = std::min<u32>(nt, std::max<u32>(count, 1));
+        CloudQueue queue(count);
         std::vector<std::string> errs(nt);
         auto work = [&](u32 t) {
             try {
-                for (u32 q = t; q < count; q += nt) {
+                for (u32 q; (q = queue.take()) < count;) {
                     Cloud& C = cl[q];
                     if (C.n == 0) continue;
                     std::vector<host::Entry> cols(C.ci.size());
@@ -179,12 +178,71 @@ extern "C" int tt_topo_forward(tt_ctx* c, const float* x, const uint32_t* sizes,
                 }
             } catch (const std::exception& e) {
                 errs[t] = e.what();
+                queue.halt();
             }
         };
         std::vector<std::thread> pool;
-        for (u32 t = 1; t < nt; ++t) pool.emplace_back(work, t);
+        auto join = [&] {
+            for (auto& th : pool) th.join();
+            pool.clear();
+        };
+        // device front end, cloud by cloud; each cloud goes to the reducers
+        // once its outputs are on the host
+        auto front_end = [&] {
+            u64 off = 0;
+            for (u32 q = 0; q < count; ++q) {
+                Cloud& C = cl[q];
+                C.n = sizes[q];
+                C.off = off;
+                off += C.n;
+                if (C.n == 0) {
+                    queue.publish(q);
+                    continue;
+                }
+                const u32 n = C.n;
+                f32* mat = c->arena.get<f32>(S_MAT, u64(n) * n + 1);
+                u32* rowmax = c->arena.get<u32>(S_ROWMAX, u64(n) + 1);
+                dense_matrix(c, x + C.off * dim, n, dim, kind, p, mat, rowmax);
+                min_bits(c, rowmax, n, rowmax + n);
+                u32 b = 0;
+                TT_CUDA(cudaMemcpyAsync(&b, rowmax + n, 4, cudaMemcpyDeviceToHost, c->stream));
+                TT_CUDA(cudaStreamSynchronize(c->stream));
+                C.thr = bitsf(b);
+                Complex cx{mat, nullptr, nullptr, nullptr, n, C.thr};
+                Dim0Out r;
+                dim0(c, cx, 1, r);
+                C.mat.resize(u64(n) * n);
+                C.h0d.resize(r.nh0);
+                C.h0e.resize(r.nh0);
+                C.ci.resize(r.ncols);
+                C.cd.resize(r.ncols);
+                C.emi.resize(r.ncols);
+                C.emf.resize(r.ncols);
+                TT_CUDA(cudaMemcpyAsync(C.mat.data(), mat, 4 * u64(n) * n, cudaMemcpyDeviceToHost, c->stream));
+                if (r.nh0) {
+                    TT_CUDA(cudaMemcpyAsync(C.h0d.data(), r.h0, 4 * r.nh0, cudaMemcpyDeviceToHost, c->stream));
+                    TT_CUDA(cudaMemcpyAsync(C.h0e.data(), r.h0_edge, 8 * r.nh0, cudaMemcpyDeviceToHost, c->stream));
+                }
+                if (r.ncols) {
+                    TT_CUDA(cudaMemcpyAsync(C.ci.data(), r.cidx, 8 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+                    TT_CUDA(cudaMemcpyAsync(C.cd.data(), r.cd, 4 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+                    TT_CUDA(cudaMemcpyAsync(C.emi.data(), r.emi, 8 * r.ncols, cudaMemcpyDeviceToHost, c->stream));
+                    TT_CUDA(cudaMemcpyAsync(C.emf.data(), r.emf, r.ncols, cudaMemcpyDeviceToHost, c->stream));
+                }
+                TT_CUDA(cudaStreamSynchronize(c->stream));
+                queue.publish(q);
+            }
+        };
+        try {
+            for (u32 t = 1; t < nt; ++t) pool.emplace_back(work, t);
+            front_end();
+        } catch (...) {
+            queue.halt();
+            join();
+            throw;
+        }
         work(0);
-        for (auto& th : pool) th.join();
+        join();
         for (auto& e : errs)
             if (!e.empty()) throw Error(TT_ERR_INTERNAL, e);
         // pack, with global point ids
