@@ -300,10 +300,11 @@ struct BucketQueue {
     // Empties the queue; entries of the next column are expected in [a, b]
     // (outside it they only share the end buckets).
     void reset(float a, float b) {
-        for (uint32_t w = 0; w < kBuckets / 64; ++w) {
-            for (uint64_t m = live[w]; m; m &= m - 1) bk[(w << 6) + uint32_t(__builtin_ctzll(m))].clear();
-            live[w] = 0;
-        }
+        if (count)   // an emptied bucket has cleared its own bit
+            for (uint32_t w = 0; w < kBuckets / 64; ++w) {
+                for (uint64_t m = live[w]; m; m &= m - 1) bk[(w << 6) + uint32_t(__builtin_ctzll(m))].clear();
+                live[w] = 0;
+            }
         lo = ord(a);
         const uint32_t span = ord(b) > lo ? ord(b) - lo : 0;
         shift = 0;
@@ -414,20 +415,18 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
             }
             if (!emergent) push_coboundary(col);
         } else {
-            bool check = true;
+            // the first cofacet with the column's diameter pairs it when no
+            // earlier column owns it and it has no zero-apparent facet;
+            // otherwise the whole coboundary goes into the queue
+            uint32_t cv[34];
             cx.decode(col.idx, nv, vd);
-            cx.cofacets(vd, nv, col.d, hc.thr, [&](const Entry& cf, uint32_t, uint32_t) {
-                if (check && cf.d == col.d) {
-                    if (pivots.find(cf.idx) == kNone && cx.zero_apparent_facet(cf, nv + 1).idx == kNone) {
-                        pivot = cf;
-                        emergent = true;
-                        return false;
-                    }
-                    check = false;
-                }
-                wc.push(cf);
-                return true;
-            });
+            const uint64_t z = cx.zero_cofacet(vd, nv, col.d, cv);
+            if (z != kNone && pivots.find(z) == kNone && cx.zero_apparent_facet(Entry{z, col.d}, nv + 1).idx == kNone) {
+                pivot = Entry{z, col.d};
+                emergent = true;
+            } else {
+                push_coboundary(col);
+            }
         }
         if (emergent) {
             ++st.emergent;
