@@ -66,6 +66,9 @@ def small() -> None:
         # the first cloud of the topological-loss workload: its H1 columns
         # take thousands of additions in the host reduction
         "circle": synth.circles()[0],
+        # C(600, 4) > 2^32: the host reduction of dimension 2 keeps wide
+        # (64-bit index + diameter) queue entries
+        "torus600": synth.torus(600, 17),
     }
     # dense distance matrices + enclosing radius, every metric path
     for cname in ["u3", "g17", "g32", "g9", "grid4"]:
@@ -110,7 +113,7 @@ def small() -> None:
              probe("sdim0", x, metric, str(k)) | {"g_" + a: b for a, b in probe("knng", x, metric, str(k)).items()})
     # full diagrams (tops::persistence, dense, canonical order is applied by tests)
     for cname, metric, maxdim in [("torus", "l2", 2), ("grid4", "l1", 2), ("u3", "l2", 1),
-                                  ("grid4", "linf", 1), ("circle", "l2", 1)]:
+                                  ("grid4", "linf", 1), ("circle", "l2", 1), ("torus600", "l2", 2)]:
         x = clouds[cname]
         save(f"bars_{cname}_{metric}_{maxdim}", x, metric, "bars", {"maxdim": maxdim},
              probe("bars", x, metric, str(maxdim)))

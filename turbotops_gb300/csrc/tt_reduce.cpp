@@ -272,119 +272,205 @@ struct PivotMap {
     }
 };
 
+// Order-preserving bits of a diameter (>= 0 or +inf; -0 is taken as +0,
+// which it equals) and back.
+inline uint32_t dbits(float d) {
+    uint32_t u;
+    std::memcpy(&u, &d, 4);
+    if (u == 0x80000000u) u = 0;
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+inline float from_dbits(uint32_t u) {
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float d;
+    std::memcpy(&d, &u, 4);
+    return d;
+}
+
+// What the working coboundary stores per entry: the Entry itself, or, when
+// every index of the dimension fits in 32 bits, one 64-bit key (diameter
+// bits above the complemented index) whose integer order is the filtration
+// order — half the bytes, and compares without branches.
+struct WideKey {
+    using T = Entry;
+    static T make(const Entry& e) { return e; }
+    static Entry entry(const T& t) { return t; }
+    static bool less(const T& a, const T& b) { return precedes(a, b); }
+    static bool same(const T& a, const T& b) { return a.idx == b.idx; }
+    static uint32_t bits(const T& t) { return dbits(t.d); }
+};
+struct PackedKey {
+    using T = uint64_t;
+    static T make(const Entry& e) { return uint64_t(dbits(e.d)) << 32 | (0xffffffffu - uint32_t(e.idx)); }
+    static Entry entry(T t) { return Entry{0xffffffffu - uint32_t(t), from_dbits(uint32_t(t >> 32))}; }
+    static bool less(T a, T b) { return a < b; }
+    static bool same(T a, T b) { return a == b; }
+    static uint32_t bits(T t) { return uint32_t(t >> 32); }
+};
+
 // The working coboundary: a priority queue in filtration order (smallest
 // diameter first, larger index first among equal diameters) with pairwise
-// cancellation of equal indices at the top. Entries go into buckets by the
-// order-preserving bits of their diameter between the column's birth (no
-// entry is earlier) and the largest diameter of the complex; only the lowest
-// non-empty bucket is kept as a binary heap, and a bitmap finds the next one.
-// A push is an append and a pop works in a small heap, where one heap over the
-// whole column (the long reductions of noisy circles hold a million entries,
-// and two in five of them surface to cancel) paid a walk through memory for
-// both. Buckets are monotone in the diameter and equal keys share a bucket, so
-// the entries surface in exactly the order of a single heap.
+// cancellation of equal indices at the top. Entries go into buckets by their
+// diameter bits between the column's birth (no entry is earlier) and the
+// largest diameter of the complex. A push is an append to one of few enough
+// buckets that their tails stay in cache: most entries of a column lie
+// beyond its pivot and are never looked at again. The lowest non-empty
+// bucket is sorted when it comes to the top and read with a cursor. Entries
+// pushed into it after that are sorted at the next read and merged into a
+// second, smaller sorted run (folded into the first when it grows past an
+// eighth of it); the front is the earlier of the two runs' heads. Buckets
+// are monotone in the diameter and equal keys share a bucket, so the entries
+// surface in exactly the order of a single heap over the whole column.
+template <class K>
 struct BucketQueue {
-    static constexpr uint32_t kBits = 14, kBuckets = 1u << kBits;
-    std::vector<std::vector<Entry>> bk = std::vector<std::vector<Entry>>(kBuckets);
+    using T = typename K::T;
+    static constexpr uint32_t kBits = 10, kBuckets = 1u << kBits;
+    std::vector<std::vector<T>> bk = std::vector<std::vector<T>>(kBuckets);
     std::vector<uint64_t> live = std::vector<uint64_t>(kBuckets / 64, 0);   // non-empty buckets
-    uint32_t cur = kBuckets;   // buckets below cur are empty; bk[cur] is a heap
+    std::vector<T> aux, pend, tmp;   // second run, pushes since the last read, merge buffer
+    uint32_t cur = kBuckets;         // buckets below cur are empty
+    bool ready = false;              // bk[cur] is sorted from pos on, aux from apos on
+    size_t pos = 0, apos = 0;
     uint32_t lo = 0, shift = 0;
     uint64_t count = 0;
 
-    static bool later(const Entry& a, const Entry& b) { return precedes(b, a); }
-    static uint32_t ord(float d) {
-        uint32_t u;
-        std::memcpy(&u, &d, 4);
-        return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-    }
     // Empties the queue; entries of the next column are expected in [a, b]
     // (outside it they only share the end buckets).
     void reset(float a, float b) {
-        if (count)   // an emptied bucket has cleared its own bit
-            for (uint32_t w = 0; w < kBuckets / 64; ++w) {
-                for (uint64_t m = live[w]; m; m &= m - 1) bk[(w << 6) + uint32_t(__builtin_ctzll(m))].clear();
-                live[w] = 0;
-            }
-        lo = ord(a);
-        const uint32_t span = ord(b) > lo ? ord(b) - lo : 0;
+        for (uint32_t w = 0; w < kBuckets / 64; ++w) {
+            for (uint64_t m = live[w]; m; m &= m - 1) bk[(w << 6) + uint32_t(__builtin_ctzll(m))].clear();
+            live[w] = 0;
+        }
+        aux.clear();
+        pend.clear();
+        lo = dbits(a);
+        const uint32_t span = dbits(b) > lo ? dbits(b) - lo : 0;
         shift = 0;
         while ((span >> shift) >= kBuckets) ++shift;
         cur = kBuckets;
+        ready = false;
+        pos = apos = 0;
         count = 0;
     }
-    uint32_t bucket(float d) const {
-        const uint32_t u = ord(d);
+    uint32_t bucket(uint32_t u) const {
         if (u <= lo) return 0;
         const uint32_t x = (u - lo) >> shift;
         return x < kBuckets ? x : kBuckets - 1;
     }
-    void push(const Entry& e) {
-        const uint32_t x = bucket(e.d);
-        std::vector<Entry>& v = bk[x];
-        live[x >> 6] |= 1ull << (x & 63);
-        v.push_back(e);
-        ++count;
-        if (x == cur) std::push_heap(v.begin(), v.end(), later);
-        else if (x < cur) cur = x;   // the bucket was empty: one entry is a heap
+    void mark(uint32_t x) { live[x >> 6] |= 1ull << (x & 63); }
+    void unmark(uint32_t x) { live[x >> 6] &= ~(1ull << (x & 63)); }
+    // merges the unread parts of v (from *vp) and w (from wp) into v
+    void merge_into(std::vector<T>& v, size_t* vp, const std::vector<T>& w, size_t wp) {
+        tmp.resize(v.size() - *vp + w.size() - wp);
+        std::merge(v.begin() + ptrdiff_t(*vp), v.end(), w.begin() + ptrdiff_t(wp), w.end(), tmp.begin(), K::less);
+        v.swap(tmp);
+        *vp = 0;
     }
-    bool empty() const { return count == 0; }
-    // the lowest non-empty bucket as the current heap (count > 0, so a push
-    // has set cur below kBuckets)
+    // turns the current bucket back into an unsorted one
+    void unready() {
+        std::vector<T>& v = bk[cur];
+        v.erase(v.begin(), v.begin() + ptrdiff_t(pos));
+        v.insert(v.end(), aux.begin() + ptrdiff_t(apos), aux.end());
+        v.insert(v.end(), pend.begin(), pend.end());
+        aux.clear();
+        pend.clear();
+        pos = apos = 0;
+        ready = false;
+        if (v.empty()) unmark(cur);
+    }
+    void push(const Entry& e) {
+        const T t = K::make(e);
+        const uint32_t x = bucket(K::bits(t));
+        ++count;
+        if (ready && x == cur) {
+            pend.push_back(t);
+            return;
+        }
+        if (ready && x < cur) unready();
+        bk[x].push_back(t);
+        mark(x);
+        if (x < cur) cur = x;
+    }
+    // the lowest non-empty bucket sorted under the cursors (count > 0, so a
+    // push has set cur below kBuckets)
     void settle() {
-        if (!bk[cur].empty()) return;
+        if (ready) {
+            if (!pend.empty()) {
+                std::sort(pend.begin(), pend.end(), K::less);
+                merge_into(aux, &apos, pend, 0);
+                pend.clear();
+                if (8 * aux.size() > bk[cur].size() - pos) {
+                    merge_into(bk[cur], &pos, aux, 0);
+                    aux.clear();
+                }
+            }
+            if (pos < bk[cur].size() || apos < aux.size()) return;
+            bk[cur].clear();
+            aux.clear();
+            unmark(cur);
+            ready = false;
+        }
         uint32_t w = cur >> 6;
         uint64_t m = live[w] & (~0ull << (cur & 63));
         while (!m) m = live[++w];
         cur = (w << 6) + uint32_t(__builtin_ctzll(m));
-        std::make_heap(bk[cur].begin(), bk[cur].end(), later);
+        std::sort(bk[cur].begin(), bk[cur].end(), K::less);
+        pos = apos = 0;
+        ready = true;
     }
-    const Entry& front() {
-        settle();
-        return bk[cur].front();
-    }
-    void pop() {
-        std::vector<Entry>& v = bk[cur];
-        std::pop_heap(v.begin(), v.end(), later);
-        v.pop_back();
-        --count;
-        if (v.empty()) live[cur >> 6] &= ~(1ull << (cur & 63));
-    }
-    Entry pop_pivot() {
-        Entry piv{kNone, 0};
-        while (!empty()) {
-            const Entry f = front();
-            if (piv.idx == kNone) {
+    // The first entry that does not cancel, left in the queue (idx kNone when
+    // everything cancels).
+    Entry get_pivot() {
+        T piv{};
+        bool have = false, in_aux = false;
+        while (count) {
+            settle();
+            const std::vector<T>& v = bk[cur];
+            const bool fa = apos < aux.size() && (pos == v.size() || K::less(aux[apos], v[pos]));
+            const T f = fa ? aux[apos] : v[pos];
+            if (!have) {
                 piv = f;
-                pop();
-            } else if (f.idx == piv.idx) {
-                pop();
-                piv.idx = kNone;
+                have = true;
+                in_aux = fa;
+            } else if (K::same(f, piv)) {
+                have = false;
             } else {
                 break;
             }
+            if (fa) ++apos;
+            else ++pos;
+            --count;
         }
-        return piv;
-    }
-    Entry get_pivot() {
-        const Entry p = pop_pivot();
-        if (p.idx != kNone) push(p);
-        return p;
+        if (!have) return Entry{kNone, 0};
+        // still in the run it was read from unless that bucket ran out
+        size_t& p = in_aux ? apos : pos;
+        const std::vector<T>& v = in_aux ? aux : bk[cur];
+        if (ready && p > 0 && p <= v.size() && K::same(v[p - 1], piv)) {
+            --p;
+            ++count;
+            return K::entry(piv);
+        }
+        const Entry e = K::entry(piv);
+        push(e);
+        return e;
     }
 };
 
 }  // namespace
 
-Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const std::vector<Entry>& cols,
-                   const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
-                   ReduceStats& st) {
-    const Binom B(hc.n, maxdim + 2);
+namespace {
+
+template <class K>
+Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const std::vector<Entry>& cols,
+                    const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
+                    ReduceStats& st) {
     const Cx cx{hc, B, {}};
     const uint32_t nv = dim + 1;
     Bars bars;
     PivotMap pivots(cols.size() + 16);
     std::vector<uint64_t> off{0};
     std::vector<Entry> red, wr;
-    BucketQueue wc;
+    BucketQueue<K> wc;
     // the largest diameter an entry can have: the threshold, else the largest
     // distance of the complex
     float dmax = hc.thr;
@@ -486,6 +572,18 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
         if (pivots.k[s] != kNone) pivot_list.push_back(pivots.k[s]);
     std::sort(pivot_list.begin(), pivot_list.end());
     return bars;
+}
+
+}  // namespace
+
+Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const std::vector<Entry>& cols,
+                   const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
+                   ReduceStats& st) {
+    const Binom B(hc.n, maxdim + 2);
+    // every cofacet index below 2^32: the packed queue keys
+    if (B(hc.n, dim + 2) <= (uint64_t(1) << 32))
+        return reduce_columns<PackedKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st);
+    return reduce_columns<WideKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st);
 }
 
 }  // namespace host
