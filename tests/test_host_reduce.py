@@ -117,3 +117,21 @@ def test_torus_config_pivots_vs_reference(shim):
     e = O.emergent(mat=mat, cidx=r["cidx"], cd=r["cd"])
     _, _, piv, _ = reduce(shim, mat, thr, 1, 2, r["cidx"], r["cd"], e["emi"], e["emf"])
     assert np.array_equal(np.sort(piv), np.sort(ref))
+
+
+@pytest.mark.parametrize("metric", ["l1", "linf"])
+def test_lattice_config_pivots_vs_reference(shim, metric):
+    """Configuration 2 (3000 distinct points of {0..15}^4, enclosing radius):
+    the reference's tie-heavy dimension-1 columns reduce to its pivot set.
+    C(3000, 3) > 2^32, so the queue keeps wide entries here, and most
+    cofacets share their diameter with many others."""
+    from turbotops_gb300 import synth
+    cfg = json.load(open(os.path.join(GOLDEN, "configs.json")))[f"lattice3000_{metric}"]
+    ref = np.load(os.path.join(GOLDEN, f"cfg_lattice3000_{metric}_piv.npz"))["piv"]
+    mat = O.dense(synth.lattice(), metric)
+    thr = O.enclosing_radius(mat)
+    assert float(thr) == cfg["thr"]
+    r = O.dim0(mat=mat, thr=thr, maxdim=2)
+    e = O.emergent(mat=mat, cidx=r["cidx"], cd=r["cd"])
+    _, _, piv, _ = reduce(shim, mat, thr, 1, 2, r["cidx"], r["cd"], e["emi"], e["emf"])
+    assert np.array_equal(np.sort(piv), np.sort(ref))

@@ -27,9 +27,28 @@ namespace host {
 
 namespace {
 
+#ifndef TT_FRONT
+#define TT_FRONT 8
+#endif
+
 constexpr uint64_t kNone = std::numeric_limits<uint64_t>::max();
 
 inline bool precedes(const Entry& a, const Entry& b) { return a.d < b.d || (a.d == b.d && a.idx > b.idx); }
+
+// Order-preserving bits of a diameter (>= 0 or +inf; -0 is taken as +0,
+// which it equals) and back.
+inline uint32_t dbits(float d) {
+    uint32_t u;
+    std::memcpy(&u, &d, 4);
+    u = u == 0x80000000u ? 0u : u;
+    return u ^ ((0u - (u >> 31)) | 0x80000000u);   // negative: ~u; else u | sign bit
+}
+inline float from_dbits(uint32_t u) {
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float d;
+    std::memcpy(&d, &u, 4);
+    return d;
+}
 
 // C(v, k) for v <= n, k <= K, overflow-checked.
 struct Binom {
@@ -54,7 +73,8 @@ struct Binom {
 struct Cx {
     const HostComplex& c;
     const Binom& B;
-    mutable std::vector<float> cdw;   // dense: diameter of the cofacet through each vertex
+    mutable std::vector<float> cdw;      // dense: diameter of the cofacet through each vertex
+    mutable std::vector<uint32_t> ubw;   // and its order-preserving bits
 
     float dist(uint32_t i, uint32_t j) const {
         if (i == j) return 0.0f;
@@ -142,43 +162,63 @@ struct Cx {
         }
     }
 
-    // Every cofacet with diameter <= cap, in the order of cofacets(): fn(Entry).
-    // Dense: the diameters through all vertices are taken row by row first,
-    // then emitted per range of vertices between the simplex's own, where the
-    // index is one binomial row plus a constant.
+    // The cofacets with diameter <= cap whose diameter bits lie in (lo, hi],
+    // in the order of cofacets(): fn(Entry). Returns the smallest diameter
+    // bits above hi among the cofacets with diameter <= cap (UINT32_MAX when
+    // there is none). Dense: the diameters through all vertices are taken row
+    // by row first, then emitted per range of vertices between the simplex's
+    // own, where the index is one binomial row plus a constant.
     template <typename F>
-    void all_cofacets(const uint32_t* vd, uint32_t nv, float diam, float cap, F&& fn) const {
+    uint32_t window_cofacets(const uint32_t* vd, uint32_t nv, float diam, float cap, uint32_t lo, uint32_t hi,
+                             F&& fn) const {
+        const uint32_t cb = dbits(cap);
+        hi = std::min(hi, cb);
+        uint32_t above = UINT32_MAX;
         if (!c.mat) {
             cofacets(vd, nv, diam, cap, [&](const Entry& e, uint32_t, uint32_t) {
-                fn(e);
+                const uint32_t u = dbits(e.d);
+                if (u > hi) above = std::min(above, u);
+                else if (u > lo) fn(e);
                 return true;
             });
-            return;
+            return above;
         }
         const uint32_t n = c.n;
         cdw.resize(n);
+        ubw.resize(n);
         float* cd = cdw.data();
+        uint32_t* ub = ubw.data();
         const float* r0 = c.mat + uint64_t(vd[0]) * n;
         for (uint32_t w = 0; w < n; ++w) cd[w] = std::max(diam, r0[w]);
         for (uint32_t i = 1; i < nv; ++i) {
             const float* r = c.mat + uint64_t(vd[i]) * n;
             for (uint32_t w = 0; w < n; ++w) cd[w] = std::max(cd[w], r[w]);
         }
+        // diameter bits, the simplex's own vertices outside every window
+        for (uint32_t w = 0; w < n; ++w) ub[w] = dbits(cd[w]);
+        for (uint32_t i = 0; i < nv; ++i) ub[vd[i]] = UINT32_MAX;
+        for (uint32_t w = 0; w < n; ++w) {
+            const uint32_t owed = uint32_t(ub[w] > hi) & uint32_t(ub[w] <= cb);
+            above = std::min(above, ub[w] | (owed - 1u));   // not owed: UINT32_MAX
+        }
+        if (hi <= lo) return above;
+        const uint32_t width = hi - lo;   // u in (lo, hi]: u - lo - 1 < width
         uint64_t A = 0, S[34];
         S[nv] = 0;
         for (uint32_t i = nv; i-- > 0;) S[i] = S[i + 1] + B(vd[i], nv - i);
-        uint32_t hi = n;   // w in [lo, hi): the vertices above vd[t] and below vd[t - 1]
+        uint32_t top = n;   // w in [bot, top): the vertices above vd[t] and below vd[t - 1]
         for (uint32_t t = 0; t <= nv; ++t) {
-            const uint32_t lo = t < nv ? vd[t] + 1 : 0;
+            const uint32_t bot = t < nv ? vd[t] + 1 : 0;
             const uint64_t base = A + S[t];
             const uint64_t* Bk = B.row(nv + 1 - t);
-            for (uint32_t w = hi; w-- > lo;)
-                if (cd[w] <= cap) fn(Entry{base + Bk[w], cd[w]});
+            for (uint32_t w = top; w-- > bot;)
+                if (ub[w] - lo - 1 < width) fn(Entry{base + Bk[w], cd[w]});
             if (t < nv) {
                 A += B(vd[t], nv + 1 - t);
-                hi = vd[t];
+                top = vd[t];
             }
         }
+        return above;
     }
 
     // first cofacet in descending order with diameter d (its vertices in cv)
@@ -271,21 +311,6 @@ struct PivotMap {
             if (ok[i] != kNone) insert(ok[i], ov[i]);
     }
 };
-
-// Order-preserving bits of a diameter (>= 0 or +inf; -0 is taken as +0,
-// which it equals) and back.
-inline uint32_t dbits(float d) {
-    uint32_t u;
-    std::memcpy(&u, &d, 4);
-    if (u == 0x80000000u) u = 0;
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-inline float from_dbits(uint32_t u) {
-    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
-    float d;
-    std::memcpy(&d, &u, 4);
-    return d;
-}
 
 // What the working coboundary stores per entry: the Entry itself, or, when
 // every index of the dimension fits in 32 bits, one 64-bit key (diameter
@@ -464,7 +489,7 @@ template <class K>
 Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const std::vector<Entry>& cols,
                     const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
                     ReduceStats& st) {
-    const Cx cx{hc, B, {}};
+    const Cx cx{hc, B, {}, {}};
     const uint32_t nv = dim + 1;
     Bars bars;
     PivotMap pivots(cols.size() + 16);
@@ -481,16 +506,49 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
         for (uint64_t i = 0; i < m; ++i)
             if (v[i] < INFINITY) dmax = std::max(dmax, v[i]);
     }
+    // Push frontier. Only cofacets whose diameter bits are at most `front`
+    // go into the queue; a simplex with cofacets above it is owed them, and
+    // owed_min is the smallest owed diameter. The queue's first entry that
+    // does not cancel is then the column's pivot, since every owed entry comes
+    // later in the filtration order; when the queue cancels out, the frontier
+    // moves past owed_min (by a width that doubles each time) and the owed
+    // simplices push their cofacets in the new window. Most cofacets of a
+    // column lie far beyond its pivot and are never pushed at all.
     uint32_t vd[34];
-    auto push_coboundary = [&](const Entry& s) {
+    uint32_t front = 0, grow = 1, owed_min = UINT32_MAX;
+    std::vector<Entry> owed, owed2;
+    auto push_window = [&](const Entry& s, uint32_t lo, std::vector<Entry>& still) {
         cx.decode(s.idx, nv, vd);
-        cx.all_cofacets(vd, nv, s.d, hc.thr, [&](const Entry& e) { wc.push(e); });
+        const uint32_t a = cx.window_cofacets(vd, nv, s.d, hc.thr, lo, front, [&](const Entry& e) { wc.push(e); });
+        if (a != UINT32_MAX) {
+            still.push_back(s);
+            owed_min = std::min(owed_min, a);
+        }
     };
+    auto push_coboundary = [&](const Entry& s) { push_window(s, 0, owed); };
+    auto get_pivot = [&]() {
+        for (;;) {
+            const Entry p = wc.get_pivot();
+            if (p.idx != kNone || owed.empty()) return p;
+            const uint32_t lo = front;
+            front = owed_min > UINT32_MAX - grow ? UINT32_MAX : owed_min + grow;
+            grow = grow > (UINT32_MAX >> 1) ? UINT32_MAX : 2 * grow;
+            owed_min = UINT32_MAX;
+            owed2.clear();
+            for (const Entry& s : owed) push_window(s, lo, owed2);
+            owed.swap(owed2);
+        }
+    };
+    const uint32_t top_bits = dbits(dmax);
     for (uint64_t c = 0; c < cols.size(); ++c) {
         const Entry col = cols[c];
         const float birth = col.d;
         wc.reset(col.d, dmax);
         wr.clear();
+        owed.clear();
+        owed_min = UINT32_MAX;
+        grow = std::max<uint32_t>(1, (top_bits > dbits(birth) ? top_bits - dbits(birth) : 0) >> TT_FRONT);
+        front = dbits(birth) + grow;
         Entry pivot{kNone, 0};
         bool emergent = false;
         if (em_idx) {
@@ -517,7 +575,7 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
         if (emergent) {
             ++st.emergent;
         } else {
-            pivot = wc.get_pivot();
+            pivot = get_pivot();
         }
         bool fresh = emergent;
         for (;;) {
@@ -540,14 +598,14 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
                     wr.push_back(red[t]);
                     push_coboundary(red[t]);
                 }
-                pivot = wc.get_pivot();
+                pivot = get_pivot();
                 continue;
             }
             const Entry fa = cx.zero_apparent_facet(pivot, nv + 1);
             if (fa.idx != kNone) {
                 wr.push_back(fa);
                 push_coboundary(fa);
-                pivot = wc.get_pivot();
+                pivot = get_pivot();
                 continue;
             }
             if (pivot.d > birth) {
