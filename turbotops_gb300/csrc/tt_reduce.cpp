@@ -506,14 +506,14 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
         for (uint64_t i = 0; i < m; ++i)
             if (v[i] < INFINITY) dmax = std::max(dmax, v[i]);
     }
-    // Push frontier. Only cofacets whose diameter bits are at most `front`
-    // go into the queue; a simplex with cofacets above it is owed them, and
-    // owed_min is the smallest owed diameter. The queue's first entry that
-    // does not cancel is then the column's pivot, since every owed entry comes
-    // later in the filtration order; when the queue cancels out, the frontier
-    // moves past owed_min (by a width that doubles each time) and the owed
-    // simplices push their cofacets in the new window. Most cofacets of a
-    // column lie far beyond its pivot and are never pushed at all.
+    // Push frontier (dense complexes). Only cofacets whose diameter bits are
+    // at most `front` go into the queue; a simplex with cofacets above it is
+    // owed them, and owed_min is the smallest owed diameter. The queue's first
+    // entry that does not cancel is then the column's pivot, since every owed
+    // entry comes later in the filtration order; when the queue cancels out,
+    // the frontier moves past owed_min (by a width that doubles each time) and
+    // the owed simplices push their cofacets in the new window. Most cofacets
+    // of a column lie far beyond its pivot and are never pushed at all.
     uint32_t vd[34];
     uint32_t front = 0, grow = 1, owed_min = UINT32_MAX;
     std::vector<Entry> owed, owed2;
@@ -548,7 +548,10 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
         owed.clear();
         owed_min = UINT32_MAX;
         grow = std::max<uint32_t>(1, (top_bits > dbits(birth) ? top_bits - dbits(birth) : 0) >> TT_FRONT);
-        front = dbits(birth) + grow;
+        // A graph complex pushes everything at once: a simplex has only its
+        // common neighbours as cofacets, and a raise would repeat the row
+        // walks that find them.
+        front = hc.mat ? dbits(birth) + grow : UINT32_MAX;
         Entry pivot{kNone, 0};
         bool emergent = false;
         if (em_idx) {
