@@ -197,5 +197,28 @@ def cli_cases() -> None:
         json.dump(out, f, indent=1)
 
 
+def graph_bars() -> None:
+    """Whole diagrams of kNN-graph complexes from the reference CLI (``--graph
+    knn``, points as .bin): the CSR path of the host reduction is checked
+    against them. Saved as gbars_<name>.npz (x, metric, params, bars)."""
+    runs = [("circle400_l2_k8", synth.circles(1, 400, 0.1, 21)[0], "l2", 8, "inf"),
+            ("gauss300_l1_k10", synth.gauss(300, 5, 22), "l1", 10, "inf"),
+            ("grid200_linf_k6", synth.grid(200, 3, 6, 23), "linf", 6, "inf"),
+            ("uniform500_l2_k12_t0p15", synth.uniform(500, 3, 24), "l2", 12, "0.15")]
+    with tempfile.TemporaryDirectory() as td:
+        for name, x, metric, k, thr in runs:
+            pts = os.path.join(td, "p.bin")
+            np.ascontiguousarray(x, np.float32).tofile(pts)
+            r = subprocess.run([CLI, "run", pts, "--dim", str(x.shape[1]), "--graph", "knn", "-k", str(k),
+                                "--metric", metric, "--maxdim", "1", "--threshold", thr, "--quiet"],
+                               check=True, capture_output=True, text=True)
+            bars = np.array([[float(t) for t in line.split()] for line in r.stdout.splitlines()],
+                            np.float64).astype(np.float32).reshape(-1, 3)
+            np.savez_compressed(os.path.join(HERE, f"gbars_{name}.npz"), x=x, metric=np.array(metric),
+                                stage=np.array("gbars"), params=np.array(json.dumps({"k": k, "thr": thr})),
+                                bars=bars)
+
+
 if __name__ == "__main__" and os.path.exists(CLI):
     cli_cases()
+    graph_bars()

@@ -135,3 +135,42 @@ def test_lattice_config_pivots_vs_reference(shim, metric):
     e = O.emergent(mat=mat, cidx=r["cidx"], cd=r["cd"])
     _, _, piv, _ = reduce(shim, mat, thr, 1, 2, r["cidx"], r["cd"], e["emi"], e["emf"])
     assert np.array_equal(np.sort(piv), np.sort(ref))
+
+
+GBARS = cases("gbars")
+
+
+def reduce_csr(L, csr, n, thr, cidx, cd, emi, emf):
+    rp, ci, w = (np.ascontiguousarray(a) for a in csr)
+    cidx = np.ascontiguousarray(cidx, np.uint64)
+    cd = np.ascontiguousarray(cd, np.float32)
+    k = cidx.size
+    birth = np.empty(k + 1, np.float32)
+    death = np.empty(k + 1, np.float32)
+    piv = np.empty(k + 1, np.uint64)
+    nb, npv, em = (np.zeros(1, np.uint64) for _ in range(3))
+    rc = L.hr_compute_pairs(None, _p(rp), _p(ci), _p(w), n, float(thr), 1, 1, _p(cidx), _p(cd), k, _p(emi),
+                            _p(emf), _p(birth), _p(death), _p(nb), _p(piv), _p(npv), _p(em))
+    assert rc == 0
+    b = int(nb[0])
+    return birth[:b], death[:b]
+
+
+@pytest.mark.parametrize("c", GBARS, ids=ids(GBARS))
+def test_knn_graph_diagram_vs_reference(shim, c):
+    """tops::persistence on the kNN graph of a cloud (the reference CLI's
+    --graph knn, maxdim 1): dim0 H0 + compute_pairs(1) over the CSR complex,
+    whole diagram bit for bit (the graph-complex path of the reduction)."""
+    x, metric = c["x"], c["metric"]
+    n = x.shape[0]
+    thr = thr_of(c["params"]["thr"])
+    csr = O.knn_graph(x, metric, O.knn(x, metric, c["params"]["k"]))
+    r = O.dim0(csr=csr, n=n, thr=thr, maxdim=1)
+    e = O.emergent(csr=csr, n=n, cidx=r["cidx"], cd=r["cd"])
+    b, d = reduce_csr(shim, csr, n, thr, r["cidx"], r["cd"], e["emi"], e["emf"])
+    h0 = r["h0"].reshape(-1, 2)
+    got = canonical(np.concatenate([np.column_stack([np.zeros(len(h0), np.float32), h0]),
+                                    np.column_stack([np.ones(len(b), np.float32), b, d])]).astype(np.float32))
+    ref = canonical(c["bars"])
+    assert got.shape == ref.shape
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
