@@ -13,6 +13,14 @@
 // column owns it and it has no zero-apparent facet; for dimension 1 the GPU
 // supplies that cofacet and flag per column, and only the ownership lookup
 // runs here.
+//
+// Only the priority queue differs from the reference's binary heap: diameter
+// buckets read as sorted runs (BucketQueue), 64-bit packed keys where every
+// index of the dimension fits in 32 bits, and, on dense complexes, a push
+// frontier that leaves the cofacets beyond the column's current reach owed
+// instead of queued. Equal entries are indistinguishable and surface in the
+// same order, so the pivots, the stored reductions and the pairs are the
+// reference's.
 #include "tt_reduce.h"
 
 #include <algorithm>
