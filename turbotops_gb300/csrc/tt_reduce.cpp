@@ -139,6 +139,25 @@ struct Cx {
             return;
         }
         // CSR: common neighbours walked down from the top of the sorted rows
+        if (nv == 2) {   // an edge: two rows, the smaller head steps without a branch
+            const uint32_t a = vd[0], b = vd[1];
+            uint64_t pa = c.rp[a + 1], pb = c.rp[b + 1];
+            const uint64_t la = c.rp[a], lb = c.rp[b];
+            while (pa > la && pb > lb) {
+                const uint32_t xa = c.ci[pa - 1], xb = c.ci[pb - 1];
+                if (xa != xb) {
+                    pa -= xa > xb;
+                    pb -= xb > xa;
+                    continue;
+                }
+                const uint32_t t = uint32_t(a > xa) + uint32_t(b > xa);
+                const float cd = std::max(diam, std::max(c.w[pa - 1], c.w[pb - 1]));
+                if (cd <= cap && !fn(Entry{A[t] + B(xa, 3 - t) + S[t], cd}, xa, t)) return;
+                --pa;
+                --pb;
+            }
+            return;
+        }
         uint64_t p[34], lo[34];
         for (uint32_t i = 0; i < nv; ++i) {
             lo[i] = c.rp[vd[i]];
