@@ -45,3 +45,35 @@ extern "C" int hr_compute_pairs(const float* mat, const uint64_t* rp, const uint
         return -1;
     }
 }
+
+// graph_pairs_dim1 (the boundary reduction of a graph complex's triangles)
+// behind the same outputs as hr_compute_pairs for dimension 1; also returns
+// the triangle count.
+extern "C" int hr_graph_pairs_dim1(const uint64_t* rp, const uint32_t* ci, const float* w, uint32_t n, float thr,
+                                   const uint64_t* cidx, const float* cd, uint64_t ncols, float* birth,
+                                   float* death, uint64_t* bidx, uint64_t* didx, uint64_t* nbars,
+                                   uint64_t* ntri) {
+    try {
+        tt::host::HostComplex hc;
+        hc.rp = rp;
+        hc.ci = ci;
+        hc.w = w;
+        hc.n = n;
+        hc.thr = thr;
+        std::vector<tt::host::Entry> cols(ncols);
+        for (uint64_t i = 0; i < ncols; ++i) cols[i] = tt::host::Entry{cidx[i], cd[i]};
+        tt::host::ReduceStats st;
+        const tt::host::Bars b = tt::host::graph_pairs_dim1(hc, cols, st);
+        for (size_t i = 0; i < b.birth.size(); ++i) {
+            birth[i] = b.birth[i];
+            death[i] = b.death[i];
+            bidx[i] = b.birth_idx[i];
+            didx[i] = b.death_idx[i];
+        }
+        *nbars = b.birth.size();
+        *ntri = tt::host::graph_triangles(hc);
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}

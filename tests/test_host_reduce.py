@@ -174,3 +174,70 @@ def test_knn_graph_diagram_vs_reference(shim, c):
     ref = canonical(c["bars"])
     assert got.shape == ref.shape
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def graph_pairs(L, csr, n, thr, cidx, cd):
+    rp, ci, w = (np.ascontiguousarray(a) for a in csr)
+    cidx = np.ascontiguousarray(cidx, np.uint64)
+    cd = np.ascontiguousarray(cd, np.float32)
+    k = cidx.size
+    birth = np.empty(k + 1, np.float32)
+    death = np.empty(k + 1, np.float32)
+    bi = np.empty(k + 1, np.uint64)
+    di = np.empty(k + 1, np.uint64)
+    nb, nt = np.zeros(1, np.uint64), np.zeros(1, np.uint64)
+    L.hr_graph_pairs_dim1.restype = C.c_int
+    L.hr_graph_pairs_dim1.argtypes = [C.c_void_p] * 3 + [C.c_uint32, C.c_float] + [C.c_void_p] * 2 + \
+        [C.c_uint64] + [C.c_void_p] * 6
+    assert L.hr_graph_pairs_dim1(_p(rp), _p(ci), _p(w), n, float(thr), _p(cidx), _p(cd), k, _p(birth), _p(death),
+                                 _p(bi), _p(di), _p(nb), _p(nt)) == 0
+    b = int(nb[0])
+    return birth[:b], death[:b]
+
+
+@pytest.mark.parametrize("c", GBARS, ids=ids(GBARS))
+def test_knn_graph_boundary_diagram_vs_reference(shim, c):
+    """The boundary reduction of a graph complex's triangles
+    (graph_pairs_dim1, which the sparse front end uses for kNN graphs) gives
+    the reference CLI's whole diagram bit for bit."""
+    x, metric = c["x"], c["metric"]
+    n = x.shape[0]
+    thr = thr_of(c["params"]["thr"])
+    csr = O.knn_graph(x, metric, O.knn(x, metric, c["params"]["k"]))
+    r = O.dim0(csr=csr, n=n, thr=thr, maxdim=1)
+    b, d = graph_pairs(shim, csr, n, thr, r["cidx"], r["cd"])
+    h0 = r["h0"].reshape(-1, 2)
+    got = canonical(np.concatenate([np.column_stack([np.zeros(len(h0), np.float32), h0]),
+                                    np.column_stack([np.ones(len(b), np.float32), b, d])]).astype(np.float32))
+    ref = canonical(c["bars"])
+    assert got.shape == ref.shape
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_graph_boundary_equals_coboundary_in_order(shim, seed):
+    """graph_pairs_dim1 and compute_pairs(1) emit the same bars in the same
+    order on kNN and radius graphs (ties from lattice points, finite
+    thresholds)."""
+    from turbotops_gb300 import synth
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(30, 200))
+    if seed % 3 == 0:
+        x, metric = synth.uniform(n, 3, seed), "l2"
+    elif seed % 3 == 1:
+        x, metric = synth.grid(min(n, 216), 3, 6, seed), ["l1", "linf"][seed % 2]
+    else:
+        x, metric = synth.circles(1, n, 0.1, seed)[0], "l2"
+    n = x.shape[0]
+    if seed % 2:
+        csr = O.knn_graph(x, metric, O.knn(x, metric, int(rng.integers(3, 10))))
+    else:
+        csr = O.radius_graph(x, metric, 2.0 if metric != "l2" else 0.35)
+    thr = float("inf") if seed % 4 < 2 else float(np.quantile(csr[2], 0.7))
+    thr = np.float32(thr)
+    r = O.dim0(csr=csr, n=n, thr=thr, maxdim=1)
+    e = O.emergent(csr=csr, n=n, cidx=r["cidx"], cd=r["cd"])
+    b1, d1 = reduce_csr(shim, csr, n, thr, r["cidx"], r["cd"], e["emi"], e["emf"])
+    b2, d2 = graph_pairs(shim, csr, n, thr, r["cidx"], r["cd"])
+    assert np.array_equal(b1.view(np.uint32), b2.view(np.uint32))
+    assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))

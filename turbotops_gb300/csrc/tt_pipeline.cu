@@ -69,14 +69,24 @@ void h0_bars(tt_ctx* c, const Dim0Out& r, Result& out) {
 std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim, const Dim0Out& r, Result& out) {
     const auto ci = to_host(c, r.cidx, r.ncols);
     const auto cd = to_host(c, r.cd, r.ncols);
-    const auto emi = to_host(c, r.emi, r.ncols);
-    const auto emf = to_host(c, r.emf, r.ncols);
+    // A graph complex with at most 8 triangles a kept edge (kNN graphs: under
+    // one) is reduced through the boundary matrix of its triangles: the same
+    // pairs and bars in the same order, without cancelling the whole
+    // coboundary of every essential edge.
+    const bool boundary = !hc.mat && maxdim == 1 && host::graph_triangles(hc) <= 8 * r.m;
+    std::vector<u8> emf;
+    std::vector<u64> emi;
+    if (!boundary) {
+        emi = to_host(c, r.emi, r.ncols);
+        emf = to_host(c, r.emf, r.ncols);
+    }
     sync(c);
     std::vector<host::Entry> cols(r.ncols);
     for (u64 i = 0; i < r.ncols; ++i) cols[i] = host::Entry{ci[i], cd[i]};
     std::vector<u64> piv;
     host::ReduceStats st;
-    const host::Bars b = host::compute_pairs(hc, 1, maxdim, cols, emi.data(), emf.data(), piv, st);
+    const host::Bars b = boundary ? host::graph_pairs_dim1(hc, cols, st)
+                                  : host::compute_pairs(hc, 1, maxdim, cols, emi.data(), emf.data(), piv, st);
     for (u64 i = 0; i < b.birth.size(); ++i) out.add(1, b.birth[i], b.death[i]);
     out.columns.push_back(st.columns);
     out.emergent.push_back(st.emergent);

@@ -674,5 +674,143 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
     return reduce_columns<WideKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st);
 }
 
+namespace {
+
+inline uint64_t choose2(uint64_t v) { return v * (v - 1) / 2; }
+inline uint64_t choose3(uint64_t v) { return uint64_t((unsigned __int128)v * (v - 1) * (v - 2) / 6); }
+
+// Every triangle a > b > c of the graph complex: its edge (a, b) is the upper
+// slot s of row a, (a, c) and (b, c) the slots pa of row a and pb of row b.
+// fn(a, s, pa, pb, diameter).
+template <typename F>
+void for_each_triangle(const HostComplex& hc, F&& fn) {
+    for (uint32_t a = 0; a < hc.n; ++a)
+        for (uint64_t s = hc.rp[a]; s < hc.rp[a + 1]; ++s) {
+            const uint32_t b = hc.ci[s];
+            if (b >= a) break;   // rows ascend: the upper slots come first
+            if (!(hc.w[s] <= hc.thr)) continue;
+            uint64_t pa = hc.rp[a], pb = hc.rp[b];
+            const uint64_t ea = hc.rp[a + 1], eb = hc.rp[b + 1];
+            while (pa < ea && pb < eb) {
+                const uint32_t xa = hc.ci[pa], xb = hc.ci[pb];
+                if (xa >= b || xb >= b) break;
+                if (xa != xb) {
+                    pa += xa < xb;
+                    pb += xb < xa;
+                    continue;
+                }
+                if (hc.w[pa] <= hc.thr && hc.w[pb] <= hc.thr)
+                    fn(a, s, pa, pb, std::max(hc.w[s], std::max(hc.w[pa], hc.w[pb])));
+                ++pa;
+                ++pb;
+            }
+        }
+}
+
+}  // namespace
+
+uint64_t graph_triangles(const HostComplex& hc) {
+    uint64_t t = 0;
+    for_each_triangle(hc, [&](uint32_t, uint64_t, uint64_t, uint64_t, float) { ++t; });
+    return t;
+}
+
+// Boundary-matrix reduction of dimension 2 (the standard persistence
+// algorithm: columns in filtration order, a column whose lowest entry, its
+// latest edge, is owned by an earlier column adds that column). The
+// filtration order is the reducer's (diameter ascending, larger index first
+// among equal diameters), and the persistence pairing of one total order is
+// unique, so an edge is paired with the same triangle as by compute_pairs.
+// Edges that are never a lowest entry are essential; they cost nothing here,
+// where the coboundary reducer cancels their whole coboundaries.
+Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, ReduceStats& st) {
+    const uint32_t n = hc.n;
+    const uint64_t nnz = n ? hc.rp[n] : 0;
+    // kept edges by upper slot, ranked in filtration order
+    struct Edge {
+        float d;
+        uint64_t idx, slot;
+    };
+    std::vector<Edge> edges;
+    for (uint32_t a = 0; a < n; ++a)
+        for (uint64_t s = hc.rp[a]; s < hc.rp[a + 1] && hc.ci[s] < a; ++s)
+            if (hc.w[s] <= hc.thr) edges.push_back(Edge{hc.w[s], choose2(a) + hc.ci[s], s});
+    std::sort(edges.begin(), edges.end(),
+              [](const Edge& x, const Edge& y) { return x.d < y.d || (x.d == y.d && x.idx > y.idx); });
+    if (edges.size() >= UINT32_MAX) throw std::length_error("gb300: too many edges for the boundary reduction");
+    std::vector<uint32_t> rank(nnz, UINT32_MAX);
+    for (uint32_t r = 0; r < edges.size(); ++r) rank[edges[r].slot] = r;
+    // triangles in filtration order, each with its three edge ranks
+    struct Tri {
+        float d;
+        uint64_t idx;
+        uint32_t e[3];
+    };
+    std::vector<Tri> tris;
+    for_each_triangle(hc, [&](uint32_t a, uint64_t s, uint64_t pa, uint64_t pb, float d) {
+        tris.push_back(Tri{d, choose3(a) + choose2(hc.ci[s]) + hc.ci[pa], {rank[s], rank[pa], rank[pb]}});
+    });
+    std::sort(tris.begin(), tris.end(),
+              [](const Tri& x, const Tri& y) { return x.d < y.d || (x.d == y.d && x.idx > y.idx); });
+    if (tris.size() >= UINT32_MAX) throw std::length_error("gb300: too many triangles for the boundary reduction");
+    // reduced columns (edge ranks, descending) stored back to back
+    std::vector<uint32_t> owner(edges.size(), UINT32_MAX);   // edge rank -> triangle
+    std::vector<uint64_t> off(tris.size() + 1, 0);
+    std::vector<uint32_t> store, cur, tmp;
+    for (uint32_t t = 0; t < tris.size(); ++t) {
+        cur.assign(tris[t].e, tris[t].e + 3);
+        std::sort(cur.begin(), cur.end(), std::greater<uint32_t>());
+        while (!cur.empty() && owner[cur[0]] != UINT32_MAX) {
+            const uint32_t o = owner[cur[0]];
+            const uint32_t* q = store.data() + off[o];
+            const uint32_t* qe = store.data() + off[o + 1];
+            tmp.clear();
+            size_t i = 0;
+            while (i < cur.size() && q < qe) {
+                if (cur[i] > *q) tmp.push_back(cur[i++]);
+                else if (*q > cur[i]) tmp.push_back(*q++);
+                else ++i, ++q;
+            }
+            tmp.insert(tmp.end(), cur.begin() + ptrdiff_t(i), cur.end());
+            tmp.insert(tmp.end(), q, qe);
+            cur.swap(tmp);
+        }
+        if (!cur.empty()) {
+            owner[cur[0]] = t;
+            store.insert(store.end(), cur.begin(), cur.end());
+        }
+        off[t + 1] = store.size();
+    }
+    // bars in column order, as compute_pairs emits them
+    Bars bars;
+    for (const Entry& c : cols) {
+        uint32_t u = uint32_t((1.0 + std::sqrt(1.0 + 8.0 * double(c.idx))) / 2.0);
+        while (choose2(u) > c.idx) --u;
+        while (choose2(u + 1) <= c.idx) ++u;
+        const uint32_t v = uint32_t(c.idx - choose2(u));
+        const uint32_t* b = hc.ci + hc.rp[u];
+        const uint32_t* e = hc.ci + hc.rp[u + 1];
+        const uint32_t* it = std::lower_bound(b, e, v);
+        if (it == e || *it != v) throw std::logic_error("gb300: a column's edge is not in the graph");
+        const uint32_t r = rank[uint64_t(it - hc.ci)];
+        if (r == UINT32_MAX) throw std::logic_error("gb300: a column's edge is above the threshold");
+        const uint32_t t = owner[r];
+        if (t == UINT32_MAX) {
+            bars.birth.push_back(c.d);
+            bars.death.push_back(INFINITY);
+            bars.birth_idx.push_back(c.idx);
+            bars.death_idx.push_back(kNone);
+        } else if (tris[t].d > c.d) {
+            bars.birth.push_back(c.d);
+            bars.death.push_back(tris[t].d);
+            bars.birth_idx.push_back(c.idx);
+            bars.death_idx.push_back(tris[t].idx);
+        }
+    }
+    st.columns = cols.size();
+    st.emergent = 0;
+    return bars;
+}
+
 }  // namespace host
 }  // namespace tt

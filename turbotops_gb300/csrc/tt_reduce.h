@@ -45,5 +45,17 @@ Bars compute_pairs(const HostComplex& cx, uint32_t dim, uint32_t maxdim, const s
                    const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivots,
                    ReduceStats& st);
 
+// Triangles (dimension-2 simplices with diameter <= thr) of a graph complex
+// (hc.mat == nullptr), counted without storing them.
+uint64_t graph_triangles(const HostComplex& hc);
+
+// The same pairs and bars as compute_pairs(hc, 1, 1, cols, ...) on a graph
+// complex, from the boundary matrix of its triangles instead of the
+// coboundaries of its edges: essential edges are never reduced. `cols` are
+// the dimension-1 columns (non-tree, non-apparent edges, descending
+// filtration order); bars come out in their order, as compute_pairs emits
+// them. st.emergent stays 0 (no emergent shortcut is taken).
+Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, ReduceStats& st);
+
 }  // namespace host
 }  // namespace tt
