@@ -241,3 +241,38 @@ def test_graph_boundary_equals_coboundary_in_order(shim, seed):
     b2, d2 = graph_pairs(shim, csr, n, thr, r["cidx"], r["cd"])
     assert np.array_equal(b1.view(np.uint32), b2.view(np.uint32))
     assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
+
+
+def _csr(n, edges):
+    """Symmetric CSR (rows ascending) of an undirected weighted edge list."""
+    rows = [[] for _ in range(n)]
+    for u, v, w in edges:
+        rows[u].append((v, w))
+        rows[v].append((u, w))
+    rp = np.zeros(n + 1, np.uint64)
+    ci, ww = [], []
+    for u in range(n):
+        for v, w in sorted(rows[u]):
+            ci.append(v)
+            ww.append(w)
+        rp[u + 1] = len(ci)
+    return rp, np.array(ci, np.uint32), np.array(ww, np.float32)
+
+
+@pytest.mark.parametrize("n,edges", [
+    (3, []),                                                          # no edges
+    (2, [(0, 1, 1.0)]),                                               # one edge, no column
+    (3, [(0, 1, 1.0), (1, 2, 1.0), (0, 2, 1.0)]),                     # a triangle of ties
+    (4, [(0, 1, 1.0), (1, 2, 1.0), (2, 3, 1.0), (3, 0, 1.0)]),        # an essential 4-cycle
+    (4, [(0, 1, 1.0), (1, 2, 1.0), (2, 3, 1.0), (3, 0, 1.0), (0, 2, 1.5)]),   # the cycle dies at 1.5
+    (5, [(0, 1, 0.5), (1, 2, 0.5), (2, 0, 2.0), (2, 3, 0.5), (3, 4, 0.5), (4, 2, 2.0), (0, 3, 3.0)]),
+])
+def test_graph_boundary_small_graphs(shim, n, edges):
+    csr = _csr(n, edges)
+    thr = np.float32(np.inf)
+    r = O.dim0(csr=csr, n=n, thr=thr, maxdim=1)
+    e = O.emergent(csr=csr, n=n, cidx=r["cidx"], cd=r["cd"])
+    b1, d1 = reduce_csr(shim, csr, n, thr, r["cidx"], r["cd"], e["emi"], e["emf"])
+    b2, d2 = graph_pairs(shim, csr, n, thr, r["cidx"], r["cd"])
+    assert np.array_equal(b1.view(np.uint32), b2.view(np.uint32))
+    assert np.array_equal(d1.view(np.uint32), d2.view(np.uint32))
