@@ -69,10 +69,10 @@ void h0_bars(tt_ctx* c, const Dim0Out& r, Result& out) {
 std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim, const Dim0Out& r, Result& out) {
     const auto ci = to_host(c, r.cidx, r.ncols);
     const auto cd = to_host(c, r.cd, r.ncols);
-    // A graph complex with at most 8 triangles a kept edge (kNN graphs: under
-    // one) is reduced through the boundary matrix of its triangles: the same
-    // pairs and bars in the same order, without cancelling the whole
-    // coboundary of every essential edge.
+    // A graph complex with at most 8 triangles a kept edge (the benchmark's
+    // 32-dimensional kNN graph: 0.77) is reduced through the boundary matrix
+    // of its triangles: the same pairs and bars in the same order, without
+    // cancelling the whole coboundary of every essential edge.
     const bool boundary = !hc.mat && maxdim == 1 && host::graph_triangles(hc) <= 8 * r.m;
     std::vector<u8> emf;
     std::vector<u64> emi;
