@@ -15,11 +15,15 @@ one such front end; the metric is front ends (diagrams) per second.
          inside the timed region
   roofline   the dominant stage (exact kNN lists: tile order + k_knn_tc), timed
              alone; tensor work counted over the Gram tiles actually computed
-  cpu_baseline   the oracle port of the same front end on the host cores, a
-         bounded sample of the kNN queries scaled to the whole cloud
+  cpu_baseline   the reference's own front end on the host cores (two whole
+         front ends), or the oracle port on a sample where it did not build
 
---impl reference runs only the CPU arm (the oracle port; the reference's own
-build cannot run on this host) on rank 0 and prints its line.
+--impl reference runs only the CPU arm on rank 0 and prints its line: the
+unmodified reference (compiled on this host by build() from its installed copy
+in baseline/_ref, oracle/_ref/refbench) runs its own knn_lists_exact ->
+knn_graph -> Reducer::dim0 on the whole cloud every step, on every host
+thread; where the reference did not build, the oracle port on a bounded
+sample stands in.
 Multi-GPU: independent replicas per rank (weak scaling, no collective).
 """
 from __future__ import annotations
@@ -110,12 +114,19 @@ def dist_env():
     return ws, rank, local
 
 
+def pg_backend(impl: str, cuda: bool) -> str:
+    """The process group's backends: host tensors (the timing reduction) go
+    to gloo, device tensors to NCCL; the CPU arm and CPU-only hosts use gloo
+    alone (NCCL cannot be created without a GPU)."""
+    return "cpu:gloo,cuda:nccl" if cuda and impl != "reference" else "gloo"
+
+
 def max_over_ranks(v: float, ws: int) -> float:
     if ws == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64)
+    t = torch.tensor([v], dtype=torch.float64)   # host tensor: reduced by the gloo backend
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -127,8 +138,28 @@ def barrier(ws: int):
 
 
 # ----------------------------------------------------------------------------
-# CPU arm: the oracle port of the same front end.
+# CPU arm: the reference itself (oracle/_ref/refbench, compiled on this host
+# from the reference's installed copy), else the oracle port.
 # ----------------------------------------------------------------------------
+REFBENCH = os.path.join(ROOT, "oracle", "_ref", "refbench")
+
+
+def ref_bench(stage: str, x, metric: str, k: int, maxdim: int, warmup: int, steps: int,
+              threads: int = 0) -> dict:
+    """Runs the unmodified reference's own functions for `stage` (see
+    oracle/refbench.cpp) on the points x on the host cores and returns its
+    JSON: per-step seconds and mean seconds per phase."""
+    import tempfile
+
+    import numpy as np
+    with tempfile.TemporaryDirectory() as td:
+        pts = os.path.join(td, "p.bin")
+        np.ascontiguousarray(x, np.float32).tofile(pts)
+        r = subprocess.run([REFBENCH, stage, pts, str(x.shape[0]), str(x.shape[1]), metric, str(k), str(maxdim),
+                            str(warmup), str(steps), str(threads)], check=True, capture_output=True, text=True)
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
 def cpu_front_seconds(x, sample: int, threads: int) -> tuple[float, dict]:
     """Seconds for one whole front end on the host, from a bounded sample."""
     import numpy as np
@@ -158,13 +189,28 @@ def cpu_front_seconds(x, sample: int, threads: int) -> tuple[float, dict]:
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
-    import numpy as np  # noqa: F401
-
-    from oracle import oracle as O
     from turbotops_gb300 import synth
-    O.lib()
     x = synth.gmm(N, DIM)
     threads = os.cpu_count() or 1
+    if os.path.exists(REFBENCH):
+        r = ref_bench("knnfront", x, METRIC_NAME, K, MAXDIM, args.warmup, args.steps)
+        sec = statistics.mean(r["steps_s"])
+        value = 1.0 / sec
+        sample = f"the whole {N}-point front end every step (no sampling)"
+        line = {"metric": METRIC, "value": value, "unit": "diagrams/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"knn-complex front end, gmm {N}x{DIM}, k={K}, {METRIC_NAME}, "
+                                       f"maxdim {MAXDIM}",
+                           "stages": "knn_lists_exact -> knn_graph -> Reducer<u64, SparseComplex>::dim0"},
+                "impl": "reference",
+                "cpu_baseline": {"value": value, "unit": "diagrams/s", "cores": r["threads"], "kind": "reference",
+                                 "sample": sample, **{k: round(v, 4) for k, v in r["phases_s"].items()}},
+                "e2e": {"value": value, "unit": "diagrams/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+    from oracle import oracle as O
+    O.lib()
     sample = args.cpu_sample
     for _ in range(args.warmup):
         cpu_front_seconds(x, max(sample // 4, threads), threads)
@@ -313,15 +359,22 @@ def run_gpu(args, ws, rank, local):
         if mt and (int(mt.group(2)), int(mt.group(3)), int(mt.group(4))) == (N, DIM, K):
             traffic = int(mt.group(1))
 
-    # ---- CPU baseline (rank 0, N=1 only)
+    # ---- CPU baseline (rank 0, N=1 only): the reference's own front end
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        s, det = cpu_front_seconds(x_h, args.cpu_sample, threads)
-        cpu = {"value": 1.0 / s, "unit": "diagrams/s", "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_sample} of {N} kNN queries on all host threads (+ graph/dim0 on a "
-                         f"20000-point sub-cloud), scaled to the whole front end",
-               **{k: round(v, 4) for k, v in det.items()}}
+        if os.path.exists(REFBENCH):
+            r = ref_bench("knnfront", x_h, METRIC_NAME, K, MAXDIM, 0, 2)
+            sec = statistics.mean(r["steps_s"])
+            cpu = {"value": 1.0 / sec, "unit": "diagrams/s", "cores": r["threads"], "kind": "reference",
+                   "sample": f"2 whole front ends of the {N}-point cloud, all host threads",
+                   **{k: round(v, 4) for k, v in r["phases_s"].items()}}
+        else:
+            s, det = cpu_front_seconds(x_h, args.cpu_sample, threads)
+            cpu = {"value": 1.0 / s, "unit": "diagrams/s", "cores": threads, "kind": "port",
+                   "sample": f"{args.cpu_sample} of {N} kNN queries on all host threads (+ graph/dim0 on a "
+                             f"20000-point sub-cloud), scaled to the whole front end",
+                   **{k: round(v, 4) for k, v in det.items()}}
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -478,7 +531,8 @@ def main():
     ws, rank, local = dist_env()
     if ws > 1:
         import torch.distributed as dist
-        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
+        import torch
+        dist.init_process_group(pg_backend(args.impl, torch.cuda.is_available()))
     try:
         if args.impl == "reference":
             return run_reference(args, ws, rank)

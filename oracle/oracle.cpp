@@ -3,6 +3,7 @@
 // CPU leg load it, as the checker. Compiled with -ffp-contract=off: every fused
 // multiply-add below is an explicit fmaf where the reference fuses.
 #include "oracle.h"
+#include "aarch64_math.h"
 
 #include <algorithm>
 #include <cmath>
@@ -85,10 +86,17 @@ f32 ipow(f32 x, u32 p) {
     return r;
 }
 
-// pow01_8 (metric.hpp:50-89), one lane. The reference's reciprocal estimate
-// rcp_ps is modelled here as an exact division; hardware estimates differ
-// (x86 VRCPPS, aarch64 FRECPE+FRECPS), so non-integer p at dim >= 8 is NOT
-// pinned to the reference's bits.
+// The Lp model: the reference's non-integer-p arithmetic as it runs on an
+// aarch64 host (SIMDe's NEON translation, glibc powf), aarch64_math.h.
+// Bits of g_lp_model select where GCC's default contraction (-ffp-contract=
+// fast) fuses a multiply into the following add; the default is the one that
+// reproduces the reference built on the GB300 machine's Grace host.
+//   bit 0  SIMDe's portable fnmadd, -(a*b) + c, fused (rcp refinement)
+//   bit 1  lg = (e - 127) + S * 2.885..., fused
+//   bit 2  glibc powf rounds y*log2(x) halfway away from zero (aarch64 port)
+int g_lp_model = 7;
+
+// pow01_8 (metric.hpp:50-89), one lane.
 f32 pow01(f32 x, f32 p) {
     u32 xi;
     std::memcpy(&xi, &x, 4);
@@ -97,8 +105,9 @@ f32 pow01(f32 x, f32 p) {
     f32 m;
     std::memcpy(&m, &mi, 4);
     const f32 m1 = m + 1.0f;
-    f32 r = 1.0f / m1;
-    r = r * std::fmaf(-m1, r, 2.0f);
+    f32 r = a64::rcp_ps(m1);
+    const f32 nm = (g_lp_model & 1) ? std::fmaf(-m1, r, 2.0f) : -(m1 * r) + 2.0f;
+    r = r * nm;
     const f32 t = (m - 1.0f) * r;
     const f32 t2 = t * t;
     f32 S = 1.0f / 13.0f;
@@ -109,7 +118,8 @@ f32 pow01(f32 x, f32 p) {
     S = std::fmaf(t2, S, 1.0f / 3.0f);
     S = std::fmaf(t2, S, 1.0f);
     S = S * t;
-    const f32 lg = (e - 127.0f) + S * 2.885390081777927f;
+    const f32 lg = (g_lp_model & 2) ? std::fmaf(S, 2.885390081777927f, e - 127.0f)
+                                    : (e - 127.0f) + S * 2.885390081777927f;
     const f32 y = std::max(p * lg, -126.0f);
     const f32 k = std::nearbyint(y);
     const f32 f = (y - k) * 0.6931471805599453f;
@@ -128,6 +138,8 @@ f32 pow01(f32 x, f32 p) {
     return x < 1e-30f ? 0.0f : out;
 }
 
+f32 powf_ref(f32 x, f32 y) { return a64::ref_powf(x, y, (g_lp_model & 4) != 0); }
+
 // kern::lp (metric.hpp:183-207).
 f32 lp(const f32* a, const f32* b, u32 dim, f32 p) {
     const f32 M = linf(a, b, dim);
@@ -145,9 +157,9 @@ f32 lp(const f32* a, const f32* b, u32 dim, f32 p) {
     }
     for (; k < dim; ++k) {
         const f32 x = std::min(1.0f, std::fabs(a[k] - b[k]) * inv);
-        s += integral ? ipow(x, u32(p)) : std::pow(x, p);
+        s += integral ? ipow(x, u32(p)) : powf_ref(x, p);
     }
-    return M * std::pow(s, 1.0f / p);
+    return M * powf_ref(s, 1.0f / p);
 }
 
 f32 dist(int kind, f32 p, const f32* a, const f32* b, u32 dim) {
@@ -383,6 +395,11 @@ std::vector<std::vector<std::pair<u32, f32>>> rows_from_lists(const f32* x, u32 
 }  // namespace
 
 extern "C" {
+
+void or_set_lp_model(int model) { g_lp_model = model; }
+int or_get_lp_model(void) { return g_lp_model; }
+float or_powf(float x, float y) { return powf_ref(x, y); }
+float or_rcp(float x) { return a64::rcp_ps(x); }
 
 float or_dist(int kind, float p, const float* a, const float* b, uint32_t dim) {
     return dist(kind, p, a, b, dim);

@@ -7,8 +7,12 @@
  *
  * Parity: pinned against golden vectors dumped by the reference itself
  * (oracle/refprobe.cpp, fixtures in tests/golden) for L1, L2, L-inf and integer-p
- * Lp. For non-integer p the reference's pow01_8 uses a hardware reciprocal
- * estimate and glibc powf; see or_dist below for the model and its status.
+ * Lp, on any host. For non-integer p the reference's bits depend on the host:
+ * its pow01_8 takes a hardware reciprocal estimate and its scalar pow is the
+ * host libm's powf. The oracle models an aarch64 host (the GB300 machine's Grace
+ * CPU: FRECPE + one FRECPS step through SIMDe's NEON translation, glibc powf,
+ * GCC's default contraction), aarch64_math.h, pinned against fixtures that
+ * the reference built on that host dumped (the tests/golden a64 fixtures).
  *
  * Metric kinds: 0 = L1, 1 = L2, 2 = L-inf, 3 = Lp (p >= 1).
  */
@@ -19,6 +23,15 @@
 #ifdef __cplusplus
 extern "C" {
 #endif
+
+/* Lp model bits (oracle.cpp g_lp_model): 1 fused fnmadd in the reciprocal
+ * refinement, 2 fused lg multiply-add, 4 glibc powf's aarch64 rounding of
+ * y*log2(x). Default 7. */
+void or_set_lp_model(int model);
+int or_get_lp_model(void);
+/* The modelled scalar pow (glibc powf) and SIMDe rcp_ps (FRECPE + FRECPS). */
+float or_powf(float x, float y);
+float or_rcp(float x);
 
 /* kern::l1/l2/linf/lp (metric.hpp:92-207), reference lane order. */
 float or_dist(int kind, float p, const float* a, const float* b, uint32_t dim);

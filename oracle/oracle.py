@@ -50,6 +50,12 @@ def lib():
             build()
         L = C.CDLL(LIB)
         P = C.c_void_p
+        L.or_set_lp_model.argtypes = [C.c_int]
+        L.or_get_lp_model.restype = C.c_int
+        L.or_powf.restype = C.c_float
+        L.or_powf.argtypes = [C.c_float, C.c_float]
+        L.or_rcp.restype = C.c_float
+        L.or_rcp.argtypes = [C.c_float]
         L.or_dist.restype = C.c_float
         L.or_dist.argtypes = [C.c_int, C.c_float, P, P, C.c_uint32]
         L.or_dense.argtypes = [P, C.c_uint32, C.c_uint32, C.c_int, C.c_float, P]

@@ -1,12 +1,15 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Runs ``oracle/_ref/refprobe`` (the unmodified reference headers compiled by
-``make -C oracle ref``; only possible where the reference sources are present)
-on small seeded clouds and stores each stage's raw outputs as ``.npz``.
-The GPU machine never runs this script: it only reads the committed fixtures.
+Runs ``oracle/_ref/refprobe`` and ``oracle/_ref/turbotops`` (the unmodified
+reference compiled by ``make -C oracle install-ref ref`` from its installed
+copy) on seeded clouds and stores each stage's raw outputs as ``.npz``, or the
+canonical diagram text's SHA-256 for the full-size workloads. The tests only
+read the committed fixtures; they never run this script.
 
-    python tests/golden/make_golden.py            # small fixtures (seconds)
-    python tests/golden/make_golden.py --configs  # + checksums of the full workloads
+    python tests/golden/make_golden.py              # small fixtures (seconds)
+    python tests/golden/make_golden.py --configs    # + checksums of the full workloads' front ends
+    python tests/golden/make_golden.py --diagrams   # whole diagrams of the full workloads (minutes)
+    python tests/golden/make_golden.py --a64 DIR    # aarch64-host Lp fixtures (run on that host)
 """
 from __future__ import annotations
 
@@ -14,9 +17,11 @@ import argparse
 import hashlib
 import json
 import os
+import platform
 import subprocess
 import sys
 import tempfile
+import time
 
 import numpy as np
 
@@ -158,17 +163,6 @@ def configs() -> None:
         json.dump(res, f, indent=1, sort_keys=True)
 
 
-if __name__ == "__main__":
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--configs", action="store_true")
-    a = ap.parse_args()
-    if not os.path.exists(PROBE):
-        sys.exit("build the reference first: make -C oracle ref")
-    small()
-    if a.configs:
-        configs()
-
-
 def cli_cases() -> None:
     """Exact-text diagrams of the reference CLI on small hand-checkable inputs."""
     inputs = {"sq": "0 0\n1 0\n1 1\n0 1\n", "tri": "0 0\n1 0\n0 1\n",
@@ -219,6 +213,117 @@ def graph_bars() -> None:
                                 bars=bars)
 
 
-if __name__ == "__main__" and os.path.exists(CLI):
-    cli_cases()
-    graph_bars()
+def cli_text(x: np.ndarray, *args: str) -> tuple[str, float]:
+    """The reference CLI's canonical diagram text for the points x (.bin input)."""
+    with tempfile.TemporaryDirectory() as td:
+        pts = os.path.join(td, "p.bin")
+        np.ascontiguousarray(x, np.float32).tofile(pts)
+        t0 = time.perf_counter()
+        r = subprocess.run([CLI, "run", pts, "--dim", str(x.shape[1]), *args, "--quiet"], check=True,
+                           capture_output=True, text=True)
+        return r.stdout, time.perf_counter() - t0
+
+
+def text_summary(text: str) -> dict:
+    counts: dict[str, int] = {}
+    for line in text.splitlines():
+        d = line.split(" ", 1)[0]
+        counts[d] = counts.get(d, 0) + 1
+    return {"sha256": hashlib.sha256(text.encode()).hexdigest(), "bars": counts}
+
+
+# Whole diagrams of the benchmark workloads at full size: (name, points,
+# CLI arguments). The reference's text for L1, L2 and L-inf is the same on
+# every host (exact lane-order arithmetic), so these are generated wherever
+# the reference builds; the lp:1.5 ones depend on the host and come from a64().
+def diagram_cases() -> list[tuple[str, np.ndarray, list[str]]]:
+    cases = [("torus1000_l2_maxdim2", synth.torus(), ["--maxdim", "2"]),
+             ("lattice3000_linf_maxdim2", synth.lattice(), ["--maxdim", "2", "--metric", "linf"]),
+             ("lattice3000_l1_maxdim2", synth.lattice(), ["--maxdim", "2", "--metric", "l1"]),
+             ("gmm100k_knn15_l2_maxdim1", synth.gmm(), ["--graph", "knn", "-k", "15", "--maxdim", "1"]),
+             ("gmm100k_l2_maxdim0", synth.gmm(), ["--maxdim", "0"])]
+    for i, c in enumerate(synth.circle_batch()[:8]):
+        cases.append((f"batch{i}_l2_maxdim1", c, ["--maxdim", "1"]))
+    for i, c in enumerate(synth.circles()[:8]):
+        cases.append((f"circle{i}_l2_maxdim1", c, ["--maxdim", "1"]))
+    return cases
+
+
+def diagrams(only: str | None = None) -> None:
+    path = os.path.join(HERE, "diagrams.json")
+    res = json.load(open(path)) if os.path.exists(path) else {}
+    for name, x, args in diagram_cases():
+        if only and only not in name:
+            continue
+        text, secs = cli_text(x, *args)
+        res[name] = {"args": args, "n": int(x.shape[0]), "dim": int(x.shape[1]), **text_summary(text),
+                     "reference_seconds": round(secs, 2), "host": platform.machine()}
+        print(name, res[name], flush=True)
+        with open(path, "w") as f:
+            json.dump(res, f, indent=1, sort_keys=True)
+
+
+def a64(out: str) -> None:
+    """Non-integer Lp fixtures from the reference built on an aarch64 host (the
+    GB300 machine's Grace CPU): its distance bits depend on the host's reciprocal
+    estimate and libm, so these are generated there and committed as
+    *_a64.npz, plus the full-size lp:1.5 workload's checksums and diagram."""
+    if platform.machine() != "aarch64":
+        sys.exit("a64 fixtures must be generated on an aarch64 host")
+    global HERE
+    os.makedirs(out, exist_ok=True)
+    home, HERE = HERE, out
+    clouds = {"u3": synth.uniform(200, 3, 11), "g17": synth.gauss(150, 17, 12), "g32": synth.gauss(120, 32, 13),
+              "g9": synth.gauss(140, 9, 14), "grid4": synth.grid(300, 4, 6, 15), "g8": synth.gauss(130, 8, 16),
+              "g40": synth.gauss(100, 40, 17)}
+    for cname, x in clouds.items():
+        for metric in ["lp:1.5", "lp:2.5", "lp:12", "lp:1.1"]:
+            save(f"dense_{cname}_{metric.replace(':', '')}_a64", x, metric, "dense", {}, probe("dense", x, metric))
+    for cname, metric, k in [("g9", "lp:1.5", 7), ("g32", "lp:1.5", 15), ("u3", "lp:2.5", 6),
+                             ("g17", "lp:1.1", 9)]:
+        x = clouds[cname]
+        tag = metric.replace(":", "")
+        save(f"knn_{cname}_{tag}_{k}_a64", x, metric, "knn", {"k": k},
+             probe("knng", x, metric, str(k)) | probe("knn", x, metric, str(k)))
+    for cname, metric in [("g9", "lp:1.5"), ("u3", "lp:2.5")]:
+        x = clouds[cname]
+        save(f"mst_{cname}_{metric.replace(':', '')}_a64", x, metric, "mst", {"thr": "inf"},
+             probe("mst", x, metric, "inf"))
+    for cname, metric, maxdim in [("u3", "lp:1.5", 1), ("g9", "lp:2.5", 2)]:
+        x = clouds[cname]
+        save(f"bars_{cname}_{metric.replace(':', '')}_{maxdim}_a64", x, metric, "bars", {"maxdim": maxdim},
+             probe("bars", x, metric, str(maxdim)))
+    HERE = home
+    # the full-size lp:1.5 kNN workload
+    x = synth.gmm()
+    r = probe("knng", x, "lp:1.5", "15") | probe("knn", x, "lp:1.5", "15")
+    res = {"gmm100k_lp1.5_k15": {"ids_sha": sha(r["ids"]), "nnz": int(r["ci"].size),
+                                 "csr_sha": sha(r["rp"], r["ci"], r["w"])}}
+    text, secs = cli_text(x, "--graph", "knn", "-k", "15", "--maxdim", "1", "--metric", "lp:1.5")
+    res["gmm100k_knn15_lp1.5_maxdim1"] = {"args": ["--graph", "knn", "-k", "15", "--maxdim", "1", "--metric",
+                                                   "lp:1.5"], "n": 100000, "dim": 32, **text_summary(text),
+                                          "reference_seconds": round(secs, 2), "host": platform.machine()}
+    with open(os.path.join(out, "configs_a64.json"), "w") as f:
+        json.dump(res, f, indent=1, sort_keys=True)
+    print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--configs", action="store_true", help="+ checksums of the full workloads' front ends")
+    ap.add_argument("--diagrams", nargs="?", const="", default=None,
+                    help="whole diagrams of the full workloads (optionally only names containing this)")
+    ap.add_argument("--a64", metavar="DIR", help="only the aarch64 Lp fixtures, written to DIR")
+    a = ap.parse_args()
+    if not os.path.exists(PROBE):
+        sys.exit("build the reference first: make -C oracle install-ref ref")
+    if a.a64:
+        a64(a.a64)
+    elif a.diagrams is not None:
+        diagrams(a.diagrams or None)
+    else:
+        small()
+        cli_cases()
+        graph_bars()
+        if a.configs:
+            configs()

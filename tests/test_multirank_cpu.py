@@ -52,4 +52,15 @@ def test_reference_arm_under_torchrun_prints_one_line():
     assert len(out) == 1
     d = json.loads(out[0])
     assert d["impl"] == "reference" and d["metric"] == "diagrams/s" and d["value"] > 0
-    assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    kind = "reference" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "refbench")) else "port"
+    assert d["cpu_baseline"]["kind"] == kind and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_backend_string():
+    sys.path.insert(0, ROOT)
+    import bench
+    # GPU arm on a GPU host: the timing reduction's host tensor must reach gloo,
+    # which a plain "nccl" group would not have
+    assert bench.pg_backend("gb300", True) == "cpu:gloo,cuda:nccl"
+    assert bench.pg_backend("reference", True) == "gloo"
+    assert bench.pg_backend("gb300", False) == "gloo"

@@ -10,6 +10,7 @@
 // intrinsics).
 #pragma once
 #include "tt_common.cuh"
+#include "tt_libm.cuh"
 
 namespace tt {
 
@@ -115,15 +116,17 @@ __device__ __forceinline__ f32 ipow_dev(f32 x, u32 p) {
 }
 
 // pow01_8 (metric.hpp:50-89), one lane: x^p for x in [0, 1] via
-// exp2(p * log2 x) with the reference's series and constants. The reciprocal
-// estimate of (m + 1) is an exact division here (followed by the reference's
-// own Newton step); the reference's rcp_ps is a hardware estimate.
+// exp2(p * log2 x) with the reference's series and constants, as the
+// reference runs it on an aarch64 host: rcp_ps is FRECPE plus one FRECPS
+// step (tt_libm.cuh), and GCC's default contraction fuses the two
+// multiply-adds that SIMDe leaves as separate operations (the fnmadd of the
+// Newton step, written -(a*b) + c, and lg = (e - 127) + S * 2.885...).
 __device__ __forceinline__ f32 pow01_dev(f32 x, f32 p) {
     const u32 xi = __float_as_uint(x);
     const f32 e = __int2float_rn(int((xi & 0x7f800000u) >> 23));
     const f32 m = __uint_as_float((xi & 0x007fffffu) | 0x3f800000u);
     const f32 m1 = __fadd_rn(m, 1.0f);
-    f32 r = __fdiv_rn(1.0f, m1);
+    f32 r = rcp_a64_2to3(m1);
     r = __fmul_rn(r, __fmaf_rn(-m1, r, 2.0f));
     const f32 t = __fmul_rn(__fsub_rn(m, 1.0f), r);
     const f32 t2 = __fmul_rn(t, t);
@@ -135,7 +138,7 @@ __device__ __forceinline__ f32 pow01_dev(f32 x, f32 p) {
     S = __fmaf_rn(t2, S, 1.0f / 3.0f);
     S = __fmaf_rn(t2, S, 1.0f);
     S = __fmul_rn(S, t);
-    const f32 lg = __fadd_rn(__fsub_rn(e, 127.0f), __fmul_rn(S, 2.885390081777927f));
+    const f32 lg = __fmaf_rn(S, 2.885390081777927f, __fsub_rn(e, 127.0f));
     const f32 y = fmaxf(__fmul_rn(p, lg), -126.0f);
     const f32 k = rintf(y);
     const f32 f = __fmul_rn(__fsub_rn(y, k), 0.6931471805599453f);
@@ -150,19 +153,20 @@ __device__ __forceinline__ f32 pow01_dev(f32 x, f32 p) {
     return x < 1e-30f ? 0.0f : __uint_as_float(pb);
 }
 
-// x^y for the Lp kernel's scalar std::pow calls: double-precision pow
-// rounded once to float.
-__device__ __forceinline__ f32 powf_dev(f32 x, f32 y) { return f32(pow(double(x), double(y))); }
+// The scalar std::pow(float, float) calls of kern::lp: glibc's powf.
+__device__ __forceinline__ f32 powf_dev(f32 x, f32 y) { return powf_a64(x, y); }
 
-// kern::lp (metric.hpp:183-207).
+// kern::lp (metric.hpp:183-207) up to its final root: M = max |a_k - b_k|
+// and the sum s of (|a_k - b_k| / M)^p; the distance is M * powf(s, 1/p)
+// (0 when M == 0).
 template <typename A, typename B>
-__device__ __forceinline__ f32 lp_acc(const A& a, const B& b, u32 dim, f32 p) {
-    const f32 M = linf_acc(a, b, dim);
-    if (M == 0.0f) return 0.0f;
+__device__ __forceinline__ void lp_parts(const A& a, const B& b, u32 dim, f32 p, f32& M, f32& s) {
+    M = linf_acc(a, b, dim);
+    s = 0.0f;
+    if (M == 0.0f) return;
     const f32 inv = __fdiv_rn(1.0f, M);
     const bool integral = p == floorf(p) && p <= 8.0f;
     u32 k = 0;
-    f32 s = 0.0f;
     if (!integral && dim >= 8) {
         f32 acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (; k + 8 <= dim; k += 8)
@@ -175,7 +179,25 @@ __device__ __forceinline__ f32 lp_acc(const A& a, const B& b, u32 dim, f32 p) {
         const f32 x = fminf(1.0f, __fmul_rn(fabsf(__fsub_rn(a(k), b(k))), inv));
         s = __fadd_rn(s, integral ? ipow_dev(x, u32(p)) : powf_dev(x, p));
     }
-    return __fmul_rn(M, powf_dev(s, __fdiv_rn(1.0f, p)));
+}
+
+__device__ __forceinline__ f32 lp_root(f32 M, f32 s, f32 p) {
+    return M == 0.0f ? 0.0f : __fmul_rn(M, powf_dev(s, __fdiv_rn(1.0f, p)));
+}
+
+// A lower bound of lp_root(M, s, p) from float arithmetic: powf's result is
+// within 1 ulp of s^(1/p), and the fast exp2/log2 path errs by far less than
+// the 2^-14 relative margin taken here, so a candidate whose bound already
+// exceeds a threshold cannot pass it (scans skip the exact root for it).
+__device__ __forceinline__ f32 lp_root_lower(f32 M, f32 s, f32 p) {
+    return __fmul_rd(__fmul_rd(M, __powf(s, __fdividef(1.0f, p))), 1.0f - 0x1p-14f);
+}
+
+template <typename A, typename B>
+__device__ __forceinline__ f32 lp_acc(const A& a, const B& b, u32 dim, f32 p) {
+    f32 M, s;
+    lp_parts(a, b, dim, p, M, s);
+    return lp_root(M, s, p);
 }
 
 template <typename A, typename B>

@@ -62,6 +62,8 @@ struct KnnOp {
         visit(s, i, j, __fsqrt_rn(sq), nullptr);
         s.thr_s = sq_bound(s.d[K - 1]);
     }
+    // Largest distance that can still enter the list (Lp pre-test).
+    __device__ __forceinline__ f32 bound(const State& s) const { return s.d[K - 1]; }
     __device__ __forceinline__ static bool lt(f32 d, u32 j, f32 e, u32 i) { return d < e || (d == e && j < i); }
     __device__ __forceinline__ void visit(State& s, u32 i, u32 j, f32 d, const u32*) const {
         if (j == i || !lt(d, j, s.d[K - 1], s.j[K - 1])) return;
@@ -101,6 +103,7 @@ struct RadiusCountOp {
         u64 c;
     };
     __device__ __forceinline__ void init(State& s, u32) const { s.c = 0; }
+    __device__ __forceinline__ f32 bound(const State&) const { return tau; }
     __device__ __forceinline__ void visit(State& s, u32 i, u32 j, f32 d, const u32*) const {
         s.c += (j != i && d <= tau);
     }
@@ -116,6 +119,7 @@ struct RadiusFillOp {
         u64 o;
     };
     __device__ __forceinline__ void init(State& s, u32 i) const { s.o = rp[i]; }
+    __device__ __forceinline__ f32 bound(const State&) const { return tau; }
     __device__ __forceinline__ void visit(State& s, u32 i, u32 j, f32 d, const u32*) const {
         if (j != i && d <= tau) {
             ci[s.o] = j;
@@ -145,6 +149,10 @@ struct ForeignOp {
         if (tcomp[0] == s.c || sq > s.thr_s) return;
         visit(s, i, j, __fsqrt_rn(sq), tcomp);
         s.thr_s = sq_bound(__uint_as_float(u32(s.key >> kIdxBits)));
+    }
+    // The current proposal's distance (NaN while there is none: never skips).
+    __device__ __forceinline__ f32 bound(const State& s) const {
+        return __uint_as_float(u32(s.key >> kIdxBits));
     }
     __device__ __forceinline__ void visit(State& s, u32 i, u32 j, f32 d, const u32* tcomp) const {
         if (tcomp[0] == s.c) return;
@@ -232,7 +240,17 @@ k_scan(const f32* __restrict__ x, u32 n, u32 dim_rt, f32 p, Op op, const u32* __
         }
         __syncthreads();
         if (active) {
-            if (kRt) {
+            if constexpr (KIND == M_LP) {
+                // Lp: the exact root (glibc powf replay, double precision)
+                // only for candidates a float lower bound cannot reject
+                for (u32 r = 0; r < rows; ++r) {
+                    f32 M, sum;
+                    if (kRt) lp_parts(Row{qg}, Row{tile + r * dim}, dim, p, M, sum);
+                    else lp_parts(RegRow<QN>{q}, Row{tile + r * QN}, QN, p, M, sum);
+                    if (lp_root_lower(M, sum, p) > op.bound(st)) continue;
+                    op.visit(st, i, j0 + r, lp_root(M, sum, p), kComp ? tc + r : nullptr);
+                }
+            } else if (kRt) {
                 for (u32 r = 0; r < rows; ++r) {
                     const f32 d = metric_dist(KIND, p, Row{qg}, Row{tile + r * dim}, dim);
                     op.visit(st, i, j0 + r, d, kComp ? tc + r : nullptr);
