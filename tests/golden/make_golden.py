@@ -170,23 +170,34 @@ def cli_cases() -> None:
               # loop, a comment and comma separators; a 6-cycle (one H1 bar that never dies)
               "ecyc": "0 1 1\n1 2 1\n2 3 1\n3 0 1\n0 2 1.5\n",
               "edup": "0 1 2\n1 0 1\n1 2 1\n2 0 3\n3 3 0\n# comment\n2,3,0.5\n0\t3\t2.5\n",
-              "ehex": "0 1 1\n1 2 1\n2 3 1\n3 4 1\n4 5 1\n5 0 1\n"}
+              "ehex": "0 1 1\n1 2 1\n2 3 1\n3 4 1\n4 5 1\n5 0 1\n",
+              # coordinates strtof reads differently from a double parse rounded to
+              # float: a near-midpoint decimal (one rounding: 1 + 2^-23), hex floats,
+              # an underscore digit separator (an error for strtof)
+              "mid": "0 0\n1.0000000596046447753906250001 0\n0 1\n",
+              "hexf": "0x0p0 0\n0x1.8p1 0\n0 0x1p-1\n0x1.4p1 0x1.8p0\n",
+              "under": "0 0\n1_000 0\n"}
     runs = [("sq", ["--maxdim", "1"]), ("sq", ["--maxdim", "1", "--metric", "l1"]),
             ("sq", ["--maxdim", "1", "--metric", "linf"]), ("sq", ["--maxdim", "1", "--metric", "lp:3"]),
             ("sq", ["--maxdim", "1", "--threshold", "1"]), ("tri", []),
             ("sq", ["--graph", "knn", "-k", "2", "--maxdim", "1"]), ("sq", ["--maxdim", "2"]),
             ("ecyc", ["--edges", "--maxdim", "1"]), ("ecyc", ["--edges", "--maxdim", "1", "--threshold", "1"]),
             ("edup", ["--edges", "--maxdim", "1"]), ("ehex", ["--edges", "--maxdim", "1"]),
-            ("ehex", ["--edges"])]
+            ("ehex", ["--edges"]), ("mid", ["--maxdim", "1"]), ("hexf", ["--maxdim", "1"]),
+            ("under", [])]
     out = []
     with tempfile.TemporaryDirectory() as td:
         for name, text in inputs.items():
             with open(os.path.join(td, name + ".txt"), "w") as f:
                 f.write(text)
         for name, args in runs:
-            r = subprocess.run([CLI, "run", os.path.join(td, name + ".txt"), *args, "--quiet"], check=True,
+            r = subprocess.run([CLI, "run", os.path.join(td, name + ".txt"), *args, "--quiet"],
                                capture_output=True, text=True)
-            out.append({"input": inputs[name], "args": args, "stdout": r.stdout})
+            case = {"input": inputs[name], "args": args, "stdout": r.stdout}
+            if r.returncode:
+                case["rc"] = r.returncode
+                case["stderr"] = r.stderr.replace(td + os.sep, "")
+            out.append(case)
     with open(os.path.join(HERE, "cli_cases.json"), "w") as f:
         json.dump(out, f, indent=1)
 

@@ -9,7 +9,9 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-CASES = json.load(open(os.path.join(ROOT, "tests", "golden", "cli_cases.json")))
+ALL_CASES = json.load(open(os.path.join(ROOT, "tests", "golden", "cli_cases.json")))
+CASES = [c for c in ALL_CASES if "rc" not in c]
+ERR_CASES = [c for c in ALL_CASES if "rc" in c]
 
 
 def cli(*args, stdin=None):
@@ -25,6 +27,29 @@ def test_cli_golden_diagrams(case, tmp_path):
     r = cli("run", str(p), *case["args"], "--quiet")
     assert r.returncode == 0, r.stderr
     assert r.stdout == case["stdout"]
+
+
+@pytest.mark.parametrize("case", ERR_CASES, ids=[c["input"].split()[-2] for c in ERR_CASES])
+def test_cli_golden_errors(case, tmp_path):
+    """Inputs the reference CLI rejects while parsing: same exit code, same message."""
+    p = tmp_path / "in.txt"
+    p.write_text(case["input"])
+    r = cli("run", str(p), *case["args"], "--quiet")
+    assert r.returncode == case["rc"] and r.stderr == case["stderr"], r.stderr
+
+
+def test_coordinates_parse_like_strtof():
+    """One rounding from the text to float32 (the host's strtof), not a double
+    parse rounded again; hex floats accepted; Python-only spellings rejected."""
+    import numpy as np
+    from turbotops_gb300.cli import CliError, _parse_f32
+    bits = lambda t: int(np.float32(_parse_f32(t, "coordinate")).view(np.uint32))
+    assert bits("1.0000000596046447753906250001") == 0x3F800001
+    assert float(np.float32(float("1.0000000596046447753906250001"))) == 1.0   # what double-then-float gives
+    assert _parse_f32("0x1.8p1", "coordinate") == 3.0
+    for bad in ["1_000", "1.5x", "", "0x"]:
+        with pytest.raises(CliError):
+            _parse_f32(bad, "coordinate")
 
 
 @pytest.mark.gpu

@@ -43,12 +43,29 @@ class CliError(Exception):
     pass
 
 
+_strtof = None
+
+
 def _parse_f32(tok: str, what: str) -> float:
-    try:
-        v = float(tok)
-    except ValueError:
-        raise CliError(f"bad {what} '{tok}'") from None
-    return float(np.float32(v))
+    """The host C library's strtof over the whole token, as the reference's
+    parse_f32 does (src/turbotops.cpp:119-124): one rounding from the decimal
+    (or hexadecimal) text to float32, 'inf'/'nan' spellings accepted, trailing
+    characters an error."""
+    global _strtof
+    if _strtof is None:
+        import ctypes
+        libc = ctypes.CDLL(None)
+        _strtof = libc.strtof
+        _strtof.restype = ctypes.c_float
+        _strtof.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+    import ctypes
+    raw = tok.encode("utf-8", "surrogateescape")
+    buf = ctypes.create_string_buffer(raw)
+    end = ctypes.c_void_p()
+    v = _strtof(ctypes.cast(buf, ctypes.c_char_p), ctypes.byref(end))
+    if not raw or end.value is None or end.value - ctypes.addressof(buf) != len(raw):
+        raise CliError(f"bad {what} '{tok}'")
+    return float(v)
 
 
 def _parse_u32(tok: str, what: str) -> int:
