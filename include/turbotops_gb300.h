@@ -2,7 +2,7 @@
  *
  * Plain C: no exceptions, no C++ or torch types cross this boundary. Every
  * entry point returns a TT_* status; tt_last_error() holds the message. The
- * C++ host layer (turbotops_gb300/host) maps statuses back to the exception
+ * C++ glue (include/turbotops_gb300.hpp) maps statuses back to the exception
  * types and messages the reference throws (std::invalid_argument,
  * std::overflow_error, std::length_error).
  *
@@ -66,6 +66,16 @@ uint64_t tt_ctx_filter_tiles(const tt_ctx* ctx);
  * the largest |D - exact| / (|a|^2 + |b|^2); the filter's margins hold while
  * it stays below 2^-19. */
 int tt_tc_gram_check(tt_ctx* ctx, uint32_t products, uint64_t seed, double* max_rel);
+/* Failure detection, no reference counterpart. tt_selftest_wait_timeout
+ * launches one kernel whose mbarrier wait nobody completes, bounded by
+ * `polls` (1 .. 2^20) polls: the wait runs out, the kernel records it in its
+ * error word and ends normally, and the call returns TT_ERR_TIMEOUT — the
+ * path every bounded wait in the library takes — leaving the context usable.
+ * tt_ctx_inject_alloc_failure makes the nth next device-arena allocation of
+ * the context fail as if cudaMalloc had (host-side injection, no device
+ * call): that call returns TT_ERR_LENGTH ("device memory exhausted"). */
+int tt_selftest_wait_timeout(tt_ctx* ctx, uint32_t polls);
+int tt_ctx_inject_alloc_failure(tt_ctx* ctx, uint32_t nth);
 /* Stream-ordered copy of bytes between any two device or host addresses
  * (lets bindings move context-owned results into their own buffers). */
 int tt_copy_async(tt_ctx* ctx, void* dst, const void* src, size_t bytes);

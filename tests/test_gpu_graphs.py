@@ -15,17 +15,11 @@ RADIUS = cases("radius")
 MST = cases("mst")
 
 
-def exact(metric):
-    return metric in ("l1", "l2", "linf")
-
-
 @pytest.mark.parametrize("c", KNN, ids=ids(KNN))
 def test_knn_vs_reference(c):
     k = c["params"]["k"]
     x = dev(c["x"])
     i, d = ops.knn(ctx(), x, k, c["metric"])
-    if not exact(c["metric"]):
-        pytest.skip("Lp lists depend on the final root's rounding (see DESIGN)")
     assert np.array_equal(host(i).view(np.uint32).ravel(), c["ids"])
     rp, ci, w = ops.knn_graph(ctx(), x, k, c["metric"])
     assert np.array_equal(host(rp).view(np.uint64), c["rp"])
@@ -48,7 +42,7 @@ def test_mst_vs_reference(c):
     assert np.array_equal(bits(bars), bits(c["h0"]))
 
 
-@pytest.mark.parametrize("metric", ["l2", "l1", "linf"])
+@pytest.mark.parametrize("metric", ["l2", "l1", "linf", "lp:1.5", "lp:2.5"])
 @pytest.mark.parametrize("n,dim,k,kind", [(1000, 32, 15, "gauss"), (700, 3, 8, "grid"), (513, 5, 31, "gauss"),
                                           (129, 16, 1, "gauss"), (6, 4, 15, "gauss")])
 def test_knn_graph_vs_oracle(metric, n, dim, k, kind):
@@ -63,7 +57,7 @@ def test_knn_graph_vs_oracle(metric, n, dim, k, kind):
     assert np.array_equal(bits(host(w)), bits(ow))
 
 
-@pytest.mark.parametrize("metric", ["l2", "l1", "linf"])
+@pytest.mark.parametrize("metric", ["l2", "l1", "linf", "lp:1.5"])
 @pytest.mark.parametrize("n,dim", [(2000, 32), (1500, 3), (300, 7), (2, 3)])
 def test_mst_vs_oracle(metric, n, dim):
     x = synth.gauss(n, dim, 3 * n + dim) if dim != 3 else synth.grid(n, 3, 20, n)
@@ -73,7 +67,7 @@ def test_mst_vs_oracle(metric, n, dim):
 
 def test_radius_vs_oracle_ties():
     x = synth.grid(800, 4, 7, 3)
-    for metric, tau in [("l1", 3.0), ("linf", 1.0), ("l2", 2.0)]:
+    for metric, tau in [("l1", 3.0), ("linf", 1.0), ("l2", 2.0), ("lp:1.5", 2.5), ("lp:3", 2.0)]:
         rp, ci, w = ops.radius_graph(ctx(), dev(x), tau, metric)
         orp, oci, ow = O.radius_graph(x, metric, tau)
         assert np.array_equal(host(rp).view(np.uint64), orp)

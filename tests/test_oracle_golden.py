@@ -1,9 +1,9 @@
 """Pin the CPU oracle to the reference's own outputs (golden fixtures).
 
-Bit-exact for every integer/index output and for every distance of the
-L1/L2/L-inf and integer-p Lp kernels.  Non-integer p is listed as a known
-gap: the oracle models the reference's hardware reciprocal estimate with an
-exact division, so only a loose relative tolerance is asserted there.
+Bit-exact for every integer/index output and every distance. Non-integer p
+Lp fixtures (the *_a64 ones) come from the reference built on an aarch64 host
+(the GB300 machine's Grace CPU), whose reciprocal estimate and libm the oracle
+models (oracle/aarch64_math.h); the other fixtures are host-independent.
 """
 import numpy as np
 import pytest
@@ -30,12 +30,6 @@ def test_dense_matrix(c):
     n = c["x"].shape[0]
     m = O.dense(c["x"], c["metric"]).ravel()
     ref = c["mat"]
-    if c["metric"] == "lp:1.5" and c["x"].shape[1] >= 8:
-        np.testing.assert_allclose(m, ref, rtol=1e-4)
-        return
-    if c["metric"] == "lp:1.5":
-        np.testing.assert_allclose(m, ref, rtol=1e-6)
-        return
     assert np.array_equal(bits(m), bits(ref))
     assert bits(O.enclosing_radius(m.reshape(n, n))) == bits(c["encl"])[0]
 

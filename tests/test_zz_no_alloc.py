@@ -34,7 +34,7 @@ def _static(L, x: torch.Tensor, metric: str):
     return mat, radius
 
 
-@pytest.mark.parametrize("metric", ["l2", "l1", "linf"])
+@pytest.mark.parametrize("metric", ["l2", "l1", "linf", "lp:1.5"])
 def test_static_matches_context_entry_point_twice(metric):
     L = capi.load()
     ctx = capi.Context(0)
@@ -46,6 +46,36 @@ def test_static_matches_context_entry_point_twice(metric):
         assert np.array_equal(mat.cpu().numpy().view(np.uint32), ref_mat.cpu().numpy().view(np.uint32))
         got = radius.cpu().numpy().view(np.uint32)[0]
         assert got == np.float32(ref_radius).view(np.uint32)
+
+
+def test_static_empty_cloud_radius_is_inf():
+    L = capi.load()
+    x = torch.zeros((0, 3), dtype=torch.float32, device="cuda")
+    mat, radius = _static(L, x, "l2")
+    assert mat.numel() == 0 and float(radius.item()) == float("inf")
+
+
+def test_static_allocates_no_device_memory():
+    """After a first call per metric (which loads that metric's kernels), a
+    further call leaves the device's free memory exactly where it was:
+    nothing is allocated."""
+    L = capi.load()
+    x = torch.from_numpy(synth.gauss(2000, 16, 43)).cuda()
+    free0, _ = torch.cuda.mem_get_info()
+    for metric in ("l2", "l1", "lp:1.5"):
+        _static(L, x, metric)
+        n, dim = x.shape
+        kind, p = capi.metric_parse(metric)
+        mat = torch.empty((n, n), dtype=torch.float32, device=x.device)
+        radius = torch.empty(1, dtype=torch.float32, device=x.device)
+        free1, _ = torch.cuda.mem_get_info()
+        st = L.tt_dense_distances_static(x.data_ptr(), n, dim, kind, p, mat.data_ptr(), radius.data_ptr(),
+                                         C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert st == capi.OK
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free1
+        del mat, radius
+    assert free0 > 0
 
 
 def test_static_rejects_n_above_its_scratch_before_any_work():

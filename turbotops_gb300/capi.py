@@ -56,6 +56,8 @@ _SIGS = {
     "tt_ctx_filter_evals": (u64, [P]),
     "tt_ctx_filter_tiles": (u64, [P]),
     "tt_tc_gram_check": (i32, [P, u32, u64, P]),
+    "tt_selftest_wait_timeout": (i32, [P, u32]),
+    "tt_ctx_inject_alloc_failure": (i32, [P, u32]),
     "tt_metric_parse": (i32, [C.c_char_p, C.POINTER(i32), C.POINTER(f32)]),
     "tt_dense_distances": (i32, [P, P, u32, u32, i32, f32, P, C.POINTER(f32)]),
     "tt_dense_distances_static": (i32, [P, u32, u32, i32, f32, P, P, P]),

@@ -192,6 +192,14 @@ int tt_tc_gram_check(tt_ctx* c, uint32_t products, uint64_t seed, double* max_re
     });
 }
 
+int tt_selftest_wait_timeout(tt_ctx* c, uint32_t polls) {
+    return guard(c, [&] { selftest_wait_timeout(c, polls); });
+}
+
+int tt_ctx_inject_alloc_failure(tt_ctx* c, uint32_t nth) {
+    return guard(c, [&] { c->arena.fail_in = nth; });
+}
+
 int tt_copy_async(tt_ctx* c, void* dst, const void* src, size_t bytes) {
     return guard(c, [&] {
         if (bytes) TT_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));

@@ -68,15 +68,21 @@ struct Arena {
         size_t bytes = 0;
     };
     std::vector<Slab> slabs;   // indexed by slot
+    // Host-side fault injection (tt_ctx_inject_alloc_failure): the
+    // fail_in-th next slab allocation reports cudaErrorMemoryAllocation
+    // without calling cudaMalloc. 0 = off.
+    unsigned fail_in = 0;
     void* get(int slot, size_t bytes) {
         if (slot >= int(slabs.size())) slabs.resize(slot + 1);
         Slab& s = slabs[slot];
         if (s.bytes < bytes) {
             if (s.p) TT_CUDA(cudaFree(s.p));
             s.p = nullptr;
+            s.bytes = 0;
             size_t b = bytes < 256 ? 256 : bytes;
             b = (b + b / 8 + 255) & ~size_t(255);   // headroom against regrowth
-            cudaError_t e = cudaMalloc(&s.p, b);
+            const bool inject = fail_in && --fail_in == 0;
+            cudaError_t e = inject ? cudaErrorMemoryAllocation : cudaMalloc(&s.p, b);
             if (e != cudaSuccess) {
                 cudaGetLastError();
                 throw Error(TT_ERR_LENGTH, "device memory exhausted (" + std::to_string(b) + " bytes)");

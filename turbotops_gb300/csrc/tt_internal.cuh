@@ -95,6 +95,7 @@ u64 assemble2(tt_ctx* c, const Complex& cx, const u64* keys, u64 m, const u64* p
 void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists,
                bool defer = false);
 double tc_gram_check(tt_ctx* c, u32 products, u64 seed);   // tt_knn_tc.cu
+void selftest_wait_timeout(tt_ctx* c, u32 polls);           // tt_diag.cu
 u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* ids, u32 k,
               u64* rp, u32** ci, f32** w);
 u64 radius_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32 tau, u64* rp,

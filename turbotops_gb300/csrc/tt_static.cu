@@ -15,7 +15,10 @@
 // Set-up: the first call on a device (with that device current) resolves the
 // array's device address with cudaGetSymbolAddress; in host code the array's
 // name is only a host-side stand-in, so kernels must be given that address.
-// Make the first call on each device before any stream capture begins.
+// Make the first call on each device before any stream capture begins. The
+// resolved address is kept for the life of the process: it must not outlive
+// the device's primary context, so a caller that resets the device
+// (cudaDeviceReset) must not call this entry point on it afterwards.
 //
 // Every call on a device shares the one array and leaves its last contents
 // in it; the row maxima are cleared at the start of each call. Calls whose
