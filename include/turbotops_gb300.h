@@ -175,6 +175,11 @@ int tt_mst_deaths(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int
  * (TT_ERR_LENGTH beyond, *nnz always set). */
 int tt_knn_graph_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
                    uint64_t* row_ptr_h, uint32_t* col_h, float* weight_h, uint64_t cap, uint64_t* nnz);
+/* Host-buffer form of tt_radius_graph (radius_graph, graph.hpp:170-201):
+ * points and tau in, the CsrGraph of the pairs with d <= tau out; capacities
+ * as in tt_knn_graph_h (a first call with cap = 0 returns the count). */
+int tt_radius_graph_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, float tau,
+                      uint64_t* row_ptr_h, uint32_t* col_h, float* weight_h, uint64_t cap, uint64_t* nnz);
 
 /* Device results of the kNN flag-complex front end: the graph plus dim0. */
 typedef struct tt_knn_front_out {
@@ -212,6 +217,24 @@ int tt_dense_front_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, in
                      uint32_t maxdim, float* thr_inout, float* mat_h, float* h0_h, uint64_t* nh0,
                      uint64_t* essential, uint64_t* col_idx_h, float* col_d_h, uint64_t* col_cf_h,
                      uint8_t* col_cf_app_h, uint64_t col_cap, uint64_t* ncols, uint64_t* nedges);
+
+/* RedZeD front ends with host buffers: what redzed::detail::Engine::run
+ * (redzed.hpp:1316-1408) reads before its reduction — make_dense +
+ * enclosing_radius (rips.hpp:370-416) and build_edges (redzed.hpp:545-613)
+ * for dense full Rips, build_edges over a weighted graph (SparseGeom) — so
+ * the reference's RedZeD engine can run on the host from what the GPU built.
+ *   tt_dense_redzed_h: points -> the n x n matrix (mat_h, may be NULL), the
+ *     threshold (thr_inout: +inf in, the enclosing radius out) and the edges
+ *     with d <= threshold in (d asc, combinatorial index asc) order,
+ *     vertices i < j (diam_h: count floats, verts_h: 2 count ints).
+ *   tt_graph_redzed_h: host CSR (row_ptr n + 1, 2m columns and weights, rows
+ *     sorted by id) -> its edges with w <= threshold in the same order.
+ * *count always receives the edge count; TT_ERR_LENGTH when it exceeds cap
+ * (nothing copied: call again with a larger buffer). n <= 131072. */
+int tt_dense_redzed_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, float* thr_inout,
+                      float* mat_h, float* diam_h, int32_t* verts_h, uint64_t cap, uint64_t* count);
+int tt_graph_redzed_h(tt_ctx* ctx, const uint64_t* row_ptr_h, const uint32_t* col_h, const float* weight_h,
+                      uint32_t n, float threshold, float* diam_h, int32_t* verts_h, uint64_t cap, uint64_t* count);
 
 /* Reducer::assemble(1) (rips.hpp:981-1023) over the dense matrix mat_dev:
  * the dimension-2 columns generated from the sorted kept edges

@@ -68,6 +68,7 @@ _SIGS = {
     "tt_radius_graph": (i32, [P, P, u32, u32, i32, f32, f32, C.POINTER(CsrOut)]),
     "tt_mst_deaths": (i32, [P, P, u32, u32, i32, f32, P]),
     "tt_knn_graph_h": (i32, [P, P, u32, u32, i32, f32, u32, P, P, P, u64, C.POINTER(u64)]),
+    "tt_radius_graph_h": (i32, [P, P, u32, u32, i32, f32, f32, P, P, P, u64, C.POINTER(u64)]),
     "tt_assemble": (i32, [P, P, u32, f32, P, u64, P, u64, C.POINTER(u64), C.POINTER(P), C.POINTER(P),
                           C.POINTER(u64)]),
     "tt_persistence_h": (i32, [P, P, u32, u32, i32, f32, u32, f32, i32, u32, C.POINTER(C.POINTER(Barcode))]),
@@ -76,6 +77,8 @@ _SIGS = {
     "tt_knn_front": (i32, [P, P, u32, u32, i32, f32, u32, u32, C.POINTER(KnnFrontOut)]),
     "tt_knn_front_h": (i32, [P, P, u32, u32, i32, f32, u32, u32, P, P, P, u64, C.POINTER(u64), P,
                              C.POINTER(u64), C.POINTER(u64), P, P, P, P, u64, C.POINTER(u64), C.POINTER(u64)]),
+    "tt_dense_redzed_h": (i32, [P, P, u32, u32, i32, f32, C.POINTER(f32), P, P, P, u64, C.POINTER(u64)]),
+    "tt_graph_redzed_h": (i32, [P, P, P, P, u32, f32, P, P, u64, C.POINTER(u64)]),
     "tt_dense_front_h": (i32, [P, P, u32, u32, i32, f32, u32, C.POINTER(f32), P, P, C.POINTER(u64),
                                C.POINTER(u64), P, P, P, P, u64, C.POINTER(u64), C.POINTER(u64)]),
 }

@@ -389,6 +389,29 @@ int tt_knn_graph_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int ki
     });
 }
 
+int tt_radius_graph_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, float tau,
+                      uint64_t* rp_h, uint32_t* col_h, float* w_h, uint64_t cap, uint64_t* nnz_out) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (std::isnan(tau) || tau < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
+        if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
+        check_finite_dev(c, x, u64(n) * dim);
+        u64* rp = c->arena.get<u64>(S_OUT0, u64(n) + 1);
+        u32* ci = nullptr;
+        f32* w = nullptr;
+        const u64 nnz = radius_graph(c, x, n, dim, kind, p, tau, rp, &ci, &w);
+        if (nnz_out) *nnz_out = nnz;
+        if (nnz > cap) throw Error(TT_ERR_LENGTH, "gb300: graph exceeds the output capacity");
+        TT_CUDA(cudaMemcpyAsync(rp_h, rp, 8 * (u64(n) + 1), cudaMemcpyDeviceToHost, c->stream));
+        if (nnz) {
+            TT_CUDA(cudaMemcpyAsync(col_h, ci, 4 * nnz, cudaMemcpyDeviceToHost, c->stream));
+            TT_CUDA(cudaMemcpyAsync(w_h, w, 4 * nnz, cudaMemcpyDeviceToHost, c->stream));
+        }
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
 int tt_knn_front(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
                  uint32_t maxdim, tt_knn_front_out* out) {
     return guard(c, [&] {
@@ -522,6 +545,72 @@ int tt_dense_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int 
         if (essential) *essential = r.essential;
         if (ncols) *ncols = r.ncols;
         if (nedges) *nedges = r.m;
+    });
+}
+
+int tt_dense_redzed_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, float* thr_inout,
+                      float* mat_h, float* diam_h, int32_t* verts_h, uint64_t cap, uint64_t* count) {
+    return guard(c, [&] {
+        check_metric(kind, p);
+        if (!thr_inout || !count) invalid("gb300: null output");
+        const float t = *thr_inout;
+        if (std::isnan(t) || t < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
+        if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
+        check_finite_dev(c, x, u64(n) * dim);
+        f32* mat = c->arena.get<f32>(S_MAT, u64(n) * n + 1);
+        u32* rowmax = c->arena.get<u32>(S_ROWMAX, u64(n) + 1);
+        dense_matrix(c, x, n, dim, kind, p, mat, std::isinf(t) ? rowmax : nullptr);
+        float thr = t;
+        if (std::isinf(t) && n) {
+            min_bits(c, rowmax, n, rowmax + n);
+            u32 b = 0;
+            TT_CUDA(cudaMemcpyAsync(&b, rowmax + n, 4, cudaMemcpyDeviceToHost, c->stream));
+            TT_CUDA(cudaStreamSynchronize(c->stream));
+            thr = bitsf(b);
+        }
+        *thr_inout = thr;
+        f32* d = nullptr;
+        int32_t* v = nullptr;
+        const u64 m = n ? redzed_edges_owned(c, Complex{mat, nullptr, nullptr, nullptr, n, thr}, &d, &v) : 0;
+        *count = m;
+        if (mat_h && n)
+            TT_CUDA(cudaMemcpyAsync(mat_h, mat, sizeof(f32) * n * n, cudaMemcpyDeviceToHost, c->stream));
+        if (m > cap) {
+            TT_CUDA(cudaStreamSynchronize(c->stream));
+            throw Error(TT_ERR_LENGTH, "gb300: edge list exceeds the output capacity");
+        }
+        if (m && diam_h) TT_CUDA(cudaMemcpyAsync(diam_h, d, 4 * m, cudaMemcpyDeviceToHost, c->stream));
+        if (m && verts_h) TT_CUDA(cudaMemcpyAsync(verts_h, v, 8 * m, cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int tt_graph_redzed_h(tt_ctx* c, const uint64_t* rp_h, const uint32_t* ci_h, const float* w_h, uint32_t n,
+                      float thr, float* diam_h, int32_t* verts_h, uint64_t cap, uint64_t* count) {
+    return guard(c, [&] {
+        if (!count || (n && !rp_h)) invalid("gb300: null buffer");
+        if (std::isnan(thr) || thr < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        const u64 nnz = n ? rp_h[n] : 0;
+        u64* rp = c->arena.get<u64>(S_OUT0, u64(n) + 1);
+        u32* ci = c->arena.get<u32>(S_OUT1, nnz + 1);
+        f32* w = c->arena.get<f32>(S_OUT2, nnz + 1);
+        if (n) TT_CUDA(cudaMemcpyAsync(rp, rp_h, 8 * (u64(n) + 1), cudaMemcpyHostToDevice, c->stream));
+        if (nnz) {
+            TT_CUDA(cudaMemcpyAsync(ci, ci_h, 4 * nnz, cudaMemcpyHostToDevice, c->stream));
+            TT_CUDA(cudaMemcpyAsync(w, w_h, 4 * nnz, cudaMemcpyHostToDevice, c->stream));
+        }
+        f32* d = nullptr;
+        int32_t* v = nullptr;
+        const u64 m = n ? redzed_edges_owned(c, Complex{nullptr, rp, ci, w, n, thr}, &d, &v) : 0;
+        *count = m;
+        if (m > cap) {
+            TT_CUDA(cudaStreamSynchronize(c->stream));
+            throw Error(TT_ERR_LENGTH, "gb300: edge list exceeds the output capacity");
+        }
+        if (m && diam_h) TT_CUDA(cudaMemcpyAsync(diam_h, d, 4 * m, cudaMemcpyDeviceToHost, c->stream));
+        if (m && verts_h) TT_CUDA(cudaMemcpyAsync(verts_h, v, 8 * m, cudaMemcpyDeviceToHost, c->stream));
+        TT_CUDA(cudaStreamSynchronize(c->stream));
     });
 }
 

@@ -134,6 +134,7 @@ enum Slot : int {
     S_TC_KEY2, S_TC_VAL2, S_TC_CELL, S_TC_LO, S_TC_ERR, S_TC_SPV,
     S_EDGE_CNT, S_EDGE_SORT, S_EDGE_IDX, S_EDGE_INV,               // ordered edge generation
     S_GRAPH_LONG, S_GRAPH_CI, S_GRAPH_W,                           // kNN graph: long rows; its columns and weights
+    S_RZ_D, S_RZ_V,                                                // RedZeD edge lists sized to their count
     S_NSLOTS
 };
 

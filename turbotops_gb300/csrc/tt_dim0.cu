@@ -626,4 +626,20 @@ u64 redzed_edges(tt_ctx* c, const Complex& cx, f32* d, int32_t* verts, u64 cap) 
     return m;
 }
 
+// The same edge list in context-owned device arrays sized to its count
+// (slots S_RZ_D / S_RZ_V), for the host-buffer entry points.
+u64 redzed_edges_owned(tt_ctx* c, const Complex& cx, f32** d, int32_t** verts) {
+    if (cx.n > 131072) invalid("gb300: edge lists support n <= 131072 vertices");
+    u64* keys = nullptr;
+    const u64 m = sorted_edge_keys(c, cx, 1, &keys);
+    *d = c->arena.get<f32>(S_RZ_D, m + 1);
+    *verts = c->arena.get<int32_t>(S_RZ_V, 2 * m + 2);
+    if (m) {
+        k_emit_redzed<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, m, *d, *verts);
+        TT_LAUNCH("k_emit_redzed");
+        ++c->launches;
+    }
+    return m;
+}
+
 }  // namespace tt

@@ -86,6 +86,7 @@ struct Complex {
 void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out);
 // RedZeD EdgeList (d asc, comb asc): diam + vertex pairs (i < j).
 u64 redzed_edges(tt_ctx* c, const Complex& cx, f32* d, int32_t* verts, u64 cap);
+u64 redzed_edges_owned(tt_ctx* c, const Complex& cx, f32** d, int32_t** verts);
 
 // ---- tt_assemble.cu
 u64 assemble2(tt_ctx* c, const Complex& cx, const u64* keys, u64 m, const u64* piv_sorted, u64 npiv,
