@@ -380,6 +380,7 @@ def run_gpu(args, ws, rank, local):
     if rank == 0 and not args.no_extras:
         extras["batch"] = batch_block(ctx, dev)
         extras["topo"] = topo_block(dev)
+        extras["legs"] = legs_block(local, args.all_legs, not args.no_cpu)
 
     value = ws * 1000.0 / ms_step
     line = {
@@ -407,6 +408,50 @@ def run_gpu(args, ws, rank, local):
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def legs_block(index: int, all_legs: bool, with_reference: bool, reps: int = 3) -> dict:
+    """The other benchmark workloads end to end through the public API
+    (turbotops_gb300.persistence: host points in, whole diagram out — GPU
+    front end plus host reduction), each beside the unmodified reference's
+    own time for the same workload on this host's cores (one run of
+    oracle/_ref/refbench), with the SM clocks sampled during our runs.
+    Default: the 1000-point torus (maxdim 2), the 100k kNN complex (L2 and
+    lp:1.5, maxdim 1), its complete-graph H0 (maxdim 0); --all-legs adds the
+    3000-point lattice under L-inf (maxdim 2, ~80 s for the reference)."""
+    import numpy as np  # noqa: F401
+
+    from turbotops_gb300 import api, synth
+    legs = [("torus1000 full Rips l2 maxdim 2", synth.torus(), dict(maxdim=2), ("dense", "l2", 15, 2)),
+            ("gmm100k knn k=15 l2 maxdim 1", synth.gmm(), dict(maxdim=1, graph="knn", k=15),
+             ("knnwhole", "l2", 15, 1)),
+            ("gmm100k knn k=15 lp:1.5 maxdim 1", synth.gmm(), dict(maxdim=1, graph="knn", k=15, metric="lp:1.5"),
+             ("knnwhole", "lp:1.5", 15, 1)),
+            ("gmm100k complete-graph H0 l2 (maxdim 0)", synth.gmm(), dict(maxdim=0), ("mst", "l2", 15, 0))]
+    if all_legs:
+        legs.append(("lattice3000 full Rips linf maxdim 2", synth.lattice(), dict(maxdim=2, metric="linf"),
+                     ("dense", "linf", 15, 2)))
+    out = {}
+    for name, x, kw, ref in legs:
+        api.persistence(x, **kw)   # warm-up (buffers, kernels)
+        clocks = Clocks(index)
+        clocks.start()
+        ts, bars = [], 0
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            dgms, _ = api.persistence(x, **kw)
+            ts.append(time.perf_counter() - t0)
+            bars = sum(len(g) for g in dgms)
+        clk = clocks.stop()
+        leg = {"seconds": statistics.mean(ts), "diagrams_per_s": 1.0 / statistics.mean(ts), "bars": bars,
+               "steps": reps, "clocks": clk}
+        if with_reference and os.path.exists(REFBENCH):
+            r = ref_bench(ref[0], x, ref[1], ref[2], ref[3], 0, 1)
+            leg["reference"] = {"seconds": r["steps_s"][0], "cores": r["threads"], "stage": ref[0],
+                                "bars": r["check"], "same_bar_count": r["check"] == bars}
+            leg["speedup"] = r["steps_s"][0] / leg["seconds"]
+        out[name] = leg
+    return out
 
 
 def batch_block(ctx, dev, reps: int = 5) -> dict:
@@ -526,6 +571,7 @@ def main():
                     help="points (smaller only for profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / differentiable blocks")
+    ap.add_argument("--all-legs", action="store_true", help="also the lattice workload among the other legs")
     args = ap.parse_args()
     N = args.n
     ws, rank, local = dist_env()

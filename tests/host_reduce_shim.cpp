@@ -15,6 +15,10 @@
 // (the emergent test then runs on the host). Bars go to birth/death (at most
 // ncols each), pivots (ascending) to piv (at most ncols). Returns 0, or -1 on
 // an exception.
+// Host threads compute_pairs may use (0: every hardware thread).
+static unsigned g_threads = 0;
+extern "C" void hr_set_threads(unsigned t) { g_threads = t; }
+
 extern "C" int hr_compute_pairs(const float* mat, const uint64_t* rp, const uint32_t* ci, const float* w, uint32_t n,
                                 float thr, uint32_t dim, uint32_t maxdim, const uint64_t* cidx, const float* cd,
                                 uint64_t ncols, const uint64_t* em_idx, const uint8_t* em_app, float* birth,
@@ -31,7 +35,7 @@ extern "C" int hr_compute_pairs(const float* mat, const uint64_t* rp, const uint
         for (uint64_t i = 0; i < ncols; ++i) cols[i] = tt::host::Entry{cidx[i], cd[i]};
         std::vector<uint64_t> pv;
         tt::host::ReduceStats st;
-        const tt::host::Bars b = tt::host::compute_pairs(hc, dim, maxdim, cols, em_idx, em_app, pv, st);
+        const tt::host::Bars b = tt::host::compute_pairs(hc, dim, maxdim, cols, em_idx, em_app, pv, st, g_threads);
         for (size_t i = 0; i < b.birth.size(); ++i) {
             birth[i] = b.birth[i];
             death[i] = b.death[i];

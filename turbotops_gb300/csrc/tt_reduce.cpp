@@ -24,11 +24,16 @@
 #include "tt_reduce.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <limits>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 
 namespace tt {
 namespace host {
@@ -512,27 +517,26 @@ struct BucketQueue {
 
 namespace {
 
+// One column's reduction with its own working state (so that several run at
+// once): cols[c] is reduced, as compute_pairs does, until its pivot has no
+// owner in `pivots` and no zero-apparent facet (or the column cancels out),
+// reading the stored reductions (off / red) of the owners it meets. The
+// simplices it added are left in wr.
 template <class K>
-Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const std::vector<Entry>& cols,
-                    const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
-                    ReduceStats& st) {
-    const Cx cx{hc, B, {}, {}};
-    const uint32_t nv = dim + 1;
-    Bars bars;
-    PivotMap pivots(cols.size() + 16);
-    std::vector<uint64_t> off{0};
-    std::vector<Entry> red, wr;
+struct ColumnReducer {
+    const HostComplex& hc;
+    const Cx cx;
+    const uint32_t nv;
+    float dmax = 0;
+    uint32_t top_bits = 0;
     BucketQueue<K> wc;
-    // the largest diameter an entry can have: the threshold, else the largest
-    // distance of the complex
-    float dmax = hc.thr;
-    if (!(dmax < INFINITY)) {
-        dmax = 0;
-        const float* v = hc.mat ? hc.mat : hc.w;
-        const uint64_t m = hc.mat ? uint64_t(hc.n) * hc.n : (hc.n ? hc.rp[hc.n] : 0);
-        for (uint64_t i = 0; i < m; ++i)
-            if (v[i] < INFINITY) dmax = std::max(dmax, v[i]);
-    }
+    std::vector<Entry> owed, owed2, wr;
+    uint32_t vd[34];
+    uint32_t front = 0, grow = 1, owed_min = UINT32_MAX;
+
+    ColumnReducer(const HostComplex& h, const Binom& B, uint32_t dim, float dm)
+        : hc(h), cx{h, B, {}, {}}, nv(dim + 1), dmax(dm), top_bits(dbits(dm)) {}
+
     // Push frontier (dense complexes). Only cofacets whose diameter bits are
     // at most `front` go into the queue; a simplex with cofacets above it is
     // owed them, and owed_min is the smallest owed diameter. The queue's first
@@ -541,19 +545,16 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
     // the frontier moves past owed_min (by a width that doubles each time) and
     // the owed simplices push their cofacets in the new window. Most cofacets
     // of a column lie far beyond its pivot and are never pushed at all.
-    uint32_t vd[34];
-    uint32_t front = 0, grow = 1, owed_min = UINT32_MAX;
-    std::vector<Entry> owed, owed2;
-    auto push_window = [&](const Entry& s, uint32_t lo, std::vector<Entry>& still) {
+    void push_window(const Entry& s, uint32_t lo, std::vector<Entry>& still) {
         cx.decode(s.idx, nv, vd);
         const uint32_t a = cx.window_cofacets(vd, nv, s.d, hc.thr, lo, front, [&](const Entry& e) { wc.push(e); });
         if (a != UINT32_MAX) {
             still.push_back(s);
             owed_min = std::min(owed_min, a);
         }
-    };
-    auto push_coboundary = [&](const Entry& s) { push_window(s, 0, owed); };
-    auto get_pivot = [&]() {
+    }
+    void push_coboundary(const Entry& s) { push_window(s, 0, owed); }
+    Entry get_pivot() {
         for (;;) {
             const Entry p = wc.get_pivot();
             if (p.idx != kNone || owed.empty()) return p;
@@ -565,29 +566,28 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
             for (const Entry& s : owed) push_window(s, lo, owed2);
             owed.swap(owed2);
         }
-    };
-    const uint32_t top_bits = dbits(dmax);
-    for (uint64_t c = 0; c < cols.size(); ++c) {
+    }
+
+    // Returns the pivot (idx kNone: the column cancelled out, an essential
+    // class) and whether the emergent-pair shortcut paired it.
+    std::pair<Entry, bool> reduce(const std::vector<Entry>& cols, uint64_t c, const PivotMap& pivots,
+                                  const std::vector<uint64_t>& off, const std::vector<Entry>& red,
+                                  const uint64_t* em_idx, const uint8_t* em_app) {
         const Entry col = cols[c];
-        const float birth = col.d;
         wc.reset(col.d, dmax);
         wr.clear();
         owed.clear();
         owed_min = UINT32_MAX;
-        grow = std::max<uint32_t>(1, (top_bits > dbits(birth) ? top_bits - dbits(birth) : 0) >> TT_FRONT);
+        grow = std::max<uint32_t>(1, (top_bits > dbits(col.d) ? top_bits - dbits(col.d) : 0) >> TT_FRONT);
         // A graph complex pushes everything at once: a simplex has only its
         // common neighbours as cofacets, and a raise would repeat the row
         // walks that find them.
-        front = hc.mat ? dbits(birth) + grow : UINT32_MAX;
-        Entry pivot{kNone, 0};
-        bool emergent = false;
+        front = hc.mat ? dbits(col.d) + grow : UINT32_MAX;
         if (em_idx) {
             // GPU-supplied first zero cofacet and its zero-apparent-facet flag
-            if (em_idx[c] != kNone && !em_app[c] && pivots.find(em_idx[c]) == kNone) {
-                pivot = Entry{em_idx[c], col.d};
-                emergent = true;
-            }
-            if (!emergent) push_coboundary(col);
+            if (em_idx[c] != kNone && !em_app[c] && pivots.find(em_idx[c]) == kNone)
+                return {Entry{em_idx[c], col.d}, true};
+            push_coboundary(col);
         } else {
             // the first cofacet with the column's diameter pairs it when no
             // earlier column owns it and it has no zero-apparent facet;
@@ -595,31 +595,13 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
             uint32_t cv[34];
             cx.decode(col.idx, nv, vd);
             const uint64_t z = cx.zero_cofacet(vd, nv, col.d, cv);
-            if (z != kNone && pivots.find(z) == kNone && cx.zero_apparent_facet(Entry{z, col.d}, nv + 1).idx == kNone) {
-                pivot = Entry{z, col.d};
-                emergent = true;
-            } else {
-                push_coboundary(col);
-            }
+            if (z != kNone && pivots.find(z) == kNone && cx.zero_apparent_facet(Entry{z, col.d}, nv + 1).idx == kNone)
+                return {Entry{z, col.d}, true};
+            push_coboundary(col);
         }
-        if (emergent) {
-            ++st.emergent;
-        } else {
-            pivot = get_pivot();
-        }
-        bool fresh = emergent;
+        Entry pivot = get_pivot();
         for (;;) {
-            if (pivot.idx == kNone) {
-                bars.birth.push_back(birth);
-                bars.death.push_back(INFINITY);
-                bars.birth_idx.push_back(col.idx);
-                bars.death_idx.push_back(kNone);
-                break;
-            }
-            if (fresh) {
-                pivots.insert(pivot.idx, c);
-                break;
-            }
+            if (pivot.idx == kNone) return {pivot, false};
             const uint64_t j = pivots.find(pivot.idx);
             if (j != kNone) {
                 wr.push_back(cols[j]);
@@ -631,6 +613,9 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
                 pivot = get_pivot();
                 continue;
             }
+            // (a simplex with a zero-apparent facet is paired with that facet,
+            // so it is never an owned pivot: the order of the two tests above
+            // does not matter)
             const Entry fa = cx.zero_apparent_facet(pivot, nv + 1);
             if (fa.idx != kNone) {
                 wr.push_back(fa);
@@ -638,8 +623,120 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
                 pivot = get_pivot();
                 continue;
             }
-            if (pivot.d > birth) {
-                bars.birth.push_back(birth);
+            return {pivot, false};
+        }
+    }
+};
+
+// A column's reduction as one worker left it, waiting for its commit.
+struct Pending {
+    Entry pivot;
+    bool emergent = false;
+    std::vector<Entry> wr;
+};
+
+// Worker threads for the batch-parallel reduction: run(count, fn) calls
+// fn(worker, i) for every i < count, spread over the workers and the caller.
+struct Pool {
+    std::vector<std::thread> th;
+    std::mutex mu;
+    std::condition_variable cv, done_cv;
+    uint64_t gen = 0, count = 0;
+    std::atomic<uint64_t> next{0};
+    unsigned busy = 0;
+    bool quit = false;
+    std::function<void(unsigned, uint64_t)> fn;
+
+    explicit Pool(unsigned workers) {
+        for (unsigned w = 1; w <= workers; ++w)
+            th.emplace_back([this, w] {
+                uint64_t seen = 0;
+                for (;;) {
+                    {
+                        std::unique_lock<std::mutex> l(mu);
+                        cv.wait(l, [&] { return quit || gen != seen; });
+                        if (quit) return;
+                        seen = gen;
+                    }
+                    drain(w);
+                    std::lock_guard<std::mutex> l(mu);
+                    if (--busy == 0) done_cv.notify_one();
+                }
+            });
+    }
+    void drain(unsigned w) {
+        for (uint64_t i; (i = next.fetch_add(1, std::memory_order_relaxed)) < count;) fn(w, i);
+    }
+    template <typename F>
+    void run(uint64_t n, F&& f) {
+        {
+            std::lock_guard<std::mutex> l(mu);
+            fn = std::forward<F>(f);
+            count = n;
+            next.store(0, std::memory_order_relaxed);
+            busy = unsigned(th.size());
+            ++gen;
+        }
+        cv.notify_all();
+        drain(0);
+        std::unique_lock<std::mutex> l(mu);
+        done_cv.wait(l, [&] { return busy == 0; });
+    }
+    ~Pool() {
+        {
+            std::lock_guard<std::mutex> l(mu);
+            quit = true;
+        }
+        cv.notify_all();
+        for (auto& t : th) t.join();
+    }
+};
+
+// compute_pairs' loop over the columns, with the same pivots, stored
+// reductions and bars as the sequential algorithm.
+//
+// With several threads the columns go in batches. First every column of a
+// batch is reduced in parallel against the pivots of the columns before the
+// batch (read-only during the pass). Then the batch is committed in column
+// order: a column whose result names a pivot that an earlier column of the
+// same batch has just claimed (or whose emergent cofacet it claimed) is
+// reduced again, now against every pivot before it. This gives the sequential
+// result: until a reduction meets a simplex without an owner in the snapshot,
+// every lookup it makes has the answer the sequential algorithm gets (a
+// simplex has at most one owner, and one with a zero-apparent facet has
+// none); an essential result or an unclaimed pivot is therefore final. The
+// batch shrinks when such clashes are frequent and grows when they are rare.
+template <class K>
+Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const std::vector<Entry>& cols,
+                    const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
+                    ReduceStats& st, unsigned threads) {
+    Bars bars;
+    PivotMap pivots(cols.size() + 16);
+    std::vector<uint64_t> off{0};
+    std::vector<Entry> red;
+    // the largest diameter an entry can have: the threshold, else the largest
+    // distance of the complex
+    float dmax = hc.thr;
+    if (!(dmax < INFINITY)) {
+        dmax = 0;
+        const float* v = hc.mat ? hc.mat : hc.w;
+        const uint64_t m = hc.mat ? uint64_t(hc.n) * hc.n : (hc.n ? hc.rp[hc.n] : 0);
+        for (uint64_t i = 0; i < m; ++i)
+            if (v[i] < INFINITY) dmax = std::max(dmax, v[i]);
+    }
+    auto commit = [&](uint64_t c, const Entry& pivot, bool emergent, std::vector<Entry>& wr) {
+        const Entry col = cols[c];
+        if (pivot.idx == kNone) {
+            bars.birth.push_back(col.d);
+            bars.death.push_back(INFINITY);
+            bars.birth_idx.push_back(col.idx);
+            bars.death_idx.push_back(kNone);
+        } else if (emergent) {
+            ++st.emergent;
+            pivots.insert(pivot.idx, c);
+        } else {
+            if (pivot.d > col.d) {
+                bars.birth.push_back(col.d);
                 bars.death.push_back(pivot.d);
                 bars.birth_idx.push_back(col.idx);
                 bars.death_idx.push_back(pivot.idx);
@@ -650,9 +747,48 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
                 if (x + 1 < wr.size() && wr[x].idx == wr[x + 1].idx) x += 2;
                 else red.push_back(wr[x++]);
             }
-            break;
         }
         off.push_back(red.size());
+    };
+    std::vector<ColumnReducer<K>> workers;
+    workers.reserve(std::max(1u, threads));
+    workers.emplace_back(hc, B, dim, dmax);
+    if (threads <= 1) {
+        ColumnReducer<K>& w = workers[0];
+        for (uint64_t c = 0; c < cols.size(); ++c) {
+            const auto r = w.reduce(cols, c, pivots, off, red, em_idx, em_app);
+            commit(c, r.first, r.second, w.wr);
+        }
+    } else {
+        for (unsigned t = 1; t < threads; ++t) workers.emplace_back(hc, B, dim, dmax);
+        Pool pool(threads - 1);
+        std::vector<Pending> pend;
+        uint64_t batch = 256;
+        for (uint64_t c0 = 0; c0 < cols.size();) {
+            const uint64_t nb = std::min<uint64_t>(batch, cols.size() - c0);
+            if (pend.size() < nb) pend.resize(nb);
+            pool.run(nb, [&](unsigned w, uint64_t i) {
+                ColumnReducer<K>& r = workers[w];
+                const auto res = r.reduce(cols, c0 + i, pivots, off, red, em_idx, em_app);
+                pend[i].pivot = res.first;
+                pend[i].emergent = res.second;
+                pend[i].wr.swap(r.wr);
+            });
+            uint64_t clashes = 0;
+            for (uint64_t i = 0; i < nb; ++i) {
+                Pending& p = pend[i];
+                if (p.pivot.idx != kNone && pivots.find(p.pivot.idx) != kNone) {
+                    ++clashes;
+                    const auto res = workers[0].reduce(cols, c0 + i, pivots, off, red, em_idx, em_app);
+                    commit(c0 + i, res.first, res.second, workers[0].wr);
+                } else {
+                    commit(c0 + i, p.pivot, p.emergent, p.wr);
+                }
+            }
+            c0 += nb;
+            if (clashes * 16 > nb) batch = std::max<uint64_t>(32, batch / 2);
+            else if (clashes * 64 < nb) batch = std::min<uint64_t>(1u << 16, batch * 2);
+        }
     }
     st.columns = cols.size();
     pivot_list.clear();
@@ -666,12 +802,14 @@ Bars reduce_columns(const HostComplex& hc, const Binom& B, uint32_t dim, const s
 
 Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const std::vector<Entry>& cols,
                    const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivot_list,
-                   ReduceStats& st) {
+                   ReduceStats& st, unsigned threads) {
     const Binom B(hc.n, maxdim + 2);
+    // automatic: every hardware thread, for enough columns to pay for them
+    if (threads == 0) threads = cols.size() < 4096 ? 1u : std::max(1u, std::thread::hardware_concurrency());
     // every cofacet index below 2^32: the packed queue keys
     if (B(hc.n, dim + 2) <= (uint64_t(1) << 32))
-        return reduce_columns<PackedKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st);
-    return reduce_columns<WideKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st);
+        return reduce_columns<PackedKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st, threads);
+    return reduce_columns<WideKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st, threads);
 }
 
 namespace {

@@ -40,10 +40,12 @@ struct ReduceStats {
 // column-local part of the emergent-pair test may be supplied precomputed
 // (em_idx / em_app per column, UINT64_MAX = no zero cofacet); otherwise the
 // reducer evaluates it. Returns the bars; `pivots` receives the index of every
-// pivot (dimension-(dim+1) simplex) found.
+// pivot (dimension-(dim+1) simplex) found. `threads` host threads reduce
+// batches of columns in parallel (0: every hardware thread); the results do
+// not depend on it.
 Bars compute_pairs(const HostComplex& cx, uint32_t dim, uint32_t maxdim, const std::vector<Entry>& cols,
                    const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivots,
-                   ReduceStats& st);
+                   ReduceStats& st, unsigned threads = 0);
 
 // Triangles (dimension-2 simplices with diameter <= thr) of a graph complex
 // (hc.mat == nullptr), counted without storing them.

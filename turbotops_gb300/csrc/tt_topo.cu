@@ -174,7 +174,7 @@ extern "C" int tt_topo_forward(tt_ctx* c, const float* x, const uint32_t* sizes,
                     host::HostComplex hc{C.mat.data(), nullptr, nullptr, nullptr, C.n, C.thr};
                     std::vector<u64> piv;
                     host::ReduceStats st;
-                    C.bars = host::compute_pairs(hc, 1, 1, cols, C.emi.data(), C.emf.data(), piv, st);
+                    C.bars = host::compute_pairs(hc, 1, 1, cols, C.emi.data(), C.emf.data(), piv, st, 1);
                 }
             } catch (const std::exception& e) {
                 errs[t] = e.what();
