@@ -16,6 +16,7 @@
 //   tops::gb300::knn_graph_exact(PointCloud, k)         graph.hpp:211-225 + :286-304
 //   tops::gb300::mst_h0(PointCloud, threshold)          mst.hpp:25-99
 //   tops::gb300::redzed_dense / redzed_graph            redzed.hpp:1433-1460
+//   tops::gb300::persistence_batch(clouds, sizes, ...)  persistence() once per cloud
 //
 // Engines, as the reference's mode auto picks them (turbotops.hpp:121-162):
 // H1 of dense full Rips and of graphs of mean degree >= 16 goes to the
@@ -37,11 +38,14 @@
 #define TURBOTOPS_GB300_HPP
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <limits>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -337,6 +341,134 @@ inline CsrGraph radius_graph(const PointCloud& pc, f32 tau) {
     check(st, c);
     g.m = nnz / 2;
     return g;
+}
+
+// Whole diagrams of many dense full-Rips clouds (the reference runs
+// persistence(points, n, dim, Options) once per cloud; for maxdim 1 its mode
+// auto takes RedZeD, turbotops.hpp:121-162, :230-259): the batched GPU front
+// end computes every cloud's distance matrix, enclosing radius and sorted
+// edge list in one graph launch (tt_batch_*), then the reference's RedZeD
+// engine reduces the clouds on `threads` host threads (0: all), each fed with
+// its cloud's matrix and edge list. Each cloud is relabelled in k-d tree order
+// first, as the reference does. Other option sets run cloud by cloud through
+// persistence() above. clouds[q] points at sizes[q] x dim floats.
+struct BatchTiming {
+    double front_s = 0, copy_s = 0, reduce_s = 0;
+};
+inline std::vector<Result> persistence_batch(const std::vector<const f32*>& clouds, const std::vector<u32>& sizes,
+                                             u32 dim, const Options& o, u32 threads = 0,
+                                             BatchTiming* timing = nullptr) {
+    using clk = std::chrono::steady_clock;
+    auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    const size_t count = clouds.size();
+    std::vector<Result> out(count);
+    if (clouds.size() != sizes.size()) throw std::invalid_argument("persistence_batch: clouds and sizes differ");
+    tt_ctx* c = ctx();
+    int kind = 0;
+    float p = 2.0f;
+    check(tt_metric_parse(o.metric.c_str(), &kind, &p), nullptr);
+    std::string why;
+    const bool batched = count && o.graph == Options::Graph::Full && std::isinf(o.threshold) && o.maxdim == 1 &&
+                         detail::select_mode(o.mode, 2048, 1, INFINITY, why) == Engine::RedZeD;
+    if (!batched) {
+        for (size_t q = 0; q < count; ++q) out[q] = gb300::persistence(clouds[q], sizes[q], dim, o);
+        return out;
+    }
+    const Metric metric = Metric::minkowski(p);
+    // points, relabelled per cloud in k-d tree order, back to back
+    u64 total = 0;
+    for (u32 s : sizes) total += s;
+    std::vector<f32> pts(total * dim);
+    {
+        u64 at = 0;
+        for (size_t q = 0; q < count; ++q) {
+            const u32 n = sizes[q];
+            for (u64 i = 0; i < u64(n) * dim; ++i)
+                if (!std::isfinite(clouds[q][i])) throw std::invalid_argument("persistence: non-finite coordinate");
+            const PointCloud cloud{clouds[q], n, dim, metric};
+            const KdTree t(cloud);
+            for (u32 i = 0; i < n; ++i) std::copy_n(clouds[q] + u64(t.perm[i]) * dim, dim, pts.data() + (at + i) * dim);
+            at += n;
+        }
+    }
+    auto t0 = clk::now();
+    tt_batch* b = nullptr;
+    check(tt_batch_create(c, sizes.data(), u32(count), dim, kind, p, 1, &b), c);
+    struct Destroy {
+        tt_batch* b;
+        ~Destroy() { tt_batch_destroy(b); }
+    } guard{b};
+    check(tt_copy_async(c, tt_batch_points(b), pts.data(), sizeof(f32) * pts.size()), c);
+    check(tt_ctx_synchronize(c), c);
+    check(tt_batch_run(b, 1), c);
+    tt_batch_out bo;
+    check(tt_batch_result(b, &bo), c);
+    if (timing) timing->front_s = secs(t0);
+    t0 = clk::now();
+    std::vector<f32> radius(count);
+    std::vector<u64> eoff(count + 1);
+    check(tt_copy_async(c, radius.data(), bo.radius_dev, 4 * count), c);
+    check(tt_copy_async(c, eoff.data(), bo.edge_offset_dev, 8 * (count + 1)), c);
+    check(tt_ctx_synchronize(c), c);
+    std::vector<rips::DenseComplex> cx(count);
+    std::vector<redzed::detail::EdgeList> el(count);
+    {
+        u64 moff = 0;
+        for (size_t q = 0; q < count; ++q) {
+            const u32 n = sizes[q];
+            cx[q].n = n;
+            cx[q].full = true;
+            cx[q].threshold = radius[q];
+            cx[q].mat.resize(u64(n) * n);
+            check(tt_copy_async(c, cx[q].mat.data(), bo.mats_dev + moff, 4 * u64(n) * n), c);
+            moff += u64(n) * n;
+            const u64 m = eoff[q + 1] - eoff[q];
+            el[q].count = m;
+            el[q].diam.resize(m);
+            el[q].verts.resize(2 * m);
+            if (m) {
+                check(tt_copy_async(c, el[q].diam.data(), bo.diam_dev + eoff[q], 4 * m), c);
+                check(tt_copy_async(c, el[q].verts.data(), bo.verts_dev + 2 * eoff[q], 8 * m), c);
+            }
+        }
+        check(tt_ctx_synchronize(c), c);
+    }
+    if (timing) timing->copy_s = secs(t0);
+    t0 = clk::now();
+    // the clouds' reductions, largest first, on the host threads
+    std::vector<size_t> order(count);
+    for (size_t q = 0; q < count; ++q) order[q] = q;
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t bb) { return sizes[a] > sizes[bb]; });
+    std::atomic<size_t> next{0};
+    std::vector<std::string> errs;
+    std::mutex emu;
+    const u32 nt = std::max<u32>(1, std::min<u32>(threads ? threads : std::thread::hardware_concurrency(),
+                                                  u32(count)));
+    auto work = [&] {
+        for (size_t k; (k = next.fetch_add(1)) < count;) {
+            const size_t q = order[k];
+            try {
+                const auto tq = clk::now();
+                GpuEdgesDense geo(cx[q], &el[q]);
+                u64 edges = 0;
+                Result r = redzed_result(redzed::detail::run(geo, 1, cx[q].threshold, &edges), 1, "dense-redzed",
+                                         why, cx[q].threshold, edges);
+                r.stats.seconds_total = std::chrono::duration<double>(clk::now() - tq).count();
+                out[q] = std::move(r);
+                std::vector<f32>().swap(cx[q].mat);
+            } catch (const std::exception& e) {
+                std::lock_guard<std::mutex> l(emu);
+                errs.push_back(e.what());
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (u32 t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    if (!errs.empty()) throw std::runtime_error(errs[0]);
+    if (timing) timing->reduce_s = secs(t0);
+    return out;
 }
 
 // mst::h0 (mst.hpp:25-99): the H0 bars of the complete graph, deaths above

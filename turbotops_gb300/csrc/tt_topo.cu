@@ -161,6 +161,8 @@ extern "C" int tt_topo_forward(tt_ctx* c, const float* x, const uint32_t* sizes,
         std::vector<Cloud> cl(count);
         // host reducers (the calling thread joins them after the front end)
         u32 nt = threads > 0 ? u32(threads) : std::max(1u, std::thread::hardware_concurrency());
+        // threads beyond one per cloud go into each cloud's own reduction
+        const unsigned per_cloud = count ? std::max<u32>(1, nt / std::max<u32>(count, 1)) : 1;
         nt = std::min<u32>(nt, std::max<u32>(count, 1));
         CloudQueue queue(count);
         std::vector<std::string> errs(nt);
@@ -174,7 +176,7 @@ extern "C" int tt_topo_forward(tt_ctx* c, const float* x, const uint32_t* sizes,
                     host::HostComplex hc{C.mat.data(), nullptr, nullptr, nullptr, C.n, C.thr};
                     std::vector<u64> piv;
                     host::ReduceStats st;
-                    C.bars = host::compute_pairs(hc, 1, 1, cols, C.emi.data(), C.emf.data(), piv, st, 1);
+                    C.bars = host::compute_pairs(hc, 1, 1, cols, C.emi.data(), C.emf.data(), piv, st, per_cloud);
                 }
             } catch (const std::exception& e) {
                 errs[t] = e.what();
