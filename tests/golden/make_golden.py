@@ -10,6 +10,7 @@ read the committed fixtures; they never run this script.
     python tests/golden/make_golden.py --configs    # + checksums of the full workloads' front ends
     python tests/golden/make_golden.py --diagrams   # whole diagrams of the full workloads (minutes)
     python tests/golden/make_golden.py --a64 DIR    # aarch64-host Lp fixtures (run on that host)
+    python tests/golden/make_golden.py --higher     # diagrams above the benchmark dimensions
 """
 from __future__ import annotations
 
@@ -224,6 +225,34 @@ def graph_bars() -> None:
                                 bars=bars)
 
 
+def higher_dims() -> None:
+    """Diagrams beyond the benchmark's dimensions: dense full Rips up to
+    maxdim 3 and 4 (tops::persistence, refprobe "bars"), and flag complexes of
+    kNN and radius graphs up to maxdim 3 (the CLI, --graph knn / --threshold)."""
+    for name, x, metric, maxdim in [("u70", synth.uniform(70, 3, 41), "l2", 3),
+                                    ("g50", synth.gauss(50, 4, 42), "l1", 4),
+                                    ("torus150", synth.torus(150, 43), "l2", 3),
+                                    ("grid60", synth.grid(60, 3, 4, 44), "linf", 3)]:
+        save(f"bars_{name}_{metric}_{maxdim}", x, metric, "bars", {"maxdim": maxdim},
+             probe("bars", x, metric, str(maxdim)))
+    runs = [("knn400_l2_k10_d2", synth.circles(1, 400, 0.2, 45)[0], "l2", ["--graph", "knn", "-k", "10"], 2),
+            ("knn200_l1_k8_d3", synth.gauss(200, 3, 46), "l1", ["--graph", "knn", "-k", "8"], 3),
+            ("radius300_l2_t0p3_d2", synth.uniform(300, 3, 47), "l2", ["--threshold", "0.3"], 2),
+            ("radius120_linf_t1_d3", synth.grid(120, 3, 5, 48), "linf", ["--threshold", "1"], 3)]
+    with tempfile.TemporaryDirectory() as td:
+        for name, x, metric, args, maxdim in runs:
+            pts = os.path.join(td, "p.bin")
+            np.ascontiguousarray(x, np.float32).tofile(pts)
+            r = subprocess.run([CLI, "run", pts, "--dim", str(x.shape[1]), *args, "--metric", metric, "--maxdim",
+                                str(maxdim), "--quiet"], check=True, capture_output=True, text=True)
+            bars = np.array([[float(t) for t in line.split()] for line in r.stdout.splitlines()],
+                            np.float64).astype(np.float32).reshape(-1, 3)
+            np.savez_compressed(os.path.join(HERE, f"hbars_{name}.npz"), x=x, metric=np.array(metric),
+                                stage=np.array("hbars"),
+                                params=np.array(json.dumps({"args": args, "maxdim": maxdim})),
+                                bars=bars, text=np.array(r.stdout))
+
+
 def cli_text(x: np.ndarray, *args: str) -> tuple[str, float]:
     """The reference CLI's canonical diagram text for the points x (.bin input)."""
     with tempfile.TemporaryDirectory() as td:
@@ -325,11 +354,14 @@ if __name__ == "__main__":
     ap.add_argument("--diagrams", nargs="?", const="", default=None,
                     help="whole diagrams of the full workloads (optionally only names containing this)")
     ap.add_argument("--a64", metavar="DIR", help="only the aarch64 Lp fixtures, written to DIR")
+    ap.add_argument("--higher", action="store_true", help="only the higher-dimension diagrams")
     a = ap.parse_args()
     if not os.path.exists(PROBE):
         sys.exit("build the reference first: make -C oracle install-ref ref")
     if a.a64:
         a64(a.a64)
+    elif a.higher:
+        higher_dims()
     elif a.diagrams is not None:
         diagrams(a.diagrams or None)
     else:

@@ -81,3 +81,45 @@ extern "C" int hr_graph_pairs_dim1(const uint64_t* rp, const uint32_t* ci, const
         return -1;
     }
 }
+
+// The host assemble (tt_reduce.cpp assemble): the dimension-(dim + 1) columns
+// of `ns` dimension-dim simplices minus the ascending pivots; with nidx !=
+// NULL also every cofacet (the next dimension's simplices). Returns 0, -1 on
+// an exception, -2 when a buffer is too small (counts still written).
+extern "C" int hr_assemble(const float* mat, const uint64_t* rp, const uint32_t* ci, const float* w, uint32_t n,
+                           float thr, uint32_t dim, uint32_t maxdim, const uint64_t* sidx, const float* sd,
+                           uint64_t ns, const uint64_t* piv, uint64_t npiv, uint64_t* cidx, float* cd, uint64_t cap,
+                           uint64_t* ncols, uint64_t* nidx, float* nd, uint64_t ncap, uint64_t* nnext,
+                           uint64_t* napp) {
+    try {
+        tt::host::HostComplex hc;
+        hc.mat = mat;
+        hc.rp = rp;
+        hc.ci = ci;
+        hc.w = w;
+        hc.n = n;
+        hc.thr = thr;
+        std::vector<tt::host::Entry> simp(ns);
+        for (uint64_t i = 0; i < ns; ++i) simp[i] = tt::host::Entry{sidx[i], sd[i]};
+        std::vector<uint64_t> pv(piv, piv + npiv);
+        std::vector<tt::host::Entry> next;
+        uint64_t skipped = 0;
+        const std::vector<tt::host::Entry> cols =
+            tt::host::assemble(hc, dim, maxdim, simp, pv, nidx ? &next : nullptr, &skipped, g_threads);
+        *ncols = cols.size();
+        *nnext = next.size();
+        *napp = skipped;
+        if (cols.size() > cap || next.size() > ncap) return -2;
+        for (size_t i = 0; i < cols.size(); ++i) {
+            cidx[i] = cols[i].idx;
+            cd[i] = cols[i].d;
+        }
+        for (size_t i = 0; i < next.size(); ++i) {
+            nidx[i] = next[i].idx;
+            nd[i] = next[i].d;
+        }
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}

@@ -166,3 +166,18 @@ def test_scipy_sparse_input_and_csr_validation():
             api.persistence_graph(rp, ci, ww, len(rp) - 1, maxdim=1)
     with pytest.raises(ValueError, match="threshold must be non-negative"):
         api.persistence_graph(rp, ci, ww, 4, maxdim=1, threshold=-1.0)
+
+
+HBARS = cases("hbars")
+
+
+@pytest.mark.parametrize("c", HBARS, ids=ids(HBARS))
+def test_graph_input_higher_dims_vs_reference(c):
+    """kNN- and radius-graph flag complexes up to maxdim 3 through the public
+    API (GPU graph and dim0, host reduction and assemble): the reference
+    CLI's exact text."""
+    args, maxdim = c["params"]["args"], c["params"]["maxdim"]
+    kw = {"graph": "knn", "k": int(args[3])} if args[0] == "--graph" else {"threshold": float(np.float32(args[1]))}
+    dgms, info = tg.persistence(c["x"], maxdim=maxdim, metric=c["metric"], **kw)
+    from turbotops_gb300 import api
+    assert api.format_diagram(dgms) == str(c["text"])

@@ -30,6 +30,9 @@ def shim(tmp_path_factory):
     L = C.CDLL(so)
     P = C.c_void_p
     L.hr_set_threads.argtypes = [C.c_uint]
+    L.hr_assemble.restype = C.c_int
+    L.hr_assemble.argtypes = [P, P, P, P, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, P, P, C.c_uint64, P,
+                              C.c_uint64, P, P, C.c_uint64, P, P, P, C.c_uint64, P, P]
     L.hr_compute_pairs.restype = C.c_int
     L.hr_compute_pairs.argtypes = [P, P, P, P, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, P, P, C.c_uint64,
                                    P, P, P, P, P, P, P, P]
@@ -56,9 +59,64 @@ def reduce(L, mat, thr, dim, maxdim, cidx, cd, emi=None, emf=None):
     return birth[:b], death[:b], piv[: int(npv[0])], int(em[0])
 
 
+def _cx_args(cx):
+    """(mat, rp, ci, w, n) pointers for a dense matrix or ((rp, ci, w), n)."""
+    if isinstance(cx, tuple):
+        (rp, ci, w), n = cx
+        return None, _p(rp), _p(ci), _p(w), n
+    return _p(cx), None, None, None, cx.shape[0]
+
+
+def reduce_any(L, cx, thr, dim, maxdim, cidx, cd):
+    """compute_pairs(dim) (host emergent test) on a dense or CSR complex."""
+    cidx = np.ascontiguousarray(cidx, np.uint64)
+    cd = np.ascontiguousarray(cd, np.float32)
+    k = cidx.size
+    birth, death = np.empty(k + 1, np.float32), np.empty(k + 1, np.float32)
+    piv = np.empty(k + 1, np.uint64)
+    nb, npv, em = (np.zeros(1, np.uint64) for _ in range(3))
+    rc = L.hr_compute_pairs(*_cx_args(cx), float(thr), dim, maxdim, _p(cidx), _p(cd), k, None, None, _p(birth),
+                            _p(death), _p(nb), _p(piv), _p(npv), _p(em))
+    assert rc == 0
+    return birth[: int(nb[0])], death[: int(nb[0])], piv[: int(npv[0])]
+
+
+def host_assemble(L, cx, thr, dim, maxdim, sidx, sd, piv, want_next):
+    """The product's host assemble (tt_reduce.cpp) through the shim."""
+    sidx = np.ascontiguousarray(sidx, np.uint64)
+    sd = np.ascontiguousarray(sd, np.float32)
+    piv = np.ascontiguousarray(np.sort(piv), np.uint64)
+    cap = ncap = 1 << 16
+    while True:
+        ci_, cd_ = np.empty(cap, np.uint64), np.empty(cap, np.float32)
+        ni_, nd_ = np.empty(ncap, np.uint64), np.empty(ncap, np.float32)
+        nc, nn, na = (np.zeros(1, np.uint64) for _ in range(3))
+        rc = L.hr_assemble(*_cx_args(cx), float(thr), dim, maxdim, _p(sidx), _p(sd), sidx.size, _p(piv), piv.size,
+                           _p(ci_), _p(cd_), cap, _p(nc), _p(ni_) if want_next else None, _p(nd_), ncap, _p(nn),
+                           _p(na))
+        if rc == -2:
+            cap, ncap = max(cap, int(nc[0])), max(ncap, int(nn[0]))
+            continue
+        assert rc == 0
+        c, m = int(nc[0]), int(nn[0])
+        return ci_[:c], cd_[:c], ni_[:m], nd_[:m]
+
+
+def higher(L, cx, thr, maxdim, eidx, ed, piv):
+    """Dimensions 2..maxdim: host assemble then compute_pairs, per dimension."""
+    rows, sidx, sd = [], eidx, ed
+    for dim in range(1, maxdim):
+        ci_, cd_, ni_, nd_ = host_assemble(L, cx, thr, dim, maxdim, sidx, sd, piv, dim + 1 < maxdim)
+        b, d, piv = reduce_any(L, cx, thr, dim + 1, maxdim, ci_, cd_)
+        rows.append(np.column_stack([np.full(len(b), dim + 1, np.float32), b, d]))
+        sidx, sd = ni_, nd_
+    return rows
+
+
 def diagram(L, x, metric, maxdim, host_emergent=False):
     """tops::persistence on a dense cloud: threshold = enclosing radius,
-    dim0 H0, compute_pairs(1), assemble(1) + compute_pairs(2)."""
+    dim0 H0, compute_pairs(1), assemble(1) + compute_pairs(2) (the oracle's
+    assemble), and above dimension 2 the product's host assemble."""
     mat = O.dense(x, metric)
     thr = O.enclosing_radius(mat)
     r = O.dim0(mat=mat, thr=thr, maxdim=maxdim)
@@ -72,7 +130,9 @@ def diagram(L, x, metric, maxdim, host_emergent=False):
             emi, emf = e["emi"], e["emf"]
         b, d, piv, _ = reduce(L, mat, thr, 1, maxdim, r["cidx"], r["cd"], emi, emf)
         rows.append(np.column_stack([np.ones(len(b), np.float32), b, d]))
-        if maxdim >= 2:
+        if maxdim >= 3:
+            rows += higher(L, mat, thr, maxdim, r["eidx"], r["ed"], piv)
+        elif maxdim == 2:
             a = O.assemble(mat, thr, r["eidx"], r["ed"], piv)
             b2, d2, _, _ = reduce(L, mat, thr, 2, maxdim, a["c2idx"], a["c2d"])
             rows.append(np.column_stack([np.full(len(b2), 2, np.float32), b2, d2]))
@@ -324,3 +384,33 @@ def test_parallel_reduction_equals_sequential(shim, case):
                                   b.view(np.uint32) if b.dtype == np.float32 else b)
         else:
             assert a == b
+
+
+HBARS = cases("hbars")
+
+
+@pytest.mark.parametrize("c", HBARS, ids=ids(HBARS))
+def test_graph_higher_dims_vs_reference(shim, c):
+    """Flag complexes of kNN and radius graphs up to maxdim 3 (the reference
+    CLI's diagrams): the oracle's sparse dim0, then compute_pairs(1) and the
+    product's host assemble + compute_pairs for every higher dimension."""
+    x, metric, args, maxdim = c["x"], c["metric"], c["params"]["args"], c["params"]["maxdim"]
+    n = x.shape[0]
+    if args[0] == "--graph":
+        csr = O.knn_graph(x, metric, O.knn(x, metric, int(args[3])))
+        thr = np.float32(np.inf)
+    else:
+        thr = np.float32(args[1])
+        csr = O.radius_graph(x, metric, thr)
+    csr = tuple(np.ascontiguousarray(a) for a in csr)
+    r = O.dim0(csr=csr, n=n, thr=thr, maxdim=maxdim)
+    h0 = r["h0"].reshape(-1, 2)
+    rows = [np.column_stack([np.zeros(len(h0), np.float32), h0])]
+    b, d, piv = reduce_any(shim, (csr, n), thr, 1, maxdim, r["cidx"], r["cd"])
+    rows.append(np.column_stack([np.ones(len(b), np.float32), b, d]))
+    rows += higher(shim, (csr, n), thr, maxdim, r["eidx"], r["ed"], piv)
+    got = canonical(np.concatenate(rows).astype(np.float32))
+    got = got[got[:, 1] != got[:, 2]]
+    ref = canonical(c["bars"])
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))

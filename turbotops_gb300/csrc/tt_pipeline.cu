@@ -93,6 +93,35 @@ std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim,
     return piv;
 }
 
+// Dimensions 2 .. maxdim on the host, for any complex: assemble(dim)
+// (rips.hpp:981-1023) from every simplex of dimension dim (dimension 1: the
+// kept edges dim0 sorted on the device), then compute_pairs(dim + 1), as the
+// reference's Reducer::run (:1025-1031) alternates them. `piv` are the
+// dimension-1 pivots.
+void higher_dims(tt_ctx* c, const host::HostComplex& hc, const Dim0Out& r, std::vector<u64> piv, u32 maxdim,
+                 Result& out) {
+    const auto keys = to_host(c, r.keys, r.m);
+    sync(c);
+    std::vector<host::Entry> simp(r.m);
+    for (u64 i = 0; i < r.m; ++i) simp[i] = host::Entry{kIdxMask - (keys[i] & kIdxMask), bitsf(u32(keys[i] >> kIdxBits))};
+    for (u32 dim = 1; dim < maxdim; ++dim) {
+        std::vector<host::Entry> next;
+        u64 napp = 0;
+        std::sort(piv.begin(), piv.end());
+        const std::vector<host::Entry> cols =
+            host::assemble(hc, dim, maxdim, simp, piv, dim + 1 < maxdim ? &next : nullptr, &napp);
+        out.apparent.push_back(napp);
+        std::vector<u64> piv2;
+        host::ReduceStats st;
+        const host::Bars b = host::compute_pairs(hc, dim + 1, maxdim, cols, nullptr, nullptr, piv2, st);
+        for (u64 i = 0; i < b.birth.size(); ++i) out.add(dim + 1, b.birth[i], b.death[i]);
+        out.columns.push_back(st.columns);
+        out.emergent.push_back(st.emergent);
+        piv.swap(piv2);
+        simp.swap(next);
+    }
+}
+
 // Sparse front end on a device CSR graph (symmetric, rows sorted): dim0 on
 // the device, H0 bars, then compute_pairs(1) on the host over the host copy
 // of the graph (the caller's, or copied back here).
@@ -104,7 +133,6 @@ void sparse_tail(tt_ctx* c, u64* rp, u32* gci, f32* gw, const u64* hrp_in, const
     out.edges = r.m;
     h0_bars(c, r, out);
     if (maxdim == 0) return;
-    if (maxdim >= 2) invalid("gb300: maxdim 2 on graph input is not supported by the GPU front end");
     out.apparent.push_back(r.m - (n - r.essential) - r.ncols);
     std::vector<u64> hrp;
     std::vector<u32> hci;
@@ -117,7 +145,8 @@ void sparse_tail(tt_ctx* c, u64* rp, u32* gci, f32* gw, const u64* hrp_in, const
     }
     host::HostComplex hc{nullptr, hrp_in ? hrp_in : hrp.data(), hci_in ? hci_in : hci.data(),
                          hw_in ? hw_in : hw.data(), n, thr};
-    reduce_dim1(c, hc, maxdim, r, out);
+    std::vector<u64> piv = reduce_dim1(c, hc, maxdim, r, out);
+    if (maxdim >= 2) higher_dims(c, hc, r, std::move(piv), maxdim, out);
 }
 
 void check_points(const f32* x, u32 n, u32 dim) {
@@ -152,8 +181,6 @@ void persistence_points(tt_ctx* c, const f32* x_h, u32 n, u32 dim, int kind, f32
         for (u64 e = 0; e < essential; ++e) out.add(0, 0.0f, INFINITY);
         return;
     }
-    if (maxdim > 2) invalid("gb300: the GPU front end supports maxdim <= 2");
-
     if (!knn && std::isinf(thr)) {   // dense full Rips cut at the enclosing radius
         out.method = "dense";
         f32* mat = c->arena.get<f32>(S_MAT, u64(n) * n + 1);
@@ -179,8 +206,14 @@ void persistence_points(tt_ctx* c, const f32* x_h, u32 n, u32 dim, int kind, f32
         const auto hm = to_host(c, mat, u64(n) * n);
         sync(c);
         host::HostComplex hc{hm.data(), nullptr, nullptr, nullptr, n, t};
-        const std::vector<u64> piv = reduce_dim1(c, hc, maxdim, r, out);
+        std::vector<u64> piv = reduce_dim1(c, hc, maxdim, r, out);
         if (maxdim < 2) return;
+        // the device assembles dimension 2 (C(n, 3) < 2^33, n <= 3740);
+        // higher dimensions, or larger clouds, go through the host assemble
+        if (maxdim > 2 || n > 3740) {
+            higher_dims(c, hc, r, std::move(piv), maxdim, out);
+            return;
+        }
         u64* pd = c->arena.get<u64>(S_PIV, piv.size() + 1);
         if (!piv.empty())
             TT_CUDA(cudaMemcpyAsync(pd, piv.data(), 8 * piv.size(), cudaMemcpyHostToDevice, c->stream));
@@ -265,7 +298,6 @@ void persistence_graph(tt_ctx* c, const u64* rp_h, const u32* ci_h, const f32* w
         }
     }
     if (!ok) invalid("persistence: CsrGraph invariant violated (see CsrGraph::valid)");
-    if (maxdim > 2) invalid("gb300: the GPU front end supports maxdim <= 2");
     out.ensure(maxdim);
     out.method = "sparse";
     out.threshold = thr;

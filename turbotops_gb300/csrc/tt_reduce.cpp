@@ -290,6 +290,17 @@ struct Cx {
         return kNone;
     }
 
+    // zero_apparent_cofacet_v / zero_apparent_facet_v (rips.hpp:637-648) of
+    // the simplex s with vertices vd (nv, descending): is s in a zero-apparent
+    // pair, as the cofacet's facet or as the facet's cofacet?
+    bool in_zero_apparent_pair(const uint32_t* vd, uint32_t nv, const Entry& s) const {
+        uint32_t cv[34], fv[34], gv[34];
+        const uint64_t c = zero_cofacet(vd, nv, s.d, cv);
+        if (c != kNone && zero_facet(cv, nv + 1, s.d, gv) == s.idx) return true;
+        const uint64_t f = zero_facet(vd, nv, s.d, fv);
+        return f != kNone && zero_cofacet(fv, nv - 1, s.d, gv) == s.idx;
+    }
+
     // zero_apparent_facet: the zero facet whose zero cofacet is s
     Entry zero_apparent_facet(const Entry& s, uint32_t nv) const {
         uint32_t vd[34], fv[34], cv[34];
@@ -810,6 +821,66 @@ Bars compute_pairs(const HostComplex& hc, uint32_t dim, uint32_t maxdim, const s
     if (B(hc.n, dim + 2) <= (uint64_t(1) << 32))
         return reduce_columns<PackedKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st, threads);
     return reduce_columns<WideKey>(hc, B, dim, cols, em_idx, em_app, pivot_list, st, threads);
+}
+
+std::vector<Entry> assemble(const HostComplex& hc, uint32_t dim, uint32_t maxdim,
+                            const std::vector<Entry>& simplices, const std::vector<uint64_t>& pivots_sorted,
+                            std::vector<Entry>* next, uint64_t* skipped, unsigned threads) {
+    const Binom B(hc.n, maxdim + 2);
+    const uint32_t nv = dim + 1;
+    if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
+    threads = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(threads, simplices.size() / 256 + 1)));
+    std::vector<std::vector<Entry>> cols(threads), nexts(threads);
+    std::vector<uint64_t> skip(threads, 0);
+    std::vector<std::string> errs(threads);
+    auto work = [&](unsigned t) {
+        try {
+            const Cx cx{hc, B, {}, {}};
+            uint32_t vd[34], cv[34];
+            const uint64_t lo = simplices.size() * t / threads, hi = simplices.size() * (t + 1) / threads;
+            for (uint64_t s = lo; s < hi; ++s) {
+                cx.decode(simplices[s].idx, nv, vd);
+                // the cofacets through a vertex above the simplex's largest
+                // (t == 0): every simplex of the next dimension exactly once
+                cx.cofacets(vd, nv, simplices[s].d, hc.thr, [&](const Entry& cf, uint32_t w, uint32_t tt) {
+                    if (tt > 0) return false;
+                    if (next) nexts[t].push_back(cf);
+                    if (std::binary_search(pivots_sorted.begin(), pivots_sorted.end(), cf.idx)) return true;
+                    cv[0] = w;
+                    for (uint32_t i = 0; i < nv; ++i) cv[i + 1] = vd[i];
+                    if (cx.in_zero_apparent_pair(cv, nv + 1, cf)) {
+                        ++skip[t];
+                        return true;
+                    }
+                    cols[t].push_back(cf);
+                    return true;
+                });
+            }
+        } catch (const std::exception& e) {
+            errs[t] = e.what();
+        }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < threads; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool) th.join();
+    for (const auto& e : errs)
+        if (!e.empty()) throw std::runtime_error(e);
+    std::vector<Entry> out;
+    uint64_t total = 0;
+    for (const auto& v : cols) total += v.size();
+    out.reserve(total);
+    for (const auto& v : cols) out.insert(out.end(), v.begin(), v.end());
+    std::sort(out.begin(), out.end(), [](const Entry& a, const Entry& b) { return precedes(b, a); });
+    if (next) {
+        next->clear();
+        for (const auto& v : nexts) next->insert(next->end(), v.begin(), v.end());
+    }
+    if (skipped) {
+        *skipped = 0;
+        for (uint64_t x : skip) *skipped += x;
+    }
+    return out;
 }
 
 namespace {

@@ -47,6 +47,17 @@ Bars compute_pairs(const HostComplex& cx, uint32_t dim, uint32_t maxdim, const s
                    const uint64_t* em_idx, const uint8_t* em_app, std::vector<uint64_t>& pivots,
                    ReduceStats& st, unsigned threads = 0);
 
+// Reducer::assemble(dim) (rips.hpp:981-1023): the dimension-(dim + 1)
+// columns — every cofacet of the dimension-dim `simplices` (any order) through
+// a vertex above the simplex's largest, so each once; neither a pivot of
+// dimension dim (`pivots_sorted`, ascending) nor in a zero-apparent pair —
+// in descending filtration order. With `next`, every such cofacet: the
+// simplices of the following dimension. *skipped receives the apparent
+// count. `threads` host threads (0: all) split the simplices.
+std::vector<Entry> assemble(const HostComplex& hc, uint32_t dim, uint32_t maxdim,
+                            const std::vector<Entry>& simplices, const std::vector<uint64_t>& pivots_sorted,
+                            std::vector<Entry>* next, uint64_t* skipped, unsigned threads = 0);
+
 // Triangles (dimension-2 simplices with diameter <= thr) of a graph complex
 // (hc.mat == nullptr), counted without storing them.
 uint64_t graph_triangles(const HostComplex& hc);
