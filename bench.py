@@ -514,6 +514,12 @@ def batch_block(ctx, dev, reps: int = 5) -> dict:
     b.run()   # capture
     out = capi.BatchOut()
     ctx.check(ctx.L.tt_batch_result(b.h, C.byref(out)))
+    tr, tc_, ns, fc = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_int()
+    tms = (C.c_float * 8)()
+    ctx.check(ctx.L.tt_batch_tuning(b.h, C.byref(tr), C.byref(tc_), tms, C.byref(ns), C.byref(fc)))
+    tuning = {"tile": [tr.value, tc_.value], "from_cache": bool(fc.value),
+              "candidates_ms": {"x".join(map(str, s)): round(tms[i], 4)
+                                for i, s in enumerate([(16, 64), (32, 64), (64, 64), (32, 128), (64, 128)][:ns.value])}}
     bs = torch.cuda.ExternalStream(out.stream, device=dev)
     ms = []
     for _ in range(reps):
@@ -557,7 +563,23 @@ def batch_block(ctx, dev, reps: int = 5) -> dict:
             "batched_diagrams_per_s": len(sizes) * 1000.0 / batch_ms, "per_cloud_ms": plain_ms,
             "per_cloud_diagrams_per_s": len(sizes) * 1000.0 / plain_ms,
             "batched_over_per_cloud": plain_ms / batch_ms,
-            "hbm_bytes_written_matrices": 4 * sum(n * n for n in sizes)}
+            "hbm_bytes_written_matrices": 4 * sum(n * n for n in sizes), "autotuner": tuning,
+            "hbm": batch_traffic(sizes, edges, batch_ms)}
+
+
+def batch_traffic(sizes, edges: int, ms: float) -> dict:
+    """Algorithmic HBM bytes of one batched run: the matrices written (4 B a
+    pair, full layout) and their lower triangles read twice (count, keys),
+    the kept keys written once and moved by 4 stable radix passes (read for
+    the histogram, read and written by the scatter: 24 B an edge a pass), the
+    edge list emitted (8 B key read, 12 B written)."""
+    pk, src = peaks()
+    mat = 4 * sum(n * n for n in sizes)
+    tri = 4 * sum(n * (n - 1) // 2 for n in sizes)
+    b = mat + 2 * tri + 8 * edges + 4 * 24 * edges + 20 * edges
+    gbs = b / (ms * 1e-3) / 1e9
+    return {"algorithmic_bytes": b, "achieved_gbs": gbs, "peak_gbs": pk["hbm_gbs"], "frac": gbs / pk["hbm_gbs"],
+            "peak_source": src}
 
 
 def topo_block(dev, reps: int = 2) -> dict:

@@ -275,6 +275,14 @@ float* tt_batch_points(tt_batch* b);
 int tt_batch_run(tt_batch* b, int wait);
 int tt_batch_result(tt_batch* b, tt_batch_out* out);
 void tt_batch_destroy(tt_batch* b);
+/* The autotuner's pick, no reference counterpart: the first run of a batch
+ * times every distance-tile shape on its points (the pick is cached per
+ * metric, dimension and size class) and keeps the fastest. tile_rows x
+ * tile_cols is the shape in use; shape_ms (room for 8) the time of each
+ * candidate's pass (0 where the pick came from the cache, *from_cache = 1);
+ * *shapes the number of candidates. Valid after the first tt_batch_run. */
+int tt_batch_tuning(tt_batch* b, uint32_t* tile_rows, uint32_t* tile_cols, float* shape_ms, uint32_t* shapes,
+                    int* from_cache);
 
 /* ---- Differentiable persistence (no counterpart in the reference) ----
  * tt_topo_forward: for clouds stored back to back in x_dev (sizes[q] points

@@ -12,14 +12,23 @@
 //                   from one work list (uneven clouds balance themselves) and
 //                   fold row maxima
 //   k_batch_radius  per-cloud minimum of the row maxima
-//   k_batch_edges   kept edges of every cloud as 64-bit keys
+//   k_batch_rowcount + scan   kept pairs per row and their offsets (the
+//                   total kept count stays on the device)
+//   k_batch_edges   the kept edges of every cloud, compacted, as 64-bit keys
 //                     cloud << (31 + ib) | d bits << ib | index
-//                   so one radix sort orders all clouds at once
+//                   in (cloud, index) order, so one stable radix sort of the
+//                   bits above the index field (cloud and d: 40 bits for 512
+//                   clouds, four passes) orders all clouds at once by
+//                   (cloud, d, index); the sort reads its key count from the
+//                   device and skips the tiles beyond it
 //   k_batch_emit    EdgeList (diameter, vertex pair) + per-cloud offsets
-// Buffers are sized for the worst case (every pair kept; unused keys are
-// all-ones and sort last), so no step reads a count back to the host and
-// the whole sequence is captured into a CUDA graph once and replayed.
+// Buffers are sized for the worst case (every pair kept), so no step reads a
+// count back to the host and the whole sequence is captured into a CUDA
+// graph once and replayed.
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "tt_internal.cuh"
@@ -29,17 +38,26 @@ namespace tt {
 
 namespace {
 
-constexpr int BT_R = 32, BT_C = 64, BT_Y = 4;
+// Distance tiles of BT_R rows x BT_C columns, 256 threads (BT_C x 256 / BT_C);
+// the shape is picked per batch by the autotuner below.
+constexpr int BT_THREADS = 256;
+struct TileShape {
+    int r, c;
+};
+constexpr TileShape kShapes[] = {{16, 64}, {32, 64}, {64, 64}, {32, 128}, {64, 128}};
+constexpr int kNumShapes = int(sizeof(kShapes) / sizeof(kShapes[0]));
 
 struct Tile {
     u32 cloud, i0, j0;
 };
 
-template <int KIND>
-__global__ void __launch_bounds__(BT_C* BT_Y)
+template <int KIND, int BT_R, int BT_C>
+__global__ void __launch_bounds__(BT_THREADS)
 k_batch_dense(const f32* __restrict__ x, const u64* __restrict__ pt_off, const u64* __restrict__ mat_off,
               const u32* __restrict__ sizes, const Tile* __restrict__ tiles, u32 ntiles, u32 dim, f32 p,
               f32* __restrict__ mats, u32* __restrict__ rowmax, u32* __restrict__ next) {
+    constexpr int BT_Y = BT_THREADS / BT_C;
+    static_assert(BT_C % 32 == 0 && BT_R <= BT_THREADS, "warps span whole tile rows");
     __shared__ u32 smax[BT_R];
     __shared__ u32 tile_id;
     const u32 tx = threadIdx.x, ty = threadIdx.y, tid = ty * BT_C + tx;
@@ -94,15 +112,37 @@ __global__ void k_batch_radius(const u32* __restrict__ rowmax, const u32* __rest
     }
 }
 
-// One warp per row of one cloud (rows listed globally).
-// Every pair (c, i, j), j < i, owns key slot pair_off[c] + i (i - 1) / 2 + j:
-// a kept pair writes its key there (coalesced, no shared counter), the rest
-// keep the all-ones fill and sort last.
+// Kept pairs (j < i, d <= the cloud's radius) per row: one warp per row of
+// one cloud (rows listed globally), the count into row_cnt.
+__global__ void k_batch_rowcount(const f32* __restrict__ mats, const u64* __restrict__ mat_off,
+                                 const u32* __restrict__ sizes, const u64* __restrict__ pt_off,
+                                 const u32* __restrict__ row_cloud, u64 rows, const u32* __restrict__ radius,
+                                 u64* __restrict__ row_cnt) {
+    const int lane = threadIdx.x & 31;
+    const u64 warps = (u64(gridDim.x) * blockDim.x) >> 5;
+    for (u64 r = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < rows; r += warps) {
+        const u32 c = row_cloud[r];
+        const u32 n = sizes[c];
+        const u32 i = u32(r - pt_off[c]);
+        const f32 thr = __uint_as_float(radius[c]);
+        const f32* row = mats + mat_off[c] + u64(i) * n;
+        u64 kept = 0;
+        for (u32 j0 = 0; j0 < i; j0 += 32) {
+            const u32 j = j0 + lane;
+            kept += __popc(__ballot_sync(0xffffffffu, j < i && row[j] <= thr));
+        }
+        if (lane == 0) row_cnt[r] = kept;
+    }
+}
+
+// The kept pairs written compacted, at row_off[row] + rank in the row: the
+// array runs over (cloud, index) ascending (rows ascending, j ascending in a
+// row), so a stable sort on the bits above the index field alone orders it
+// by (cloud, d, index). Key: cloud << (31 + ib) | d bits << ib | index.
 __global__ void k_batch_edges(const f32* __restrict__ mats, const u64* __restrict__ mat_off,
-                              const u64* __restrict__ pair_off, const u32* __restrict__ sizes,
-                              const u64* __restrict__ pt_off, const u32* __restrict__ row_cloud, u64 rows,
-                              const u32* __restrict__ radius, int ib, u64* __restrict__ keys,
-                              u64* __restrict__ per_cloud) {
+                              const u32* __restrict__ sizes, const u64* __restrict__ pt_off,
+                              const u32* __restrict__ row_cloud, u64 rows, const u32* __restrict__ radius, int ib,
+                              const u64* __restrict__ row_off, u64* __restrict__ keys, u64* __restrict__ per_cloud) {
     const int lane = threadIdx.x & 31;
     const u64 warps = (u64(gridDim.x) * blockDim.x) >> 5;
     for (u64 r = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < rows; r += warps) {
@@ -112,23 +152,24 @@ __global__ void k_batch_edges(const f32* __restrict__ mats, const u64* __restric
         const f32 thr = __uint_as_float(radius[c]);
         const f32* row = mats + mat_off[c] + u64(i) * n;
         const u64 rbase = u64(i) * (i - 1) / 2;
-        u64* slots = keys + pair_off[c] + rbase;
-        u64 kept = 0;
+        u64 pos = row_off[r];
         for (u32 j0 = 0; j0 < i; j0 += 32) {
             const u32 j = j0 + lane;
             const f32 d = j < i ? row[j] : INFINITY;
             const bool keep = j < i && d <= thr;
-            kept += __popc(__ballot_sync(0xffffffffu, keep));
-            if (keep) slots[j] = (u64(c) << (31 + ib)) | (u64(__float_as_uint(d)) << ib) | (rbase + j);
+            const u32 bal = __ballot_sync(0xffffffffu, keep);
+            if (keep)
+                keys[pos + __popc(bal & ((1u << lane) - 1u))] =
+                    (u64(c) << (31 + ib)) | (u64(__float_as_uint(d)) << ib) | (rbase + j);
+            pos += __popc(bal);
         }
+        const u64 kept = pos - row_off[r];
         if (lane == 0 && kept) atomicAdd((unsigned long long*)&per_cloud[c], (unsigned long long)kept);
     }
 }
 
-// Exclusive scan of the per-cloud edge counts (one CTA; clouds <= 65536);
-// *count = all kept edges.
-__global__ void k_batch_offsets(const u64* __restrict__ per_cloud, u32 clouds, u64* __restrict__ off,
-                                unsigned long long* __restrict__ count) {
+// Exclusive scan of the per-cloud edge counts (one CTA; clouds <= 65536).
+__global__ void k_batch_offsets(const u64* __restrict__ per_cloud, u32 clouds, u64* __restrict__ off) {
     __shared__ u64 part[1024];
     const u32 t = threadIdx.x;
     const u32 per = (clouds + blockDim.x - 1) / blockDim.x;
@@ -150,10 +191,7 @@ __global__ void k_batch_offsets(const u64* __restrict__ per_cloud, u32 clouds, u
         off[c] = run;
         run += per_cloud[c];
     }
-    if (t == blockDim.x - 1) {
-        off[clouds] = run;
-        *count = run;
-    }
+    if (t == blockDim.x - 1) off[clouds] = run;
 }
 
 __global__ void k_batch_emit(const u64* __restrict__ keys, const unsigned long long* __restrict__ count, int ib,
@@ -180,7 +218,6 @@ struct Batch {
     f32 p = 2.0f;
     int ib = 0;
     u64 total_pts = 0, total_mat = 0, total_pairs = 0;
-    u32 ntiles = 0;
     // device buffers (one cudaMalloc each, owned)
     f32* x = nullptr;
     f32* mats = nullptr;
@@ -190,10 +227,17 @@ struct Batch {
     u64* mat_off = nullptr;
     u64* pair_off = nullptr;   // first key slot of every cloud's pairs
     u32* sizes = nullptr;
-    Tile* tiles = nullptr;
+    Tile* tiles[kNumShapes] = {};
+    u32 ntiles[kNumShapes] = {};
+    int shape = 1;                      // index into kShapes
+    bool tuned = false, tuned_from_cache = false;
+    float tune_ms[kNumShapes] = {};
     u32* row_cloud = nullptr;
     u32* next = nullptr;
     u64* keys = nullptr;
+    u64* kbuf = nullptr;       // the sort's other buffer
+    u64* row_cnt = nullptr;    // kept pairs per row, then their exclusive scan
+    u64* row_off = nullptr;
     unsigned long long* count = nullptr;
     u64* per_cloud = nullptr;
     u64* edge_off = nullptr;
@@ -201,6 +245,7 @@ struct Batch {
     int32_t* ev = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    u64 graph_kernels = 0;   // kernels one run launches
     bool use_graph = true;
     std::vector<void*> owned;
 
@@ -216,6 +261,80 @@ struct Batch {
         return static_cast<T*>(p);
     }
 
+    template <int R, int C>
+    void launch_dense_rc(int si, cudaStream_t s) {
+        const dim3 blk(C, BT_THREADS / C);
+        const u32 nt = ntiles[si];
+        const u32 grid = u32(std::min<u64>(nt, u64(owner->sms) * 8));
+        const Tile* tl = tiles[si];
+        switch (kind) {
+            case M_L1: k_batch_dense<M_L1, R, C><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            case M_L2: k_batch_dense<M_L2, R, C><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            case M_LINF: k_batch_dense<M_LINF, R, C><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            default: k_batch_dense<M_LP, R, C><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+        }
+        TT_LAUNCH("k_batch_dense");
+    }
+    void launch_dense(int si, cudaStream_t s) {
+        switch (si) {
+            case 0: launch_dense_rc<16, 64>(si, s); break;
+            case 1: launch_dense_rc<32, 64>(si, s); break;
+            case 2: launch_dense_rc<64, 64>(si, s); break;
+            case 3: launch_dense_rc<32, 128>(si, s); break;
+            default: launch_dense_rc<64, 128>(si, s); break;
+        }
+    }
+
+    // The autotuner: every tile shape times the distance pass once on this
+    // batch (CUDA events on the batch's stream, after one untimed pass that
+    // loads the kernels); the fastest serves every later run. The pick is
+    // cached per (metric, dimension, cloud count, size classes), so later
+    // batches of the same kind skip the timing.
+    void tune() {
+        static std::mutex mu;
+        static std::map<std::string, int> cache;
+        std::string key = std::to_string(kind) + "/" + std::to_string(dim) + "/" + std::to_string(clouds) + "/" +
+                          std::to_string(maxn >> 6) + "/" + std::to_string(total_pts >> 12);
+        {
+            std::lock_guard<std::mutex> l(mu);
+            auto it = cache.find(key);
+            if (it != cache.end()) {
+                shape = it->second;
+                tuned_from_cache = true;
+                return;
+            }
+        }
+        cudaStream_t s = sctx.stream;
+        cudaEvent_t e0, e1;
+        TT_CUDA(cudaEventCreate(&e0));
+        TT_CUDA(cudaEventCreate(&e1));
+        float best = 0;
+        int pick = 1;
+        for (int si = 0; si < kNumShapes; ++si) {
+            for (int rep = 0; rep < 2; ++rep) {
+                TT_CUDA(cudaMemsetAsync(rowmax, 0, total_pts * sizeof(u32), s));
+                TT_CUDA(cudaMemsetAsync(next, 0, sizeof(u32), s));
+                TT_CUDA(cudaEventRecord(e0, s));
+                launch_dense(si, s);
+                TT_CUDA(cudaEventRecord(e1, s));
+                sctx.launches += 1;
+            }
+            TT_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            TT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            tune_ms[si] = ms;
+            if (si == 0 || ms < best) {
+                best = ms;
+                pick = si;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        shape = pick;
+        std::lock_guard<std::mutex> l(mu);
+        cache[key] = pick;
+    }
+
     void enqueue() {
         cudaStream_t s = sctx.stream;
         TT_CUDA(cudaMemsetAsync(rowmax, 0, total_pts * sizeof(u32), s));
@@ -223,30 +342,28 @@ struct Batch {
         TT_CUDA(cudaMemsetAsync(next, 0, sizeof(u32), s));
         TT_CUDA(cudaMemsetAsync(count, 0, sizeof(unsigned long long), s));
         TT_CUDA(cudaMemsetAsync(per_cloud, 0, clouds * sizeof(u64), s));
-        TT_CUDA(cudaMemsetAsync(keys, 0xff, total_pairs * sizeof(u64), s));
-        const dim3 blk(BT_C, BT_Y);
-        const u32 grid = u32(std::min<u64>(ntiles, u64(owner->sms) * 8));
-        switch (kind) {
-            case M_L1: k_batch_dense<M_L1><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tiles, ntiles, dim, p, mats, rowmax, next); break;
-            case M_L2: k_batch_dense<M_L2><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tiles, ntiles, dim, p, mats, rowmax, next); break;
-            case M_LINF: k_batch_dense<M_LINF><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tiles, ntiles, dim, p, mats, rowmax, next); break;
-            default: k_batch_dense<M_LP><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tiles, ntiles, dim, p, mats, rowmax, next); break;
-        }
-        TT_LAUNCH("k_batch_dense");
+        launch_dense(shape, s);
+
         const u32 g2 = u32(std::min<u64>((total_pts + 255) / 256, u64(owner->sms) * 16));
         k_batch_radius<<<g2, 256, 0, s>>>(rowmax, row_cloud, total_pts, radius);
         TT_LAUNCH("k_batch_radius");
         const u32 g3 = u32(std::min<u64>((total_pts * 32 + 255) / 256, u64(owner->sms) * 32));
-        k_batch_edges<<<g3, 256, 0, s>>>(mats, mat_off, pair_off, sizes, pt_off, row_cloud, total_pts, radius, ib,
+        k_batch_rowcount<<<g3, 256, 0, s>>>(mats, mat_off, sizes, pt_off, row_cloud, total_pts, radius, row_cnt);
+        TT_LAUNCH("k_batch_rowcount");
+        scan_exclusive<u64>(&sctx, row_cnt, row_off, total_pts, reinterpret_cast<u64*>(count), 0);
+        k_batch_edges<<<g3, 256, 0, s>>>(mats, mat_off, sizes, pt_off, row_cloud, total_pts, radius, ib, row_off,
                                          keys, per_cloud);
         TT_LAUNCH("k_batch_edges");
-        k_batch_offsets<<<1, 1024, 0, s>>>(per_cloud, clouds, edge_off, count);
+        k_batch_offsets<<<1, 1024, 0, s>>>(per_cloud, clouds, edge_off);
         TT_LAUNCH("k_batch_offsets");
-        radix_sort_inplace<u32>(&sctx, keys, nullptr, total_pairs, 31 + ib + bits_for(clouds));
+        // the kept keys only (a count on the device), the bits above the
+        // index field only (stable: ties keep the index order)
+        const bool swapped = radix_sort<u32>(&sctx, keys, nullptr, total_pairs, kbuf, nullptr,
+                                             31 + bits_for(clouds), ib, count);
         const u32 g4 = u32(std::min<u64>((total_pairs + 255) / 256, u64(owner->sms) * 32));
-        k_batch_emit<<<g4, 256, 0, s>>>(keys, count, ib, ed, ev);
+        k_batch_emit<<<g4, 256, 0, s>>>(swapped ? kbuf : keys, count, ib, ed, ev);
         TT_LAUNCH("k_batch_emit");
-        sctx.launches += 5;
+        sctx.launches += 6;
     }
 
     static int bits_for(u64 v) {
@@ -283,7 +400,7 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         b->sctx.sms = c->sms;
         TT_CUDA(cudaStreamCreateWithFlags(&b->sctx.stream, cudaStreamNonBlocking));
         std::vector<u64> pt_off(clouds + 1, 0), mat_off(clouds + 1, 0), pair_off(clouds + 1, 0);
-        std::vector<Tile> tiles;
+        std::vector<Tile> tiles[kNumShapes];
         std::vector<u32> row_cloud;
         u64 pairs = 0;
         for (u32 q = 0; q < clouds; ++q) {
@@ -294,8 +411,9 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
             mat_off[q + 1] = mat_off[q] + u64(n) * n;
             pairs += u64(n) * (n - 1) / 2;
             pair_off[q + 1] = pairs;
-            for (u32 i0 = 0; i0 < n; i0 += BT_R)
-                for (u32 j0 = 0; j0 < n; j0 += BT_C) tiles.push_back(Tile{q, i0, j0});
+            for (int si = 0; si < kNumShapes; ++si)
+                for (u32 i0 = 0; i0 < n; i0 += u32(kShapes[si].r))
+                    for (u32 j0 = 0; j0 < n; j0 += u32(kShapes[si].c)) tiles[si].push_back(Tile{q, i0, j0});
             for (u32 i = 0; i < n; ++i) row_cloud.push_back(q);
         }
         b->ib = std::max(1, Batch::bits_for(u64(b->maxn) * (b->maxn - 1) / 2 + 1));
@@ -304,7 +422,6 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         b->total_pts = pt_off[clouds];
         b->total_mat = mat_off[clouds];
         b->total_pairs = std::max<u64>(pairs, 1);
-        b->ntiles = u32(tiles.size());
         b->x = b->alloc<f32>(b->total_pts * dim);
         b->mats = b->alloc<f32>(b->total_mat);
         b->rowmax = b->alloc<u32>(b->total_pts);
@@ -313,10 +430,16 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         b->mat_off = b->alloc<u64>(clouds + 1);
         b->pair_off = b->alloc<u64>(clouds + 1);
         b->sizes = b->alloc<u32>(clouds);
-        b->tiles = b->alloc<Tile>(tiles.size());
+        for (int si = 0; si < kNumShapes; ++si) {
+            b->ntiles[si] = u32(tiles[si].size());
+            b->tiles[si] = b->alloc<Tile>(tiles[si].size());
+        }
         b->row_cloud = b->alloc<u32>(row_cloud.size());
         b->next = b->alloc<u32>(1);
         b->keys = b->alloc<u64>(b->total_pairs);
+        b->kbuf = b->alloc<u64>(b->total_pairs);
+        b->row_cnt = b->alloc<u64>(b->total_pts);
+        b->row_off = b->alloc<u64>(b->total_pts);
         b->count = b->alloc<unsigned long long>(1);
         b->per_cloud = b->alloc<u64>(clouds);
         b->edge_off = b->alloc<u64>(clouds + 1);
@@ -327,10 +450,11 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         TT_CUDA(cudaMemcpyAsync(b->mat_off, mat_off.data(), 8 * (clouds + 1), cudaMemcpyHostToDevice, s));
         TT_CUDA(cudaMemcpyAsync(b->pair_off, pair_off.data(), 8 * (clouds + 1), cudaMemcpyHostToDevice, s));
         TT_CUDA(cudaMemcpyAsync(b->sizes, sizes_h, 4 * clouds, cudaMemcpyHostToDevice, s));
-        TT_CUDA(cudaMemcpyAsync(b->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, s));
+        for (int si = 0; si < kNumShapes; ++si)
+            TT_CUDA(cudaMemcpyAsync(b->tiles[si], tiles[si].data(), sizeof(Tile) * tiles[si].size(),
+                                    cudaMemcpyHostToDevice, s));
         TT_CUDA(cudaMemcpyAsync(b->row_cloud, row_cloud.data(), 4 * row_cloud.size(), cudaMemcpyHostToDevice, s));
-        // size the sort's scratch outside any capture: the same calls, no graph
-        b->sctx.arena.get<u64>(S_SORT_A, b->total_pairs);
+        // size the sort's and the row scan's scratch outside any capture
         radix_reserve(&b->sctx, b->total_pairs);
         TT_CUDA(cudaStreamSynchronize(s));
     } catch (...) {
@@ -342,14 +466,22 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
 }
 
 void batch_run(Batch* b) {
+    if (!b->tuned) {   // the first run: pick the tile shape on this batch's points
+        b->tune();
+        b->tuned = true;
+    }
     if (!b->use_graph) {
+        const u64 before = b->sctx.launches;
         b->enqueue();
+        b->graph_kernels = b->sctx.launches - before;
         return;
     }
     if (!b->exec) {
         TT_CUDA(cudaStreamBeginCapture(b->sctx.stream, cudaStreamCaptureModeThreadLocal));
         try {
+            const u64 before = b->sctx.launches;
             b->enqueue();
+            b->graph_kernels = b->sctx.launches - before;
         } catch (...) {
             cudaGraph_t g = nullptr;
             cudaStreamEndCapture(b->sctx.stream, &g);
@@ -388,13 +520,26 @@ int tt_batch_create(tt_ctx* c, const uint32_t* sizes, uint32_t count, uint32_t d
 
 float* tt_batch_points(tt_batch* b) { return b ? reinterpret_cast<Batch*>(b)->x : nullptr; }
 
+int tt_batch_tuning(tt_batch* bh, uint32_t* tile_rows, uint32_t* tile_cols, float* shape_ms, uint32_t* shapes,
+                    int* from_cache) {
+    Batch* b = reinterpret_cast<Batch*>(bh);
+    if (!b) return TT_ERR_INVALID;
+    if (tile_rows) *tile_rows = u32(kShapes[b->shape].r);
+    if (tile_cols) *tile_cols = u32(kShapes[b->shape].c);
+    if (shapes) *shapes = u32(kNumShapes);
+    if (shape_ms)
+        for (int si = 0; si < kNumShapes; ++si) shape_ms[si] = b->tune_ms[si];
+    if (from_cache) *from_cache = b->tuned_from_cache ? 1 : 0;
+    return TT_OK;
+}
+
 int tt_batch_run(tt_batch* bh, int wait) {
     Batch* b = reinterpret_cast<Batch*>(bh);
     if (!b) return TT_ERR_INVALID;
     try {
         TT_CUDA(cudaSetDevice(b->owner->device));
         batch_run(b);
-        b->owner->launches += 5 + 8 * 5;   // the graph's kernels (dense, radius, edges, offsets, emit, 8 sort passes)
+        b->owner->launches += b->graph_kernels;   // the kernels one run launches
         if (wait) TT_CUDA(cudaStreamSynchronize(b->sctx.stream));
         return TT_OK;
     } catch (const Error& e) {

@@ -53,7 +53,8 @@ void scan_exclusive(tt_ctx* c, const T* in, T* out, u64 n, T* total, int depth =
 // Stable LSD sort on key bits [lo_bit, 64); the bits above lo_bit are sorted
 // as far as the keys differ there (force_bits > 0: exactly that many).
 template <typename V>
-bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits = 0, int lo_bit = 0);
+bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits = 0, int lo_bit = 0,
+                const unsigned long long* ndev = nullptr);
 template <typename V>
 void radix_sort_inplace(tt_ctx* c, u64* keys, V* vals, u64 n, int force_bits = 0);
 void radix_reserve(tt_ctx* c, u64 n);   // every slot radix_sort of n keys may grow

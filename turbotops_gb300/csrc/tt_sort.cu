@@ -98,9 +98,13 @@ __global__ void k_tile_scan(const T* __restrict__ in, u64 n, const T* __restrict
 // Radix sort kernels.
 // ---------------------------------------------------------------------------
 // Digits of up to RS_MAXBITS bits (a pass sorts `width` bits from `shift`).
+// ndev (optional): the key count lives on the device (a graph-captured sort of
+// a data-dependent number of keys, n the capacity); tiles past it are empty.
 __global__ void __launch_bounds__(RS_THREADS)
-k_rs_upsweep(const u64* __restrict__ keys, u64 n, int shift, u32 width, u32* __restrict__ hist, u32 tiles) {
+k_rs_upsweep(const u64* __restrict__ keys, u64 n, const unsigned long long* __restrict__ ndev, int shift, u32 width,
+             u32* __restrict__ hist, u32 tiles) {
     __shared__ u32 h[RS_WARPS][RS_BINS];
+    if (ndev) n = min(n, u64(*ndev));
     const u32 nd = 1u << width, mask = nd - 1u;
     for (u32 t = threadIdx.x; t < RS_WARPS * nd; t += RS_THREADS) h[t / nd][t % nd] = 0;
     __syncthreads();
@@ -123,9 +127,12 @@ k_rs_upsweep(const u64* __restrict__ keys, u64 n, int shift, u32 width, u32* __r
 template <typename V>
 __global__ void __launch_bounds__(RS_THREADS)
 k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __restrict__ vin,
-             V* __restrict__ vout, u64 n, int shift, u32 width, const u32* __restrict__ offs, u32 tiles) {
+             V* __restrict__ vout, u64 n, const unsigned long long* __restrict__ ndev, int shift, u32 width,
+             const u32* __restrict__ offs, u32 tiles) {
     __shared__ u32 cnt[RS_WARPS][RS_BINS];   // per-warp running count, then warp prefix
     __shared__ u32 gbase[RS_BINS];
+    if (ndev) n = min(n, u64(*ndev));
+    if (u64(blockIdx.x) * RS_TILE >= n) return;
     const u32 nd = 1u << width, mask = nd - 1u;
     for (u32 t = threadIdx.x; t < RS_WARPS * nd; t += RS_THREADS) cnt[t / nd][t % nd] = 0;
     for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) gbase[d] = offs[u64(d) * tiles + blockIdx.x];
@@ -237,7 +244,8 @@ template void scan_exclusive<u32>(tt_ctx*, const u32*, u32*, u64, u32*, int);
 // buffers that hold the result: the caller's (keys, vals) or the arena
 // scratch (kbuf, vbuf) — 'swapped' tells which.
 template <typename V>
-bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits, int lo_bit) {
+bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int force_bits, int lo_bit,
+                const unsigned long long* ndev) {
     if (n <= 1) return false;
     int bits = force_bits;
     if (bits <= 0) {
@@ -264,10 +272,11 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
     int shift = lo_bit;
     for (int q = 0; q < passes; ++q) {
         const int width = (lo_bit + bits - shift + (passes - q) - 1) / (passes - q);
-        k_rs_upsweep<<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, shift, u32(width), hist, tiles);
+        k_rs_upsweep<<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, ndev, shift, u32(width), hist, tiles);
         TT_LAUNCH("k_rs_upsweep");
         scan_exclusive<u32>(c, hist, hist, u64(tiles) << width, nullptr, 0);
-        k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, shift, u32(width), hist, tiles);
+        k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift, u32(width), hist,
+                                                             tiles);
         TT_LAUNCH("k_rs_scatter");
         c->launches += 2;
         std::swap(ka, kb);
@@ -278,8 +287,8 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
     return swapped;
 }
 
-template bool radix_sort<u32>(tt_ctx*, u64*, u32*, u64, u64*, u32*, int, int);
-template bool radix_sort<u64>(tt_ctx*, u64*, u64*, u64, u64*, u64*, int, int);
+template bool radix_sort<u32>(tt_ctx*, u64*, u32*, u64, u64*, u32*, int, int, const unsigned long long*);
+template bool radix_sort<u64>(tt_ctx*, u64*, u64*, u64, u64*, u64*, int, int, const unsigned long long*);
 
 // Sort keys in place (result always back in `keys`, payload in `vals`).
 template <typename V>
