@@ -233,6 +233,20 @@ int tt_dense_front_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, in
  * (nothing copied: call again with a larger buffer). n <= 131072. */
 int tt_dense_redzed_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, float* thr_inout,
                       float* mat_h, float* diam_h, int32_t* verts_h, uint64_t cap, uint64_t* count);
+/* tt_dense_redzed_h plus RedZeD's static leftover-coface predicate
+ * (redzed.hpp:1238-1273, :728-765, :1193-1202) for every kept edge, computed
+ * on the GPU: leftover_h (n x ceil(n / 64) words, row u, bit v for u < v) has
+ * bit (u, v) set when some w != u, v has d(u, w) <= d(u, v) and d(v, w) <=
+ * d(u, v) and makes {u, v, w} ready (w < u; u < w < v with d(w, v) < d(u, v);
+ * w > v with both strictly shorter) — what the engine's
+ * has_leftover_coface answers for that edge when its active enumeration
+ * excluded no vertex. */
+int tt_dense_redzed_pred_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p,
+                           float* thr_inout, float* mat_h, float* diam_h, int32_t* verts_h, uint64_t cap,
+                           uint64_t* count, uint64_t* leftover_h);
+/* The same predicate bits for a full n x n matrix already on the device
+ * (mat_dev, e.g. one cloud of a batch, tt_batch_out.mats_dev) cut at thr. */
+int tt_redzed_leftover_h(tt_ctx* ctx, const float* mat_dev, uint32_t n, float threshold, uint64_t* leftover_h);
 int tt_graph_redzed_h(tt_ctx* ctx, const uint64_t* row_ptr_h, const uint32_t* col_h, const float* weight_h,
                       uint32_t n, float threshold, float* diam_h, int32_t* verts_h, uint64_t cap, uint64_t* count);
 

@@ -112,7 +112,31 @@ inline CsrGraph radius_graph(const PointCloud& pc, f32 tau);
 // non-templates) hand over the prebuilt list instead of running the host pass.
 struct GpuEdgesDense : redzed::detail::DenseGeom {
     redzed::detail::EdgeList* prebuilt;
-    GpuEdgesDense(const rips::DenseComplex& cx, redzed::detail::EdgeList* e) : DenseGeom(cx), prebuilt(e) {}
+    // RedZeD's static leftover-coface predicate per kept edge, from the GPU
+    // (tt_dense_redzed_pred_h): n x ceil(n / 64) words, or null
+    const std::vector<uint64_t>* leftover = nullptr;
+    GpuEdgesDense(const rips::DenseComplex& cx, redzed::detail::EdgeList* e,
+                  const std::vector<uint64_t>* left = nullptr)
+        : DenseGeom(cx), prebuilt(e), leftover(left) {}
+    // has_leftover_coface's scan (redzed.hpp:728-765): for an edge with no
+    // vertex excluded (no seen bit), the GPU's answer; otherwise the
+    // reference's own scan. The engine asks only about cycle-closing edges at
+    // maxdim 1 with the radius graph grown to the edge's length, which is the
+    // predicate's definition.
+    template <class Ready>
+    bool any_common_radius_neighbor(const int32_t* xv, int m, size_t r, const std::vector<uint64_t>& seenbits,
+                                    const std::vector<char>& seen, Ready&& ready) const {
+        if (leftover && m == 2) {
+            bool none = true;
+            for (size_t w = 0; w < seenbits.size() && none; ++w) none = seenbits[w] == 0;
+            if (none) {
+                const size_t words = size_t(words_of(n));
+                return ((*leftover)[size_t(xv[0]) * words + size_t(xv[1] >> 6)] >> (xv[1] & 63)) & 1u;
+            }
+        }
+        return DenseGeom::any_common_radius_neighbor(xv, m, r, seenbits, seen, std::forward<Ready>(ready));
+    }
+    static int words_of(int n) { return (n + 63) / 64; }
 };
 template <typename Rank>
 struct GpuEdgesSparse : redzed::detail::SparseGeom<Rank> {
@@ -130,9 +154,10 @@ inline void build_edges(const GpuEdgesSparse<Rank>& geo, redzed::detail::value_t
 }
 
 // redzed::compute over make_dense(points) cut at the threshold (+inf: the
-// enclosing radius), the matrix and the edge list from the GPU.
+// enclosing radius), the matrix and the edge list from the GPU, and at
+// maxdim 1 the leftover-coface predicate too (unless device_predicate is off).
 inline rips::Barcode redzed_dense(const f32* points, u32 n, u32 dim, const Metric& m, u32 maxdim, f32 threshold,
-                                  u64* edges = nullptr, f32* thr_out = nullptr) {
+                                  u64* edges = nullptr, f32* thr_out = nullptr, bool device_predicate = true) {
     tt_ctx* c = ctx();
     rips::DenseComplex cx;
     cx.n = n;
@@ -144,15 +169,17 @@ inline rips::Barcode redzed_dense(const f32* points, u32 n, u32 dim, const Metri
     el.verts.resize(2 * cap);
     f32 thr = threshold;
     u64 count = 0;
-    check(tt_dense_redzed_h(c, points, n, dim, int(m.kind), m.p, &thr, cx.mat.data(), el.diam.data(),
-                            el.verts.data(), cap, &count),
+    const bool pred = device_predicate && maxdim == 1;
+    std::vector<uint64_t> left(pred ? size_t(n) * size_t((n + 63) / 64) : 0);
+    check(tt_dense_redzed_pred_h(c, points, n, dim, int(m.kind), m.p, &thr, cx.mat.data(), el.diam.data(),
+                                 el.verts.data(), cap, &count, pred ? left.data() : nullptr),
           c);
     el.count = count;
     el.diam.resize(count);
     el.verts.resize(2 * count);
     cx.threshold = thr;
     if (thr_out) *thr_out = thr;
-    GpuEdgesDense geo(cx, &el);
+    GpuEdgesDense geo(cx, &el, pred ? &left : nullptr);
     return redzed::detail::run(geo, maxdim, cx.threshold, edges);
 }
 
@@ -357,7 +384,7 @@ struct BatchTiming {
 };
 inline std::vector<Result> persistence_batch(const std::vector<const f32*>& clouds, const std::vector<u32>& sizes,
                                              u32 dim, const Options& o, u32 threads = 0,
-                                             BatchTiming* timing = nullptr) {
+                                             BatchTiming* timing = nullptr, bool device_predicate = true) {
     using clk = std::chrono::steady_clock;
     auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
     const size_t count = clouds.size();
@@ -412,10 +439,15 @@ inline std::vector<Result> persistence_batch(const std::vector<const f32*>& clou
     check(tt_ctx_synchronize(c), c);
     std::vector<rips::DenseComplex> cx(count);
     std::vector<redzed::detail::EdgeList> el(count);
+    std::vector<std::vector<uint64_t>> left(device_predicate ? count : 0);
     {
         u64 moff = 0;
         for (size_t q = 0; q < count; ++q) {
             const u32 n = sizes[q];
+            if (device_predicate) {   // the leftover-coface predicate of every edge, on the device
+                left[q].resize(size_t(n) * ((n + 63) / 64));
+                check(tt_redzed_leftover_h(c, bo.mats_dev + moff, n, radius[q], left[q].data()), c);
+            }
             cx[q].n = n;
             cx[q].full = true;
             cx[q].threshold = radius[q];
@@ -449,7 +481,7 @@ inline std::vector<Result> persistence_batch(const std::vector<const f32*>& clou
             const size_t q = order[k];
             try {
                 const auto tq = clk::now();
-                GpuEdgesDense geo(cx[q], &el[q]);
+                GpuEdgesDense geo(cx[q], &el[q], device_predicate ? &left[q] : nullptr);
                 u64 edges = 0;
                 Result r = redzed_result(redzed::detail::run(geo, 1, cx[q].threshold, &edges), 1, "dense-redzed",
                                          why, cx[q].threshold, edges);

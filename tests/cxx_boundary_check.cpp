@@ -124,6 +124,37 @@ int main() {
         same_result(persistence(x.data(), 700, 3, o), gb300::persistence(x.data(), 700, 3, o), 1,
                     std::string("dense redzed ") + metric);
     }
+    // the device's leftover-coface predicate bits against their definition
+    for (const char* metric : {"l2", "linf"}) {
+        const auto x = cloud(333, 3, 14, std::string(metric) == "linf");
+        const Metric mt = Metric::parse(metric);
+        const u32 n = 333, words = (n + 63) / 64;
+        std::vector<f32> mat(u64(n) * n), diam(u64(n) * n);
+        std::vector<int32_t> verts(2 * u64(n) * n);
+        std::vector<uint64_t> bits(u64(n) * words);
+        f32 thr = INFINITY;
+        u64 count = 0;
+        gb300::check(tt_dense_redzed_pred_h(gb300::ctx(), x.data(), n, 3, int(mt.kind), mt.p, &thr, mat.data(),
+                                            diam.data(), verts.data(), diam.size(), &count, bits.data()),
+                     gb300::ctx());
+        u64 set = 0;
+        for (u32 u = 0; u < n; ++u)
+            for (u32 v = u + 1; v < n; ++v) {
+                const f32 d = mat[u64(u) * n + v];
+                bool want = false;
+                if (d <= thr)
+                    for (u32 w = 0; w < n && !want; ++w) {
+                        if (w == u || w == v) continue;
+                        const f32 du = mat[u64(u) * n + w], dv = mat[u64(v) * n + w];
+                        want = du <= d && dv <= d && (w < u || (w < v ? dv < d : (du < d && dv < d)));
+                    }
+                const bool got = (bits[u64(u) * words + (v >> 6)] >> (v & 63)) & 1u;
+                if (got != want) fail(std::string("leftover predicate bit differs (") + metric + ")");
+                set += got;
+            }
+        if (!set) fail("leftover predicate: no bit set");
+        ++checks;
+    }
     // a kNN graph of mean degree >= 16: RedZeD on the graph
     {
         const auto x = cloud(3000, 8, 13);

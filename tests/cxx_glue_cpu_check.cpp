@@ -31,6 +31,54 @@ inline void build_edges(const CountingDense& geo, redzed::detail::value_t t, con
 }
 }  // namespace tops::gb300
 
+// RedZeD's leftover-coface predicate per edge, from its definition (the
+// device computes the same bits): some w != u, v within d(u, v) of both, with
+// w < u, or u < w < v and d(w, v) < d, or w > v and both strictly shorter.
+static std::vector<uint64_t> leftover_bits(const rips::DenseComplex& cx) {
+    const u32 n = cx.n, words = (n + 63) / 64;
+    std::vector<uint64_t> bits(size_t(n) * words, 0);
+    for (u32 u = 0; u < n; ++u)
+        for (u32 v = u + 1; v < n; ++v) {
+            const f32 d = cx.dist(u, v);
+            if (!(d <= cx.threshold)) continue;
+            for (u32 w = 0; w < n; ++w) {
+                if (w == u || w == v) continue;
+                const f32 du = cx.dist(u, w), dv = cx.dist(v, w);
+                if (!(du <= d && dv <= d)) continue;
+                if (w < u || (w < v ? dv < d : (du < d && dv < d))) {
+                    bits[size_t(u) * words + (v >> 6)] |= uint64_t(1) << (v & 63);
+                    break;
+                }
+            }
+        }
+    return bits;
+}
+
+// The glue geometry with every predicate answer it gives from the bits
+// checked against the reference's own scan.
+namespace tops::gb300 {
+struct CheckedDense : GpuEdgesDense {
+    using GpuEdgesDense::GpuEdgesDense;
+    mutable long answered = 0, wrong = 0;
+    template <class Ready>
+    bool any_common_radius_neighbor(const int32_t* xv, int m, size_t r, const std::vector<uint64_t>& sb,
+                                    const std::vector<char>& seen, Ready&& ready) const {
+        const bool mine = GpuEdgesDense::any_common_radius_neighbor(xv, m, r, sb, seen, ready);
+        bool none = true;
+        for (uint64_t w : sb) none = none && w == 0;
+        if (m == 2 && none && leftover) {
+            ++answered;
+            wrong += mine != redzed::detail::DenseGeom::any_common_radius_neighbor(xv, m, r, sb, seen, ready);
+        }
+        return mine;
+    }
+};
+inline void build_edges(const CheckedDense& geo, redzed::detail::value_t t, const redzed::detail::BinomialTable& b,
+                        redzed::detail::EdgeList& out) {
+    build_edges(static_cast<const GpuEdgesDense&>(geo), t, b, out);
+}
+}  // namespace tops::gb300
+
 static bool same(const rips::Barcode& a, const rips::Barcode& b) {
     if (a.ndims() != b.ndims()) return false;
     for (u32 d = 0; d < a.ndims(); ++d) {
@@ -64,6 +112,20 @@ int main() {
         if (overload_calls != before + 1) { std::printf("FAIL overload not taken (seed %u)\n", seed); return 1; }
         if (!same(ref, got)) { std::printf("FAIL dense diagram differs (seed %u)\n", seed); return 1; }
         ++checks;
+        // the leftover-coface predicate answered from precomputed bits
+        {
+            const std::vector<uint64_t> bits = leftover_bits(cx);
+            redzed::detail::EdgeList el2;
+            redzed::detail::build_edges(plain, cx.threshold, bt, el2);
+            gb300::CheckedDense cgeo(cx, &el2, &bits);
+            const rips::Barcode got2 = redzed::detail::run(cgeo, 1, cx.threshold);
+            if (cgeo.answered == 0 || cgeo.wrong != 0) {
+                std::printf("FAIL predicate answered %ld, wrong %ld (seed %u)\n", cgeo.answered, cgeo.wrong, seed);
+                return 1;
+            }
+            if (!same(ref, got2)) { std::printf("FAIL diagram with the predicate differs (seed %u)\n", seed); return 1; }
+            ++checks;
+        }
         // sparse: a kNN graph
         const CsrGraph g = knn_graph(pc, knn_lists_exact(pc, 10));
         const rips::Barcode sref = redzed::compute_graph(g, 1);

@@ -79,6 +79,8 @@ _SIGS = {
                              C.POINTER(u64), C.POINTER(u64), P, P, P, P, u64, C.POINTER(u64), C.POINTER(u64)]),
     "tt_batch_tuning": (i32, [P, P, P, P, P, P]),
     "tt_dense_redzed_h": (i32, [P, P, u32, u32, i32, f32, C.POINTER(f32), P, P, P, u64, C.POINTER(u64)]),
+    "tt_dense_redzed_pred_h": (i32, [P, P, u32, u32, i32, f32, C.POINTER(f32), P, P, P, u64, C.POINTER(u64), P]),
+    "tt_redzed_leftover_h": (i32, [P, P, u32, f32, P]),
     "tt_graph_redzed_h": (i32, [P, P, P, P, u32, f32, P, P, u64, C.POINTER(u64)]),
     "tt_dense_front_h": (i32, [P, P, u32, u32, i32, f32, u32, C.POINTER(f32), P, P, C.POINTER(u64),
                                C.POINTER(u64), P, P, P, P, u64, C.POINTER(u64), C.POINTER(u64)]),

@@ -550,6 +550,12 @@ int tt_dense_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int 
 
 int tt_dense_redzed_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, float* thr_inout,
                       float* mat_h, float* diam_h, int32_t* verts_h, uint64_t cap, uint64_t* count) {
+    return tt_dense_redzed_pred_h(c, x_h, n, dim, kind, p, thr_inout, mat_h, diam_h, verts_h, cap, count, nullptr);
+}
+
+int tt_dense_redzed_pred_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int kind, float p,
+                           float* thr_inout, float* mat_h, float* diam_h, int32_t* verts_h, uint64_t cap,
+                           uint64_t* count, uint64_t* leftover_h) {
     return guard(c, [&] {
         check_metric(kind, p);
         if (!thr_inout || !count) invalid("gb300: null output");
@@ -582,6 +588,25 @@ int tt_dense_redzed_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int
         }
         if (m && diam_h) TT_CUDA(cudaMemcpyAsync(diam_h, d, 4 * m, cudaMemcpyDeviceToHost, c->stream));
         if (m && verts_h) TT_CUDA(cudaMemcpyAsync(verts_h, v, 8 * m, cudaMemcpyDeviceToHost, c->stream));
+        if (leftover_h && n) {
+            const u64 words = u64(n) * ((n + 63) / 64);
+            auto* bits = c->arena.get<unsigned long long>(S_MISC1, words);
+            redzed_leftover(c, mat, n, thr, bits);
+            TT_CUDA(cudaMemcpyAsync(leftover_h, bits, 8 * words, cudaMemcpyDeviceToHost, c->stream));
+        }
+        TT_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int tt_redzed_leftover_h(tt_ctx* c, const float* mat_dev, uint32_t n, float thr, uint64_t* leftover_h) {
+    return guard(c, [&] {
+        if (!leftover_h || (n && !mat_dev)) invalid("gb300: null buffer");
+        if (std::isnan(thr) || thr < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        if (!n) return;
+        const u64 words = u64(n) * ((n + 63) / 64);
+        auto* bits = c->arena.get<unsigned long long>(S_MISC1, words);
+        redzed_leftover(c, mat_dev, n, thr, bits);
+        TT_CUDA(cudaMemcpyAsync(leftover_h, bits, 8 * words, cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaStreamSynchronize(c->stream));
     });
 }

@@ -88,6 +88,7 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out);
 // RedZeD EdgeList (d asc, comb asc): diam + vertex pairs (i < j).
 u64 redzed_edges(tt_ctx* c, const Complex& cx, f32* d, int32_t* verts, u64 cap);
 u64 redzed_edges_owned(tt_ctx* c, const Complex& cx, f32** d, int32_t** verts);
+void redzed_leftover(tt_ctx* c, const f32* mat, u32 n, f32 thr, unsigned long long* bits);   // tt_redzed_pred.cu
 
 // ---- tt_assemble.cu
 u64 assemble2(tt_ctx* c, const Complex& cx, const u64* keys, u64 m, const u64* piv_sorted, u64 npiv,

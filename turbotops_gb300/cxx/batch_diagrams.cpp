@@ -10,7 +10,8 @@
 // clouds.bin: u32 count, u32 dim, count x u32 sizes, then the points (float32,
 // row-major, clouds back to back). Every ref_stride-th cloud (0: none) is
 // also computed by tops::persistence; its canonical diagram must equal the
-// batch's. Prints one JSON line: the batch's seconds per run (front end, host
+// batch's. The batch runs once more with the engine's own leftover-coface
+// scan instead of the device's predicate: same bars, same order. Prints one JSON line: the batch's seconds per run (front end, host
 // copies, reductions), the reference's seconds for the compared clouds, and
 // whether every compared diagram was identical.
 #include <chrono>
@@ -81,6 +82,15 @@ int main(int argc, char** argv) {
         sum.copy_s += tm.copy_s / reps;
         sum.reduce_s += tm.reduce_s / reps;
     }
+    // the same batch with the engine's own leftover-coface scan (no device
+    // predicate): the diagrams must not change, only the host time
+    gb300::BatchTiming tn;
+    const auto res_np = gb300::persistence_batch(clouds, sizes, dim, o, threads, &tn, false);
+    bool same_np = res_np.size() == res.size();
+    for (size_t q = 0; same_np && q < res.size(); ++q)
+        for (u32 d = 0; d <= o.maxdim && same_np; ++d)
+            same_np = res[q].barcode.birth[d] == res_np[q].barcode.birth[d] &&
+                      res[q].barcode.death[d] == res_np[q].barcode.death[d];
     u64 bars = 0;
     for (const Result& r : res)
         for (u32 d = 0; d < r.barcode.ndims(); ++d) bars += r.barcode.birth[d].size();
@@ -100,9 +110,10 @@ int main(int argc, char** argv) {
     for (double s : run_s) mean += s / run_s.size();
     std::printf("{\"clouds\": %u, \"points\": %llu, \"bars\": %llu, \"batch_s\": %.6f, \"front_s\": %.6f, "
                 "\"copy_s\": %.6f, \"reduce_s\": %.6f, \"threads\": %u, \"reps\": %d, \"reference_s\": %.6f, "
-                "\"reference_clouds\": %u, \"identical\": %s}\n",
+                "\"reference_clouds\": %u, \"identical\": %s, \"reduce_s_without_device_predicate\": %.6f, "
+                "\"same_without_device_predicate\": %s}\n",
                 count, (unsigned long long)total, (unsigned long long)bars, mean, sum.front_s, sum.copy_s,
                 sum.reduce_s, threads ? threads : std::thread::hardware_concurrency(), reps, ref_s, compared,
-                same ? "true" : "false");
-    return same ? 0 : 1;
+                same ? "true" : "false", tn.reduce_s, same_np ? "true" : "false");
+    return same && same_np ? 0 : 1;
 }
