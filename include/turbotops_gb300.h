@@ -55,6 +55,13 @@ int tt_ctx_synchronize(tt_ctx* ctx);
  * 1 = always the exhaustive scan, 2 = the filter wherever it applies.
  * Every engine returns the same lists. */
 int tt_ctx_set_knn_mode(tt_ctx* ctx, int mode);
+/* Options::memory_budget (turbotops.hpp:81, rips.hpp:383-416): the bytes a
+ * dense distance matrix may take; 0 = half of the host's physical memory.
+ * The dense entry points (tt_persistence_h with a full graph and an infinite
+ * threshold, tt_dense_front_h, tt_dense_redzed_h) return TT_ERR_LENGTH with
+ * make_dense's message when even the lower triangle, n(n-1)/2 floats, exceeds
+ * it. It never changes a result. */
+int tt_ctx_set_memory_budget(tt_ctx* ctx, uint64_t bytes);
 /* Exact distance evaluations the last filtered kNN let through. */
 uint64_t tt_ctx_filter_evals(const tt_ctx* ctx);
 /* Candidate tiles (128 x 128 Gram blocks) the last filtered kNN computed;

@@ -223,6 +223,7 @@ inline Result persistence(const f32* points, u32 n, u32 dim, const Options& o) {
     if (o.approximate)
         throw std::invalid_argument("persistence: approximate kNN (HNSW) is not offered by the GB300 front end");
     tt_ctx* c = ctx();
+    check(tt_ctx_set_memory_budget(c, o.memory_budget), c);   // make_dense's budget (rips.hpp:383-416)
     int kind = 0;
     float p = 2.0f;
     check(tt_metric_parse(o.metric.c_str(), &kind, &p), nullptr);
@@ -418,6 +419,12 @@ inline std::vector<Result> persistence_batch(const std::vector<const f32*>& clou
             at += n;
         }
     }
+    // make_dense's budget, cloud by cloud (rips.hpp:383-416)
+    const u64 budget = o.memory_budget ? o.memory_budget : default_memory_budget();
+    for (u32 s : sizes)
+        if (rips::dense_bytes(s, false) > budget)
+            throw std::length_error("rips: the dense distance matrix exceeds the memory budget; use a finite "
+                                    "threshold or a sparse graph");
     auto t0 = clk::now();
     tt_batch* b = nullptr;
     check(tt_batch_create(c, sizes.data(), u32(count), dim, kind, p, 1, &b), c);

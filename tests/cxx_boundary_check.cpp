@@ -213,6 +213,26 @@ int main() {
         bad_k.k = 0;
         same_throw<std::invalid_argument>([&] { persistence(x.data(), 50, 3, bad_k); },
                                           [&] { gb300::persistence(x.data(), 50, 3, bad_k); }, "k");
+        // make_dense's memory budget: 50 points need 4900 bytes of lower triangle
+        for (const Mode mode : {Mode::Auto, Mode::Coboundary}) {
+            Options small;
+            small.memory_budget = 4899;
+            small.mode = mode;
+            same_throw<std::length_error>([&] { persistence(x.data(), 50, 3, small); },
+                                          [&] { gb300::persistence(x.data(), 50, 3, small); }, "memory budget");
+            small.memory_budget = 4900;
+            same_result(persistence(x.data(), 50, 3, small), gb300::persistence(x.data(), 50, 3, small), 1,
+                        "budget just enough");
+        }
+        {
+            Options small;
+            small.memory_budget = 4899;
+            const std::vector<const f32*> clouds{x.data()};
+            const std::vector<u32> sizes{50};
+            same_throw<std::length_error>([&] { persistence(x.data(), 50, 3, small); },
+                                          [&] { gb300::persistence_batch(clouds, sizes, 3, small); },
+                                          "memory budget, batch");
+        }
         x[17] = NAN;
         Options o;
         same_throw<std::invalid_argument>([&] { persistence(x.data(), 50, 3, o); },

@@ -185,7 +185,11 @@ def cli_cases() -> None:
             ("ecyc", ["--edges", "--maxdim", "1"]), ("ecyc", ["--edges", "--maxdim", "1", "--threshold", "1"]),
             ("edup", ["--edges", "--maxdim", "1"]), ("ehex", ["--edges", "--maxdim", "1"]),
             ("ehex", ["--edges"]), ("mid", ["--maxdim", "1"]), ("hexf", ["--maxdim", "1"]),
-            ("under", [])]
+            ("under", []),
+            # make_dense's memory budget: 4 points need 24 bytes of lower triangle
+            ("sq", ["--maxdim", "1", "--memory-budget", "16"]), ("sq", ["--maxdim", "1", "--memory-budget", "24"]),
+            ("sq", ["--maxdim", "0", "--memory-budget", "16"]), ("sq", ["--memory-budget", "0.5k"]),
+            ("sq", ["--memory-budget", "1x"]), ("sq", ["--memory-budget", "0"])]
     out = []
     with tempfile.TemporaryDirectory() as td:
         for name, text in inputs.items():
@@ -355,6 +359,7 @@ if __name__ == "__main__":
                     help="whole diagrams of the full workloads (optionally only names containing this)")
     ap.add_argument("--a64", metavar="DIR", help="only the aarch64 Lp fixtures, written to DIR")
     ap.add_argument("--higher", action="store_true", help="only the higher-dimension diagrams")
+    ap.add_argument("--cli", action="store_true", help="only the CLI text cases")
     a = ap.parse_args()
     if not os.path.exists(PROBE):
         sys.exit("build the reference first: make -C oracle install-ref ref")
@@ -362,6 +367,8 @@ if __name__ == "__main__":
         a64(a.a64)
     elif a.higher:
         higher_dims()
+    elif a.cli:
+        cli_cases()
     elif a.diagrams is not None:
         diagrams(a.diagrams or None)
     else:

@@ -118,6 +118,14 @@ def test_persistence_validation_messages():
         tg.persistence(y)
     with pytest.raises(ValueError, match="unknown 'cosine'"):
         tg.persistence(x, metric="cosine")
+    # make_dense's memory budget: 10 points need 180 bytes of lower triangle
+    with pytest.raises(ValueError, match="rips: the dense distance matrix exceeds the memory budget"):
+        tg.persistence(x, memory_budget=179)
+    a, _ = tg.persistence(x, memory_budget=180)
+    b, _ = tg.persistence(x)
+    assert all(np.array_equal(u, v) for u, v in zip(a, b))
+    c, _ = tg.persistence(x, maxdim=0, memory_budget=1)       # the MST path takes no matrix
+    assert np.array_equal(np.sort(c[0][:, 1]), np.sort(b[0][:, 1]))
 
 
 def test_graph_input_equals_point_knn_path():

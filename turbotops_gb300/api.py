@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 import time
 
 import numpy as np
@@ -25,6 +26,18 @@ def _context(device: int = 0) -> capi.Context:
     return _CTX[device]
 
 
+def _budget(memory_budget: int) -> int:
+    """Options::memory_budget with the reference's default
+    (memory.hpp:17-33): half of the physical memory, 8 GiB if unknown."""
+    if memory_budget:
+        return int(memory_budget)
+    try:
+        m = os.sysconf("SC_PHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    except (ValueError, OSError):
+        m = 0
+    return m // 2 if m > 0 else 8 << 30
+
+
 def persistence(x, maxdim=1, threshold=math.inf, metric="l2", graph="full", k=15, approximate=False,
                 recall_samples=0, threads=0, memory_budget=0, device=0):
     """Persistence diagrams of the Vietoris–Rips filtration (see turbo_tops.persistence).
@@ -32,8 +45,11 @@ def persistence(x, maxdim=1, threshold=math.inf, metric="l2", graph="full", k=15
     ``x`` is an (n, d) point cloud or a scipy sparse matrix (the flag complex
     of the weighted graph, as the reference's ``persistence_csr``).
     ``approximate`` (HNSW) is not offered: the GPU computes exact kNN lists.
-    ``threads`` and ``memory_budget`` are accepted and ignored (the results
-    never depended on them).
+    ``threads`` is accepted and ignored (the results never depended on it).
+    ``memory_budget`` (bytes, 0 = half of the host's physical memory) refuses
+    a dense complex whose distance matrix would exceed it, with make_dense's
+    message, as ValueError — the reference module's translation of its
+    std::length_error (rips.hpp:383-416).
     """
     if hasattr(x, "tocsr"):
         rp, ci, w, n = csr_graph(x)
@@ -46,8 +62,14 @@ def persistence(x, maxdim=1, threshold=math.inf, metric="l2", graph="full", k=15
     if x.ndim != 2:
         raise ValueError("x must be a 2-d array (n, d)")
     kind, p = capi.metric_parse(str(metric))
-    ctx = _context(device)
     n, dim = x.shape
+    if graph == "full" and maxdim > 0 and math.isinf(threshold) and n * (n - 1) // 2 * 4 > _budget(memory_budget):
+        if not np.isfinite(x).all():
+            raise ValueError("persistence: non-finite coordinate")
+        raise ValueError("rips: the dense distance matrix exceeds the memory budget; use a finite threshold "
+                         "or a sparse graph")
+    ctx = _context(device)
+    ctx.check(ctx.L.tt_ctx_set_memory_budget(ctx.h, int(memory_budget)))
     out = C.POINTER(capi.Barcode)()
     t0 = time.perf_counter()
     ctx.check(ctx.L.tt_persistence_h(ctx.h, x.ctypes.data, n, dim, kind, p, int(maxdim), float(threshold),

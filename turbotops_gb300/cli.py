@@ -34,6 +34,8 @@ options:
   --mode M            boundary | coboundary | auto (diagrams never depend on it)
   --coboundary, --boundary, --no-coboundary, --engine E   accepted, as --mode
   --threads N         accepted (results never depend on it)
+  --memory-budget B   bytes, with optional k/m/g suffix (default: half of RAM); a dense
+                      complex whose distance matrix exceeds it is refused, as the reference does
   --output FILE       write the diagram to FILE instead of stdout
   --quiet             no summary on stderr
 """
@@ -66,6 +68,32 @@ def _parse_f32(tok: str, what: str) -> float:
     if not raw or end.value is None or end.value - ctypes.addressof(buf) != len(raw):
         raise CliError(f"bad {what} '{tok}'")
     return float(v)
+
+
+def _parse_bytes(tok: str) -> int:
+    """The reference's parse_bytes (src/turbotops.cpp:86-100): the C library's
+    strtod, then, if anything follows the number, its first character must
+    be k, m or g (either case: KiB, MiB, GiB); the product must be positive
+    and is truncated to whole bytes."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    strtod = libc.strtod
+    strtod.restype = ctypes.c_double
+    strtod.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+    raw = tok.encode("utf-8", "surrogateescape")
+    buf = ctypes.create_string_buffer(raw)
+    end = ctypes.c_void_p()
+    v = strtod(ctypes.cast(buf, ctypes.c_char_p), ctypes.byref(end))
+    at = (end.value or ctypes.addressof(buf)) - ctypes.addressof(buf)
+    mul = 1.0
+    if at < len(raw):
+        mul = {ord("k"): 1024.0, ord("m"): 1024.0 ** 2, ord("g"): 1024.0 ** 3}.get(raw[at] | 0x20)
+        if mul is None:
+            raise CliError(f"bad byte count '{tok}'")
+    if not v > 0:
+        raise CliError(f"bad byte count '{tok}'")
+    b = v * mul
+    return (1 << 64) - 1 if b >= 2.0 ** 64 else int(b)
 
 
 def _parse_u32(tok: str, what: str) -> int:
@@ -166,7 +194,7 @@ def run(argv: list[str]) -> int:
         raise CliError("run: missing <input>\n" + USAGE)
     path = argv[0]
     o = {"maxdim": 1, "threshold": math.inf, "metric": "l2", "graph": "full", "k": 15, "dim": 0,
-         "output": None, "quiet": False, "edges": False}
+         "output": None, "quiet": False, "edges": False, "memory_budget": 0}
     it = iter(argv[1:])
     for a in it:
         def val():
@@ -201,6 +229,8 @@ def run(argv: list[str]) -> int:
                 o["quiet"] = True
         elif a == "--threads":
             _parse_u32(val(), "threads")
+        elif a == "--memory-budget":
+            o["memory_budget"] = _parse_bytes(val())
         elif a == "--output":
             o["output"] = val()
         elif a == "--edges":
@@ -225,7 +255,7 @@ def run(argv: list[str]) -> int:
         else:
             x = read_bin_points(path, o["dim"]) if path.endswith(".bin") else read_text_points(path)
             dgms, info = api.persistence(x, maxdim=o["maxdim"], threshold=o["threshold"], metric=o["metric"],
-                                         graph=o["graph"], k=o["k"])
+                                         graph=o["graph"], k=o["k"], memory_budget=o["memory_budget"])
     except (ValueError, OverflowError, MemoryError) as e:
         raise CliError(str(e)) from None
     text = api.format_diagram(dgms)

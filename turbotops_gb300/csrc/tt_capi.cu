@@ -182,6 +182,10 @@ int tt_ctx_set_knn_mode(tt_ctx* c, int mode) {
     });
 }
 
+int tt_ctx_set_memory_budget(tt_ctx* c, uint64_t bytes) {
+    return guard(c, [&] { c->memory_budget = bytes; });
+}
+
 uint64_t tt_ctx_filter_evals(const tt_ctx* c) { return c ? c->filter_evals : 0; }
 uint64_t tt_ctx_filter_tiles(const tt_ctx* c) { return c ? c->filter_tiles : 0; }
 
@@ -506,6 +510,7 @@ int tt_dense_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int 
         if (!thr_inout) invalid("gb300: null threshold");
         const float t = *thr_inout;
         if (std::isnan(t) || t < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        check_dense_budget(c, n);
         f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
         if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
         check_finite_dev(c, x, u64(n) * dim);
@@ -561,6 +566,7 @@ int tt_dense_redzed_pred_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim
         if (!thr_inout || !count) invalid("gb300: null output");
         const float t = *thr_inout;
         if (std::isnan(t) || t < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
+        check_dense_budget(c, n);
         f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
         if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
         check_finite_dev(c, x, u64(n) * dim);

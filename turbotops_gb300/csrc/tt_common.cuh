@@ -152,6 +152,7 @@ struct tt_ctx {
     double last_kernel_ms = 0.0;   // device time of the last stage (CUDA events)
     uint64_t launches = 0;          // kernels launched through this context
     int knn_mode = 0;               // 0 auto, 1 exhaustive scan, 2 tensor-core filter where applicable
+    uint64_t memory_budget = 0;     // bytes a dense distance matrix may take (0: half the host's memory)
     uint64_t filter_evals = 0;      // exact evaluations the last tensor-core kNN let through
     uint64_t filter_tiles = 0;      // 128 x 128 Gram tiles the last tensor-core kNN computed
     cudaStream_t aux = nullptr;     // copies overlapped with compute (created on first use)

@@ -19,12 +19,32 @@
 #include <string>
 #include <vector>
 
+#include <unistd.h>
+
 #include "tt_internal.cuh"
 #include "tt_reduce.h"
 
 namespace tt {
 
 void set_thread_error(const std::string& msg);
+
+// make_dense's memory budget (rips.hpp:383-416, turbotops.hpp:215): the full
+// layout when it fits, else the lower triangle, else std::length_error. The
+// device always holds the full matrix; the budget only decides whether the
+// reference would have refused the complex, with its message. The default
+// is the reference's: half of the host's physical memory (8 GiB if unknown).
+void check_dense_budget(const tt_ctx* c, u32 n) {
+    u64 budget = c->memory_budget;
+    if (!budget) {
+        const long pages = sysconf(_SC_PHYS_PAGES), page = sysconf(_SC_PAGE_SIZE);
+        const u64 m = pages > 0 && page > 0 ? u64(pages) * u64(page) : 0;
+        budget = m ? m / 2 : (u64(8) << 30);
+    }
+    if (u64(n) * (n ? n - 1 : 0) / 2 * sizeof(f32) > budget)
+        throw Error(TT_ERR_LENGTH,
+                    "rips: the dense distance matrix exceeds the memory budget; use a finite threshold or a "
+                    "sparse graph");
+}
 
 namespace {
 
@@ -182,6 +202,7 @@ void persistence_points(tt_ctx* c, const f32* x_h, u32 n, u32 dim, int kind, f32
         return;
     }
     if (!knn && std::isinf(thr)) {   // dense full Rips cut at the enclosing radius
+        check_dense_budget(c, n);
         out.method = "dense";
         f32* mat = c->arena.get<f32>(S_MAT, u64(n) * n + 1);
         u32* rowmax = c->arena.get<u32>(S_ROWMAX, u64(n) + 1);
