@@ -132,7 +132,9 @@ typedef struct tt_dim0_out {
 /* Reducer::dim0 (rips.hpp:685-870). The complex is the dense full matrix
  * mat_dev (n x n) when it is not NULL, else the CSR graph rp/ci/w (device;
  * CsrGraph layout core.hpp:92-98, rows sorted by neighbour id). Edges with
- * d <= threshold are kept. maxdim >= 1 computes apparent flags and columns. */
+ * d <= threshold are kept. maxdim >= 1 computes apparent flags and columns.
+ * n <= 131072 (edge indices must fit the packed keys' 33-bit field; the
+ * host-buffer entry points and tt_persistence_h take larger complexes). */
 int tt_dim0(tt_ctx* ctx, const float* mat_dev, const uint64_t* rp_dev, const uint32_t* ci_dev,
             const float* w_dev, uint32_t n, float threshold, uint32_t maxdim, tt_dim0_out* out);
 
@@ -195,7 +197,8 @@ typedef struct tt_knn_front_out {
 } tt_knn_front_out;
 
 /* knn_lists_exact -> knn_graph -> Reducer::dim0 of rips::compute_graph
- * (turbotops.hpp:260-298, threshold +inf), all on the device. */
+ * (turbotops.hpp:260-298, threshold +inf), all on the device. n <= 131072
+ * (packed edge keys, as tt_dim0); tt_knn_front_h takes any n. */
 int tt_knn_front(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
                  uint32_t maxdim, tt_knn_front_out* out);
 
@@ -237,7 +240,7 @@ int tt_dense_front_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, in
  *   tt_graph_redzed_h: host CSR (row_ptr n + 1, 2m columns and weights, rows
  *     sorted by id) -> its edges with w <= threshold in the same order.
  * *count always receives the edge count; TT_ERR_LENGTH when it exceeds cap
- * (nothing copied: call again with a larger buffer). n <= 131072. */
+ * (nothing copied: call again with a larger buffer). */
 int tt_dense_redzed_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, float* thr_inout,
                       float* mat_h, float* diam_h, int32_t* verts_h, uint64_t cap, uint64_t* count);
 /* tt_dense_redzed_h plus RedZeD's static leftover-coface predicate

@@ -163,6 +163,20 @@ int main() {
         o.k = 14;
         same_result(persistence(x.data(), 3000, 8, o), gb300::persistence(x.data(), 3000, 8, o), 1, "knn redzed");
     }
+    // more than 131072 vertices: edge indices beyond the packed keys' 33 bits
+    // (wide edge keys on the device), RedZeD's graph engine (k = 15) and the
+    // library's own reduction (k = 6)
+    {
+        const u32 n = 140000;
+        const auto x = cloud(n, 3, 15);
+        for (const u32 k : {15u, 6u}) {
+            Options o;
+            o.graph = Options::Graph::Knn;
+            o.k = k;
+            same_result(persistence(x.data(), n, 3, o), gb300::persistence(x.data(), n, 3, o), 1,
+                        "knn n = 140000, k = " + std::to_string(k));
+        }
+    }
     // kNN flag complex (L2 in R^32: the tensor-core filter path; lp:1.5), radius graph, MST
     {
         const auto x = cloud(2000, 32, 9);

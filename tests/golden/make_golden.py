@@ -285,7 +285,10 @@ def diagram_cases() -> list[tuple[str, np.ndarray, list[str]]]:
              ("lattice3000_linf_maxdim2", synth.lattice(), ["--maxdim", "2", "--metric", "linf"]),
              ("lattice3000_l1_maxdim2", synth.lattice(), ["--maxdim", "2", "--metric", "l1"]),
              ("gmm100k_knn15_l2_maxdim1", synth.gmm(), ["--graph", "knn", "-k", "15", "--maxdim", "1"]),
-             ("gmm100k_l2_maxdim0", synth.gmm(), ["--maxdim", "0"])]
+             ("gmm100k_l2_maxdim0", synth.gmm(), ["--maxdim", "0"]),
+             # above 131072 points: edge indices wider than the packed 33-bit key field
+             ("gmm150k_knn15_l2_maxdim1", synth.gmm(150_000, seed=6), ["--graph", "knn", "-k", "15", "--maxdim", "1"]),
+             ("gmm150k_l2_maxdim0", synth.gmm(150_000, seed=6), ["--maxdim", "0"])]
     for i, c in enumerate(synth.circle_batch()[:8]):
         cases.append((f"batch{i}_l2_maxdim1", c, ["--maxdim", "1"]))
     for i, c in enumerate(synth.circles()[:8]):

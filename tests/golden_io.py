@@ -45,6 +45,8 @@ def workload_points(name: str):
         return synth.lattice()
     if name.startswith("gmm100k"):
         return synth.gmm()
+    if name.startswith("gmm150k"):
+        return synth.gmm(150_000, seed=6)
     if name.startswith("batch"):
         return synth.circle_batch()[int(name[5:name.index("_")])]
     if name.startswith("circle"):

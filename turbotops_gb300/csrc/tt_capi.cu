@@ -268,6 +268,7 @@ int tt_dim0(tt_ctx* c, const float* mat, const uint64_t* rp, const uint32_t* ci,
         if (!out) invalid("gb300: null output");
         if (std::isnan(thr) || thr < 0.0f) invalid("persistence: threshold must be non-negative or +inf");
         if (n > 1 && !mat && !(rp && ci && w)) invalid("gb300: null complex");
+        if (n > kPackedMaxN) invalid("gb300: tt_dim0's packed edge keys support n <= 131072 vertices");
         Complex cx{mat, rp, ci, w, n, thr};
         Dim0Out r;
         dim0(c, cx, maxdim, r);
@@ -422,6 +423,7 @@ int tt_knn_front(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, 
         check_metric(kind, p);
         if (k == 0) invalid("persistence: k must be >= 1");
         if (!out) invalid("gb300: null output");
+        if (n > kPackedMaxN) invalid("gb300: tt_knn_front's packed edge keys support n <= 131072 vertices");
         u64* rp = nullptr;
         u32* ci = nullptr;
         f32* w = nullptr;

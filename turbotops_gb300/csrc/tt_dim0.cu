@@ -171,27 +171,32 @@ __global__ void k_edge_fill(Rows rows, u32 n, f32 thr, const u64* __restrict__ o
     }
 }
 
-// Sorted (dbits, q) pairs -> packed filtration keys; inv[q] = sorted
-// position of the edge that index order puts at q.
-__global__ void k_edge_pack(const u64* __restrict__ skey, const u64* __restrict__ sidx, u64 m, int redzed,
+// Sorted (dbits, q) pairs -> filtration keys (packed, or as they are in the
+// wide layout, where sidx stays the index table); inv[q] = sorted position of
+// the edge that index order puts at q.
+__global__ void k_edge_pack(const u64* __restrict__ skey, const u64* __restrict__ sidx, u64 m, int redzed, int wide,
                             u64* __restrict__ keys, u32* __restrict__ inv) {
     for (u64 r = u64(blockIdx.x) * blockDim.x + threadIdx.x; r < m; r += u64(gridDim.x) * blockDim.x) {
         const u64 k = skey[r];
-        const u64 idx = sidx[u32(k)];
-        keys[r] = ((k >> 32) << kIdxBits) | (redzed ? idx : kIdxMask - idx);
+        if (wide) {
+            keys[r] = k;
+        } else {
+            const u64 idx = sidx[u32(k)];
+            keys[r] = ((k >> 32) << kIdxBits) | (redzed ? idx : kIdxMask - idx);
+        }
         inv[u32(k)] = u32(r);
     }
 }
 
-__global__ void k_apparent_dense(const f32* __restrict__ mat, u32 n, const u64* __restrict__ keys, u64 m,
+__global__ void k_apparent_dense(const f32* __restrict__ mat, u32 n, const u64* __restrict__ keys, EdgeFmt fmt, u64 m,
                                  u8* __restrict__ app, u32* __restrict__ emw, u8* __restrict__ emf) {
     const DenseCx cx{mat, n};
     const int lane = threadIdx.x & 31;
     const u64 warps = (u64(gridDim.x) * blockDim.x) >> 5;
     for (u64 e = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; e < m; e += warps) {
         const u64 key = keys[e];
-        const f32 d = key_d(key);
-        const u64 idx = key_idx(key);
+        const f32 d = fmt.d(key);
+        const u64 idx = fmt.rips(key);
         u32 a, b;
         decode_edge(idx, a, b);
         const u32 w = warp_top_cofacet2(cx, a, b, d);
@@ -257,13 +262,13 @@ struct CsrCx {
 // edge's sorted position.
 // (32 registers: 64 warps an SM to hide the walk's load latency.)
 __global__ void __launch_bounds__(256, 8)
-    k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, const u32* __restrict__ inv, u64 m, u8* __restrict__ app,
-                   u32* __restrict__ emw, u8* __restrict__ emf) {
+    k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, EdgeFmt fmt, const u32* __restrict__ inv, u64 m,
+                   u8* __restrict__ app, u32* __restrict__ emw, u8* __restrict__ emf) {
     for (u64 t = u64(blockIdx.x) * blockDim.x + threadIdx.x; t < m; t += u64(gridDim.x) * blockDim.x) {
         const u64 e = inv[t];
         const u64 key = keys[e];
-        const f32 d = key_d(key);
-        const u64 idx = key_idx(key);
+        const f32 d = fmt.d(key);
+        const u64 idx = fmt.rips(key);
         u32 a, b;
         decode_edge(idx, a, b);
         f32 wax = 0.0f, wbx = 0.0f;
@@ -311,7 +316,7 @@ __global__ void k_iota(u32* __restrict__ p, u32 n) {
 // (The survivors' list grows by one atomic per warp: ranks from a ballot.
 // The first round offers all m edges; later rounds read their count from
 // the previous round's counter, so rounds run without a host round trip.)
-__global__ void k_bv_offer(const u64* __restrict__ keys, const u32* __restrict__ live,
+__global__ void k_bv_offer(const u64* __restrict__ keys, EdgeFmt fmt, const u32* __restrict__ live,
                            const u32* __restrict__ nlive_in, u32 m, const u32* __restrict__ comp,
                            u32* __restrict__ best, u32* __restrict__ live_out, u32* __restrict__ nlive_out) {
     const u32 lane = threadIdx.x & 31;
@@ -324,7 +329,7 @@ __global__ void k_bv_offer(const u64* __restrict__ keys, const u32* __restrict__
         if (t < nlive) {
             r = all ? t : live[t];
             u32 a, b;
-            decode_edge(key_idx(keys[r]), a, b);
+            decode_edge(fmt.rips(keys[r]), a, b);
             const u32 ca = comp[a], cb = comp[b];
             if (ca != cb) {
                 atomicMin(&best[ca], r);
@@ -345,7 +350,8 @@ __global__ void k_bv_offer(const u64* __restrict__ keys, const u32* __restrict__
 // hooks onto the other side; of a mutual pair only the larger root hooks.
 // (The hook count is summed per warp: one atomic a warp. A round whose offer
 // found no edge between components has nothing to hook: live == 0.)
-__global__ void k_bv_hook(const u64* __restrict__ keys, const u32* __restrict__ comp, const u32* __restrict__ best,
+__global__ void k_bv_hook(const u64* __restrict__ keys, EdgeFmt fmt, const u32* __restrict__ comp,
+                          const u32* __restrict__ best,
                           u32* __restrict__ parent, u8* __restrict__ tree, u32 n, u32* __restrict__ hooks,
                           const u32* __restrict__ live) {
     if (*live == 0) return;
@@ -355,7 +361,7 @@ __global__ void k_bv_hook(const u64* __restrict__ keys, const u32* __restrict__ 
         const u32 r = best[c];
         if (r == NOV) continue;
         u32 a, b;
-        decode_edge(key_idx(keys[r]), a, b);
+        decode_edge(fmt.rips(keys[r]), a, b);
         const u32 o = comp[a] == c ? comp[b] : comp[a];
         tree[r] = 1;
         if (best[o] == r && c < o) continue;   // mutual: o hooks onto c
@@ -382,15 +388,16 @@ __global__ void k_bv_flatten(const u32* __restrict__ parent, u32* __restrict__ c
 // --------------------------------------------------------------------------
 // One flag word per edge: finite H0 bar << 32 | column (m < 2^32, so one
 // scan counts both without a carry between the halves).
-__global__ void k_flags_dim0(const u64* __restrict__ keys, const u8* __restrict__ tree, const u8* __restrict__ app,
-                             u64 m, int want_cols, u64* __restrict__ f) {
+__global__ void k_flags_dim0(const u64* __restrict__ keys, EdgeFmt fmt, const u8* __restrict__ tree,
+                             const u8* __restrict__ app, u64 m, int want_cols, u64* __restrict__ f) {
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
         const bool t = tree[e];
-        f[e] = (u64(t && key_d(keys[e]) > 0.0f) << 32) | u64(want_cols && !t && !(app && app[e]));
+        f[e] = (u64(t && fmt.d(keys[e]) > 0.0f) << 32) | u64(want_cols && !t && !(app && app[e]));
     }
 }
 
-__global__ void k_emit_dim0(const u64* __restrict__ keys, const u8* __restrict__ tree, const u8* __restrict__ app,
+__global__ void k_emit_dim0(const u64* __restrict__ keys, EdgeFmt fmt, const u8* __restrict__ tree,
+                            const u8* __restrict__ app,
                             const u32* __restrict__ emw, const u8* __restrict__ emf, u64 m, int want_cols,
                             const u64* __restrict__ o2, const u64* __restrict__ tot,
                             f32* __restrict__ h0, u64* __restrict__ h0_edge, u64* __restrict__ cidx,
@@ -398,16 +405,16 @@ __global__ void k_emit_dim0(const u64* __restrict__ keys, const u8* __restrict__
     const u64 ncols = tot[0] & 0xffffffffull;
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
         const u64 key = keys[e];
-        const f32 d = key_d(key);
+        const f32 d = fmt.d(key);
         const bool t = tree[e];
         const u64 oe = o2[e];   // exclusive counts: H0 bars << 32 | columns
         if (t && d > 0.0f) {
             h0[oe >> 32] = d;
-            h0_edge[oe >> 32] = key_idx(key);   // the bar's critical (death) edge
+            h0_edge[oe >> 32] = fmt.rips(key);   // the bar's critical (death) edge
         }
         if (want_cols && !t && !(app && app[e])) {
             const u64 o = ncols - 1 - (oe & 0xffffffffull);   // descending order (rips.hpp:867)
-            const u64 idx = key_idx(key);
+            const u64 idx = fmt.rips(key);
             cidx[o] = idx;
             cd[o] = d;
             const u32 w = emw[e];
@@ -442,7 +449,9 @@ inline u32 grid_for(u64 work, u32 per_block) {
 // Slots: S_EDGE_CNT, S_EDGE_SORT, S_EDGE_IDX, S_EDGE_KEYS (result),
 // S_EDGE_INV (result: index order -> sorted position),
 // and the sort's own (S_SORT_A, S_SORT_HIST, S_SCAN*, S_MISC3).
-static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys_out) {
+// Above kPackedMaxN vertices the keys take the wide layout (EdgeFmt) and
+// *eidx_out the index table; otherwise *eidx_out is null.
+static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys_out, u64** eidx_out) {
     const u32 n = cx.n;
     u64 m = 0;
     u64* off = c->arena.get<u64>(S_EDGE_CNT, u64(n) + 2);
@@ -469,6 +478,8 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
     }
     if (m >= 0xffffffffull) invalid("gb300: more than 2^32 - 1 kept edges");
     u64* keys = c->arena.get<u64>(S_EDGE_KEYS, m + 1);
+    const bool wide = n > kPackedMaxN;
+    *eidx_out = nullptr;
     if (m) {
         u64* skey = c->arena.get<u64>(S_EDGE_SORT, m + 1);
         u64* sidx = c->arena.get<u64>(S_EDGE_IDX, m + 1);
@@ -483,7 +494,8 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
         const bool sw = dbits > 0 && radix_sort<u32>(c, skey, static_cast<u32*>(nullptr), m, kb,
                                                      static_cast<u32*>(nullptr), dbits, 32);
         u32* inv = c->arena.get<u32>(S_EDGE_INV, m + 1);
-        k_edge_pack<<<grid_for(m, 256), 256, 0, c->stream>>>(sw ? kb : skey, sidx, m, redzed, keys, inv);
+        k_edge_pack<<<grid_for(m, 256), 256, 0, c->stream>>>(sw ? kb : skey, sidx, m, redzed, wide, keys, inv);
+        if (wide) *eidx_out = sidx;
         TT_LAUNCH("k_edge_pack");
         c->launches += 2;
     }
@@ -492,9 +504,9 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
 }
 
 void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
-    if (cx.n > 131072) invalid("gb300: dim0 supports n <= 131072 vertices");
     out = Dim0Out{};
-    const u64 m = sorted_edge_keys(c, cx, 0, &out.keys);
+    const u64 m = sorted_edge_keys(c, cx, 0, &out.keys, &out.eidx);
+    const EdgeFmt fmt{out.eidx};
     out.m = m;
     if (m >= 0xffffffffull) invalid("gb300: more than 2^32 - 1 kept edges");
     const u32 n = cx.n;
@@ -512,10 +524,10 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
         u32* inv = c->arena.get<u32>(S_EDGE_INV, m + 1);
         cudaStream_t s = side.fork();
         if (cx.mat)
-            k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, s>>>(cx.mat, n, out.keys, m, app, emw, emf);
+            k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, s>>>(cx.mat, n, out.keys, fmt, m, app, emw, emf);
         else
-            k_apparent_csr<<<grid_for(m, 256), 256, 0, s>>>(CsrCx{cx.rp, cx.ci, cx.w}, out.keys, inv, m, app, emw,
-                                                            emf);
+            k_apparent_csr<<<grid_for(m, 256), 256, 0, s>>>(CsrCx{cx.rp, cx.ci, cx.w}, out.keys, fmt, inv, m, app,
+                                                            emw, emf);
         TT_LAUNCH("k_apparent");
         ++c->launches;
     }
@@ -544,8 +556,8 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
             const int first = round;
             for (int q = 0; q < kPerTrip && round < kRounds; ++q, ++round) {
                 k_bv_offer<<<grid_for(known, 256), 256, 0, c->stream>>>(
-                    out.keys, live0, round ? ctr + 2 * (round - 1) : nullptr, u32(m), comp, best, live1, ctr + 2 * round);
-                k_bv_hook<<<grid_for(n, 256), 256, 0, c->stream>>>(out.keys, comp, best, parent, tree, n,
+                    out.keys, fmt, live0, round ? ctr + 2 * (round - 1) : nullptr, u32(m), comp, best, live1, ctr + 2 * round);
+                k_bv_hook<<<grid_for(n, 256), 256, 0, c->stream>>>(out.keys, fmt, comp, best, parent, tree, n,
                                                                    ctr + 2 * round + 1, ctr + 2 * round);
                 k_bv_flatten<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, comp, best, n, ctr + 2 * round);
                 TT_LAUNCH("boruvka");
@@ -569,7 +581,7 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
     u64* o2 = f2 + m + 2;
     u64* tot = c->arena.get<u64>(S_COUNT, 4);
     if (m) {
-        k_flags_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, m, want_cols, f2);
+        k_flags_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, fmt, tree, out.app, m, want_cols, f2);
         TT_LAUNCH("k_flags_dim0");
         scan_exclusive<u64>(c, f2, o2, m, tot);
         c->launches += 1;
@@ -589,7 +601,8 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
     out.emf = c->arena.get<u8>(S_OUT4, h[1] + 1);
     out.h0_edge = c->arena.get<u64>(S_OUT5, h[0] + 1);
     if (m) {
-        k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, tree, out.app, emw, emf, m, want_cols, o2, tot,
+        k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, fmt, tree, out.app, emw, emf, m, want_cols, o2,
+                                                             tot,
                                                              out.h0, out.h0_edge, out.cidx, out.cd, out.emi, out.emf);
         TT_LAUNCH("k_emit_dim0");
         ++c->launches;
@@ -599,12 +612,13 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
 }
 
 namespace {
-__global__ void k_emit_redzed(const u64* __restrict__ keys, u64 m, f32* __restrict__ d, int32_t* __restrict__ v) {
+__global__ void k_emit_redzed(const u64* __restrict__ keys, EdgeFmt fmt, u64 m, f32* __restrict__ d,
+                              int32_t* __restrict__ v) {
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
         const u64 k = keys[e];
         u32 a, b;
-        decode_edge(k & kIdxMask, a, b);
-        d[e] = key_d(k);
+        decode_edge(fmt.redzed(k), a, b);
+        d[e] = fmt.d(k);
         v[2 * e] = int32_t(b);
         v[2 * e + 1] = int32_t(a);
     }
@@ -615,11 +629,11 @@ __global__ void k_emit_redzed(const u64* __restrict__ keys, u64 m, f32* __restri
 // (d asc, combinatorial index asc) order, vertices (i < j). Writes up to cap
 // edges to the device buffers d / verts and returns the edge count.
 u64 redzed_edges(tt_ctx* c, const Complex& cx, f32* d, int32_t* verts, u64 cap) {
-    if (cx.n > 131072) invalid("gb300: edge lists support n <= 131072 vertices");
     u64* keys = nullptr;
-    const u64 m = sorted_edge_keys(c, cx, 1, &keys);
+    u64* eidx = nullptr;
+    const u64 m = sorted_edge_keys(c, cx, 1, &keys, &eidx);
     if (m && m <= cap) {
-        k_emit_redzed<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, m, d, verts);
+        k_emit_redzed<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, EdgeFmt{eidx}, m, d, verts);
         TT_LAUNCH("k_emit_redzed");
         ++c->launches;
     }
@@ -629,13 +643,13 @@ u64 redzed_edges(tt_ctx* c, const Complex& cx, f32* d, int32_t* verts, u64 cap) 
 // The same edge list in context-owned device arrays sized to its count
 // (slots S_RZ_D / S_RZ_V), for the host-buffer entry points.
 u64 redzed_edges_owned(tt_ctx* c, const Complex& cx, f32** d, int32_t** verts) {
-    if (cx.n > 131072) invalid("gb300: edge lists support n <= 131072 vertices");
     u64* keys = nullptr;
-    const u64 m = sorted_edge_keys(c, cx, 1, &keys);
+    u64* eidx = nullptr;
+    const u64 m = sorted_edge_keys(c, cx, 1, &keys, &eidx);
     *d = c->arena.get<f32>(S_RZ_D, m + 1);
     *verts = c->arena.get<int32_t>(S_RZ_V, 2 * m + 2);
     if (m) {
-        k_emit_redzed<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, m, *d, *verts);
+        k_emit_redzed<<<grid_for(m, 256), 256, 0, c->stream>>>(keys, EdgeFmt{eidx}, m, *d, *verts);
         TT_LAUNCH("k_emit_redzed");
         ++c->launches;
     }

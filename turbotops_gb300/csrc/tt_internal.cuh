@@ -16,12 +16,17 @@ __host__ __device__ inline u64 key_rips(f32 d, u64 idx) {
     return (u64(fbits(d)) << kIdxBits) | (kIdxMask - idx);
 }
 
+// Edge indices fit the packed key's 33-bit field while n <= kPackedMaxN.
+constexpr u32 kPackedMaxN = 131072;
+
 // Simplex index helpers (combinatorial number system, rips.hpp:505-580).
 __device__ __forceinline__ void decode_edge(u64 idx, u32& a, u32& b) {
     // rips.hpp decode, nv = 2 closed form (:549-557): a > b. The FP32 closed
     // form is within one of the answer for idx < 2^40 (relative error below
-    // 2^-23 on a root below 2^21); the integer steps make it exact.
-    u64 v = u64((1.0f + sqrtf(fmaf(8.0f, float(idx), 1.0f))) * 0.5f);
+    // 2^-23 on a root below 2^21), the FP64 one for every 64-bit idx; the
+    // integer steps make it exact.
+    u64 v = idx < (1ull << 40) ? u64((1.0f + sqrtf(fmaf(8.0f, float(idx), 1.0f))) * 0.5f)
+                               : u64((1.0 + sqrt(fma(8.0, double(idx), 1.0))) * 0.5);
     while (v * (v - 1) / 2 > idx) --v;
     while ((v + 1) * v / 2 <= idx) ++v;
     a = u32(v);
@@ -41,6 +46,19 @@ __device__ __forceinline__ void sort3(u32& a, u32& b, u32& c) {   // descending
 }
 __device__ __forceinline__ f32 key_d(u64 k) { return __uint_as_float(u32(k >> kIdxBits)); }
 __device__ __forceinline__ u64 key_idx(u64 k) { return kIdxMask - (k & kIdxMask); }
+
+// Sorted edge keys come in two layouts. Packed (eidx == nullptr, n <=
+// kPackedMaxN): float bits of d << 33 | the index field above. Wide (larger
+// n, whose edge indices need more than 33 bits): float bits of d << 32 | q,
+// q the edge's position among the kept edges in index order (descending for
+// the Ripser order, ascending for RedZeD's, so that integer order is still
+// the filtration order), and eidx[q] the edge's index.
+struct EdgeFmt {
+    const u64* eidx = nullptr;
+    __device__ __forceinline__ f32 d(u64 k) const { return eidx ? __uint_as_float(u32(k >> 32)) : key_d(k); }
+    __device__ __forceinline__ u64 rips(u64 k) const { return eidx ? eidx[u32(k)] : key_idx(k); }
+    __device__ __forceinline__ u64 redzed(u64 k) const { return eidx ? eidx[u32(k)] : (k & kIdxMask); }
+};
 
 
 // ---- tt_dense.cu
@@ -63,6 +81,7 @@ void radix_reserve(tt_ctx* c, u64 n);   // every slot radix_sort of n keys may g
 struct Dim0Out {
     u64 m = 0;            // kept edges
     u64* keys = nullptr;  // m sorted Ripser keys (device)
+    u64* eidx = nullptr;  // wide layout (n > kPackedMaxN): edge index by index-order position
     u8* app = nullptr;    // m apparent flags (device), maxdim >= 1
     u8* tree = nullptr;   // m spanning-tree flags (device)
     u64 ncols = 0;        // dim-1 columns

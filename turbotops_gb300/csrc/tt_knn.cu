@@ -412,11 +412,12 @@ u64 radius_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32 t
     return nnz;
 }
 
-// One Borůvka proposal round over the complete graph: best[root] receives the
-// minimum (d, combinatorial index) edge leaving each component.
+// One Borůvka proposal scan over the complete graph: near[i] receives point
+// i's minimum (d, combinatorial index) edge to another component, as float
+// bits of d << 32 | the other endpoint (~0 when every point shares i's).
 void foreign_nearest(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* comp,
-                     unsigned long long* best, u32* err) {
-    scan_all(c, kind, x, n, dim, p, ForeignOp{comp, best}, comp, err);
+                     unsigned long long* near, u32* err) {
+    scan_all(c, kind, x, n, dim, p, ForeignOp{comp, near}, comp, err);
 }
 
 void check_device_error(tt_ctx* c, const u32* err) { check_error_word(c, err); }

@@ -4,53 +4,78 @@
 // finite H0 deaths are the weights of a minimum spanning tree, and every MST
 // of a graph has the same multiset of weights, so any MST gives the same
 // sorted death list. Here each round proposes, for every component, its
-// minimum outgoing edge under the strict order (d, combinatorial index)
-// (the all-pairs scan of tt_knn.cu); the proposals form a forest (only
-// mutual proposals close 2-cycles, broken by component id); components
-// merge, and after at most ceil(log2 n) rounds one tree remains. The deaths
-// are then sorted by a radix sort on their float bits.
+// minimum outgoing edge under the strict order (d, combinatorial index):
+// the all-pairs scan of tt_knn.cu finds each point's nearest point of
+// another component, then two passes over the points take the component's
+// minimum distance and, among its points at that distance, the minimum
+// edge index (64-bit: any n). The proposals form a forest (only mutual
+// proposals close 2-cycles, broken by component id); components merge, and
+// after at most ceil(log2 n) rounds one tree remains. The deaths are then
+// sorted by a radix sort on their float bits.
 #include "tt_internal.cuh"
 
 namespace tt {
 
 void foreign_nearest(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* comp,
-                     unsigned long long* best, u32* err);
+                     unsigned long long* near, u32* err);
 void check_device_error(tt_ctx* c, const u32* err);
 u32* device_error_word(tt_ctx* c);
 
 namespace {
 
-__global__ void k_mst_init(u32* __restrict__ comp, u32* __restrict__ parent, unsigned long long* __restrict__ best,
-                           u32 n) {
+constexpr u32 kNoD = 0xffffffffu;   // no proposal (above every float's bits)
+
+__global__ void k_mst_init(u32* __restrict__ comp, u32* __restrict__ parent, u32* __restrict__ bd,
+                           u64* __restrict__ bi, u32 n) {
     for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         comp[v] = v;
         parent[v] = v;
-        best[v] = ~0ull;
+        bd[v] = kNoD;
+        bi[v] = ~0ull;
     }
 }
 
-__global__ void k_mst_hook(const u32* __restrict__ comp, const unsigned long long* __restrict__ best,
+// Per component: the smallest distance bits among its points' proposals ...
+__global__ void k_mst_min_d(const u32* __restrict__ comp, const unsigned long long* __restrict__ near,
+                            u32* __restrict__ bd, u32 n) {
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const u64 k = near[i];
+        if (k != ~0ull) atomicMin(&bd[comp[i]], u32(k >> 32));
+    }
+}
+
+// ... and the smallest edge index among the proposals at that distance.
+__global__ void k_mst_min_idx(const u32* __restrict__ comp, const unsigned long long* __restrict__ near,
+                              const u32* __restrict__ bd, unsigned long long* __restrict__ bi, u32 n) {
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const u64 k = near[i];
+        const u32 c = comp[i];
+        if (k != ~0ull && u32(k >> 32) == bd[c]) atomicMin(&bi[c], (unsigned long long)edge_idx(i, u32(k)));
+    }
+}
+
+__global__ void k_mst_hook(const u32* __restrict__ comp, const u32* __restrict__ bd, const u64* __restrict__ bi,
                            u32* __restrict__ parent, u32 n, f32* __restrict__ deaths, u32* __restrict__ cnt) {
     for (u32 c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-        if (comp[c] != c) continue;
-        const u64 key = best[c];
-        if (key == ~0ull) continue;
+        if (comp[c] != c || bd[c] == kNoD) continue;
+        const u64 idx = bi[c];
         u32 a, b;
-        decode_edge(key & kIdxMask, a, b);
+        decode_edge(idx, a, b);
         const u32 o = comp[a] == c ? comp[b] : comp[a];
-        if (best[o] == key && c < o) continue;   // mutual: o hooks and records
+        if (bi[o] == idx && c < o) continue;   // mutual: o hooks and records
         parent[c] = o;
-        deaths[atomicAdd(cnt, 1u)] = __uint_as_float(u32(key >> kIdxBits));
+        deaths[atomicAdd(cnt, 1u)] = __uint_as_float(bd[c]);
     }
 }
 
-__global__ void k_mst_flatten(const u32* __restrict__ parent, u32* __restrict__ comp,
-                              unsigned long long* __restrict__ best, u32 n) {
+__global__ void k_mst_flatten(const u32* __restrict__ parent, u32* __restrict__ comp, u32* __restrict__ bd,
+                              u64* __restrict__ bi, u32 n) {
     for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         u32 r = parent[v];
         for (u32 s = 0; parent[r] != r && s < n; ++s) r = parent[r];
         comp[v] = r;
-        best[v] = ~0ull;
+        bd[v] = kNoD;
+        bi[v] = ~0ull;
     }
 }
 
@@ -71,22 +96,26 @@ inline u32 grid_for(u64 work) { return u32(std::max<u64>(1, std::min<u64>((work 
 // Sorted MST weights (n - 1 of them) into deaths (device). Returns n - 1.
 u64 mst_deaths(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32* deaths) {
     if (n < 2) return 0;
-    if (n > 131072) invalid("gb300: the complete-graph MST supports n <= 131072 points");
     u32* comp = c->arena.get<u32>(S_UF_PARENT, 2 * u64(n) + 2);
     u32* parent = comp + n + 1;
-    unsigned long long* best = c->arena.get<unsigned long long>(S_UF_BEST, n + 1);
+    unsigned long long* near = c->arena.get<unsigned long long>(S_UF_BEST, n + 1);
+    u64* bi = c->arena.get<u64>(S_UF_WORK, n + 1);
+    u32* bd = c->arena.get<u32>(S_UF_WORK2, n + 1);
     u32* cnt = c->arena.get<u32>(S_MISC1, 4);
     u32* err = device_error_word(c);
-    k_mst_init<<<grid_for(n), 256, 0, c->stream>>>(comp, parent, best, n);
+    k_mst_init<<<grid_for(n), 256, 0, c->stream>>>(comp, parent, bd, bi, n);
     TT_CUDA(cudaMemsetAsync(cnt, 0, sizeof(u32), c->stream));
     c->launches += 1;
     u32 done = 0;
     for (int round = 0; round < 40 && done < n - 1; ++round) {
-        foreign_nearest(c, x, n, dim, kind, p, comp, best, err);
-        k_mst_hook<<<grid_for(n), 256, 0, c->stream>>>(comp, best, parent, n, deaths, cnt);
-        k_mst_flatten<<<grid_for(n), 256, 0, c->stream>>>(parent, comp, best, n);
+        foreign_nearest(c, x, n, dim, kind, p, comp, near, err);
+        k_mst_min_d<<<grid_for(n), 256, 0, c->stream>>>(comp, near, bd, n);
+        k_mst_min_idx<<<grid_for(n), 256, 0, c->stream>>>(comp, near, bd, reinterpret_cast<unsigned long long*>(bi),
+                                                          n);
+        k_mst_hook<<<grid_for(n), 256, 0, c->stream>>>(comp, bd, bi, parent, n, deaths, cnt);
+        k_mst_flatten<<<grid_for(n), 256, 0, c->stream>>>(parent, comp, bd, bi, n);
         TT_LAUNCH("mst round");
-        c->launches += 2;
+        c->launches += 4;
         u32 h = 0;
         TT_CUDA(cudaMemcpyAsync(&h, cnt, 4, cudaMemcpyDeviceToHost, c->stream));
         TT_CUDA(cudaStreamSynchronize(c->stream));

@@ -121,9 +121,13 @@ std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim,
 void higher_dims(tt_ctx* c, const host::HostComplex& hc, const Dim0Out& r, std::vector<u64> piv, u32 maxdim,
                  Result& out) {
     const auto keys = to_host(c, r.keys, r.m);
+    std::vector<u64> eidx;
+    if (r.eidx) eidx = to_host(c, r.eidx, r.m);
     sync(c);
     std::vector<host::Entry> simp(r.m);
-    for (u64 i = 0; i < r.m; ++i) simp[i] = host::Entry{kIdxMask - (keys[i] & kIdxMask), bitsf(u32(keys[i] >> kIdxBits))};
+    for (u64 i = 0; i < r.m; ++i)
+        simp[i] = r.eidx ? host::Entry{eidx[u32(keys[i])], bitsf(u32(keys[i] >> 32))}
+                         : host::Entry{kIdxMask - (keys[i] & kIdxMask), bitsf(u32(keys[i] >> kIdxBits))};
     for (u32 dim = 1; dim < maxdim; ++dim) {
         std::vector<host::Entry> next;
         u64 napp = 0;

@@ -130,11 +130,14 @@ struct RadiusFillOp {
     __device__ __forceinline__ void finish(const State&, u32) const {}
 };
 
-// Nearest point of another component under the strict edge order
-// (d, combinatorial index): the per-round Borůvka proposal (tt_mst.cu).
+// Each point's nearest point of another component under the strict edge
+// order (d, combinatorial index): for a fixed point i the index of edge
+// (i, j) grows with j, so the per-point minimum of (d, j) is the minimum of
+// (d, index) over i's edges. near[i] = float bits of d << 32 | j (~0: none);
+// the Borůvka round (tt_mst.cu) reduces these per component.
 struct ForeignOp {
     const u32* comp;
-    unsigned long long* best;   // per component root
+    unsigned long long* near;   // per point
     struct State {
         u64 key;
         u32 c;
@@ -148,21 +151,18 @@ struct ForeignOp {
     __device__ __forceinline__ void visit_sq(State& s, u32 i, u32 j, f32 sq, const u32* tcomp) const {
         if (tcomp[0] == s.c || sq > s.thr_s) return;
         visit(s, i, j, __fsqrt_rn(sq), tcomp);
-        s.thr_s = sq_bound(__uint_as_float(u32(s.key >> kIdxBits)));
+        s.thr_s = sq_bound(__uint_as_float(u32(s.key >> 32)));
     }
     // The current proposal's distance (NaN while there is none: never skips).
     __device__ __forceinline__ f32 bound(const State& s) const {
-        return __uint_as_float(u32(s.key >> kIdxBits));
+        return __uint_as_float(u32(s.key >> 32));
     }
-    __device__ __forceinline__ void visit(State& s, u32 i, u32 j, f32 d, const u32* tcomp) const {
+    __device__ __forceinline__ void visit(State& s, u32, u32 j, f32 d, const u32* tcomp) const {
         if (tcomp[0] == s.c) return;
-        const u32 a = i > j ? i : j, b = i > j ? j : i;
-        const u64 key = (u64(__float_as_uint(d)) << kIdxBits) | (u64(a) * (a - 1) / 2 + b);
+        const u64 key = (u64(__float_as_uint(d)) << 32) | j;
         if (key < s.key) s.key = key;
     }
-    __device__ __forceinline__ void finish(const State& s, u32) const {
-        if (s.key != ~0ull) atomicMin(&best[s.c], (unsigned long long)s.key);
-    }
+    __device__ __forceinline__ void finish(const State& s, u32 i) const { near[i] = s.key; }
 };
 
 template <typename Op>
