@@ -353,6 +353,20 @@ typedef struct tt_barcode {
     uint64_t columns[32], apparent[32], emergent[32];
 } tt_barcode;
 
+/* read_text_points (src/turbotops.cpp:126-155) on the device: the bytes of
+ * a text file (text_h, a leading UTF-8 BOM skipped; one point per '\n'-ended
+ * line, '#' starting a comment, separators ' ', '\t', '\v', '\f', '\r',
+ * ',', ';') -> *n points of *dim float32 coordinates in pts_h (row-major, up
+ * to cap floats; bytes / 2 + 1 always suffice), each the value std::strtof
+ * gives the token. Decimal and "inf" tokens are converted on the GPU
+ * (correctly rounded); other tokens, and decimals of more than 19 significant
+ * digits that the first 19 cannot decide, by the host C library's strtof.
+ * Errors (TT_ERR_INVALID), the first in file order as the reference reports
+ * them: "bad coordinate '<token>'", "inconsistent row length at point N"
+ * (the reference's CLI prefixes the path). */
+int tt_parse_points_h(tt_ctx* ctx, const char* text_h, uint64_t bytes, float* pts_h, uint64_t cap, uint32_t* n,
+                      uint32_t* dim);
+
 /* tops::persistence(points, n, dim, Options) (turbotops.hpp:211-303) with
  * the front end on the GPU and compute_pairs on the host:
  *   knn = 0, maxdim = 0          complete-graph MST H0 (mst::h0)

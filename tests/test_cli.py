@@ -29,9 +29,11 @@ def test_cli_golden_diagrams(case, tmp_path):
     assert r.stdout == case["stdout"]
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("case", ERR_CASES, ids=[c["input"].split()[-2] for c in ERR_CASES])
 def test_cli_golden_errors(case, tmp_path):
-    """Inputs the reference CLI rejects while parsing: same exit code, same message."""
+    """Inputs the reference CLI rejects: same exit code, same message (the
+    points are read on the device)."""
     p = tmp_path / "in.txt"
     p.write_text(case["input"])
     r = cli("run", str(p), *case["args"], "--quiet")
@@ -85,15 +87,22 @@ def test_cli_errors_exit_2(args, msg):
     assert r.returncode == 2 and msg in r.stderr and r.stderr.startswith("turbotops: ")
 
 
-def test_cli_rejects_bad_rows_metric_and_flags(tmp_path):
+@pytest.mark.gpu
+def test_cli_rejects_bad_rows_and_metric(tmp_path):
     p = tmp_path / "bad.txt"
     p.write_text("0 0\n1 0 2\n")
     r = cli("run", str(p))
-    assert r.returncode == 2 and "inconsistent row length" in r.stderr
+    assert r.returncode == 2 and r.stderr == f"turbotops: {p}: inconsistent row length at point 1\n"
     q = tmp_path / "ok.txt"
     q.write_text("0 0\n1 0\n")
     r = cli("run", str(q), "--metric", "cosine")
     assert r.returncode == 2 and "metric: unknown 'cosine'" in r.stderr
+
+
+def test_cli_rejects_flags(tmp_path):
+    """Option errors come before the input is read (no GPU needed)."""
+    q = tmp_path / "ok.txt"
+    q.write_text("0 0\n1 0\n")
     r = cli("run", str(q), "--frobnicate")
     assert r.returncode == 2 and "unknown option" in r.stderr
     r = cli("run", str(q), "--graph", "star")

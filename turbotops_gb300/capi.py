@@ -54,6 +54,7 @@ _SIGS = {
     "tt_copy_async": (i32, [P, P, P, C.c_size_t]),
     "tt_ctx_set_knn_mode": (i32, [P, i32]),
     "tt_ctx_set_memory_budget": (i32, [P, u64]),
+    "tt_parse_points_h": (i32, [P, P, u64, P, u64, C.POINTER(u32), C.POINTER(u32)]),
     "tt_ctx_filter_evals": (u64, [P]),
     "tt_ctx_filter_tiles": (u64, [P]),
     "tt_tc_gram_check": (i32, [P, u32, u64, P]),

@@ -106,27 +106,26 @@ def _parse_u32(tok: str, what: str) -> int:
 
 
 def read_text_points(path: str) -> np.ndarray:
+    """read_text_points (src/turbotops.cpp:126-155), converted on the GPU
+    (tt_parse_points_h): the same lines, comments, separators, strtof values
+    and messages."""
     try:
         raw = open(path, "rb").read()
     except OSError:
         raise CliError(f"cannot open {path}") from None
-    if raw.startswith(b"\xef\xbb\xbf"):
-        raw = raw[3:]
-    rows, dim = [], 0
-    for line in raw.decode("utf-8", "replace").splitlines():
-        line = line.split("#", 1)[0]
-        for ch in ",\t;":
-            line = line.replace(ch, " ")
-        toks = line.split()
-        if not toks:
-            continue
-        vals = [_parse_f32(t, "coordinate") for t in toks]
-        if not dim:
-            dim = len(vals)
-        elif len(vals) != dim:
-            raise CliError(f"{path}: inconsistent row length at point {len(rows)}")
-        rows.append(vals)
-    return np.asarray(rows, dtype=np.float32).reshape(len(rows), dim if rows else 0)
+    import ctypes
+    from . import api, capi
+    ctx = api._context(0)
+    cap = len(raw) // 2 + 2
+    pts = np.empty(cap, dtype=np.float32)
+    n, dim = ctypes.c_uint32(), ctypes.c_uint32()
+    st = ctx.L.tt_parse_points_h(ctx.h, raw, len(raw), pts.ctypes.data, cap, ctypes.byref(n), ctypes.byref(dim))
+    if st != capi.OK:
+        msg = ctx.L.tt_last_error(ctx.h).decode("utf-8", "surrogateescape")
+        if st == capi.ERR_INVALID:
+            raise CliError(f"{path}: {msg}" if msg.startswith("inconsistent row length") else msg)
+        capi.raise_for(st, msg)
+    return pts[: n.value * dim.value].reshape(n.value, dim.value).copy()
 
 
 def _parse_u64(tok: str, what: str) -> int:
@@ -291,7 +290,8 @@ def main(argv=None) -> int:
         if argv[0] == "run":
             return run(argv[1:])
         raise CliError(f"unknown command '{argv[0]}'\n" + USAGE)
-    except CliError as e:
+    except (CliError, RuntimeError, MemoryError, OverflowError, ValueError) as e:
+        # the reference's CLI: every std::exception -> "turbotops: <what>", exit 2
         sys.stderr.write(f"turbotops: {e}\n")
         return 2
 

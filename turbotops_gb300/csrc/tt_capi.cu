@@ -647,4 +647,12 @@ int tt_graph_redzed_h(tt_ctx* c, const uint64_t* rp_h, const uint32_t* ci_h, con
     });
 }
 
+int tt_parse_points_h(tt_ctx* c, const char* text_h, uint64_t bytes, float* pts_h, uint64_t cap, uint32_t* n,
+                      uint32_t* dim) {
+    return guard(c, [&] {
+        if (!n || !dim || (bytes && !text_h) || (cap && !pts_h)) invalid("gb300: null argument");
+        parse_points(c, text_h, bytes, pts_h, cap, n, dim);
+    });
+}
+
 }  // extern "C"
