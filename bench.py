@@ -570,16 +570,21 @@ def batch_block(ctx, dev, reps: int = 5) -> dict:
 def batch_traffic(sizes, edges: int, ms: float) -> dict:
     """Algorithmic HBM bytes of one batched run: the matrices written (4 B a
     pair, full layout) and their lower triangles read twice (count, keys),
-    the kept keys written once and moved by 4 stable radix passes (read for
-    the histogram, read and written by the scatter: 24 B an edge a pass), the
-    edge list emitted (8 B key read, 12 B written)."""
+    the kept keys written once and moved by the stable radix passes over the
+    cloud and distance bits (read for the histogram, read and written by the
+    scatter: 24 B an edge a pass; digits of 8 bits for sorts of 2^22 keys or
+    more, else 11), the edge list emitted (8 B key read, 12 B written)."""
     pk, src = peaks()
     mat = 4 * sum(n * n for n in sizes)
     tri = 4 * sum(n * (n - 1) // 2 for n in sizes)
-    b = mat + 2 * tri + 8 * edges + 4 * 24 * edges + 20 * edges
+    pairs = sum(n * (n - 1) // 2 for n in sizes)
+    bits = 31 + max(0, (len(sizes) - 1).bit_length())
+    digit = 8 if pairs >= 1 << 22 else 11
+    passes = -(-bits // digit)
+    b = mat + 2 * tri + 8 * edges + passes * 24 * edges + 20 * edges
     gbs = b / (ms * 1e-3) / 1e9
-    return {"algorithmic_bytes": b, "achieved_gbs": gbs, "peak_gbs": pk["hbm_gbs"], "frac": gbs / pk["hbm_gbs"],
-            "peak_source": src}
+    return {"algorithmic_bytes": b, "radix_passes": passes, "achieved_gbs": gbs, "peak_gbs": pk["hbm_gbs"],
+            "frac": gbs / pk["hbm_gbs"], "peak_source": src}
 
 
 def topo_block(dev, reps: int = 2) -> dict:

@@ -54,3 +54,26 @@ def test_batch_vs_oracle():
         assert np.array_equal(bits(host(r["diam"])[s:e]), bits(d))
         assert np.array_equal(host(r["verts"])[2 * s:2 * e], v)
     b.close()
+
+
+def test_large_batch_matches_per_cloud():
+    """A batch whose sort exceeds 4M keys (the radix sort then orders every
+    tile by digit in shared memory and writes runs): still the per-cloud
+    edge lists, bit for bit."""
+    clouds = _clouds(5, 1700, 2000, 41)
+    sizes = [c.shape[0] for c in clouds]
+    assert sum(s * (s - 1) // 2 for s in sizes) >= 1 << 22
+    b = ops.DenseBatch(ctx(), sizes, 3, "l2", use_graph=True)
+    b.load(dev(np.concatenate(clouds)))
+    for _ in range(2):
+        b.run()
+        r = b.result()
+        off = host(r["edge_offset"])
+        d_all, v_all = host(r["diam"]), host(r["verts"])
+        for q, x in enumerate(clouds):
+            mat, enc = ops.make_dense(ctx(), dev(x), "l2")
+            d, v = ops.redzed_edges(ctx(), mat=mat, threshold=enc)
+            s, e = int(off[q]), int(off[q + 1])
+            assert np.array_equal(bits(d_all[s:e]), bits(host(d))), q
+            assert np.array_equal(v_all[2 * s:2 * e], host(v)), q
+    b.close()

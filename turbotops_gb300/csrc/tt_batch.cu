@@ -58,12 +58,16 @@ k_batch_dense(const f32* __restrict__ x, const u64* __restrict__ pt_off, const u
               f32* __restrict__ mats, u32* __restrict__ rowmax, u32* __restrict__ next) {
     constexpr int BT_Y = BT_THREADS / BT_C;
     static_assert(BT_C % 32 == 0 && BT_R <= BT_THREADS, "warps span whole tile rows");
-    __shared__ u32 smax[BT_R];
+    // The matrix is symmetric bit for bit and the tiles cover both triangles,
+    // so the row maxima are also the column maxima: each thread folds the
+    // maximum of its column over its rows, one shared atomic a thread and one
+    // global atomic a column per tile.
+    __shared__ u32 cmax[BT_C];
     __shared__ u32 tile_id;
     const u32 tx = threadIdx.x, ty = threadIdx.y, tid = ty * BT_C + tx;
     for (;;) {
         if (tid == 0) tile_id = atomicAdd(next, 1u);
-        if (tid < BT_R) smax[tid] = 0u;
+        if (tid < BT_C) cmax[tid] = 0u;
         __syncthreads();
         const u32 t = tile_id;
         if (t >= ntiles) break;
@@ -72,21 +76,19 @@ k_batch_dense(const f32* __restrict__ x, const u64* __restrict__ pt_off, const u
         const f32* xc = x + pt_off[tl.cloud] * dim;
         f32* mc = mats + mat_off[tl.cloud];
         const u32 j = tl.j0 + tx;
-        for (u32 r = ty; r < BT_R; r += BT_Y) {
-            const u32 i = tl.i0 + r;
-            if (i >= n) break;
-            f32 d = 0.0f;
-            if (j < n) {
-                d = (i == j) ? 0.0f : metric_dist(KIND, p, Row{xc + u64(i) * dim}, Row{xc + u64(j) * dim}, dim);
+        u32 cm = 0;
+        if (j < n) {
+            for (u32 r = ty; r < BT_R; r += BT_Y) {
+                const u32 i = tl.i0 + r;
+                if (i >= n) break;
+                const f32 d = (i == j) ? 0.0f : metric_dist(KIND, p, Row{xc + u64(i) * dim}, Row{xc + u64(j) * dim}, dim);
                 mc[u64(i) * n + j] = d;
+                cm = max(cm, __float_as_uint(d));
             }
-            u32 v = __float_as_uint(d);
-#pragma unroll
-            for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-            if ((tx & 31) == 0) atomicMax(&smax[r], v);
+            atomicMax(&cmax[tx], cm);
         }
         __syncthreads();
-        if (tid < BT_R && tl.i0 + tid < n) atomicMax(&rowmax[pt_off[tl.cloud] + tl.i0 + tid], smax[tid]);
+        if (tid < BT_C && tl.j0 + tid < n) atomicMax(&rowmax[pt_off[tl.cloud] + tl.j0 + tid], cmax[tid]);
         __syncthreads();
     }
 }

@@ -23,6 +23,7 @@ namespace {
 constexpr int RS_THREADS = 256, RS_ITEMS = 16, RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_MAXBITS = 11, RS_BINS = 1 << RS_MAXBITS;   // digit width and bins per pass (at most)
+constexpr int RS_LBITS = 8, RS_LBINS = 1 << RS_LBITS;       // the same for the local scatter (large inputs)
 constexpr int SCAN_THREADS = 512, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 // ---------------------------------------------------------------------------
@@ -100,20 +101,26 @@ __global__ void k_tile_scan(const T* __restrict__ in, u64 n, const T* __restrict
 // Digits of up to RS_MAXBITS bits (a pass sorts `width` bits from `shift`).
 // ndev (optional): the key count lives on the device (a graph-captured sort of
 // a data-dependent number of keys, n the capacity); tiles past it are empty.
+template <int BINS>
 __global__ void __launch_bounds__(RS_THREADS)
 k_rs_upsweep(const u64* __restrict__ keys, u64 n, const unsigned long long* __restrict__ ndev, int shift, u32 width,
              u32* __restrict__ hist, u32 tiles) {
-    __shared__ u32 h[RS_WARPS][RS_BINS];
+    __shared__ u32 h[RS_WARPS][BINS];
     if (ndev) n = min(n, u64(*ndev));
     const u32 nd = 1u << width, mask = nd - 1u;
     for (u32 t = threadIdx.x; t < RS_WARPS * nd; t += RS_THREADS) h[t / nd][t % nd] = 0;
     __syncthreads();
-    const int w = threadIdx.x >> 5;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const u64 base = u64(blockIdx.x) * RS_TILE;
+    // one shared-memory atomic per distinct digit of a warp's 32 keys (keys
+    // of one digit come in runs once the higher passes see nearly sorted
+    // input, and per-key atomics on one counter would serialise)
 #pragma unroll 4
     for (int i = 0; i < RS_ITEMS; ++i) {
         const u64 k = base + u64(i) * RS_THREADS + threadIdx.x;
-        if (k < n) atomicAdd(&h[w][u32(keys[k] >> shift) & mask], 1u);
+        const u32 dg = k < n ? u32(keys[k] >> shift) & mask : u32(BINS);
+        const u32 peers = __match_any_sync(0xffffffffu, dg);
+        if (lane == __ffs(peers) - 1 && dg < u32(BINS)) atomicAdd(&h[w][dg], u32(__popc(peers)));
     }
     __syncthreads();
     for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) {
@@ -185,6 +192,104 @@ k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __res
         }
     }
 }
+
+// The same pass for large inputs, digits of at most RS_LBITS bits: the tile
+// is first ordered by digit in shared memory (stable), then written out in
+// that order, so the keys of one digit leave a tile as one contiguous run
+// (about RS_TILE / 2^width keys) instead of scattered 8-byte writes.
+template <typename V, bool VALS>
+__global__ void __launch_bounds__(RS_THREADS)
+k_rs_scatter_local(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __restrict__ vin,
+                   V* __restrict__ vout, u64 n, const unsigned long long* __restrict__ ndev, int shift, u32 width,
+                   const u32* __restrict__ offs, u32 tiles) {
+    __shared__ u64 skey[RS_TILE];
+    __shared__ V sval[VALS ? RS_TILE : 1];
+    __shared__ u32 cnt[RS_WARPS][RS_LBINS];   // per-warp running count, then warp prefix
+    __shared__ u32 gbase[RS_LBINS];
+    __shared__ u32 tstart[RS_LBINS];          // the digit's first position in the ordered tile
+    __shared__ u32 wsum[RS_WARPS];
+    if (ndev) n = min(n, u64(*ndev));
+    const u64 tbase = u64(blockIdx.x) * RS_TILE;
+    if (tbase >= n) return;
+    const u32 nd = 1u << width, mask = nd - 1u;
+    for (u32 t = threadIdx.x; t < RS_WARPS * RS_LBINS; t += RS_THREADS) cnt[t / RS_LBINS][t % RS_LBINS] = 0;
+    for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) gbase[d] = offs[u64(d) * tiles + blockIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const u32 lt = (1u << lane) - 1u;
+    // ranks within the warp's keys, item-major (as k_rs_scatter)
+    const u64 base = tbase + u64(w) * 32 * RS_ITEMS;
+    u64 key[RS_ITEMS];
+    V val[VALS ? RS_ITEMS : 1];
+    u32 rank[RS_ITEMS];
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; ++i) {
+        const u64 k = base + u64(i) * 32 + lane;
+        const bool ok = k < n;
+        key[i] = ok ? kin[k] : ~0ull;
+        if constexpr (VALS) val[i] = ok ? vin[k] : V(0);
+        const u32 dg = ok ? u32(key[i] >> shift) & mask : u32(RS_LBINS);   // RS_LBINS: no key
+        const u32 peers = __match_any_sync(0xffffffffu, dg);
+        const u32 before = __popc(peers & lt);
+        const int leader = __ffs(peers) - 1;
+        u32 prev = 0;
+        if (lane == leader && dg < u32(RS_LBINS)) {
+            prev = cnt[w][dg];
+            cnt[w][dg] = prev + __popc(peers);
+        }
+        prev = __shfl_sync(0xffffffffu, prev, leader);
+        rank[i] = prev + before;
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: exclusive prefix over warps and the digit's total; then an
+    // exclusive scan of the totals over the digits (one digit a thread)
+    u32 tot = 0;
+    const u32 d = threadIdx.x;   // RS_LBINS == RS_THREADS
+    if (d < nd) {
+#pragma unroll
+        for (int q = 0; q < RS_WARPS; ++q) {
+            const u32 c = cnt[q][d];
+            cnt[q][d] = tot;
+            tot += c;
+        }
+    }
+    u32 inc = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    u32 wpre = 0;
+#pragma unroll
+    for (int q = 0; q < RS_WARPS; ++q) wpre += q < w ? wsum[q] : 0u;
+    tstart[d] = wpre + inc - tot;
+    __syncthreads();
+    // order the tile by digit in shared memory
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; ++i) {
+        const u64 k = base + u64(i) * 32 + lane;
+        if (k < n) {
+            const u32 dg = u32(key[i] >> shift) & mask;
+            const u32 lp = tstart[dg] + cnt[w][dg] + rank[i];
+            skey[lp] = key[i];
+            if constexpr (VALS) sval[lp] = val[i];
+        }
+    }
+    __syncthreads();
+    // write out in that order: runs of one digit go to consecutive positions
+    const u32 valid = u32(min(u64(RS_TILE), n - tbase));
+    for (u32 j = threadIdx.x; j < valid; j += RS_THREADS) {
+        const u64 kk = skey[j];
+        const u32 dg = u32(kk >> shift) & mask;
+        const u32 pos = gbase[dg] + (j - tstart[dg]);
+        kout[pos] = kk;
+        if constexpr (VALS) vout[pos] = sval[j];
+    }
+}
+static_assert(RS_LBINS == RS_THREADS, "one digit a thread in the local scatter's scan");
 
 __global__ void k_minmax(const u64* __restrict__ keys, u64 n, unsigned long long* __restrict__ mm) {
     u64 lo = ~0ull, hi = 0;
@@ -267,16 +372,30 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
     V *va = vals, *vb = vbuf;
     bool swapped = false;
     // as few passes as digits of up to RS_MAXBITS bits allow, the bits
-    // spread evenly over them (25 bits: 9 + 8 + 8; 11 bits: one pass)
-    const int passes = (bits + RS_MAXBITS - 1) / RS_MAXBITS;
+    // spread evenly over them (25 bits: 9 + 8 + 8; 11 bits: one pass). Inputs
+    // far beyond L2 take digits of at most RS_LBITS bits and the local
+    // scatter: more passes, each writing contiguous runs.
+    const bool local = n >= (u64(1) << 22);
+    const int maxbits = local ? RS_LBITS : RS_MAXBITS;
+    const int passes = (bits + maxbits - 1) / maxbits;
     int shift = lo_bit;
     for (int q = 0; q < passes; ++q) {
         const int width = (lo_bit + bits - shift + (passes - q) - 1) / (passes - q);
-        k_rs_upsweep<<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, ndev, shift, u32(width), hist, tiles);
+        if (local)
+            k_rs_upsweep<RS_LBINS><<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, ndev, shift, u32(width), hist, tiles);
+        else
+            k_rs_upsweep<RS_BINS><<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, ndev, shift, u32(width), hist, tiles);
         TT_LAUNCH("k_rs_upsweep");
         scan_exclusive<u32>(c, hist, hist, u64(tiles) << width, nullptr, 0);
-        k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift, u32(width), hist,
-                                                             tiles);
+        if (local && va)
+            k_rs_scatter_local<V, true><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift,
+                                                                             u32(width), hist, tiles);
+        else if (local)
+            k_rs_scatter_local<V, false><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift,
+                                                                              u32(width), hist, tiles);
+        else
+            k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift, u32(width), hist,
+                                                                 tiles);
         TT_LAUNCH("k_rs_scatter");
         c->launches += 2;
         std::swap(ka, kb);
