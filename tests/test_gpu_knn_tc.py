@@ -115,11 +115,12 @@ def test_tile_order_prunes_and_matches_at_scale():
 
 
 def test_tensor_core_accumulation_bound():
-    """The Gram filter assumes that kind::tf32 with FP32 accumulation errs by at
-    most 2^-19 (|a|^2 + |b|^2) on TF32-exact operands (the filter's margins are
-    2^-16 of the norms). Measured on 304 seeded 128 x 128 products, issued as
-    the kNN kernel issues them: mixed exponents and signs, and rows near a
-    common offset where the sum cancels."""
+    """The Gram filter's margins are derived for an FP32 accumulation error of
+    at most 2^-17 (|a|^2 + |b|^2) in kind::tf32 on TF32-exact operands (the
+    bound that 24-bit alignment and truncation in each accumulation step
+    implies). Measured on 304 seeded 128 x 128 products, issued as the kNN
+    kernel issues them: mixed exponents and signs, and rows near a common
+    offset where the sum cancels; asserted 4x tighter than needed."""
     c = ctx()
     r = C.c_double()
     c.check(c.L.tt_tc_gram_check(c.h, 304, 12345, C.byref(r)))

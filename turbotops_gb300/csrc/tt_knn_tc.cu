@@ -25,8 +25,9 @@
 //    reassembles x bit for bit. For a loaded tile the tensor core produces
 //      D(q, c) = q~ . c~ - W(c),   W(c) <= |c~|^2 (1 - 2^-16) / 2,
 //    the norm term entering as a fifth K-step (two TF32-exact parts). Only
-//    the FP32 accumulation rounds (<= 2^-19 (|q~|^2 + |c~|^2); measured on
-//    the device by k_tc_gram_check below: under 2^-22 on GB300), so
+//    the FP32 accumulation rounds, by at most E = 2^-17 S, S = |q~|^2 +
+//    |c~|^2 (the accumulation bound below; k_tc_gram_check measures under
+//    2^-22 S on GB300), so
 //      L = |q~|^2 (1 - 2^-16) - 2 D <= |q~ - c~|^2,
 //    and with e_x >= |x - x~| (per point, rounded up) the true distance is
 //    at least sqrt(L) - e_q - e_c. A candidate is evaluated exactly when
@@ -38,6 +39,25 @@
 //    |q|^2 + |c|^2: points far from the origin filter as tightly as points
 //    near it. The epilogue is a max over the accumulator row and one
 //    compare.
+//
+// The accumulation bound. The products of TF32-exact operands are exact
+// (11-bit significands: 22 bits, within FP32's 24), and every product and
+// every partial sum of the exact values is at most |q~| |c~| <= S / 2 in
+// magnitude. The filter assumes one thing of the tensor core's FP32
+// accumulation: each accumulation step adds a block of b products (b in
+// {1, 2, 4, 8}) to the running sum by aligning the terms to the largest and
+// keeping at least 24 significant bits of it (truncating or rounding the
+// rest), then normalises the result to FP32 (within one unit in its last
+// place). That is the behaviour the published studies of NVIDIA tensor
+// cores measured (products exact, alignment to the largest term, truncation,
+// 24 bits or more), and it is the weakest of them. A step then errs by less
+// than 2^-24 S per aligned term (b products and the running sum) plus 2^-24 S
+// for the normalisation: (b + 2) 2^-24 S a step, (8 / b) steps a K = 8
+// instruction, at most 24 x 2^-24 S an instruction (b = 1), and the five
+// instructions of a tile product (four over the coordinates, one over the
+// norm term) at most 120 x 2^-24 S < E = 2^-17 S. Every margin below is
+// derived for E; the lookahead product (four instructions) has the same
+// bound with S = |q~|^2 + |c|^2.
 //
 // Pipeline per CTA (128 threads = 4 warps, one query row per thread, 128
 // queries per block, persistent over query blocks):
@@ -762,8 +782,9 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
                 // tensor core. Both operands are TF32-exact (q~: the query's
                 // head; c: rounded when the record was made), so the products
                 // are exact and only the FP32 accumulation rounds:
-                // |G - q~.c| <= 2^-19 (|q~|^2 + |c|^2). With s2 = nq + |c|^2
-                // (nq rounded down, |c|^2 within 2^-19),
+                // |G - q~.c| <= 2^-17 (|q~|^2 + |c|^2) (the accumulation
+                // bound). With s2 = nq + |c|^2 (nq rounded down, |c|^2 within
+                // 2^-19),
                 //   lower = s2 (1 - 2^-16) - 2 G - 2^-120 <= |q~ - c|^2
                 // (rounded down; the absolute term covers products in the
                 // subnormal range),
@@ -911,7 +932,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
                 const u32* oid = reinterpret_cast<const u32*>(S.pk[st] + PK_ID);
                 // Gram filter. D = G + w_hi + w_lo with G = q~ . c~ (TF32-exact
                 // heads: exact products, FP32 accumulation, |G - q~.c~| <=
-                // 2^-19 (|q~|^2 + |c~|^2)) and -w_hi - w_lo <= |c~|^2 (1 - 2^-16) / 2,
+                // 2^-17 (|q~|^2 + |c~|^2)) and -w_hi - w_lo <= |c~|^2 (1 - 2^-16) / 2,
                 // so L = nq (1 - 2^-16) - 2 D <= |q~ - c~|^2. A candidate that can
                 // enter has |q - c| <= sqrt(T), and |q - c| >= |q~ - c~| - e_q - e_c
                 // with e_c <= e_T (the tile's largest), so its L <= (sq + e_T)^2:
@@ -971,11 +992,12 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
                     // Mostly the first tile of a block: the lists are empty and
                     // every candidate passed. The tile bounds its own k-th
                     // distance. For a candidate |q~ - c~|^2 <= (|q~|^2 + |c~|^2)
-                    // (1 + 2^-18) - 2 (D + w_hi + w_lo) and |c~|^2 <= -2 (w_hi + w_lo)
-                    // (1 + 2^-15), so with N_T the tile's largest |c~|^2,
-                    // u = nq (1 + 2^-16) - 2 D + 2^-14 N_T >= |q~ - c~|^2 (rounded
-                    // up; a negative or NaN u, which only overflow can make, is
-                    // no bound). The k-th smallest of 32 group minima of u (4
+                    // (1 + 2^-16) - 2 (D - w_hi - w_lo) (the accumulation bound)
+                    // and |c~|^2 + 2 (w_hi + w_lo) <= 2^-15.6 |c~|^2, so with N_T
+                    // the tile's largest |c~|^2 (rounded down, as nq: within
+                    // 2^-18), u = nq (1 + 2^-15) - 2 D + 2^-14 N_T >= |q~ - c~|^2
+                    // (rounded up; a negative or NaN u, which only overflow can
+                    // make, is no bound). The k-th smallest of 32 group minima of u (4
                     // candidates a group) is u of k distinct candidates, whose
                     // true distances are then <= sqrt(u_k) + e_q + e_T; with the
                     // lane-ordered sums' rounding, no candidate farther than
@@ -997,7 +1019,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
                             }
                         }
                         const f32 NT = trec.w;
-                        const f32 au = __fmaf_ru(NT, 0x1p-14f, __fmul_ru(nqi, 1.0f + 0x1p-16f));
+                        const f32 au = __fmaf_ru(NT, 0x1p-14f, __fmul_ru(nqi, 1.0f + 0x1p-15f));
 #pragma unroll
                         for (int g = 0; g < 32; ++g) {
                             const f32 u = __fmaf_ru(-2.0f, gm[g], au);
@@ -1171,10 +1193,10 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
 
 // ---- a check of the tensor core's accumulation bound ------------------------
 //
-// The Gram filter's margins rest on one property of kind::tf32 with FP32
-// accumulation: for TF32-exact operands (exact products) the accumulated
-// result D of the five K-steps (32 coordinates and the augmentation) errs
-// by at most 2^-19 (|a|^2 + |b|^2) from the exact sum. This kernel measures
+// The Gram filter's margins are derived for an accumulation error of at
+// most 2^-17 (|a|^2 + |b|^2) over the five K-steps (32 coordinates and the
+// augmentation) of kind::tf32 with FP32 accumulation on TF32-exact operands
+// (the accumulation bound at the top of this file). This kernel measures
 // that error on the device: one 128 x 128 product per CTA of seeded
 // TF32-exact rows (mixed exponents 2^-8 .. 2^8 and signs, and rows near a
 // common offset, where the sum cancels), issued exactly as the kNN kernel
