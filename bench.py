@@ -631,6 +631,38 @@ def topo_block(dev, reps: int = 2) -> dict:
             "host_threads": os.cpu_count(), "batched_over_per_cloud": pt / bt}
 
 
+def batch_only(count: int) -> int:
+    """The batched front end alone (first `count` of the 512 clouds): one
+    capture with the autotuner's pick, then three timed graph replays; prints
+    one line with their device times. For profiling runs."""
+    import numpy as np
+    import torch
+
+    from turbotops_gb300 import capi, ops, synth
+    from turbotops_gb300.capi import Context
+    dev = torch.device("cuda", 0)
+    ctx = Context(0)
+    clouds = synth.circle_batch()[:count]
+    b = ops.DenseBatch(ctx, [c.shape[0] for c in clouds], 3, "l2", use_graph=True)
+    b.load(torch.from_numpy(np.concatenate(clouds)).to(dev))
+    b.run()
+    out = capi.BatchOut()
+    ctx.check(ctx.L.tt_batch_result(b.h, C.byref(out)))
+    bs = torch.cuda.ExternalStream(out.stream, device=dev)
+    ms = []
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(bs)
+        b.run(wait=False)
+        e1.record(bs)
+        e1.synchronize()
+        ms.append(round(e0.elapsed_time(e1), 3))
+    b.close()
+    print(json.dumps({"batch_clouds": count, "replay_ms": ms}))
+    return 0
+
+
 def main():
     global N
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
@@ -644,8 +676,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / differentiable blocks")
     ap.add_argument("--all-legs", action="store_true", help="also the lattice workload among the other legs")
+    ap.add_argument("--batch-only", type=int, metavar="CLOUDS", default=0,
+                    help="profiling: only the batched front end on the first CLOUDS clouds (3 graph replays)")
     args = ap.parse_args()
     N = args.n
+    if args.batch_only:
+        return batch_only(args.batch_only)
     ws, rank, local = dist_env()
     if ws > 1:
         import torch.distributed as dist

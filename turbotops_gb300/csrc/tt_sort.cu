@@ -110,18 +110,39 @@ k_rs_upsweep(const u64* __restrict__ keys, u64 n, const unsigned long long* __re
     const u32 nd = 1u << width, mask = nd - 1u;
     for (u32 t = threadIdx.x; t < RS_WARPS * nd; t += RS_THREADS) h[t / nd][t % nd] = 0;
     __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const u64 base = u64(blockIdx.x) * RS_TILE;
-    // one shared-memory atomic per distinct digit of a warp's 32 keys (keys
-    // of one digit come in runs once the higher passes see nearly sorted
-    // input, and per-key atomics on one counter would serialise)
-#pragma unroll 4
-    for (int i = 0; i < RS_ITEMS; ++i) {
-        const u64 k = base + u64(i) * RS_THREADS + threadIdx.x;
-        const u32 dg = k < n ? u32(keys[k] >> shift) & mask : u32(BINS);
-        const u32 peers = __match_any_sync(0xffffffffu, dg);
-        if (lane == __ffs(peers) - 1 && dg < u32(BINS)) atomicAdd(&h[w][dg], u32(__popc(peers)));
+    const int w = threadIdx.x >> 5;
+    // Each thread counts RS_ITEMS consecutive keys, one shared atomic per run
+    // of equal digits: nearly sorted input (the later passes) then costs one
+    // atomic a thread instead of one a key on a single counter.
+    const u64 base = u64(blockIdx.x) * RS_TILE + u64(threadIdx.x) * RS_ITEMS;
+    u64 kv[RS_ITEMS];
+    if (base + RS_ITEMS <= n && (reinterpret_cast<uintptr_t>(keys) & 15) == 0) {   // 16-byte loads
+        const ulonglong2* p = reinterpret_cast<const ulonglong2*>(keys + base);
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS / 2; ++i) {
+            const ulonglong2 v = p[i];
+            kv[2 * i] = v.x;
+            kv[2 * i + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS; ++i) kv[i] = base + i < n ? keys[base + i] : 0ull;
     }
+    const int cnt_valid = base >= n ? 0 : int(min(u64(RS_ITEMS), n - base));
+    u32 cur = 0, run = 0;
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; ++i) {
+        if (i < cnt_valid) {
+            const u32 dg = u32(kv[i] >> shift) & mask;
+            if (run && dg != cur) {
+                atomicAdd(&h[w][cur], run);
+                run = 0;
+            }
+            cur = dg;
+            ++run;
+        }
+    }
+    if (run) atomicAdd(&h[w][cur], run);
     __syncthreads();
     for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) {
         u32 s = 0;
