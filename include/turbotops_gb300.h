@@ -106,7 +106,7 @@ int tt_dense_distances(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim
  * returns TT_ERR_LENGTH before any work). Outputs: mat_dev (n x n) and
  * radius_dev (one float, device memory), in stream order on `stream`
  * (cudaStream_t; NULL = legacy default stream) of the current device.
- * The first call on each device resolves the array's address (make it
+ * The first call on each device loads the library's module there (make it
  * before any stream capture). All calls on a device share the array; calls
  * that overlap on the GPU race and must be serialised by the caller.
  * Errors: tt_last_error(NULL). */

@@ -82,6 +82,35 @@ extern "C" int hr_graph_pairs_dim1(const uint64_t* rp, const uint32_t* ci, const
     }
 }
 
+// graph_pairs_dim1 with its store capped at max_store entries: returns 1 when
+// it gave up (nothing written), 0 with the bars otherwise.
+extern "C" int hr_graph_pairs_dim1_capped(const uint64_t* rp, const uint32_t* ci, const float* w, uint32_t n,
+                                          float thr, const uint64_t* cidx, const float* cd, uint64_t ncols,
+                                          uint64_t max_store, float* birth, float* death, uint64_t* nbars) {
+    try {
+        tt::host::HostComplex hc;
+        hc.rp = rp;
+        hc.ci = ci;
+        hc.w = w;
+        hc.n = n;
+        hc.thr = thr;
+        std::vector<tt::host::Entry> cols(ncols);
+        for (uint64_t i = 0; i < ncols; ++i) cols[i] = tt::host::Entry{cidx[i], cd[i]};
+        tt::host::ReduceStats st;
+        bool gave_up = false;
+        const tt::host::Bars b = tt::host::graph_pairs_dim1(hc, cols, st, &gave_up, max_store);
+        if (gave_up) return 1;
+        for (size_t i = 0; i < b.birth.size(); ++i) {
+            birth[i] = b.birth[i];
+            death[i] = b.death[i];
+        }
+        *nbars = b.birth.size();
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
 // The host assemble (tt_reduce.cpp assemble): the dimension-(dim + 1) columns
 // of `ns` dimension-dim simplices minus the ascending pivots; with nidx !=
 // NULL also every cofacet (the next dimension's simplices). Returns 0, -1 on

@@ -126,3 +126,31 @@ def test_forward_independent_of_reduction_threads():
         u, v = getattr(a, f), getattr(b, f)
         assert torch.equal(torch.as_tensor(u), torch.as_tensor(v)), f
     assert int(a.h1_offset[6]) == int(a.h1_offset[5])   # the empty cloud has no bars
+
+
+def test_adjoint_at_configuration_size():
+    """The bench's differentiable workload itself (64 noisy circles x 512
+    points, sigma 0.1, seed 5, L2): gradient against the FP64 reference of the
+    same pairing, loss within 1e-4, and the forward bars of a sample of the
+    clouds against persistence() cloud by cloud."""
+    clouds = synth.circles()
+    assert len(clouds) == 64 and all(c.shape == (512, 3) for c in clouds)
+    x = torch.from_numpy(np.concatenate(clouds)).cuda().requires_grad_(True)
+    sizes = [c.shape[0] for c in clouds]
+    loss = topo.topo_loss(x, sizes)
+    loss.backward()
+    g = x.grad.detach().cpu().double()
+    b = topo.diagrams(x.detach(), sizes)
+    sel = _selected(b)
+    x64 = torch.from_numpy(np.concatenate(clouds)).double().requires_grad_(True)
+    l64 = _loss64(x64, b, sel)
+    l64.backward()
+    err = (g - x64.grad).norm() / x64.grad.norm()
+    assert err < TOL, float(err)
+    assert abs(float(loss) - float(l64)) <= 1e-4 * max(1.0, abs(float(l64)))
+    for q in (0, 21, 63):
+        dg, _ = tg.persistence(clouds[q], maxdim=1)
+        s1, e1 = int(b.h1_offset[q]), int(b.h1_offset[q + 1])
+        got = np.stack([b.h1_birth[s1:e1].cpu().numpy(), b.h1_death[s1:e1].cpu().numpy()], 1)
+        key = lambda a: a[np.lexsort((a[:, 1], a[:, 0]))]  # noqa: E731
+        assert np.array_equal(key(got), key(dg[1])), q

@@ -414,3 +414,34 @@ def test_graph_higher_dims_vs_reference(shim, c):
     ref = canonical(c["bars"])
     assert got.shape == ref.shape, (got.shape, ref.shape)
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_graph_boundary_store_cap_and_triangle_limit(shim):
+    """The boundary reduction gives up (for compute_pairs) once its stored
+    fill-in passes the cap, and returns the same bars under a cap it stays
+    within."""
+    from turbotops_gb300 import synth
+    x = synth.circles(1, 150, 0.1, 7)[0]
+    csr = O.knn_graph(x, "l2", O.knn(x, "l2", 8))
+    n = x.shape[0]
+    thr = np.float32(np.inf)
+    r = O.dim0(csr=csr, n=n, thr=thr, maxdim=1)
+    rp, ci, w = (np.ascontiguousarray(a) for a in csr)
+    cidx = np.ascontiguousarray(r["cidx"], np.uint64)
+    cd = np.ascontiguousarray(r["cd"], np.float32)
+    k = cidx.size
+    fn = shim.hr_graph_pairs_dim1_capped
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p] * 3 + [C.c_uint32, C.c_float] + [C.c_void_p] * 2 + [C.c_uint64, C.c_uint64] + \
+        [C.c_void_p] * 3
+
+    def run(cap):
+        birth, death = np.empty(k + 1, np.float32), np.empty(k + 1, np.float32)
+        nb = np.zeros(1, np.uint64)
+        st = fn(_p(rp), _p(ci), _p(w), n, float(thr), _p(cidx), _p(cd), k, cap, _p(birth), _p(death), _p(nb))
+        return st, birth[: int(nb[0])], death[: int(nb[0])]
+    assert run(4)[0] == 1
+    st, b, d = run(1 << 40)
+    assert st == 0
+    b0, d0 = graph_pairs(shim, csr, n, thr, r["cidx"], r["cd"])
+    assert np.array_equal(b.view(np.uint32), b0.view(np.uint32)) and np.array_equal(d.view(np.uint32), d0.view(np.uint32))

@@ -93,7 +93,7 @@ std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim,
     // 32-dimensional kNN graph: 0.77) is reduced through the boundary matrix
     // of its triangles: the same pairs and bars in the same order, without
     // cancelling the whole coboundary of every essential edge.
-    const bool boundary = !hc.mat && maxdim == 1 && host::graph_triangles(hc) <= 8 * r.m;
+    const bool boundary = !hc.mat && maxdim == 1 && host::graph_triangles(hc, 8 * r.m) <= 8 * r.m;
     std::vector<u8> emf;
     std::vector<u64> emi;
     if (!boundary) {
@@ -105,8 +105,18 @@ std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim,
     for (u64 i = 0; i < r.ncols; ++i) cols[i] = host::Entry{ci[i], cd[i]};
     std::vector<u64> piv;
     host::ReduceStats st;
-    const host::Bars b = boundary ? host::graph_pairs_dim1(hc, cols, st)
-                                  : host::compute_pairs(hc, 1, maxdim, cols, emi.data(), emf.data(), piv, st);
+    bool gave_up = false;
+    host::Bars b;
+    if (boundary) b = host::graph_pairs_dim1(hc, cols, st, &gave_up);
+    if (!boundary || gave_up) {   // (the boundary reduction's fill-in grew past its cap)
+        if (gave_up) {
+            emi = to_host(c, r.emi, r.ncols);
+            emf = to_host(c, r.emf, r.ncols);
+            sync(c);
+            st = host::ReduceStats{};
+        }
+        b = host::compute_pairs(hc, 1, maxdim, cols, emi.data(), emf.data(), piv, st);
+    }
     for (u64 i = 0; i < b.birth.size(); ++i) out.add(1, b.birth[i], b.death[i]);
     out.columns.push_back(st.columns);
     out.emergent.push_back(st.emergent);

@@ -890,10 +890,11 @@ inline uint64_t choose3(uint64_t v) { return uint64_t((unsigned __int128)v * (v 
 
 // Every triangle a > b > c of the graph complex: its edge (a, b) is the upper
 // slot s of row a, (a, c) and (b, c) the slots pa of row a and pb of row b.
-// fn(a, s, pa, pb, diameter).
-template <typename F>
-void for_each_triangle(const HostComplex& hc, F&& fn) {
-    for (uint32_t a = 0; a < hc.n; ++a)
+// fn(a, s, pa, pb, diameter). stop() is asked before each row: true ends the
+// enumeration early.
+template <typename F, typename S>
+void for_each_triangle(const HostComplex& hc, F&& fn, S&& stop) {
+    for (uint32_t a = 0; a < hc.n && !stop(); ++a)
         for (uint64_t s = hc.rp[a]; s < hc.rp[a + 1]; ++s) {
             const uint32_t b = hc.ci[s];
             if (b >= a) break;   // rows ascend: the upper slots come first
@@ -918,9 +919,9 @@ void for_each_triangle(const HostComplex& hc, F&& fn) {
 
 }  // namespace
 
-uint64_t graph_triangles(const HostComplex& hc) {
+uint64_t graph_triangles(const HostComplex& hc, uint64_t limit) {
     uint64_t t = 0;
-    for_each_triangle(hc, [&](uint32_t, uint64_t, uint64_t, uint64_t, float) { ++t; });
+    for_each_triangle(hc, [&](uint32_t, uint64_t, uint64_t, uint64_t, float) { ++t; }, [&] { return t > limit; });
     return t;
 }
 
@@ -932,7 +933,9 @@ uint64_t graph_triangles(const HostComplex& hc) {
 // unique, so an edge is paired with the same triangle as by compute_pairs.
 // Edges that are never a lowest entry are essential; they cost nothing here,
 // where the coboundary reducer cancels their whole coboundaries.
-Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, ReduceStats& st) {
+Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, ReduceStats& st, bool* gave_up,
+                      uint64_t max_store) {
+    if (gave_up) *gave_up = false;
     const uint32_t n = hc.n;
     const uint64_t nnz = n ? hc.rp[n] : 0;
     // kept edges by upper slot, ranked in filtration order
@@ -958,11 +961,15 @@ Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, Red
     std::vector<Tri> tris;
     for_each_triangle(hc, [&](uint32_t a, uint64_t s, uint64_t pa, uint64_t pb, float d) {
         tris.push_back(Tri{d, choose3(a) + choose2(hc.ci[s]) + hc.ci[pa], {rank[s], rank[pa], rank[pb]}});
-    });
+    }, [] { return false; });
     std::sort(tris.begin(), tris.end(),
               [](const Tri& x, const Tri& y) { return x.d < y.d || (x.d == y.d && x.idx > y.idx); });
     if (tris.size() >= UINT32_MAX) throw std::length_error("gb300: too many triangles for the boundary reduction");
-    // reduced columns (edge ranks, descending) stored back to back
+    // reduced columns (edge ranks, descending) stored back to back; with
+    // gave_up, at most max_store entries (default 16 a triangle): past that
+    // the fill-in of long reduction chains outgrows the coboundary
+    // reducer's memory, and the caller reduces with compute_pairs instead
+    if (gave_up && !max_store) max_store = 16 * uint64_t(tris.size()) + 4096;
     std::vector<uint32_t> owner(edges.size(), UINT32_MAX);   // edge rank -> triangle
     std::vector<uint64_t> off(tris.size() + 1, 0);
     std::vector<uint32_t> store, cur, tmp;
@@ -987,6 +994,10 @@ Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, Red
         if (!cur.empty()) {
             owner[cur[0]] = t;
             store.insert(store.end(), cur.begin(), cur.end());
+            if (gave_up && store.size() > max_store) {
+                *gave_up = true;
+                return Bars{};
+            }
         }
         off[t + 1] = store.size();
     }

@@ -59,16 +59,20 @@ std::vector<Entry> assemble(const HostComplex& hc, uint32_t dim, uint32_t maxdim
                             std::vector<Entry>* next, uint64_t* skipped, unsigned threads = 0);
 
 // Triangles (dimension-2 simplices with diameter <= thr) of a graph complex
-// (hc.mat == nullptr), counted without storing them.
-uint64_t graph_triangles(const HostComplex& hc);
+// (hc.mat == nullptr), counted without storing them; the count stops soon
+// after it exceeds `limit` (any value above limit then means "more").
+uint64_t graph_triangles(const HostComplex& hc, uint64_t limit = UINT64_MAX);
 
 // The same pairs and bars as compute_pairs(hc, 1, 1, cols, ...) on a graph
 // complex, from the boundary matrix of its triangles instead of the
 // coboundaries of its edges: essential edges are never reduced. `cols` are
 // the dimension-1 columns (non-tree, non-apparent edges, descending
 // filtration order); bars come out in their order, as compute_pairs emits
-// them. st.emergent stays 0 (no emergent shortcut is taken).
-Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, ReduceStats& st);
+// them. st.emergent stays 0 (no emergent shortcut is taken). With gave_up,
+// the stored reduced columns are capped at max_store entries (0: 16 a
+// triangle); past the cap *gave_up is set and nothing is returned.
+Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, ReduceStats& st,
+                      bool* gave_up = nullptr, uint64_t max_store = 0);
 
 }  // namespace host
 }  // namespace tt

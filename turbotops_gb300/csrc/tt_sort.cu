@@ -98,6 +98,14 @@ __global__ void k_tile_scan(const T* __restrict__ in, u64 n, const T* __restrict
 // ---------------------------------------------------------------------------
 // Radix sort kernels.
 // ---------------------------------------------------------------------------
+// The lanes holding the same digit as this lane (a sentinel digit marks an
+// empty slot). A warp whose 32 digits agree, the common case once the later
+// passes see nearly sorted input, skips the match unit.
+__device__ __forceinline__ u32 warp_peers(u32 dg) {
+    if (__all_sync(0xffffffffu, dg == __shfl_sync(0xffffffffu, dg, 0))) return 0xffffffffu;
+    return __match_any_sync(0xffffffffu, dg);
+}
+
 // Digits of up to RS_MAXBITS bits (a pass sorts `width` bits from `shift`).
 // ndev (optional): the key count lives on the device (a graph-captured sort of
 // a data-dependent number of keys, n the capacity); tiles past it are empty.
@@ -178,7 +186,7 @@ k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __res
         const bool ok = k < n;
         key[i] = ok ? kin[k] : ~0ull;
         const u32 dg = ok ? u32(key[i] >> shift) & mask : RS_BINS;   // RS_BINS: no key
-        const u32 peers = __match_any_sync(0xffffffffu, dg);
+        const u32 peers = warp_peers(dg);
         const u32 before = __popc(peers & lt);
         const int leader = __ffs(peers) - 1;
         u32 prev = 0;
@@ -250,7 +258,7 @@ k_rs_scatter_local(const u64* __restrict__ kin, u64* __restrict__ kout, const V*
         key[i] = ok ? kin[k] : ~0ull;
         if constexpr (VALS) val[i] = ok ? vin[k] : V(0);
         const u32 dg = ok ? u32(key[i] >> shift) & mask : u32(RS_LBINS);   // RS_LBINS: no key
-        const u32 peers = __match_any_sync(0xffffffffu, dg);
+        const u32 peers = warp_peers(dg);
         const u32 before = __popc(peers & lt);
         const int leader = __ffs(peers) - 1;
         u32 prev = 0;

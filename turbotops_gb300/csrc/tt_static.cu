@@ -12,19 +12,17 @@
 // library, held until the process exits). The caller passes the points and
 // both outputs.
 //
-// Set-up: the first call on a device (with that device current) resolves the
-// array's device address with cudaGetSymbolAddress; in host code the array's
-// name is only a host-side stand-in, so kernels must be given that address.
-// Make the first call on each device before any stream capture begins. The
-// resolved address is kept for the life of the process: it must not outlive
-// the device's primary context, so a caller that resets the device
-// (cudaDeviceReset) must not call this entry point on it afterwards.
+// Set-up: every call resolves the array's device address in the current
+// context with cudaGetSymbolAddress (in host code the array's name is only a
+// host-side stand-in, so kernels must be given that address); nothing is
+// cached, so a device reset between calls is harmless. The first call on a
+// device loads the library's module there: make it before any stream
+// capture begins.
 //
 // Every call on a device shares the one array and leaves its last contents
 // in it; the row maxima are cleared at the start of each call. Calls whose
 // work overlaps on the GPU (different streams, no ordering between them)
 // race on the array and must be serialised by the caller.
-#include <mutex>
 
 #include "tt_internal.cuh"
 
@@ -38,21 +36,15 @@ void set_thread_error(const std::string& msg);   // tt_capi.cu
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-u32* g_rowmax_dev[kMaxDevices] = {};
-
 __global__ void k_store_inf(f32* out) { *out = INFINITY; }
 
-// Device address of g_rowmax on the current device (resolved once).
-u32* scratch_for(int device) {
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_rowmax_dev[device]) {
-        void* p = nullptr;
-        TT_CUDA(cudaGetSymbolAddress(&p, g_rowmax));
-        g_rowmax_dev[device] = static_cast<u32*>(p);
-    }
-    return g_rowmax_dev[device];
+// Device address of g_rowmax in the current context, resolved on every call
+// (a cheap lookup once the module is loaded): an address cached across calls
+// would go stale if the caller reset the device or tore its context down.
+u32* scratch_for() {
+    void* p = nullptr;
+    TT_CUDA(cudaGetSymbolAddress(&p, g_rowmax));
+    return static_cast<u32*>(p);
 }
 
 }  // namespace
@@ -71,8 +63,7 @@ extern "C" int tt_dense_distances_static(const float* x, uint32_t n, uint32_t di
         if (!radius || (n && (!x || !mat))) invalid("gb300: null buffer");
         int device = 0;
         TT_CUDA(cudaGetDevice(&device));
-        if (device < 0 || device >= kMaxDevices) invalid("gb300: device ordinal out of range");
-        u32* rowmax = scratch_for(device);
+        u32* rowmax = scratch_for();
         tt_ctx local;   // stream holder only: its arena is never touched here
         local.device = device;
         local.stream = static_cast<cudaStream_t>(stream);
