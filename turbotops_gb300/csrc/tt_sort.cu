@@ -181,10 +181,14 @@ k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __res
     u64 key[RS_ITEMS];
     u32 rank[RS_ITEMS];
 #pragma unroll
+    for (int i = 0; i < RS_ITEMS; ++i) {   // every load first, then the ranking
+        const u64 k = base + u64(i) * 32 + lane;
+        key[i] = k < n ? kin[k] : ~0ull;
+    }
+#pragma unroll
     for (int i = 0; i < RS_ITEMS; ++i) {
         const u64 k = base + u64(i) * 32 + lane;
         const bool ok = k < n;
-        key[i] = ok ? kin[k] : ~0ull;
         const u32 dg = ok ? u32(key[i] >> shift) & mask : RS_BINS;   // RS_BINS: no key
         const u32 peers = warp_peers(dg);
         const u32 before = __popc(peers & lt);
@@ -237,11 +241,15 @@ k_rs_scatter_local(const u64* __restrict__ kin, u64* __restrict__ kout, const V*
     __shared__ u32 gbase[RS_LBINS];
     __shared__ u32 tstart[RS_LBINS];          // the digit's first position in the ordered tile
     __shared__ u32 wsum[RS_WARPS];
+    __shared__ u32 mbins[RS_WARPS][RS_LBINS]; // per-warp lane masks by digit (the ranking below)
     if (ndev) n = min(n, u64(*ndev));
     const u64 tbase = u64(blockIdx.x) * RS_TILE;
     if (tbase >= n) return;
     const u32 nd = 1u << width, mask = nd - 1u;
-    for (u32 t = threadIdx.x; t < RS_WARPS * RS_LBINS; t += RS_THREADS) cnt[t / RS_LBINS][t % RS_LBINS] = 0;
+    for (u32 t = threadIdx.x; t < RS_WARPS * RS_LBINS; t += RS_THREADS) {
+        cnt[t / RS_LBINS][t % RS_LBINS] = 0;
+        mbins[t / RS_LBINS][t % RS_LBINS] = 0;
+    }
     for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) gbase[d] = offs[u64(d) * tiles + blockIdx.x];
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -251,14 +259,34 @@ k_rs_scatter_local(const u64* __restrict__ kin, u64* __restrict__ kout, const V*
     u64 key[RS_ITEMS];
     V val[VALS ? RS_ITEMS : 1];
     u32 rank[RS_ITEMS];
+    // every load first (all in flight at once), then the ranking
 #pragma unroll
     for (int i = 0; i < RS_ITEMS; ++i) {
         const u64 k = base + u64(i) * 32 + lane;
         const bool ok = k < n;
         key[i] = ok ? kin[k] : ~0ull;
         if constexpr (VALS) val[i] = ok ? vin[k] : V(0);
+    }
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; ++i) {
+        const u64 k = base + u64(i) * 32 + lane;
+        const bool ok = k < n;
         const u32 dg = ok ? u32(key[i] >> shift) & mask : u32(RS_LBINS);   // RS_LBINS: no key
-        const u32 peers = warp_peers(dg);
+        // lanes of one digit: each sets its bit in the warp's mask for the digit
+        // (a shared atomic, instead of the match unit), all read the mask back,
+        // and the lowest of them clears it before the next item
+        const bool has = dg < u32(RS_LBINS);
+        u32 peers;
+        if (__all_sync(0xffffffffu, dg == __shfl_sync(0xffffffffu, dg, 0))) {   // one digit (warp-uniform branch)
+            peers = has ? 0xffffffffu : 0u;
+        } else {
+            if (has) atomicOr(&mbins[w][dg], 1u << lane);
+            __syncwarp();
+            peers = has ? mbins[w][dg] : 0u;
+            __syncwarp();
+            if (has && lane == u32(__ffs(peers) - 1)) mbins[w][dg] = 0u;
+            __syncwarp();
+        }
         const u32 before = __popc(peers & lt);
         const int leader = __ffs(peers) - 1;
         u32 prev = 0;
