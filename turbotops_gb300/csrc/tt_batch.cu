@@ -51,7 +51,16 @@ struct Tile {
     u32 cloud, i0, j0;
 };
 
-template <int KIND, int BT_R, int BT_C>
+// A point's coordinates held in registers (compile-time dimension).
+template <int DIM>
+struct Regs {
+    const f32 (&v)[DIM];
+    __device__ __forceinline__ f32 operator()(u32 k) const { return v[k]; }
+};
+
+// DIM > 0: the dimension at compile time (each thread keeps its column's
+// point in registers); 0: any dimension, read from memory.
+template <int KIND, int BT_R, int BT_C, int DIM>
 __global__ void __launch_bounds__(BT_THREADS)
 k_batch_dense(const f32* __restrict__ x, const u64* __restrict__ pt_off, const u64* __restrict__ mat_off,
               const u32* __restrict__ sizes, const Tile* __restrict__ tiles, u32 ntiles, u32 dim, f32 p,
@@ -78,12 +87,29 @@ k_batch_dense(const f32* __restrict__ x, const u64* __restrict__ pt_off, const u
         const u32 j = tl.j0 + tx;
         u32 cm = 0;
         if (j < n) {
-            for (u32 r = ty; r < BT_R; r += BT_Y) {
-                const u32 i = tl.i0 + r;
-                if (i >= n) break;
-                const f32 d = (i == j) ? 0.0f : metric_dist(KIND, p, Row{xc + u64(i) * dim}, Row{xc + u64(j) * dim}, dim);
-                mc[u64(i) * n + j] = d;
-                cm = max(cm, __float_as_uint(d));
+            if constexpr (DIM > 0) {
+                f32 xj[DIM];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) xj[k] = xc[u64(j) * DIM + k];
+                for (u32 r = ty; r < BT_R; r += BT_Y) {
+                    const u32 i = tl.i0 + r;
+                    if (i >= n) break;
+                    f32 xi[DIM];
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) xi[k] = xc[u64(i) * DIM + k];
+                    const f32 d = (i == j) ? 0.0f : metric_dist(KIND, p, Regs<DIM>{xi}, Regs<DIM>{xj}, DIM);
+                    mc[u64(i) * n + j] = d;
+                    cm = max(cm, __float_as_uint(d));
+                }
+            } else {
+                for (u32 r = ty; r < BT_R; r += BT_Y) {
+                    const u32 i = tl.i0 + r;
+                    if (i >= n) break;
+                    const f32 d =
+                        (i == j) ? 0.0f : metric_dist(KIND, p, Row{xc + u64(i) * dim}, Row{xc + u64(j) * dim}, dim);
+                    mc[u64(i) * n + j] = d;
+                    cm = max(cm, __float_as_uint(d));
+                }
             }
             atomicMax(&cmax[tx], cm);
         }
@@ -129,7 +155,8 @@ __global__ void k_batch_rowcount(const f32* __restrict__ mats, const u64* __rest
         const f32 thr = __uint_as_float(radius[c]);
         const f32* row = mats + mat_off[c] + u64(i) * n;
         u64 kept = 0;
-        for (u32 j0 = 0; j0 < i; j0 += 32) {
+#pragma unroll 4
+        for (u32 j0 = 0; j0 < i; j0 += 32) {   // (unrolled: several row loads in flight)
             const u32 j = j0 + lane;
             kept += __popc(__ballot_sync(0xffffffffu, j < i && row[j] <= thr));
         }
@@ -155,6 +182,7 @@ __global__ void k_batch_edges(const f32* __restrict__ mats, const u64* __restric
         const f32* row = mats + mat_off[c] + u64(i) * n;
         const u64 rbase = u64(i) * (i - 1) / 2;
         u64 pos = row_off[r];
+#pragma unroll 4
         for (u32 j0 = 0; j0 < i; j0 += 32) {
             const u32 j = j0 + lane;
             const f32 d = j < i ? row[j] : INFINITY;
@@ -263,18 +291,23 @@ struct Batch {
         return static_cast<T*>(p);
     }
 
+    template <int R, int C, int D>
+    void launch_dense_kd(u32 grid, dim3 blk, u32 nt, const Tile* tl, cudaStream_t s) {
+        switch (kind) {
+            case M_L1: k_batch_dense<M_L1, R, C, D><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            case M_L2: k_batch_dense<M_L2, R, C, D><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            case M_LINF: k_batch_dense<M_LINF, R, C, D><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            default: k_batch_dense<M_LP, R, C, D><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+        }
+    }
     template <int R, int C>
     void launch_dense_rc(int si, cudaStream_t s) {
         const dim3 blk(C, BT_THREADS / C);
         const u32 nt = ntiles[si];
         const u32 grid = u32(std::min<u64>(nt, u64(owner->sms) * 8));
         const Tile* tl = tiles[si];
-        switch (kind) {
-            case M_L1: k_batch_dense<M_L1, R, C><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
-            case M_L2: k_batch_dense<M_L2, R, C><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
-            case M_LINF: k_batch_dense<M_LINF, R, C><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
-            default: k_batch_dense<M_LP, R, C><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
-        }
+        if (dim == 3) launch_dense_kd<R, C, 3>(grid, blk, nt, tl, s);
+        else launch_dense_kd<R, C, 0>(grid, blk, nt, tl, s);
         TT_LAUNCH("k_batch_dense");
     }
     void launch_dense(int si, cudaStream_t s) {
