@@ -106,7 +106,7 @@ u64 knn_front_dev(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 
     f32* gw = w;
     after_graph(nnz, rp, gci, gw);   // before dim0: the graph is final here
     Complex cx{nullptr, rp, gci, gw, n, INFINITY};
-    dim0(c, cx, maxdim, r);
+    dim0(c, cx, maxdim, r, nnz / 2);   // symmetric, no self loops, cut at +inf: every edge kept
     *rp_out = rp;
     *ci_out = gci;
     *w_out = gw;

@@ -136,6 +136,7 @@ enum Slot : int {
     S_GRAPH_LONG, S_GRAPH_CI, S_GRAPH_W,                           // kNN graph: long rows; its columns and weights
     S_RZ_D, S_RZ_V,                                                // RedZeD edge lists sized to their count
     S_TXT, S_TXT_CNT, S_TXT_LINES, S_TXT_TOK, S_TXT_HOST,          // text ingestion
+    S_DIM0_ERR,                                                    // dim0's announced-count check
     S_NSLOTS
 };
 

@@ -144,7 +144,7 @@ __global__ void k_edge_count(Rows rows, u32 n, f32 thr, u64* __restrict__ cnt, u
 // order: the ties keep the order of q.
 template <typename Rows>
 __global__ void k_edge_fill(Rows rows, u32 n, f32 thr, const u64* __restrict__ off, u64 m, int redzed,
-                            u64* __restrict__ skey, u64* __restrict__ sidx) {
+                            u64* __restrict__ skey, u64* __restrict__ sidx, u32* __restrict__ err) {
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
     for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
@@ -162,9 +162,13 @@ __global__ void k_edge_fill(Rows rows, u32 n, f32 thr, const u64* __restrict__ o
             const u32 bal = __ballot_sync(0xffffffffu, keep);
             if (keep) {
                 const u64 p = base + __popc(bal & ((1u << lane) - 1));
-                const u64 q = redzed ? p : m - 1 - p;
-                skey[q] = (u64(__float_as_uint(d)) << 32) | q;
-                sidx[q] = vbase + u;
+                if (p < m) {
+                    const u64 q = redzed ? p : m - 1 - p;
+                    skey[q] = (u64(__float_as_uint(d)) << 32) | q;
+                    sidx[q] = vbase + u;
+                } else if (err) {
+                    atomicOr(err, 1u);   // more kept edges than the caller announced
+                }
             }
             base += __popc(bal);
         }
@@ -450,8 +454,14 @@ inline u32 grid_for(u64 work, u32 per_block) {
 // S_EDGE_INV (result: index order -> sorted position),
 // and the sort's own (S_SORT_A, S_SORT_HIST, S_SCAN*, S_MISC3).
 // Above kPackedMaxN vertices the keys take the wide layout (EdgeFmt) and
-// *eidx_out the index table; otherwise *eidx_out is null.
-static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys_out, u64** eidx_out) {
+// *eidx_out the index table; otherwise *eidx_out is null. m_known (not
+// kUnknownM): the caller knows the kept-edge count (a symmetric graph without
+// self loops cut at +inf keeps nnz / 2), so the count is not read back: the
+// sort takes all 31 distance bits, and a wrong count sets *err instead of
+// writing out of bounds.
+constexpr u64 kUnknownM = ~0ull;
+static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys_out, u64** eidx_out,
+                            u64 m_known = kUnknownM, u32* err = nullptr) {
     const u32 n = cx.n;
     u64 m = 0;
     u64* off = c->arena.get<u64>(S_EDGE_CNT, u64(n) + 2);
@@ -468,13 +478,18 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
         TT_LAUNCH("k_edge_count");
         ++c->launches;
         scan_exclusive<u64>(c, off, off, n, off + n);
-        u64 h[2];
-        TT_CUDA(cudaMemcpyAsync(h, off + n, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
-        TT_CUDA(cudaStreamSynchronize(c->stream));
-        m = h[0];
-        const u32 lo = u32(h[1]), hi = u32(h[1] >> 32);
-        const u32 diff = m ? lo ^ hi : 0u;
-        dbits = diff ? 32 - __builtin_clz(diff) : 0;
+        if (m_known != kUnknownM) {
+            m = m_known;
+            dbits = 31;   // every bit of a non-negative float: the same three passes
+        } else {
+            u64 h[2];
+            TT_CUDA(cudaMemcpyAsync(h, off + n, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+            TT_CUDA(cudaStreamSynchronize(c->stream));
+            m = h[0];
+            const u32 lo = u32(h[1]), hi = u32(h[1] >> 32);
+            const u32 diff = m ? lo ^ hi : 0u;
+            dbits = diff ? 32 - __builtin_clz(diff) : 0;
+        }
     }
     if (m >= 0xffffffffull) invalid("gb300: more than 2^32 - 1 kept edges");
     u64* keys = c->arena.get<u64>(S_EDGE_KEYS, m + 1);
@@ -484,10 +499,10 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
         u64* skey = c->arena.get<u64>(S_EDGE_SORT, m + 1);
         u64* sidx = c->arena.get<u64>(S_EDGE_IDX, m + 1);
         if (cx.mat)
-            k_edge_fill<<<g, 256, 0, c->stream>>>(DenseRows{cx.mat, n}, n, cx.thr, off, m, redzed, skey, sidx);
+            k_edge_fill<<<g, 256, 0, c->stream>>>(DenseRows{cx.mat, n}, n, cx.thr, off, m, redzed, skey, sidx, err);
         else
             k_edge_fill<<<g, 256, 0, c->stream>>>(CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off, m, redzed, skey,
-                                                  sidx);
+                                                  sidx, err);
         TT_LAUNCH("k_edge_fill");
         u64* kb = c->arena.get<u64>(S_SORT_A, m);
         // a stable sort on the distance bits that differ (none: already in order)
@@ -503,9 +518,11 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
     return m;
 }
 
-void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
+void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
     out = Dim0Out{};
-    const u64 m = sorted_edge_keys(c, cx, 0, &out.keys, &out.eidx);
+    u32* err = m_known != kUnknownM ? c->arena.get<u32>(S_DIM0_ERR, 4) : nullptr;
+    if (err) TT_CUDA(cudaMemsetAsync(err, 0, sizeof(u32), c->stream));
+    const u64 m = sorted_edge_keys(c, cx, 0, &out.keys, &out.eidx, m_known, err);
     const EdgeFmt fmt{out.eidx};
     out.m = m;
     if (m >= 0xffffffffull) invalid("gb300: more than 2^32 - 1 kept edges");
@@ -589,8 +606,11 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out) {
         TT_CUDA(cudaMemsetAsync(tot, 0, sizeof(u64), c->stream));
     }
     u64 hp = 0;
+    u32 bad = 0;
     TT_CUDA(cudaMemcpyAsync(&hp, tot, sizeof(hp), cudaMemcpyDeviceToHost, c->stream));
+    if (err) TT_CUDA(cudaMemcpyAsync(&bad, err, sizeof(bad), cudaMemcpyDeviceToHost, c->stream));
     TT_CUDA(cudaStreamSynchronize(c->stream));
+    if (bad) throw Error(TT_ERR_INTERNAL, "gb300: more kept edges than announced");
     const u64 h[2] = {hp >> 32, hp & 0xffffffffull};
     out.nh0 = h[0];
     out.ncols = h[1];

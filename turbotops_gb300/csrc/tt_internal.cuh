@@ -103,7 +103,10 @@ struct Complex {
     u32 n = 0;
     f32 thr = 0;
 };
-void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out);
+// m_known: the kept-edge count when the caller knows it (a symmetric graph
+// without self loops cut at +inf keeps nnz / 2); saves the round trip that
+// would read it back.
+void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known = ~0ull);
 // RedZeD EdgeList (d asc, comb asc): diam + vertex pairs (i < j).
 u64 redzed_edges(tt_ctx* c, const Complex& cx, f32* d, int32_t* verts, u64 cap);
 u64 redzed_edges_owned(tt_ctx* c, const Complex& cx, f32** d, int32_t** verts);
