@@ -373,7 +373,8 @@ int tt_parse_points_h(tt_ctx* ctx, const char* text_h, uint64_t bytes, float* pt
  *   knn = 0, threshold = +inf    dense full Rips cut at the enclosing radius
  *   knn = 0, threshold < inf     radius graph, sparse flag complex
  *   knn = 1                      exact kNN graph (k neighbours), sparse flag complex
- * GPU front end limits: maxdim <= 2 (dense) / <= 1 (graph input). */
+ * Any maxdim <= 30 (dimensions above the GPU's are assembled on the host);
+ * k <= 32 and dim <= 64 for the graph scans. */
 int tt_persistence_h(tt_ctx* ctx, const float* x_h, uint32_t n, uint32_t dim, int kind, float p, uint32_t maxdim,
                      float threshold, int knn, uint32_t k, tt_barcode** out);
 /* tops::persistence(const CsrGraph&, maxdim, threshold, threads, mode)

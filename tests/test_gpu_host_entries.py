@@ -96,3 +96,26 @@ def test_host_entries_reject_non_finite(bad):
     # the context stays usable
     st, r = _front_h(np.ascontiguousarray(synth.gauss(300, 6, 2), np.float32), 5)
     assert st == capi.OK and r["rp"][-1] > 0
+
+
+def test_knn_front_h_above_packed_key_range_vs_oracle():
+    """140,000 points: edge indices beyond the packed keys' 33 bits, so dim0
+    runs on the wide key layout with the kept-edge count announced by the
+    front end. H0, columns and emergent probes equal the oracle's dim0 on the
+    same graph."""
+    from oracle import oracle as O
+    n, k = 140000, 8
+    x = np.ascontiguousarray(synth.gauss(n, 3, 77), np.float32)
+    st, r = _front_h(x, k)
+    assert st == capi.OK
+    csr = (r["rp"], r["col"], r["w"])
+    o = O.dim0(csr=csr, n=n, maxdim=1)
+    assert r["edges"] == o["eidx"].size
+    assert np.array_equal(r["cidx"], o["cidx"])
+    assert np.array_equal(r["cd"].view(np.uint32), o["cd"].view(np.uint32))
+    od = o["h0"].reshape(-1, 2)[:, 1]
+    od = np.sort(od[np.isfinite(od) & (od > 0)])
+    assert np.array_equal(np.sort(r["h0"]).view(np.uint32), od.view(np.uint32))
+    e = O.emergent(csr=csr, n=n, cidx=o["cidx"], cd=o["cd"])
+    assert np.array_equal(r["cf"], e["emi"])
+    assert np.array_equal(r["ca"], e["emf"])

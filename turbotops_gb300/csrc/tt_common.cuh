@@ -167,11 +167,16 @@ struct tt_ctx {
 
 namespace tt {
 // The context's side stream (non-blocking, so it also runs beside a legacy
-// default main stream), ordered after everything issued so far on the main
-// stream. Whoever forks work onto it joins it back (side_join) before the
-// main stream reads the results.
+// default main stream; the device's highest priority, so its short kernels
+// are scheduled ahead of the main stream's waiting blocks), ordered after
+// everything issued so far on the main stream. Whoever forks work onto it
+// joins it back (side_join) before the main stream reads the results.
 inline cudaStream_t side_after_main(tt_ctx* c) {
-    if (!c->side) TT_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    if (!c->side) {
+        int least = 0, greatest = 0;
+        TT_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        TT_CUDA(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, greatest));
+    }
     for (auto& e : c->side_ev)
         if (!e) TT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     TT_CUDA(cudaEventRecord(c->side_ev[0], c->stream));

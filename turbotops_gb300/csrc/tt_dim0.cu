@@ -534,12 +534,15 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
     u8* emf = c->arena.get<u8>(S_MISC2, m + 1);
     TT_CUDA(cudaMemsetAsync(tree, 0, m + 1, c->stream));
     // The apparent/emergent scan and the spanning forest read the same sorted
-    // edges and write disjoint flags: the scan runs on the side stream while
-    // the forest's rounds (and their host round trips) run on the main one.
+    // edges and write disjoint flags. The forest's short rounds (and their
+    // host round trips) run on the side stream, which has the highest
+    // priority: its blocks are scheduled ahead of the scan's waiting blocks,
+    // and the scan, on the main stream, fills the SMs around them.
     SideScope side(c);
+    const cudaStream_t fs = n ? side.fork() : c->stream;   // the forest's stream
     if (maxdim >= 1 && m) {
         u32* inv = c->arena.get<u32>(S_EDGE_INV, m + 1);
-        cudaStream_t s = side.fork();
+        const cudaStream_t s = c->stream;
         if (cx.mat)
             k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, s>>>(cx.mat, n, out.keys, fmt, m, app, emw, emf);
         else
@@ -560,11 +563,11 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
     u32* ctr = c->arena.get<u32>(S_MISC1, 2 * kRounds);   // per round: live count, hooks
     u64 total_hooks = 0;
     if (n) {
-        k_iota<<<grid_for(n, 256), 256, 0, c->stream>>>(comp, n);
-        k_iota<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, n);
-        TT_CUDA(cudaMemsetAsync(best, 0xff, sizeof(u32) * n, c->stream));
+        k_iota<<<grid_for(n, 256), 256, 0, fs>>>(comp, n);
+        k_iota<<<grid_for(n, 256), 256, 0, fs>>>(parent, n);
+        TT_CUDA(cudaMemsetAsync(best, 0xff, sizeof(u32) * n, fs));
         c->launches += 2;
-        TT_CUDA(cudaMemsetAsync(ctr, 0, 2 * kRounds * sizeof(u32), c->stream));
+        TT_CUDA(cudaMemsetAsync(ctr, 0, 2 * kRounds * sizeof(u32), fs));
         // Three rounds a host round trip (a round after convergence finds no
         // edge between components and changes nothing); the grid covers the
         // last live count the host knows (counts only shrink).
@@ -572,26 +575,26 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
         for (int round = 0; known && round < kRounds;) {
             const int first = round;
             for (int q = 0; q < kPerTrip && round < kRounds; ++q, ++round) {
-                k_bv_offer<<<grid_for(known, 256), 256, 0, c->stream>>>(
+                k_bv_offer<<<grid_for(known, 256), 256, 0, fs>>>(
                     out.keys, fmt, live0, round ? ctr + 2 * (round - 1) : nullptr, u32(m), comp, best, live1, ctr + 2 * round);
-                k_bv_hook<<<grid_for(n, 256), 256, 0, c->stream>>>(out.keys, fmt, comp, best, parent, tree, n,
-                                                                   ctr + 2 * round + 1, ctr + 2 * round);
-                k_bv_flatten<<<grid_for(n, 256), 256, 0, c->stream>>>(parent, comp, best, n, ctr + 2 * round);
+                k_bv_hook<<<grid_for(n, 256), 256, 0, fs>>>(out.keys, fmt, comp, best, parent, tree, n,
+                                                           ctr + 2 * round + 1, ctr + 2 * round);
+                k_bv_flatten<<<grid_for(n, 256), 256, 0, fs>>>(parent, comp, best, n, ctr + 2 * round);
                 TT_LAUNCH("boruvka");
                 c->launches += 3;
                 std::swap(live0, live1);
             }
             u32 h[2 * kPerTrip] = {};
             TT_CUDA(cudaMemcpyAsync(h, ctr + 2 * first, sizeof(u32) * 2 * (round - first), cudaMemcpyDeviceToHost,
-                                    c->stream));
-            TT_CUDA(cudaStreamSynchronize(c->stream));
+                                    fs));
+            TT_CUDA(cudaStreamSynchronize(fs));
             const int last = round - first - 1;
             for (int q = 0; q <= last; ++q) total_hooks += h[2 * q + 1];
             known = h[2 * last];
             if (h[2 * last + 1] == 0) break;
         }
     }
-    side.join();   // the flags of the scan
+    side.join();   // the forest's tree flags
     // ordered compaction of H0 deaths and columns
     const int want_cols = maxdim >= 1;
     u64* f2 = c->arena.get<u64>(S_MISC0, 2 * m + 4);
