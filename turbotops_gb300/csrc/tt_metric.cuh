@@ -193,6 +193,38 @@ __device__ __forceinline__ f32 lp_root_lower(f32 M, f32 s, f32 p) {
     return __fmul_rd(__fmul_rd(M, __powf(s, __fdividef(1.0f, p))), 1.0f - 0x1p-14f);
 }
 
+// lp_parts for a caller that only needs distances up to `bound`: after each
+// 8-coordinate chunk but the last it stops, returning false, once the sum so
+// far already puts the distance above bound. Every term is >= 0 and a float
+// sum of non-negative terms never decreases, so the partial hsum8 is at most
+// the final s, and lp_root_lower of it is a lower bound of the distance as
+// much as of the final sum's root. Returns true with M and s exactly as
+// lp_parts computes them otherwise.
+template <typename A, typename B>
+__device__ __forceinline__ bool lp_parts_within(const A& a, const B& b, u32 dim, f32 p, f32 bound, f32& M, f32& s) {
+    M = linf_acc(a, b, dim);
+    s = 0.0f;
+    if (M == 0.0f) return true;
+    const f32 inv = __fdiv_rn(1.0f, M);
+    const bool integral = p == floorf(p) && p <= 8.0f;
+    u32 k = 0;
+    if (!integral && dim >= 8) {
+        f32 acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (; k + 8 <= dim; k += 8) {
+#pragma unroll
+            for (int l = 0; l < 8; ++l)
+                acc[l] = __fadd_rn(acc[l], pow01_dev(fminf(__fmul_rn(fabsf(__fsub_rn(a(k + l), b(k + l))), inv), 1.0f), p));
+            if (k + 16 <= dim && lp_root_lower(M, hsum8(acc), p) > bound) return false;
+        }
+        s = hsum8(acc);
+    }
+    for (; k < dim; ++k) {
+        const f32 x = fminf(1.0f, __fmul_rn(fabsf(__fsub_rn(a(k), b(k))), inv));
+        s = __fadd_rn(s, integral ? ipow_dev(x, u32(p)) : powf_dev(x, p));
+    }
+    return true;
+}
+
 template <typename A, typename B>
 __device__ __forceinline__ f32 lp_acc(const A& a, const B& b, u32 dim, f32 p) {
     f32 M, s;

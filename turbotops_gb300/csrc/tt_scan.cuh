@@ -245,9 +245,10 @@ k_scan(const f32* __restrict__ x, u32 n, u32 dim_rt, f32 p, Op op, const u32* __
                 // only for candidates a float lower bound cannot reject
                 for (u32 r = 0; r < rows; ++r) {
                     f32 M, sum;
-                    if (kRt) lp_parts(Row{qg}, Row{tile + r * dim}, dim, p, M, sum);
-                    else lp_parts(RegRow<QN>{q}, Row{tile + r * QN}, QN, p, M, sum);
-                    if (lp_root_lower(M, sum, p) > op.bound(st)) continue;
+                    const f32 bd = op.bound(st);
+                    const bool within = kRt ? lp_parts_within(Row{qg}, Row{tile + r * dim}, dim, p, bd, M, sum)
+                                            : lp_parts_within(RegRow<QN>{q}, Row{tile + r * QN}, QN, p, bd, M, sum);
+                    if (!within || lp_root_lower(M, sum, p) > bd) continue;
                     op.visit(st, i, j0 + r, lp_root(M, sum, p), kComp ? tc + r : nullptr);
                 }
             } else if (kRt) {
