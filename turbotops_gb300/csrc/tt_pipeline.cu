@@ -93,7 +93,7 @@ std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim,
     // 32-dimensional kNN graph: 0.77) is reduced through the boundary matrix
     // of its triangles: the same pairs and bars in the same order, without
     // cancelling the whole coboundary of every essential edge.
-    const bool boundary = !hc.mat && maxdim == 1 && host::graph_triangles(hc, 8 * r.m) <= 8 * r.m;
+    const bool boundary = !hc.mat && maxdim == 1;   // (gives up past 8 triangles a kept edge)
     std::vector<u8> emf;
     std::vector<u64> emi;
     if (!boundary) {
@@ -107,8 +107,8 @@ std::vector<u64> reduce_dim1(tt_ctx* c, const host::HostComplex& hc, u32 maxdim,
     host::ReduceStats st;
     bool gave_up = false;
     host::Bars b;
-    if (boundary) b = host::graph_pairs_dim1(hc, cols, st, &gave_up);
-    if (!boundary || gave_up) {   // (the boundary reduction's fill-in grew past its cap)
+    if (boundary) b = host::graph_pairs_dim1(hc, cols, st, &gave_up, 0, 8 * r.m);
+    if (!boundary || gave_up) {   // (too many triangles, or fill-in past the cap)
         if (gave_up) {
             emi = to_host(c, r.emi, r.ncols);
             emf = to_host(c, r.emf, r.ncols);

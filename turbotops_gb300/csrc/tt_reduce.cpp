@@ -893,8 +893,8 @@ inline uint64_t choose3(uint64_t v) { return uint64_t((unsigned __int128)v * (v 
 // fn(a, s, pa, pb, diameter). stop() is asked before each row: true ends the
 // enumeration early.
 template <typename F, typename S>
-void for_each_triangle(const HostComplex& hc, F&& fn, S&& stop) {
-    for (uint32_t a = 0; a < hc.n && !stop(); ++a)
+void for_each_triangle(const HostComplex& hc, F&& fn, S&& stop, uint32_t a0 = 0, uint32_t a1 = UINT32_MAX) {
+    for (uint32_t a = a0; a < std::min(a1, hc.n) && !stop(); ++a)
         for (uint64_t s = hc.rp[a]; s < hc.rp[a + 1]; ++s) {
             const uint32_t b = hc.ci[s];
             if (b >= a) break;   // rows ascend: the upper slots come first
@@ -919,6 +919,52 @@ void for_each_triangle(const HostComplex& hc, F&& fn, S&& stop) {
 
 }  // namespace
 
+// f(t, i0, i1) on `threads` host threads over [0, n) in chunks of `chunk`
+// handed out in order (each chunk to the next free thread).
+template <typename F>
+void parallel_chunks(unsigned threads, uint64_t n, uint64_t chunk, F&& f) {
+    if (threads <= 1 || n <= chunk) {
+        if (n) f(0u, uint64_t(0), n);
+        return;
+    }
+    std::atomic<uint64_t> next{0};
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < threads; ++t)
+        th.emplace_back([&, t] {
+            for (uint64_t i; (i = next.fetch_add(chunk)) < n;) f(t, i, std::min(n, i + chunk));
+        });
+    for (auto& x : th) x.join();
+}
+
+// Sorts v by cmp on `threads` host threads: sorted runs, then rounds of
+// pairwise merges (a total order: equal keys need no stability).
+template <typename T, typename Cmp>
+void parallel_sort(std::vector<T>& v, Cmp cmp, unsigned threads) {
+    const size_t n = v.size();
+    if (threads <= 1 || n < (size_t(1) << 16)) {
+        std::sort(v.begin(), v.end(), cmp);
+        return;
+    }
+    size_t parts = 1;
+    while (parts < threads) parts <<= 1;
+    std::vector<size_t> b(parts + 1);
+    for (size_t i = 0; i <= parts; ++i) b[i] = n * i / parts;
+    parallel_chunks(threads, parts, 1, [&](unsigned, uint64_t i0, uint64_t i1) {
+        for (uint64_t i = i0; i < i1; ++i) std::sort(v.begin() + ptrdiff_t(b[i]), v.begin() + ptrdiff_t(b[i + 1]), cmp);
+    });
+    std::vector<T> tmp(n);
+    for (size_t width = 1; width < parts; width <<= 1) {
+        parallel_chunks(threads, parts / (2 * width), 1, [&](unsigned, uint64_t j0, uint64_t j1) {
+            for (uint64_t j = j0; j < j1; ++j) {
+                const size_t lo = b[2 * width * j], mid = b[2 * width * j + width], hi = b[2 * width * (j + 1)];
+                std::merge(v.begin() + ptrdiff_t(lo), v.begin() + ptrdiff_t(mid), v.begin() + ptrdiff_t(mid),
+                           v.begin() + ptrdiff_t(hi), tmp.begin() + ptrdiff_t(lo), cmp);
+            }
+        });
+        v.swap(tmp);
+    }
+}
+
 uint64_t graph_triangles(const HostComplex& hc, uint64_t limit) {
     uint64_t t = 0;
     for_each_triangle(hc, [&](uint32_t, uint64_t, uint64_t, uint64_t, float) { ++t; }, [&] { return t > limit; });
@@ -934,36 +980,73 @@ uint64_t graph_triangles(const HostComplex& hc, uint64_t limit) {
 // Edges that are never a lowest entry are essential; they cost nothing here,
 // where the coboundary reducer cancels their whole coboundaries.
 Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, ReduceStats& st, bool* gave_up,
-                      uint64_t max_store) {
+                      uint64_t max_store, uint64_t max_tris, unsigned threads) {
     if (gave_up) *gave_up = false;
+    if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
     const uint32_t n = hc.n;
     const uint64_t nnz = n ? hc.rp[n] : 0;
-    // kept edges by upper slot, ranked in filtration order
+    // kept edges by upper slot, ranked in filtration order (rows split over
+    // the threads: per-row counts, offsets, then the edges in place)
     struct Edge {
         float d;
         uint64_t idx, slot;
     };
-    std::vector<Edge> edges;
-    for (uint32_t a = 0; a < n; ++a)
-        for (uint64_t s = hc.rp[a]; s < hc.rp[a + 1] && hc.ci[s] < a; ++s)
-            if (hc.w[s] <= hc.thr) edges.push_back(Edge{hc.w[s], choose2(a) + hc.ci[s], s});
-    std::sort(edges.begin(), edges.end(),
-              [](const Edge& x, const Edge& y) { return x.d < y.d || (x.d == y.d && x.idx > y.idx); });
+    std::vector<uint64_t> roff(uint64_t(n) + 1, 0);
+    parallel_chunks(threads, n, 4096, [&](unsigned, uint64_t a0, uint64_t a1) {
+        for (uint64_t a = a0; a < a1; ++a) {
+            uint64_t c = 0;
+            for (uint64_t s = hc.rp[a]; s < hc.rp[a + 1] && hc.ci[s] < a; ++s) c += hc.w[s] <= hc.thr;
+            roff[a + 1] = c;
+        }
+    });
+    for (uint32_t a = 0; a < n; ++a) roff[a + 1] += roff[a];
+    std::vector<Edge> edges(roff[n]);
+    parallel_chunks(threads, n, 4096, [&](unsigned, uint64_t a0, uint64_t a1) {
+        for (uint64_t a = a0; a < a1; ++a) {
+            uint64_t o = roff[a];
+            for (uint64_t s = hc.rp[a]; s < hc.rp[a + 1] && hc.ci[s] < a; ++s)
+                if (hc.w[s] <= hc.thr) edges[o++] = Edge{hc.w[s], choose2(a) + hc.ci[s], s};
+        }
+    });
+    parallel_sort(edges, [](const Edge& x, const Edge& y) { return x.d < y.d || (x.d == y.d && x.idx > y.idx); },
+                  threads);
     if (edges.size() >= UINT32_MAX) throw std::length_error("gb300: too many edges for the boundary reduction");
     std::vector<uint32_t> rank(nnz, UINT32_MAX);
-    for (uint32_t r = 0; r < edges.size(); ++r) rank[edges[r].slot] = r;
-    // triangles in filtration order, each with its three edge ranks
+    parallel_chunks(threads, edges.size(), 1 << 16, [&](unsigned, uint64_t r0, uint64_t r1) {
+        for (uint64_t r = r0; r < r1; ++r) rank[edges[r].slot] = uint32_t(r);
+    });
+    // triangles in filtration order, each with its three edge ranks (rows
+    // split over the threads; more than max_tris gives up)
     struct Tri {
         float d;
         uint64_t idx;
         uint32_t e[3];
     };
+    std::vector<std::vector<Tri>> part(threads);
+    std::atomic<uint64_t> total{0};
+    std::atomic<bool> over{false};
+    parallel_chunks(threads, n, 1024, [&](unsigned t, uint64_t a0, uint64_t a1) {
+        if (over.load(std::memory_order_relaxed)) return;
+        std::vector<Tri>& out = part[t];
+        const size_t before = out.size();
+        for_each_triangle(hc, [&](uint32_t a, uint64_t s, uint64_t pa, uint64_t pb, float d) {
+            out.push_back(Tri{d, choose3(a) + choose2(hc.ci[s]) + hc.ci[pa], {rank[s], rank[pa], rank[pb]}});
+        }, [] { return false; }, uint32_t(a0), uint32_t(a1));
+        if (total.fetch_add(out.size() - before) + (out.size() - before) > max_tris) over.store(true);
+    });
+    if (over.load()) {
+        if (!gave_up) throw std::length_error("gb300: too many triangles for the boundary reduction");
+        *gave_up = true;
+        return Bars{};
+    }
     std::vector<Tri> tris;
-    for_each_triangle(hc, [&](uint32_t a, uint64_t s, uint64_t pa, uint64_t pb, float d) {
-        tris.push_back(Tri{d, choose3(a) + choose2(hc.ci[s]) + hc.ci[pa], {rank[s], rank[pa], rank[pb]}});
-    }, [] { return false; });
-    std::sort(tris.begin(), tris.end(),
-              [](const Tri& x, const Tri& y) { return x.d < y.d || (x.d == y.d && x.idx > y.idx); });
+    tris.reserve(total.load());
+    for (auto& v : part) {
+        tris.insert(tris.end(), v.begin(), v.end());
+        std::vector<Tri>().swap(v);
+    }
+    parallel_sort(tris, [](const Tri& x, const Tri& y) { return x.d < y.d || (x.d == y.d && x.idx > y.idx); },
+                  threads);
     if (tris.size() >= UINT32_MAX) throw std::length_error("gb300: too many triangles for the boundary reduction");
     // reduced columns (edge ranks, descending) stored back to back; with
     // gave_up, at most max_store entries (default 16 a triangle): past that
@@ -972,10 +1055,10 @@ Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, Red
     if (gave_up && !max_store) max_store = 16 * uint64_t(tris.size()) + 4096;
     std::vector<uint32_t> owner(edges.size(), UINT32_MAX);   // edge rank -> triangle
     std::vector<uint64_t> off(tris.size() + 1, 0);
-    std::vector<uint32_t> store, cur, tmp;
-    for (uint32_t t = 0; t < tris.size(); ++t) {
-        cur.assign(tris[t].e, tris[t].e + 3);
-        std::sort(cur.begin(), cur.end(), std::greater<uint32_t>());
+    std::vector<uint32_t> store;
+    // Adds reduced columns to cur (descending edge ranks) while its lowest
+    // entry has an owner.
+    auto reduce = [&](std::vector<uint32_t>& cur, std::vector<uint32_t>& tmp) {
         while (!cur.empty() && owner[cur[0]] != UINT32_MAX) {
             const uint32_t o = owner[cur[0]];
             const uint32_t* q = store.data() + off[o];
@@ -991,6 +1074,12 @@ Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, Red
             tmp.insert(tmp.end(), q, qe);
             cur.swap(tmp);
         }
+    };
+    std::vector<uint32_t> cur, tmp;
+    for (uint32_t t = 0; t < tris.size(); ++t) {
+        cur.assign(tris[t].e, tris[t].e + 3);
+        std::sort(cur.begin(), cur.end(), std::greater<uint32_t>());
+        reduce(cur, tmp);
         if (!cur.empty()) {
             owner[cur[0]] = t;
             store.insert(store.end(), cur.begin(), cur.end());
@@ -1001,30 +1090,49 @@ Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, Red
         }
         off[t + 1] = store.size();
     }
-    // bars in column order, as compute_pairs emits them
+    // bars in column order, as compute_pairs emits them: each column's bar
+    // found in parallel (0: none, 1: essential, 2: finite), then compacted
+    std::vector<uint8_t> kind(cols.size(), 0);
+    std::vector<uint32_t> dtri(cols.size(), UINT32_MAX);
+    std::atomic<int> bad{0};
+    parallel_chunks(threads, cols.size(), 4096, [&](unsigned, uint64_t c0, uint64_t c1) {
+        for (uint64_t ci = c0; ci < c1; ++ci) {
+            const Entry& c = cols[ci];
+            uint32_t u = uint32_t((1.0 + std::sqrt(1.0 + 8.0 * double(c.idx))) / 2.0);
+            while (choose2(u) > c.idx) --u;
+            while (choose2(u + 1) <= c.idx) ++u;
+            const uint32_t v = uint32_t(c.idx - choose2(u));
+            const uint32_t* b = hc.ci + hc.rp[u];
+            const uint32_t* e = hc.ci + hc.rp[u + 1];
+            const uint32_t* it = std::lower_bound(b, e, v);
+            if (it == e || *it != v) {
+                bad.store(1);
+                continue;
+            }
+            const uint32_t r = rank[uint64_t(it - hc.ci)];
+            if (r == UINT32_MAX) {
+                bad.store(2);
+                continue;
+            }
+            const uint32_t t = owner[r];
+            if (t == UINT32_MAX) kind[ci] = 1;
+            else if (tris[t].d > c.d) kind[ci] = 2, dtri[ci] = t;
+        }
+    });
+    if (bad.load() == 1) throw std::logic_error("gb300: a column's edge is not in the graph");
+    if (bad.load() == 2) throw std::logic_error("gb300: a column's edge is above the threshold");
     Bars bars;
-    for (const Entry& c : cols) {
-        uint32_t u = uint32_t((1.0 + std::sqrt(1.0 + 8.0 * double(c.idx))) / 2.0);
-        while (choose2(u) > c.idx) --u;
-        while (choose2(u + 1) <= c.idx) ++u;
-        const uint32_t v = uint32_t(c.idx - choose2(u));
-        const uint32_t* b = hc.ci + hc.rp[u];
-        const uint32_t* e = hc.ci + hc.rp[u + 1];
-        const uint32_t* it = std::lower_bound(b, e, v);
-        if (it == e || *it != v) throw std::logic_error("gb300: a column's edge is not in the graph");
-        const uint32_t r = rank[uint64_t(it - hc.ci)];
-        if (r == UINT32_MAX) throw std::logic_error("gb300: a column's edge is above the threshold");
-        const uint32_t t = owner[r];
-        if (t == UINT32_MAX) {
-            bars.birth.push_back(c.d);
+    for (size_t ci = 0; ci < cols.size(); ++ci) {
+        if (!kind[ci]) continue;
+        const Entry& c = cols[ci];
+        bars.birth.push_back(c.d);
+        bars.birth_idx.push_back(c.idx);
+        if (kind[ci] == 1) {
             bars.death.push_back(INFINITY);
-            bars.birth_idx.push_back(c.idx);
             bars.death_idx.push_back(kNone);
-        } else if (tris[t].d > c.d) {
-            bars.birth.push_back(c.d);
-            bars.death.push_back(tris[t].d);
-            bars.birth_idx.push_back(c.idx);
-            bars.death_idx.push_back(tris[t].idx);
+        } else {
+            bars.death.push_back(tris[dtri[ci]].d);
+            bars.death_idx.push_back(tris[dtri[ci]].idx);
         }
     }
     st.columns = cols.size();

@@ -70,9 +70,12 @@ uint64_t graph_triangles(const HostComplex& hc, uint64_t limit = UINT64_MAX);
 // filtration order); bars come out in their order, as compute_pairs emits
 // them. st.emergent stays 0 (no emergent shortcut is taken). With gave_up,
 // the stored reduced columns are capped at max_store entries (0: 16 a
-// triangle); past the cap *gave_up is set and nothing is returned.
+// triangle) and the triangles at max_tris; past either cap *gave_up is set
+// and nothing is returned. `threads` host threads (0: all) build and sort
+// the edges and triangles; the reduction itself is sequential.
 Bars graph_pairs_dim1(const HostComplex& hc, const std::vector<Entry>& cols, ReduceStats& st,
-                      bool* gave_up = nullptr, uint64_t max_store = 0);
+                      bool* gave_up = nullptr, uint64_t max_store = 0, uint64_t max_tris = UINT64_MAX,
+                      unsigned threads = 0);
 
 }  // namespace host
 }  // namespace tt
