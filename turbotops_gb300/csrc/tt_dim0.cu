@@ -546,8 +546,12 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
         if (cx.mat)
             k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, s>>>(cx.mat, n, out.keys, fmt, m, app, emw, emf);
         else
-            k_apparent_csr<<<grid_for(m, 256), 256, 0, s>>>(CsrCx{cx.rp, cx.ci, cx.w}, out.keys, fmt, inv, m, app,
-                                                            emw, emf);
+            // six of the eight resident blocks an SM: the forest's short
+            // kernels then always find free slots instead of waiting for a
+            // wave of scan blocks to retire (measured: kNN front end of
+            // 100,000 points, dim0 0.04 ms shorter than with all eight)
+            k_apparent_csr<<<std::min<u32>(grid_for(m, 256), 6 * kSMs), 256, 0, s>>>(
+                CsrCx{cx.rp, cx.ci, cx.w}, out.keys, fmt, inv, m, app, emw, emf);
         TT_LAUNCH("k_apparent");
         ++c->launches;
     }
