@@ -98,6 +98,27 @@ def test_host_entries_reject_non_finite(bad):
     assert st == capi.OK and r["rp"][-1] > 0
 
 
+@pytest.mark.parametrize("bad", [math.nan, math.inf])
+def test_knn_front_h_non_finite_on_the_tensor_core_path(bad):
+    """The kNN front end with host buffers checks the points while the
+    tensor-core kNN already runs (L2 in R^32, 3,000 points): the same error,
+    raised before the graph is built, and the next call is exact again."""
+    from oracle import oracle as O
+    x = np.ascontiguousarray(synth.gmm(3000, 32, 8, 4), np.float32)
+    bad_x = x.copy()
+    bad_x[2999, 31] = bad
+    c = ctx()
+    st, _ = _front_h(bad_x, 15)
+    assert st == capi.ERR_INVALID
+    assert "non-finite coordinate" in c.L.tt_last_error(c.h).decode()
+    st, r = _front_h(x, 15)
+    assert st == capi.OK
+    orp, oci, ow = O.knn_graph(x, "l2", O.knn(x, "l2", 15))
+    assert np.array_equal(r["rp"], np.asarray(orp, np.uint64))
+    assert np.array_equal(r["col"], np.asarray(oci, np.uint32))
+    assert np.array_equal(r["w"].view(np.uint32), np.asarray(ow, np.float32).view(np.uint32))
+
+
 def test_knn_front_h_above_packed_key_range_vs_oracle():
     """140,000 points: edge indices beyond the packed keys' 33 bits, so dim0
     runs on the wide key layout with the kept-edge count announced by the

@@ -13,17 +13,35 @@ namespace {
 
 thread_local std::string g_error;   // errors of calls without a context
 
+// A call that checked its points asynchronously (check_finite_async) and
+// failed before reading the result reports the non-finite coordinate, which
+// the reference detects before anything else.
+bool nonfinite_pending(tt_ctx* c) {
+    if (!c || !c->fin_pending) return false;
+    c->fin_pending = false;
+    return cudaEventSynchronize(c->fin_ev) == cudaSuccess && *c->fin_host != 0;
+}
+
 template <typename F>
 int guard(tt_ctx* c, F&& f) {
     try {
         if (!c) throw Error(TT_ERR_INVALID, "gb300: null context");
+        c->fin_pending = false;
         TT_CUDA(cudaSetDevice(c->device));
         f();
         return TT_OK;
     } catch (const Error& e) {
+        if (nonfinite_pending(c)) {
+            c->last_error = "persistence: non-finite coordinate";
+            return TT_ERR_INVALID;
+        }
         (c ? c->last_error : g_error) = e.what();
         return e.status;
     } catch (const std::exception& e) {
+        if (nonfinite_pending(c)) {
+            c->last_error = "persistence: non-finite coordinate";
+            return TT_ERR_INVALID;
+        }
         (c ? c->last_error : g_error) = e.what();
         return TT_ERR_INTERNAL;
     }
@@ -51,6 +69,39 @@ void check_finite_dev(tt_ctx* c, const f32* x, u64 count) {
     TT_CUDA(cudaStreamSynchronize(c->stream));
     if (h) invalid("persistence: non-finite coordinate");
 }
+
+}  // namespace
+
+namespace tt {
+// The same check without the round trip: the flag goes to page-locked memory
+// and settle_finite reads it once the next stages are enqueued, before any
+// kernel indexes memory by a value derived from the points (the kNN kernels
+// only compare distances: a NaN never enters a list).
+void check_finite_async(tt_ctx* c, const f32* x, u64 count) {
+    c->fin_pending = false;
+    if (!count) return;
+    if (!c->fin_host) TT_CUDA(cudaMallocHost(&c->fin_host, sizeof(unsigned)));
+    if (!c->fin_ev) TT_CUDA(cudaEventCreateWithFlags(&c->fin_ev, cudaEventDisableTiming));
+    u32* flag = c->arena.get<u32>(S_MISC2, 4);
+    TT_CUDA(cudaMemsetAsync(flag, 0, sizeof(u32), c->stream));
+    const u32 grid = u32(std::min<u64>((count + 255) / 256, 4ull * u64(c->sms)));
+    k_nonfinite<<<grid, 256, 0, c->stream>>>(x, count, flag);
+    TT_LAUNCH("k_nonfinite");
+    ++c->launches;
+    TT_CUDA(cudaMemcpyAsync(c->fin_host, flag, sizeof(u32), cudaMemcpyDeviceToHost, c->stream));
+    TT_CUDA(cudaEventRecord(c->fin_ev, c->stream));
+    c->fin_pending = true;
+}
+
+void settle_finite(tt_ctx* c) {
+    if (!c->fin_pending) return;
+    c->fin_pending = false;
+    TT_CUDA(cudaEventSynchronize(c->fin_ev));
+    if (*c->fin_host) invalid("persistence: non-finite coordinate");
+}
+}  // namespace tt
+
+namespace {
 
 void check_metric(int kind, float p) {
     if (kind < TT_METRIC_L1 || kind > TT_METRIC_LP) invalid("metric: unknown kind");
@@ -158,6 +209,8 @@ void tt_ctx_destroy(tt_ctx* c) {
     }
     if (c->aux_ev) cudaEventDestroy(c->aux_ev);
     if (c->tc_host) cudaFreeHost(c->tc_host);
+    if (c->fin_host) cudaFreeHost(c->fin_host);
+    if (c->fin_ev) cudaEventDestroy(c->fin_ev);
     if (c->side) {
         cudaStreamSynchronize(c->side);
         cudaStreamDestroy(c->side);
@@ -448,7 +501,7 @@ int tt_knn_front_h(tt_ctx* c, const float* x_h, uint32_t n, uint32_t dim, int ki
         if (k == 0) invalid("persistence: k must be >= 1");
         f32* x = c->arena.get<f32>(S_PTS, u64(n) * dim + 1);
         if (n) TT_CUDA(cudaMemcpyAsync(x, x_h, sizeof(f32) * n * dim, cudaMemcpyHostToDevice, c->stream));
-        check_finite_dev(c, x, u64(n) * dim);
+        check_finite_async(c, x, u64(n) * dim);   // read in knn_graph, after the kNN is enqueued
         u64* rp = nullptr;
         u32* gci = nullptr;
         f32* gw = nullptr;

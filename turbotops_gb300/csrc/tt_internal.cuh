@@ -113,6 +113,11 @@ u64 redzed_edges_owned(tt_ctx* c, const Complex& cx, f32** d, int32_t** verts);
 // std::length_error (TT_ERR_LENGTH) with make_dense's message when the lower
 // triangle of an n-point matrix exceeds the context's memory budget.
 void check_dense_budget(const tt_ctx* c, u32 n);
+// Non-finite coordinates of count device floats, checked without a round
+// trip: settle_finite (a no-op when nothing is pending) raises the
+// reference's error once the caller has enqueued its next stages.
+void check_finite_async(tt_ctx* c, const f32* x, u64 count);
+void settle_finite(tt_ctx* c);
 // ---- tt_parse.cu
 void parse_points(tt_ctx* c, const char* text, u64 bytes, f32* pts, u64 cap, u32* n, u32* dim);
 void redzed_leftover(tt_ctx* c, const f32* mat, u32 n, f32 thr, unsigned long long* bits);   // tt_redzed_pred.cu

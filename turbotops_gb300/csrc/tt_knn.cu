@@ -300,6 +300,7 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
     if (!ids) {
         kid = c->arena.get<u32>(S_KNN_I, u64(n) * k + 1);
         knn_exact(c, x, n, dim, kind, p, k, kid, kd, true);   // its status is read at the next round trip
+        settle_finite(c);   // a pending check of the points: before the lists index anything
     } else {
         invalid("gb300: knn_graph from external lists is not supported; pass ids = NULL");
     }
