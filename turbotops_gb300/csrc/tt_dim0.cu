@@ -612,6 +612,26 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
     } else {
         TT_CUDA(cudaMemsetAsync(tot, 0, sizeof(u64), c->stream));
     }
+    // the outputs: at their largest sizes (H0 bars < n, columns <= m) when
+    // that is small, so the emit is enqueued before the counts come back;
+    // otherwise at the counted sizes, after the round trip
+    auto emit = [&](u64 nh0, u64 ncols) {
+        out.h0 = c->arena.get<f32>(S_OUT0, nh0 + 1);
+        out.cidx = c->arena.get<u64>(S_OUT1, ncols + 1);
+        out.cd = c->arena.get<f32>(S_OUT2, ncols + 1);
+        out.emi = c->arena.get<u64>(S_OUT3, ncols + 1);
+        out.emf = c->arena.get<u8>(S_OUT4, ncols + 1);
+        out.h0_edge = c->arena.get<u64>(S_OUT5, nh0 + 1);
+        if (m) {
+            k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, fmt, tree, out.app, emw, emf, m, want_cols,
+                                                                 o2, tot, out.h0, out.h0_edge, out.cidx, out.cd,
+                                                                 out.emi, out.emf);
+            TT_LAUNCH("k_emit_dim0");
+            ++c->launches;
+        }
+    };
+    const bool early = m <= (u64(1) << 24);
+    if (early) emit(n, want_cols ? m : 0);
     u64 hp = 0;
     u32 bad = 0;
     TT_CUDA(cudaMemcpyAsync(&hp, tot, sizeof(hp), cudaMemcpyDeviceToHost, c->stream));
@@ -621,19 +641,7 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
     const u64 h[2] = {hp >> 32, hp & 0xffffffffull};
     out.nh0 = h[0];
     out.ncols = h[1];
-    out.h0 = c->arena.get<f32>(S_OUT0, h[0] + 1);
-    out.cidx = c->arena.get<u64>(S_OUT1, h[1] + 1);
-    out.cd = c->arena.get<f32>(S_OUT2, h[1] + 1);
-    out.emi = c->arena.get<u64>(S_OUT3, h[1] + 1);
-    out.emf = c->arena.get<u8>(S_OUT4, h[1] + 1);
-    out.h0_edge = c->arena.get<u64>(S_OUT5, h[0] + 1);
-    if (m) {
-        k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, fmt, tree, out.app, emw, emf, m, want_cols, o2,
-                                                             tot,
-                                                             out.h0, out.h0_edge, out.cidx, out.cd, out.emi, out.emf);
-        TT_LAUNCH("k_emit_dim0");
-        ++c->launches;
-    }
+    if (!early) emit(h[0], h[1]);
     // every hook merged two components through one tree edge
     out.essential = n - total_hooks;
 }

@@ -239,9 +239,12 @@ __global__ void __launch_bounds__(kLongThreads) k_graph_rowsort_long(const u64* 
 }
 
 // One warp per row: the distinct columns of the sorted row into the CSR.
+// Enqueued before the host has read the overflow flag: with a row left to
+// the global sort, the row pointers are meaningless and nothing is written.
 __global__ void k_graph_emit(const u64* __restrict__ off, u32 n, const u32* __restrict__ scol,
                              const f32* __restrict__ sw, const u64* __restrict__ rp, u32* __restrict__ ci,
-                             f32* __restrict__ wout) {
+                             f32* __restrict__ wout, const u32* __restrict__ overflow) {
+    if (*overflow) return;
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
     for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
@@ -333,8 +336,15 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         TT_LAUNCH("k_graph_rowsort_long");
         c->launches += 4;
         // the row pointers from the distinct counts (meaningful only without
-        // overflow), read back with the overflow flag in one round trip
+        // overflow); the CSR is emitted into buffers of the largest size
+        // (2 n k entries) before the count and the overflow flag come back in
+        // one round trip, so the emit runs while the host waits
         scan_exclusive<u64>(c, ucnt, rp, n, rp + n);
+        u32* ci = c->arena.get<u32>(S_GRAPH_CI, m + 1);
+        f32* w = c->arena.get<f32>(S_GRAPH_W, m + 1);
+        k_graph_emit<<<gw, 256, 0, c->stream>>>(off, n, scol, sw, rp, ci, w, ovf);
+        TT_LAUNCH("k_graph_emit");
+        ++c->launches;
         u32 overflow = 0;
         u64 nnz = 0;
         TT_CUDA(cudaMemcpyAsync(&overflow, ovf, 4, cudaMemcpyDeviceToHost, c->stream));
@@ -342,11 +352,6 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         TT_CUDA(cudaStreamSynchronize(c->stream));
         knn_tc_settle(c);
         if (!overflow) {
-            u32* ci = c->arena.get<u32>(S_GRAPH_CI, nnz + 1);
-            f32* w = c->arena.get<f32>(S_GRAPH_W, nnz + 1);
-            k_graph_emit<<<gw, 256, 0, c->stream>>>(off, n, scol, sw, rp, ci, w);
-            TT_LAUNCH("k_graph_emit");
-            ++c->launches;
             *ci_out = ci;
             *w_out = w;
             return nnz;
