@@ -663,6 +663,55 @@ def batch_only(count: int) -> int:
     return 0
 
 
+def stage_only(stage: str, n: int, dim: int, steps: int, warmup: int) -> int:
+    """One stage alone, timed with CUDA events on the context's stream (the
+    default stream), for profiling runs: `dense` is make_dense + the enclosing
+    radius of n Gaussian points in R^dim (an n x n float32 matrix written once:
+    larger than L2 from n = 6,000, so no flush is needed), `mst` the
+    complete-graph H0 deaths of the n x 32 Gaussian mixture. Prints one line."""
+    import torch
+
+    from turbotops_gb300 import capi, ops, synth
+    from turbotops_gb300.capi import Context
+    dev = torch.device("cuda", 0)
+    ctx = Context(0)
+    stream = torch.cuda.current_stream(dev)
+    x = torch.from_numpy(synth.gauss(n, dim, 1) if stage == "dense" else synth.gmm(n, 32)).to(dev)
+    if stage == "dense":   # the allocation-free entry point: no host round trip inside the timed region
+        mat = torch.empty((n, n), dtype=torch.float32, device=dev)
+        radius = torch.empty(1, dtype=torch.float32, device=dev)
+        kind, p = capi.metric_parse("l2")
+
+        def run():
+            st = ctx.L.tt_dense_distances_static(x.data_ptr(), n, dim, kind, p, mat.data_ptr(), radius.data_ptr(),
+                                                 C.c_void_p(stream.cuda_stream))
+            if st:
+                raise RuntimeError(ctx.L.tt_last_error(None).decode())
+    else:
+        def run():
+            return ops.mst_deaths(ctx, x)
+    ms = []
+    for r in range(warmup + steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        e1.synchronize()
+        if r >= warmup:
+            ms.append(e0.elapsed_time(e1))
+    t = statistics.mean(ms)
+    line = {"stage": stage, "points": n, "dim": dim if stage == "dense" else 32, "ms": round(t, 4)}
+    if stage == "dense":
+        nbytes = 4 * n * n + 4 * n * dim   # the matrix written, the points read
+        pk, src = peaks()
+        line.update({"algorithmic_bytes": nbytes, "achieved_gbs": round(nbytes / t / 1e6, 1),
+                     "peak_gbs": pk["hbm_gbs"], "frac": round(nbytes / t / 1e6 / pk["hbm_gbs"], 3),
+                     "peak_source": src})
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     global N
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
@@ -678,10 +727,15 @@ def main():
     ap.add_argument("--all-legs", action="store_true", help="also the lattice workload among the other legs")
     ap.add_argument("--batch-only", type=int, metavar="CLOUDS", default=0,
                     help="profiling: only the batched front end on the first CLOUDS clouds (3 graph replays)")
+    ap.add_argument("--stage", choices=["dense", "mst"], default=None,
+                    help="profiling: only this stage on --points points (dense: in R^--dim)")
+    ap.add_argument("--dim", type=int, default=3, help="dimension of the dense stage's points")
     args = ap.parse_args()
     N = args.n
     if args.batch_only:
         return batch_only(args.batch_only)
+    if args.stage:
+        return stage_only(args.stage, args.n, args.dim, args.steps, args.warmup)
     ws, rank, local = dist_env()
     if ws > 1:
         import torch.distributed as dist
