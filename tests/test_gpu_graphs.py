@@ -65,6 +65,25 @@ def test_mst_vs_oracle(metric, n, dim):
     assert np.array_equal(bits(ops.h0_bars(d)), bits(O.mst_h0(x, metric)))
 
 
+@pytest.mark.parametrize("metric", ["l2", "l1", "linf", "lp:1.5"])
+@pytest.mark.parametrize("n,dim,kind", [(4200, 16, "gmm"), (5000, 3, "grid"), (4500, 2, "grid"),
+                                        (4096, 8, "gauss")])
+def test_mst_knn_seeded_rounds_vs_oracle(metric, n, dim, kind):
+    """From 4,096 points the Borůvka rounds start from 16-nearest-neighbour
+    lists and scan only the interior points that can still carry their
+    component's minimum: the same deaths as the oracle's Prim tree, also on
+    lattices where distances tie everywhere and on well-separated clusters
+    (whose last rounds have no list entry outside the component)."""
+    if kind == "gmm":
+        x = synth.gmm(n, dim, 6, n)
+    elif kind == "grid":
+        x = synth.grid(n, dim, 90 if dim == 2 else 25, n)
+    else:
+        x = synth.gauss(n, dim, n + dim)
+    d = ops.mst_deaths(ctx(), dev(x), metric)
+    assert np.array_equal(bits(ops.h0_bars(d)), bits(O.mst_h0(x, metric)))
+
+
 def test_radius_vs_oracle_ties():
     x = synth.grid(800, 4, 7, 3)
     for metric, tau in [("l1", 3.0), ("linf", 1.0), ("l2", 2.0), ("lp:1.5", 2.5), ("lp:3", 2.0)]:

@@ -137,6 +137,7 @@ enum Slot : int {
     S_RZ_D, S_RZ_V,                                                // RedZeD edge lists sized to their count
     S_TXT, S_TXT_CNT, S_TXT_LINES, S_TXT_TOK, S_TXT_HOST,          // text ingestion
     S_DIM0_ERR,                                                    // dim0's announced-count check
+    S_MST_KB, S_MST_Q,                                             // MST: interior bounds, scanned points
     S_NSLOTS
 };
 

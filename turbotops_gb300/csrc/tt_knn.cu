@@ -422,8 +422,8 @@ u64 radius_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32 t
 // i's minimum (d, combinatorial index) edge to another component, as float
 // bits of d << 32 | the other endpoint (~0 when every point shares i's).
 void foreign_nearest(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* comp,
-                     unsigned long long* near, u32* err) {
-    scan_all(c, kind, x, n, dim, p, ForeignOp{comp, near}, comp, err);
+                     unsigned long long* near, u32* err, const u32* qlist, const u32* nq) {
+    scan_all(c, kind, x, n, dim, p, ForeignOp{comp, near, qlist, nq}, comp, err);
 }
 
 void check_device_error(tt_ctx* c, const u32* err) { check_error_word(c, err); }

@@ -12,18 +12,62 @@
 // proposals close 2-cycles, broken by component id); components merge, and
 // after at most ceil(log2 n) rounds one tree remains. The deaths are then
 // sorted by a radix sort on their float bits.
+//
+// Above kKnnMin points the rounds start from each point's K nearest
+// neighbours (one exact kNN pass; the tensor-core filter for L2 in R^32):
+// the first list entry in another component is the point's nearest foreign
+// point (the list holds the K smallest (d, j) of all points), and a point
+// whose whole list lies in its own component has no foreign edge shorter than
+// its K-th distance. Such an interior point can only carry its component's
+// minimum when that K-th distance does not exceed the best proposal of the
+// component's other points, so only those interior points are scanned (a
+// listed subset of queries) before the per-component minima are taken:
+// every round's proposals are the same as with a scan of every point.
 #include "tt_internal.cuh"
 
 namespace tt {
 
 void foreign_nearest(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u32* comp,
-                     unsigned long long* near, u32* err);
+                     unsigned long long* near, u32* err, const u32* qlist = nullptr, const u32* nq = nullptr);
 void check_device_error(tt_ctx* c, const u32* err);
 u32* device_error_word(tt_ctx* c);
 
 namespace {
 
 constexpr u32 kNoD = 0xffffffffu;   // no proposal (above every float's bits)
+constexpr u32 kKnnK = 16;           // neighbours a point keeps for the rounds
+constexpr u32 kKnnMin = 4096;       // fewer points: every round scans every point
+
+// From each point's list (ascending (d, id), K entries): the first entry in
+// another component is its proposal, d bits << 32 | j; with none, near[i] =
+// ~0 and kb[i] = the K-th entry's distance bits (a lower bound on every
+// foreign edge of i).
+__global__ void k_mst_knn_near(const u32* __restrict__ ids, const f32* __restrict__ dists, u32 K,
+                               const u32* __restrict__ comp, unsigned long long* __restrict__ near,
+                               u32* __restrict__ kb, u32 n) {
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const u32 ci = comp[i];
+        u64 key = ~0ull;
+        for (u32 t = 0; t < K; ++t) {
+            const u32 j = ids[u64(i) * K + t];
+            if (comp[j] != ci) {
+                key = (u64(__float_as_uint(dists[u64(i) * K + t])) << 32) | j;
+                break;
+            }
+        }
+        near[i] = key;
+        kb[i] = __float_as_uint(dists[u64(i) * K + K - 1]);
+    }
+}
+
+// Interior points (no proposal from the list) whose K-th distance does not
+// exceed their component's best proposal so far: listed for the scan.
+__global__ void k_mst_flag(const unsigned long long* __restrict__ near, const u32* __restrict__ kb,
+                           const u32* __restrict__ comp, const u32* __restrict__ bd, u32* __restrict__ qlist,
+                           u32* __restrict__ nq, u32 n) {
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (near[i] == ~0ull && kb[i] <= bd[comp[i]]) qlist[atomicAdd(nq, 1u)] = i;
+}
 
 __global__ void k_mst_init(u32* __restrict__ comp, u32* __restrict__ parent, u32* __restrict__ bd,
                            u64* __restrict__ bi, u32 n) {
@@ -101,6 +145,19 @@ u64 mst_deaths(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32* de
     unsigned long long* near = c->arena.get<unsigned long long>(S_UF_BEST, n + 1);
     u64* bi = c->arena.get<u64>(S_UF_WORK, n + 1);
     u32* bd = c->arena.get<u32>(S_UF_WORK2, n + 1);
+    // the lists first (the kNN stage's own scratch is free again after it)
+    const bool lists = n >= kKnnMin;
+    const u32 K = std::min<u32>(kKnnK, n - 1);
+    u32* kid = nullptr;
+    f32* kd = nullptr;
+    if (lists) {
+        kid = c->arena.get<u32>(S_KNN_I, u64(n) * K + 1);
+        kd = c->arena.get<f32>(S_KNN_D, u64(n) * K + 1);
+        knn_exact(c, x, n, dim, kind, p, K, kid, kd, false);
+    }
+    u32* kb = lists ? c->arena.get<u32>(S_MST_KB, n + 1) : nullptr;
+    u32* qlist = lists ? c->arena.get<u32>(S_MST_Q, n + 2) : nullptr;
+    u32* nq = lists ? qlist + n + 1 : nullptr;
     u32* cnt = c->arena.get<u32>(S_MISC1, 4);
     u32* err = device_error_word(c);
     k_mst_init<<<grid_for(n), 256, 0, c->stream>>>(comp, parent, bd, bi, n);
@@ -108,7 +165,16 @@ u64 mst_deaths(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32* de
     c->launches += 1;
     u32 done = 0;
     for (int round = 0; round < 40 && done < n - 1; ++round) {
-        foreign_nearest(c, x, n, dim, kind, p, comp, near, err);
+        if (lists) {
+            k_mst_knn_near<<<grid_for(n), 256, 0, c->stream>>>(kid, kd, K, comp, near, kb, n);
+            k_mst_min_d<<<grid_for(n), 256, 0, c->stream>>>(comp, near, bd, n);
+            TT_CUDA(cudaMemsetAsync(nq, 0, sizeof(u32), c->stream));
+            k_mst_flag<<<grid_for(n), 256, 0, c->stream>>>(near, kb, comp, bd, qlist, nq, n);
+            c->launches += 3;
+            foreign_nearest(c, x, n, dim, kind, p, comp, near, err, qlist, nq);
+        } else {
+            foreign_nearest(c, x, n, dim, kind, p, comp, near, err);
+        }
         k_mst_min_d<<<grid_for(n), 256, 0, c->stream>>>(comp, near, bd, n);
         k_mst_min_idx<<<grid_for(n), 256, 0, c->stream>>>(comp, near, bd, reinterpret_cast<unsigned long long*>(bi),
                                                           n);

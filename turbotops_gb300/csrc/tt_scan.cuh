@@ -134,10 +134,14 @@ struct RadiusFillOp {
 // order (d, combinatorial index): for a fixed point i the index of edge
 // (i, j) grows with j, so the per-point minimum of (d, j) is the minimum of
 // (d, index) over i's edges. near[i] = float bits of d << 32 | j (~0: none);
-// the Borůvka round (tt_mst.cu) reduces these per component.
+// the Borůvka round (tt_mst.cu) reduces these per component. With qlist,
+// only the *nq points it lists are queries (the scan's grid covers n; the
+// CTAs past *nq return at once) and the other points' near[] stay as they are.
 struct ForeignOp {
     const u32* comp;
     unsigned long long* near;   // per point
+    const u32* qlist = nullptr;
+    const u32* nq = nullptr;
     struct State {
         u64 key;
         u32 c;
@@ -193,7 +197,14 @@ k_scan(const f32* __restrict__ x, u32 n, u32 dim_rt, f32 p, Op op, const u32* __
     u32* tcomp = reinterpret_cast<u32*>(tiles + 2 * kCB * dim);    // [2][kCB]
     __shared__ __align__(8) u64 bar[2];
     const u32 tid = threadIdx.x;
-    const u32 i = blockIdx.x * kQ + tid;
+    u32 i = blockIdx.x * kQ + tid;
+    if constexpr (std::is_same<Op, ForeignOp>::value) {
+        if (op.qlist) {   // a listed subset of the points (block-uniform exit past its end)
+            const u32 nq = *op.nq;
+            if (blockIdx.x * kQ >= nq) return;
+            i = i < nq ? op.qlist[i] : n;
+        }
+    }
     const bool active = i < n;
     constexpr int QN = kRt ? 1 : DIM;
     f32 q[QN];
