@@ -1,5 +1,7 @@
 """CUDA path vs the reference goldens and the oracle: exact kNN lists, the
 symmetric kNN graph, the radius graph and the complete-graph MST (H0)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -55,6 +57,22 @@ def test_knn_graph_vs_oracle(metric, n, dim, k, kind):
     assert np.array_equal(host(rp).view(np.uint64), orp)
     assert np.array_equal(host(ci).view(np.uint32), oci)
     assert np.array_equal(bits(host(w)), bits(ow))
+
+
+@pytest.mark.parametrize("metric", ["lp:1.5", "lp:2.5"])
+@pytest.mark.parametrize("n,dim,kind", [(5000, 8, "gauss"), (4500, 3, "grid"), (4200, 32, "gmm")])
+def test_lp_knn_in_cell_order_vs_oracle(metric, n, dim, kind):
+    """From 4,096 points the Lp scan takes its queries cell by cell (nearest
+    of strided pivots): the lists are the oracle's, ties on the lattice
+    included."""
+    if kind == "gmm":
+        x = synth.gmm(n, dim, 6, n)
+    elif kind == "grid":
+        x = synth.grid(n, dim, 25, n)
+    else:
+        x = synth.gauss(n, dim, n + dim)
+    i, _ = ops.knn(ctx(), dev(x), 15, metric)
+    assert np.array_equal(host(i).view(np.uint32), O.knn_rows(x, metric, 15, 0, n, os.cpu_count() or 1))
 
 
 @pytest.mark.parametrize("metric", ["l2", "l1", "linf", "lp:1.5"])

@@ -276,6 +276,50 @@ bool knn_tc_applicable(u32 n, u32 dim, int kind, u32 k, const f32* x);
 void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists, bool defer);
 void knn_tc_settle(tt_ctx* c);
 
+namespace {
+// Each point's cell: the nearest (squared L2; ties to the lower pivot) of P
+// strided pivot points, the pivots' rows staged in shared memory.
+__global__ void k_pivot_cell(const f32* __restrict__ x, u32 n, u32 dim, u32 P, u64* __restrict__ key,
+                             u32* __restrict__ val) {
+    extern __shared__ f32 pv[];   // P x dim
+    for (u32 t = threadIdx.x; t < P * dim; t += blockDim.x) pv[t] = x[(u64(t / dim) * n / P) * dim + t % dim];
+    __syncthreads();
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const f32* xi = x + u64(i) * dim;
+        u32 best = 0;
+        f32 bd = INFINITY;
+        for (u32 q = 0; q < P; ++q) {
+            f32 s = 0.0f;
+            for (u32 k = 0; k < dim; ++k) {
+                const f32 u = xi[k] - pv[q * dim + k];
+                s = fmaf(u, u, s);
+            }
+            if (s < bd) bd = s, best = q;
+        }
+        key[i] = best;
+        val[i] = i;
+    }
+}
+}  // namespace
+
+// A query order for the exhaustive scan in which neighbouring points share
+// warps: the points stably sorted by their cell among about n / 1536 pivots.
+// (The Lp scan stops a candidate's sum early once it exceeds the query's
+// bound; a warp waits for its slowest lane, so queries with similar
+// neighbourhoods in one warp stop at similar points.)
+static const u32* pivot_order(tt_ctx* c, const f32* x, u32 n, u32 dim) {
+    const u32 P = std::max<u32>(2, std::min<u32>(128, n / 1536));
+    u64* key = c->arena.get<u64>(S_TC_KEYS, n);
+    u32* val = c->arena.get<u32>(S_TC_VALS, n);
+    k_pivot_cell<<<std::min<u32>(div_up(n, 256), 8 * u32(c->sms)), 256, sizeof(f32) * P * dim, c->stream>>>(
+        x, n, dim, P, key, val);
+    TT_LAUNCH("k_pivot_cell");
+    ++c->launches;
+    u64* kb = c->arena.get<u64>(S_SORT_A, n);
+    u32* vb = c->arena.get<u32>(S_SORT_VA, n);
+    return radix_sort<u32>(c, key, val, n, kb, vb, 32 - __builtin_clz(P - 1)) ? vb : val;
+}
+
 void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, u32* ids, f32* dists, bool defer) {
     if (k == 0 || n < 2) return;
     // L2 in R^32: the tensor-core Gram filter (tt_knn_tc.cu) unless the
@@ -285,8 +329,9 @@ void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, 
         return;
     }
     u32* err = error_word(c);
-    if (k <= 16) scan_all(c, kind, x, n, dim, p, KnnOp<16>{ids, dists, k}, nullptr, err);
-    else if (k <= 32) scan_all(c, kind, x, n, dim, p, KnnOp<32>{ids, dists, k}, nullptr, err);
+    const u32* order = kind == M_LP && n >= 4096 ? pivot_order(c, x, n, dim) : nullptr;
+    if (k <= 16) scan_all(c, kind, x, n, dim, p, KnnOp<16>{ids, dists, k, order}, nullptr, err);
+    else if (k <= 32) scan_all(c, kind, x, n, dim, p, KnnOp<32>{ids, dists, k, order}, nullptr, err);
     else invalid("gb300: exact kNN supports k <= 32");
     check_error_word(c, err);
 }

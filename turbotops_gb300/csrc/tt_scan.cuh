@@ -37,11 +37,15 @@ struct RegRow {
 // Per-query visitors.
 // --------------------------------------------------------------------------
 // Top-K by (distance, id) in registers (knn_query's heap, graph.hpp:123-166).
+// With qlist, the CTAs take their queries in that order (a permutation of the
+// points): the lists are the same, since every comparison is on (distance,
+// id), and queries that lie close together share warps.
 template <int K>
 struct KnnOp {
     u32* ids;
     f32* dists;
     u32 k;
+    const u32* qlist = nullptr;
     struct State {
         f32 d[K];
         u32 j[K];
@@ -171,6 +175,11 @@ struct ForeignOp {
 
 template <typename Op>
 struct NeedsComp : std::false_type {};
+// Visitors whose queries may come from a list.
+template <typename Op>
+struct ListedQueries : std::false_type {};
+template <int K>
+struct ListedQueries<KnnOp<K>> : std::true_type {};
 template <>
 struct NeedsComp<ForeignOp> : std::true_type {};
 
@@ -204,6 +213,8 @@ k_scan(const f32* __restrict__ x, u32 n, u32 dim_rt, f32 p, Op op, const u32* __
             if (blockIdx.x * kQ >= nq) return;
             i = i < nq ? op.qlist[i] : n;
         }
+    } else if constexpr (ListedQueries<Op>::value) {
+        if (op.qlist && i < n) i = op.qlist[i];   // every point, in the list's order
     }
     const bool active = i < n;
     constexpr int QN = kRt ? 1 : DIM;
