@@ -65,10 +65,10 @@
 //   and the chosen candidate tiles into two shared-memory stages, each with
 //   one bulk copy of the tile's pack (low bits, augmentation rows, ids,
 //   record tail); warp 1 issues a stage's copies as soon as the stage is
-//   free. Thread 0 issues tcgen05.mma.kind::tf32 (M = 128, N = 128,
-//   5 x K = 8) for the next tile into the free one of two TMEM accumulators
-//   once its own epilogue is done and commits to an mbarrier; the tensor core
-//   runs it while the other warps finish the current tile, reading its Gram
+//   free. The first warp to finish a tile's epilogue issues tcgen05.mma.kind::tf32
+//   (M = 128, N = 128, 5 x K = 8) for the next tile into the free one of two
+//   TMEM accumulators and commits to an mbarrier; the tensor core runs it
+//   while the other warps finish the current tile, reading its Gram
 //   rows (tcgen05.ld 32x32b.x32, two loads in flight), filtering and running
 //   the exact path. One barrier a tile.
 // TMEM: 2 x 128 columns per CTA; shared memory is padded so that at most two
@@ -141,6 +141,7 @@ struct Shared {
     u32 tmem_base;
     u32 block;
     u32 stop[2];
+    u32 ticket[2];                       // warps done with tile it's epilogue (by tile parity)
     volatile u32 fail;                   // a bounded wait of this CTA timed out
 };
 
@@ -663,6 +664,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
         mbar_init(&S.bar_t, 1);
         fence_mbar_init();
         S.stop[0] = S.stop[1] = 0;
+        S.ticket[0] = S.ticket[1] = 0;
         S.fail = 0;
     }
     tc_fence_before();
@@ -1116,16 +1118,25 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
                     __syncwarp();   // the queue is reused by the next tile
                 }
             }
-            if (tid == 0 && it + 1 < nl) {
-                // the next tile's product, issued once this warp's epilogue is
-                // done (its copy has had the whole epilogue to land); the tensor
-                // core runs it while the other warps finish this tile
-                const int nb = sb ^ 1, ns = int((it + 1) % NSTAGE);
-                mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err, &S.fail);
-                tc_fence_after();
-                mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]), smem_addr(S.aaug),
-                         smem_addr(S.pk[ns] + PK_AUG), smem_addr(S.zeros));
-                mma_commit(&S.bar_mma[nb]);
+            // the next tile's product, issued by the first warp whose epilogue
+            // is done (its copy has had that epilogue to land; accumulator nb
+            // and stage ns were released at the last barrier); the tensor
+            // core runs it while the other warps finish this tile. The last
+            // warp to arrive resets the parity's ticket, which is next used
+            // two tiles on, after a barrier.
+            if (it + 1 < nl) {
+                u32 order = 0;
+                if (lane == 0) order = atomicAdd(&S.ticket[it & 1], 1u);
+                order = __shfl_sync(0xffffffffu, order, 0);
+                if (order == 3 && lane == 0) S.ticket[it & 1] = 0;
+                if (order == 0 && lane == 0) {
+                    const int nb = sb ^ 1, ns = int((it + 1) % NSTAGE);
+                    mbar_wait(&S.bar_b[ns], (ns ? ub1 : ub0) & 1, err, &S.fail);
+                    tc_fence_after();
+                    mma_tile(tmem + u32(nb) * TC_N, smem_addr(S.a), smem_addr(S.b[ns]), smem_addr(S.aaug),
+                             smem_addr(S.pk[ns] + PK_AUG), smem_addr(S.zeros));
+                    mma_commit(&S.bar_mma[nb]);
+                }
             }
             if (sb) ++um1; else ++um0;
             // one reader of this CTA's timeout flag (shared memory: a global
