@@ -75,6 +75,19 @@ def test_lp_knn_in_cell_order_vs_oracle(metric, n, dim, kind):
     assert np.array_equal(host(i).view(np.uint32), O.knn_rows(x, metric, 15, 0, n, os.cpu_count() or 1))
 
 
+def test_lp_scans_refuse_dimensions_above_64():
+    """The cell order of the Lp scans is skipped where the scans refuse the
+    dimension: the caller gets the scans' own error, and the context keeps
+    working."""
+    x = synth.gauss(4100, 65, 1)
+    for run in (lambda: ops.knn(ctx(), dev(x), 15, "lp:1.5"), lambda: ops.mst_deaths(ctx(), dev(x), "lp:1.5")):
+        with pytest.raises(Exception, match="1 <= dim <= 64"):
+            run()
+    y = synth.gauss(4100, 8, 2)
+    i, _ = ops.knn(ctx(), dev(y), 15, "lp:1.5")
+    assert i.shape == (4100, 15)
+
+
 @pytest.mark.parametrize("metric", ["l2", "l1", "linf", "lp:1.5"])
 @pytest.mark.parametrize("n,dim", [(2000, 32), (1500, 3), (300, 7), (2, 3)])
 def test_mst_vs_oracle(metric, n, dim):

@@ -329,7 +329,8 @@ void knn_exact(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, u32 k, 
         return;
     }
     u32* err = error_word(c);
-    const u32* order = kind == M_LP && n >= 4096 ? pivot_order(c, x, n, dim) : nullptr;
+    // (dimensions the scans refuse keep their own error: no order for them)
+    const u32* order = kind == M_LP && n >= 4096 && dim <= scan::kMaxDim ? pivot_order(c, x, n, dim) : nullptr;
     if (k <= 16) scan_all(c, kind, x, n, dim, p, KnnOp<16>{ids, dists, k, order}, nullptr, err);
     else if (k <= 32) scan_all(c, kind, x, n, dim, p, KnnOp<32>{ids, dists, k, order}, nullptr, err);
     else invalid("gb300: exact kNN supports k <= 32");
