@@ -570,17 +570,14 @@ def batch_block(ctx, dev, reps: int = 5) -> dict:
 def batch_traffic(sizes, edges: int, ms: float) -> dict:
     """Algorithmic HBM bytes of one batched run: the matrices written (4 B a
     pair, full layout) and their lower triangles read twice (count, keys),
-    the kept keys written once and moved by the stable radix passes over the
-    cloud and distance bits (read for the histogram, read and written by the
-    scatter: 24 B an edge a pass; digits of 8 bits for sorts of 2^22 keys or
-    more, else 11), the edge list emitted (8 B key read, 12 B written)."""
+    the kept keys written once and moved by the stable radix passes of every
+    cloud's keys over their 31 distance bits (read for the histogram, read
+    and written by the scatter: 24 B an edge a pass; 8-bit digits, four
+    passes), the edge list emitted (8 B key read, 12 B written)."""
     pk, src = peaks()
     mat = 4 * sum(n * n for n in sizes)
     tri = 4 * sum(n * (n - 1) // 2 for n in sizes)
-    pairs = sum(n * (n - 1) // 2 for n in sizes)
-    bits = 31 + max(0, (len(sizes) - 1).bit_length())
-    digit = 8 if pairs >= 1 << 22 else 11
-    passes = -(-bits // digit)
+    passes = -(-31 // 8)
     b = mat + 2 * tri + 8 * edges + passes * 24 * edges + 20 * edges
     gbs = b / (ms * 1e-3) / 1e9
     return {"algorithmic_bytes": b, "radix_passes": passes, "achieved_gbs": gbs, "peak_gbs": pk["hbm_gbs"],

@@ -198,30 +198,51 @@ __global__ void k_batch_edges(const f32* __restrict__ mats, const u64* __restric
     }
 }
 
-// Exclusive scan of the per-cloud edge counts (one CTA; clouds <= 65536).
-__global__ void k_batch_offsets(const u64* __restrict__ per_cloud, u32 clouds, u64* __restrict__ off) {
+// Exclusive scan of the per-cloud edge counts (one CTA; clouds <= 65536),
+// and the segmented sort's tiles of the kept keys: cloud c's ceil(count /
+// kSegTileKeys) tiles after the previous clouds', their digit counts at 256
+// per tile in the same order; *ntiles = the list's length.
+__global__ void k_batch_offsets(const u64* __restrict__ per_cloud, u32 clouds, u64* __restrict__ off,
+                                SegTile* __restrict__ tiles, u32* __restrict__ ntiles) {
     __shared__ u64 part[1024];
+    __shared__ u32 tpart[1024];
     const u32 t = threadIdx.x;
     const u32 per = (clouds + blockDim.x - 1) / blockDim.x;
     u64 s = 0;
-    for (u32 c = t * per; c < min(clouds, (t + 1) * per); ++c) s += per_cloud[c];
+    u32 ts = 0;
+    for (u32 c = t * per; c < min(clouds, (t + 1) * per); ++c) {
+        s += per_cloud[c];
+        ts += u32((per_cloud[c] + kSegTileKeys - 1) / kSegTileKeys);
+    }
     part[t] = s;
+    tpart[t] = ts;
     __syncthreads();
     if (t == 0) {
         u64 run = 0;
+        u32 trun = 0;
         for (u32 q = 0; q < blockDim.x; ++q) {
             const u64 v = part[q];
+            const u32 tv = tpart[q];
             part[q] = run;
+            tpart[q] = trun;
             run += v;
+            trun += tv;
         }
     }
     __syncthreads();
     u64 run = part[t];
+    u32 trun = tpart[t];
     for (u32 c = t * per; c < min(clouds, (t + 1) * per); ++c) {
         off[c] = run;
         run += per_cloud[c];
+        const u32 tc = u32((per_cloud[c] + kSegTileKeys - 1) / kSegTileKeys);
+        for (u32 q = 0; q < tc; ++q) tiles[trun + q] = SegTile{c, q, 256u * trun, tc};
+        trun += tc;
     }
-    if (t == blockDim.x - 1) off[clouds] = run;
+    if (t == blockDim.x - 1) {
+        off[clouds] = run;
+        *ntiles = trun;
+    }
 }
 
 __global__ void k_batch_emit(const u64* __restrict__ keys, const unsigned long long* __restrict__ count, int ib,
@@ -271,6 +292,10 @@ struct Batch {
     unsigned long long* count = nullptr;
     u64* per_cloud = nullptr;
     u64* edge_off = nullptr;
+    SegTile* seg_tiles = nullptr;   // the segmented sort's tiles of the kept keys (built on the device)
+    u32* seg_ntiles = nullptr;      // ... their number
+    u32 nseg_tiles = 0;             // capacity: every cloud's largest key count in tiles
+    u64 seg_hist = 0;               // the digit counts' capacity: 256 per tile
     f32* ed = nullptr;
     int32_t* ev = nullptr;
     cudaGraph_t graph = nullptr;
@@ -389,12 +414,13 @@ struct Batch {
         k_batch_edges<<<g3, 256, 0, s>>>(mats, mat_off, sizes, pt_off, row_cloud, total_pts, radius, ib, row_off,
                                          keys, per_cloud);
         TT_LAUNCH("k_batch_edges");
-        k_batch_offsets<<<1, 1024, 0, s>>>(per_cloud, clouds, edge_off);
+        k_batch_offsets<<<1, 1024, 0, s>>>(per_cloud, clouds, edge_off, seg_tiles, seg_ntiles);
         TT_LAUNCH("k_batch_offsets");
-        // the kept keys only (a count on the device), the bits above the
-        // index field only (stable: ties keep the index order)
-        const bool swapped = radix_sort<u32>(&sctx, keys, nullptr, total_pairs, kbuf, nullptr,
-                                             31 + bits_for(clouds), ib, count);
+        // every cloud's kept keys on their own (they are contiguous, clouds
+        // in order), by the distance bits alone (stable: ties keep the index
+        // order): four 8-bit passes, the cloud bits need none
+        const bool swapped =
+            radix_sort_segments(&sctx, keys, kbuf, edge_off, seg_tiles, seg_ntiles, nseg_tiles, seg_hist, 31, ib);
         const u32 g4 = u32(std::min<u64>((total_pairs + 255) / 256, u64(owner->sms) * 32));
         k_batch_emit<<<g4, 256, 0, s>>>(swapped ? kbuf : keys, count, ib, ed, ev);
         TT_LAUNCH("k_batch_emit");
@@ -451,6 +477,11 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
                     for (u32 j0 = 0; j0 < n; j0 += u32(kShapes[si].c)) tiles[si].push_back(Tile{q, i0, j0});
             for (u32 i = 0; i < n; ++i) row_cloud.push_back(q);
         }
+        // the segmented sort's capacity: every cloud's largest key count
+        // (every pair kept) in tiles of kSegTileKeys, 256 digit counts a tile
+        u64 seg_cap = 0;
+        for (u32 q = 0; q < clouds; ++q) seg_cap += div_up(u64(sizes_h[q]) * (sizes_h[q] - 1) / 2, u64(kSegTileKeys));
+        if (256 * seg_cap >= (1ull << 32)) invalid("gb300: batch too large for the segmented sort's counts");
         b->ib = std::max(1, Batch::bits_for(u64(b->maxn) * (b->maxn - 1) / 2 + 1));
         if (b->ib + 31 + Batch::bits_for(clouds) > 64)
             invalid("gb300: batch too large for 64-bit edge keys (clouds x largest cloud)");
@@ -478,6 +509,10 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
         b->count = b->alloc<unsigned long long>(1);
         b->per_cloud = b->alloc<u64>(clouds);
         b->edge_off = b->alloc<u64>(clouds + 1);
+        b->nseg_tiles = u32(seg_cap);
+        b->seg_hist = 256 * seg_cap;
+        b->seg_tiles = b->alloc<SegTile>(seg_cap);
+        b->seg_ntiles = b->alloc<u32>(1);
         b->ed = b->alloc<f32>(b->total_pairs);
         b->ev = b->alloc<int32_t>(2 * b->total_pairs);
         cudaStream_t s = b->sctx.stream;
@@ -490,7 +525,10 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
                                     cudaMemcpyHostToDevice, s));
         TT_CUDA(cudaMemcpyAsync(b->row_cloud, row_cloud.data(), 4 * row_cloud.size(), cudaMemcpyHostToDevice, s));
         // size the sort's and the row scan's scratch outside any capture
-        radix_reserve(&b->sctx, b->total_pairs);
+        radix_reserve_entries(&b->sctx, b->seg_hist);
+        // the row scan's levels (64-bit entries: four times as many 32-bit
+        // entries reserve at least their bytes at every level)
+        radix_reserve_entries(&b->sctx, 4 * b->total_pts);
         TT_CUDA(cudaStreamSynchronize(s));
     } catch (...) {
         b->release();

@@ -76,6 +76,16 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
 template <typename V>
 void radix_sort_inplace(tt_ctx* c, u64* keys, V* vals, u64 n, int force_bits = 0);
 void radix_reserve(tt_ctx* c, u64 n);   // every slot radix_sort of n keys may grow
+void radix_reserve_entries(tt_ctx* c, u64 entries);   // ... a sort whose histogram has that many entries
+// A tile of the segmented sort: tile t (of tcount) of segment seg; its digit
+// counts at hbase + digit * tcount + t (segments' count blocks in segment
+// order, each 256 * tcount entries).
+struct SegTile {
+    u32 seg, t, hbase, tcount;
+};
+constexpr u32 kSegTileKeys = 4096;   // keys a tile of the segmented sort
+bool radix_sort_segments(tt_ctx* c, u64* keys, u64* kbuf, const u64* seg_off, const SegTile* tl,
+                         const u32* ntiles_dev, u32 max_tiles, u64 hist_entries, int bits, int lo_bit);
 
 // ---- tt_dim0.cu
 struct Dim0Out {

@@ -98,6 +98,47 @@ __global__ void k_tile_scan(const T* __restrict__ in, u64 n, const T* __restrict
 // ---------------------------------------------------------------------------
 // Radix sort kernels.
 // ---------------------------------------------------------------------------
+// Which keys a tile (CTA b) holds and where its digit counts go. FlatTiles:
+// the plain sort, tile b = keys [b RS_TILE, ...) of n (or of the count on the
+// device), counts digit-major over the tiles. SegTiles: the segmented sort,
+// tile b = keys [seg_off[s] + t RS_TILE, ...) of segment s (tiles never
+// straddle segments), counts at hbase + digit * tcount + t, so that one
+// exclusive scan of all segments' counts in order gives every key's final
+// position (segment s's counts sum to its key count).
+// kAllBins: the count layout reserves every bin of the widest digit for
+// every tile (a segment's block of counts does not depend on the pass), so
+// a pass with narrower digits writes zeros into the bins it does not use;
+// the flat layout scans only the bins of the pass.
+struct FlatTiles {
+    static constexpr bool kAllBins = false;
+    u64 n;
+    const unsigned long long* ndev;
+    u32 tiles;
+    __device__ __forceinline__ bool valid(u32) const { return true; }
+    __device__ __forceinline__ void range(u32 b, u64& lo, u64& hi) const {
+        const u64 nn = ndev ? min(n, u64(*ndev)) : n;
+        lo = u64(b) * RS_TILE;
+        hi = lo < nn ? min(lo + RS_TILE, nn) : lo;
+    }
+    __device__ __forceinline__ u64 hidx(u32 b, u32 d) const { return u64(d) * tiles + b; }
+};
+struct SegTiles {
+    static constexpr bool kAllBins = true;
+    const SegTile* tl;
+    const u64* seg_off;
+    const u32* ntiles;   // tiles in the list (the grid covers its capacity)
+    __device__ __forceinline__ bool valid(u32 b) const { return b < *ntiles; }
+    __device__ __forceinline__ void range(u32 b, u64& lo, u64& hi) const {
+        const SegTile e = tl[b];
+        const u64 end = seg_off[e.seg + 1];
+        lo = seg_off[e.seg] + u64(e.t) * RS_TILE;
+        hi = lo < end ? min(lo + RS_TILE, end) : lo;
+    }
+    __device__ __forceinline__ u64 hidx(u32 b, u32 d) const {
+        const SegTile e = tl[b];
+        return e.hbase + u64(d) * e.tcount + e.t;
+    }
+};
 // The lanes holding the same digit as this lane (a sentinel digit marks an
 // empty slot). A warp whose 32 digits agree, the common case once the later
 // passes see nearly sorted input, skips the match unit.
@@ -109,12 +150,13 @@ __device__ __forceinline__ u32 warp_peers(u32 dg) {
 // Digits of up to RS_MAXBITS bits (a pass sorts `width` bits from `shift`).
 // ndev (optional): the key count lives on the device (a graph-captured sort of
 // a data-dependent number of keys, n the capacity); tiles past it are empty.
-template <int BINS>
+template <int BINS, typename TM>
 __global__ void __launch_bounds__(RS_THREADS)
-k_rs_upsweep(const u64* __restrict__ keys, u64 n, const unsigned long long* __restrict__ ndev, int shift, u32 width,
-             u32* __restrict__ hist, u32 tiles) {
+k_rs_upsweep(const u64* __restrict__ keys, TM tm, int shift, u32 width, u32* __restrict__ hist) {
     __shared__ u32 h[RS_WARPS][BINS];
-    if (ndev) n = min(n, u64(*ndev));
+    if (!tm.valid(blockIdx.x)) return;   // past the list: no keys, no counts
+    u64 tlo, n;   // this tile's keys: [tlo, n)
+    tm.range(blockIdx.x, tlo, n);
     const u32 nd = 1u << width, mask = nd - 1u;
     for (u32 t = threadIdx.x; t < RS_WARPS * nd; t += RS_THREADS) h[t / nd][t % nd] = 0;
     __syncthreads();
@@ -122,9 +164,9 @@ k_rs_upsweep(const u64* __restrict__ keys, u64 n, const unsigned long long* __re
     // Each thread counts RS_ITEMS consecutive keys, one shared atomic per run
     // of equal digits: nearly sorted input (the later passes) then costs one
     // atomic a thread instead of one a key on a single counter.
-    const u64 base = u64(blockIdx.x) * RS_TILE + u64(threadIdx.x) * RS_ITEMS;
+    const u64 base = tlo + u64(threadIdx.x) * RS_ITEMS;
     u64 kv[RS_ITEMS];
-    if (base + RS_ITEMS <= n && (reinterpret_cast<uintptr_t>(keys) & 15) == 0) {   // 16-byte loads
+    if (base + RS_ITEMS <= n && (reinterpret_cast<uintptr_t>(keys + base) & 15) == 0) {   // 16-byte loads
         const ulonglong2* p = reinterpret_cast<const ulonglong2*>(keys + base);
 #pragma unroll
         for (int i = 0; i < RS_ITEMS / 2; ++i) {
@@ -152,11 +194,14 @@ k_rs_upsweep(const u64* __restrict__ keys, u64 n, const unsigned long long* __re
     }
     if (run) atomicAdd(&h[w][cur], run);
     __syncthreads();
-    for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) {
+    const u32 nb = TM::kAllBins ? u32(BINS) : nd;   // bins written (those past nd: zeros)
+    for (u32 d = threadIdx.x; d < nb; d += RS_THREADS) {
         u32 s = 0;
+        if (d < nd) {
 #pragma unroll
-        for (int q = 0; q < RS_WARPS; ++q) s += h[q][d];
-        hist[u64(d) * tiles + blockIdx.x] = s;
+            for (int q = 0; q < RS_WARPS; ++q) s += h[q][d];
+        }
+        hist[tm.hidx(blockIdx.x, d)] = s;
     }
 }
 
@@ -230,11 +275,10 @@ k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __res
 // is first ordered by digit in shared memory (stable), then written out in
 // that order, so the keys of one digit leave a tile as one contiguous run
 // (about RS_TILE / 2^width keys) instead of scattered 8-byte writes.
-template <typename V, bool VALS>
+template <typename V, bool VALS, typename TM>
 __global__ void __launch_bounds__(RS_THREADS)
 k_rs_scatter_local(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __restrict__ vin,
-                   V* __restrict__ vout, u64 n, const unsigned long long* __restrict__ ndev, int shift, u32 width,
-                   const u32* __restrict__ offs, u32 tiles) {
+                   V* __restrict__ vout, TM tm, int shift, u32 width, const u32* __restrict__ offs) {
     __shared__ u64 skey[RS_TILE];
     __shared__ V sval[VALS ? RS_TILE : 1];
     __shared__ u32 cnt[RS_WARPS][RS_LBINS];   // per-warp running count, then warp prefix
@@ -242,15 +286,16 @@ k_rs_scatter_local(const u64* __restrict__ kin, u64* __restrict__ kout, const V*
     __shared__ u32 tstart[RS_LBINS];          // the digit's first position in the ordered tile
     __shared__ u32 wsum[RS_WARPS];
     __shared__ u32 mbins[RS_WARPS][RS_LBINS]; // per-warp lane masks by digit (the ranking below)
-    if (ndev) n = min(n, u64(*ndev));
-    const u64 tbase = u64(blockIdx.x) * RS_TILE;
+    if (!tm.valid(blockIdx.x)) return;
+    u64 tbase, n;   // this tile's keys: [tbase, n)
+    tm.range(blockIdx.x, tbase, n);
     if (tbase >= n) return;
     const u32 nd = 1u << width, mask = nd - 1u;
     for (u32 t = threadIdx.x; t < RS_WARPS * RS_LBINS; t += RS_THREADS) {
         cnt[t / RS_LBINS][t % RS_LBINS] = 0;
         mbins[t / RS_LBINS][t % RS_LBINS] = 0;
     }
-    for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) gbase[d] = offs[u64(d) * tiles + blockIdx.x];
+    for (u32 d = threadIdx.x; d < nd; d += RS_THREADS) gbase[d] = offs[tm.hidx(blockIdx.x, d)];
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const u32 lt = (1u << lane) - 1u;
@@ -347,6 +392,7 @@ k_rs_scatter_local(const u64* __restrict__ kin, u64* __restrict__ kout, const V*
     }
 }
 static_assert(RS_LBINS == RS_THREADS, "one digit a thread in the local scatter's scan");
+static_assert(RS_TILE == int(kSegTileKeys), "the segmented sort's tiles are the radix tiles");
 
 __global__ void k_minmax(const u64* __restrict__ keys, u64 n, unsigned long long* __restrict__ mm) {
     u64 lo = ~0ull, hi = 0;
@@ -438,18 +484,19 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
     int shift = lo_bit;
     for (int q = 0; q < passes; ++q) {
         const int width = (lo_bit + bits - shift + (passes - q) - 1) / (passes - q);
+        const FlatTiles tm{n, ndev, tiles};
         if (local)
-            k_rs_upsweep<RS_LBINS><<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, ndev, shift, u32(width), hist, tiles);
+            k_rs_upsweep<RS_LBINS><<<tiles, RS_THREADS, 0, c->stream>>>(ka, tm, shift, u32(width), hist);
         else
-            k_rs_upsweep<RS_BINS><<<tiles, RS_THREADS, 0, c->stream>>>(ka, n, ndev, shift, u32(width), hist, tiles);
+            k_rs_upsweep<RS_BINS><<<tiles, RS_THREADS, 0, c->stream>>>(ka, tm, shift, u32(width), hist);
         TT_LAUNCH("k_rs_upsweep");
         scan_exclusive<u32>(c, hist, hist, u64(tiles) << width, nullptr, 0);
         if (local && va)
-            k_rs_scatter_local<V, true><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift,
-                                                                             u32(width), hist, tiles);
+            k_rs_scatter_local<V, true><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, tm, shift, u32(width),
+                                                                             hist);
         else if (local)
-            k_rs_scatter_local<V, false><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift,
-                                                                              u32(width), hist, tiles);
+            k_rs_scatter_local<V, false><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, tm, shift, u32(width),
+                                                                              hist);
         else
             k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift, u32(width), hist,
                                                                  tiles);
@@ -466,6 +513,41 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
 template bool radix_sort<u32>(tt_ctx*, u64*, u32*, u64, u64*, u32*, int, int, const unsigned long long*);
 template bool radix_sort<u64>(tt_ctx*, u64*, u64*, u64, u64*, u64*, int, int, const unsigned long long*);
 
+// Each segment [seg_off[s], seg_off[s + 1]) sorted on its own (stable) by key
+// bits [lo_bit, lo_bit + bits): the keys never leave their segment, so bits
+// that only tell segments apart need no pass. 8-bit digits and the local
+// scatter (runs of one digit leave a tile together); the tiles and their
+// count offsets come from the caller (SegTile), the segment bounds from the
+// device. The list's length is on the device (ntiles_dev); max_tiles and
+// hist_entries bound it and its counts (the grids and the scan cover them:
+// counts past the list's only shift prefixes past its keys). Returns whether
+// the result is in kbuf.
+bool radix_sort_segments(tt_ctx* c, u64* keys, u64* kbuf, const u64* seg_off, const SegTile* tl,
+                         const u32* ntiles_dev, u32 max_tiles, u64 hist_entries, int bits, int lo_bit) {
+    const u32 ntiles = max_tiles;
+    if (ntiles == 0 || bits <= 0) return false;
+    u32* hist = c->arena.get<u32>(S_SORT_HIST, hist_entries + 1);
+    u64 *ka = keys, *kb = kbuf;
+    bool swapped = false;
+    const int passes = (bits + RS_LBITS - 1) / RS_LBITS;
+    int shift = lo_bit;
+    const SegTiles tm{tl, seg_off, ntiles_dev};
+    for (int q = 0; q < passes; ++q) {
+        const int width = (lo_bit + bits - shift + (passes - q) - 1) / (passes - q);
+        k_rs_upsweep<RS_LBINS><<<ntiles, RS_THREADS, 0, c->stream>>>(ka, tm, shift, u32(width), hist);
+        TT_LAUNCH("k_rs_upsweep");
+        scan_exclusive<u32>(c, hist, hist, hist_entries, nullptr, 0);
+        k_rs_scatter_local<u32, false><<<ntiles, RS_THREADS, 0, c->stream>>>(ka, kb, nullptr, nullptr, tm, shift,
+                                                                              u32(width), hist);
+        TT_LAUNCH("k_rs_scatter");
+        c->launches += 2;
+        std::swap(ka, kb);
+        swapped = !swapped;
+        shift += width;
+    }
+    return swapped;
+}
+
 // Sort keys in place (result always back in `keys`, payload in `vals`).
 template <typename V>
 void radix_sort_inplace(tt_ctx* c, u64* keys, V* vals, u64 n, int force_bits) {
@@ -480,10 +562,11 @@ void radix_sort_inplace(tt_ctx* c, u64* keys, V* vals, u64 n, int force_bits) {
 
 // Every scratch slot radix_sort of n keys may grow (for callers that record
 // their work into a CUDA graph, where no allocation may happen).
-void radix_reserve(tt_ctx* c, u64 n) {
-    const u64 tiles = div_up(n, RS_TILE);
-    c->arena.get<u32>(S_SORT_HIST, tiles * RS_BINS + 1);
-    u64 e = tiles * RS_BINS;   // histogram entries, scanned level by level
+void radix_reserve(tt_ctx* c, u64 n) { radix_reserve_entries(c, div_up(n, RS_TILE) * RS_BINS); }
+
+void radix_reserve_entries(tt_ctx* c, u64 entries) {
+    c->arena.get<u32>(S_SORT_HIST, entries + 1);
+    u64 e = entries;   // histogram entries, scanned level by level
     const int slots[3] = {S_SCAN, S_SCAN2, S_SCAN3};
     for (int d = 0; d < 3 && e > u64(SCAN_TILE); ++d) {
         const u64 t = (e + SCAN_TILE - 1) / SCAN_TILE;
