@@ -519,7 +519,7 @@ def batch_block(ctx, dev, reps: int = 5) -> dict:
     ctx.check(ctx.L.tt_batch_tuning(b.h, C.byref(tr), C.byref(tc_), tms, C.byref(ns), C.byref(fc)))
     tuning = {"tile": [tr.value, tc_.value], "from_cache": bool(fc.value),
               "candidates_ms": {"x".join(map(str, s)): round(tms[i], 4)
-                                for i, s in enumerate([(16, 64), (32, 64), (64, 64), (32, 128), (64, 128)][:ns.value])}}
+                                for i, s in enumerate([(32, 32), (64, 64), (96, 96)][:ns.value])}}
     bs = torch.cuda.ExternalStream(out.stream, device=dev)
     ms = []
     for _ in range(reps):

@@ -31,91 +31,45 @@
 #include <string>
 #include <vector>
 
-#include "tt_internal.cuh"
-#include "tt_metric.cuh"
+#include "tt_dense_tile.cuh"
 
 namespace tt {
 
 namespace {
 
-// Distance tiles of BT_R rows x BT_C columns, 256 threads (BT_C x 256 / BT_C);
-// the shape is picked per batch by the autotuner below.
-constexpr int BT_THREADS = 256;
+// Square distance tiles of T x T on and above each cloud's diagonal, 256
+// threads (tt_dense_tile.cuh: each computed once, an off-diagonal tile
+// written twice, row maxima folded); T is picked per batch by the autotuner
+// below.
+constexpr int BT_THREADS = 32 * dtile::kWarps;
 struct TileShape {
     int r, c;
 };
-constexpr TileShape kShapes[] = {{16, 64}, {32, 64}, {64, 64}, {32, 128}, {64, 128}};
+constexpr TileShape kShapes[] = {{32, 32}, {64, 64}, {96, 96}};
 constexpr int kNumShapes = int(sizeof(kShapes) / sizeof(kShapes[0]));
 
 struct Tile {
     u32 cloud, i0, j0;
 };
 
-// A point's coordinates held in registers (compile-time dimension).
-template <int DIM>
-struct Regs {
-    const f32 (&v)[DIM];
-    __device__ __forceinline__ f32 operator()(u32 k) const { return v[k]; }
-};
-
-// DIM > 0: the dimension at compile time (each thread keeps its column's
-// point in registers); 0: any dimension, read from memory.
-template <int KIND, int BT_R, int BT_C, int DIM>
+// Persistent CTAs pull tiles of every cloud from one work list (uneven
+// clouds balance themselves). DIM > 0: the dimension at compile time; 0: any.
+template <int KIND, int T, int DIM>
 __global__ void __launch_bounds__(BT_THREADS)
 k_batch_dense(const f32* __restrict__ x, const u64* __restrict__ pt_off, const u64* __restrict__ mat_off,
               const u32* __restrict__ sizes, const Tile* __restrict__ tiles, u32 ntiles, u32 dim, f32 p,
               f32* __restrict__ mats, u32* __restrict__ rowmax, u32* __restrict__ next) {
-    constexpr int BT_Y = BT_THREADS / BT_C;
-    static_assert(BT_C % 32 == 0 && BT_R <= BT_THREADS, "warps span whole tile rows");
-    // The matrix is symmetric bit for bit and the tiles cover both triangles,
-    // so the row maxima are also the column maxima: each thread folds the
-    // maximum of its column over its rows, one shared atomic a thread and one
-    // global atomic a column per tile.
-    __shared__ u32 cmax[BT_C];
+    __shared__ dtile::Smem<T> sm;
     __shared__ u32 tile_id;
-    const u32 tx = threadIdx.x, ty = threadIdx.y, tid = ty * BT_C + tx;
     for (;;) {
-        if (tid == 0) tile_id = atomicAdd(next, 1u);
-        if (tid < BT_C) cmax[tid] = 0u;
+        if (threadIdx.x == 0) tile_id = atomicAdd(next, 1u);
         __syncthreads();
-        const u32 t = tile_id;
+        const u32 t = tile_id;   // read before sym_tile's first barrier; rewritten after its last
         if (t >= ntiles) break;
         const Tile tl = tiles[t];
-        const u32 n = sizes[tl.cloud];
-        const f32* xc = x + pt_off[tl.cloud] * dim;
-        f32* mc = mats + mat_off[tl.cloud];
-        const u32 j = tl.j0 + tx;
-        u32 cm = 0;
-        if (j < n) {
-            if constexpr (DIM > 0) {
-                f32 xj[DIM];
-#pragma unroll
-                for (int k = 0; k < DIM; ++k) xj[k] = xc[u64(j) * DIM + k];
-                for (u32 r = ty; r < BT_R; r += BT_Y) {
-                    const u32 i = tl.i0 + r;
-                    if (i >= n) break;
-                    f32 xi[DIM];
-#pragma unroll
-                    for (int k = 0; k < DIM; ++k) xi[k] = xc[u64(i) * DIM + k];
-                    const f32 d = (i == j) ? 0.0f : metric_dist(KIND, p, Regs<DIM>{xi}, Regs<DIM>{xj}, DIM);
-                    mc[u64(i) * n + j] = d;
-                    cm = max(cm, __float_as_uint(d));
-                }
-            } else {
-                for (u32 r = ty; r < BT_R; r += BT_Y) {
-                    const u32 i = tl.i0 + r;
-                    if (i >= n) break;
-                    const f32 d =
-                        (i == j) ? 0.0f : metric_dist(KIND, p, Row{xc + u64(i) * dim}, Row{xc + u64(j) * dim}, dim);
-                    mc[u64(i) * n + j] = d;
-                    cm = max(cm, __float_as_uint(d));
-                }
-            }
-            atomicMax(&cmax[tx], cm);
-        }
-        __syncthreads();
-        if (tid < BT_C && tl.j0 + tid < n) atomicMax(&rowmax[pt_off[tl.cloud] + tl.j0 + tid], cmax[tid]);
-        __syncthreads();
+        const u64 po = pt_off[tl.cloud];
+        dtile::sym_tile<KIND, DIM, false, T>(x + po * dim, sizes[tl.cloud], dim, p, mats + mat_off[tl.cloud],
+                                             rowmax + po, tl.i0, tl.j0, sm);
     }
 }
 
@@ -316,32 +270,29 @@ struct Batch {
         return static_cast<T*>(p);
     }
 
-    template <int R, int C, int D>
-    void launch_dense_kd(u32 grid, dim3 blk, u32 nt, const Tile* tl, cudaStream_t s) {
+    template <int T, int D>
+    void launch_dense_kd(u32 grid, u32 nt, const Tile* tl, cudaStream_t s) {
         switch (kind) {
-            case M_L1: k_batch_dense<M_L1, R, C, D><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
-            case M_L2: k_batch_dense<M_L2, R, C, D><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
-            case M_LINF: k_batch_dense<M_LINF, R, C, D><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
-            default: k_batch_dense<M_LP, R, C, D><<<grid, blk, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            case M_L1: k_batch_dense<M_L1, T, D><<<grid, BT_THREADS, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            case M_L2: k_batch_dense<M_L2, T, D><<<grid, BT_THREADS, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            case M_LINF: k_batch_dense<M_LINF, T, D><<<grid, BT_THREADS, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
+            default: k_batch_dense<M_LP, T, D><<<grid, BT_THREADS, 0, s>>>(x, pt_off, mat_off, sizes, tl, nt, dim, p, mats, rowmax, next); break;
         }
     }
-    template <int R, int C>
-    void launch_dense_rc(int si, cudaStream_t s) {
-        const dim3 blk(C, BT_THREADS / C);
+    template <int T>
+    void launch_dense_t(int si, cudaStream_t s) {
         const u32 nt = ntiles[si];
-        const u32 grid = u32(std::min<u64>(nt, u64(owner->sms) * 8));
+        const u32 grid = u32(std::max<u64>(1, std::min<u64>(nt, u64(owner->sms) * 8)));
         const Tile* tl = tiles[si];
-        if (dim == 3) launch_dense_kd<R, C, 3>(grid, blk, nt, tl, s);
-        else launch_dense_kd<R, C, 0>(grid, blk, nt, tl, s);
+        if (dim == 3) launch_dense_kd<T, 3>(grid, nt, tl, s);
+        else launch_dense_kd<T, 0>(grid, nt, tl, s);
         TT_LAUNCH("k_batch_dense");
     }
     void launch_dense(int si, cudaStream_t s) {
         switch (si) {
-            case 0: launch_dense_rc<16, 64>(si, s); break;
-            case 1: launch_dense_rc<32, 64>(si, s); break;
-            case 2: launch_dense_rc<64, 64>(si, s); break;
-            case 3: launch_dense_rc<32, 128>(si, s); break;
-            default: launch_dense_rc<64, 128>(si, s); break;
+            case 0: launch_dense_t<32>(si, s); break;
+            case 1: launch_dense_t<64>(si, s); break;
+            default: launch_dense_t<96>(si, s); break;
         }
     }
 
@@ -472,9 +423,9 @@ Batch* batch_create(tt_ctx* c, const u32* sizes_h, u32 clouds, u32 dim, int kind
             mat_off[q + 1] = mat_off[q] + u64(n) * n;
             pairs += u64(n) * (n - 1) / 2;
             pair_off[q + 1] = pairs;
-            for (int si = 0; si < kNumShapes; ++si)
+            for (int si = 0; si < kNumShapes; ++si)   // the tiles on and above the diagonal
                 for (u32 i0 = 0; i0 < n; i0 += u32(kShapes[si].r))
-                    for (u32 j0 = 0; j0 < n; j0 += u32(kShapes[si].c)) tiles[si].push_back(Tile{q, i0, j0});
+                    for (u32 j0 = i0; j0 < n; j0 += u32(kShapes[si].c)) tiles[si].push_back(Tile{q, i0, j0});
             for (u32 i = 0; i < n; ++i) row_cloud.push_back(q);
         }
         // the segmented sort's capacity: every cloud's largest key count

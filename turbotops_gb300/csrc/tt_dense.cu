@@ -7,141 +7,22 @@
 // integer atomicMax on the float bits (monotone for non-negative floats).
 // The enclosing radius is the minimum of the row maxima.
 //
-// Symmetry: d(i, j) and d(j, i) are the same bits ((a - b) and (b - a) differ
-// only in sign), so only the tiles on and above the diagonal are computed,
-// and an off-diagonal tile is written twice: directly, and transposed through
-// shared memory, both times in 256-byte row segments. That halves the
-// distance arithmetic (a square root per entry for L2), which bounded the
-// all-entries form on instruction issue.
-// Tiling: a CTA of 8 warps owns a 64 x 64 tile (rows i0.., columns j0..,
-// i0 <= j0). Lane l of every warp holds the points of columns j0 + l and
-// j0 + l + 32 in registers (compile-time dimension) and warp w walks rows w,
-// w + 8, ...: the lanes of a warp read the same row point (broadcast loads,
-// 16 bytes at a time when the rows allow). Row maxima: the direct pass folds
-// each column's maximum over the tile's rows (rowmax of the column's point,
-// by symmetry), the transposed pass each row's maximum over the tile's
-// columns; one shared atomic a thread and one global atomic a row or column
-// a tile, no cross-lane reduction per entry. A tile on the diagonal covers
-// both triangles of its block, so its column maxima are its row maxima.
-#include "tt_internal.cuh"
-#include "tt_metric.cuh"
+// Tiling: the 64 x 64 tiles on and above the diagonal (tt_dense_tile.cuh:
+// each computed once, an off-diagonal tile written twice).
+#include "tt_dense_tile.cuh"
 
 namespace tt {
 
 namespace {
 
-constexpr int DN_T = 64, DN_WARPS = 8;
+constexpr int DN_T = 64;
 
-// The point of row i (DIM coordinates, 16-byte loads when VEC).
-template <int DIM, bool VEC>
-__device__ __forceinline__ void load_point(const f32* __restrict__ x, u64 i, f32 (&v)[DIM]) {
-    if constexpr (VEC) {
-        const float4* r = reinterpret_cast<const float4*>(x + i * DIM);
-#pragma unroll
-        for (int k = 0; k < DIM / 4; ++k) {
-            const float4 t = __ldg(r + k);
-            v[4 * k] = t.x, v[4 * k + 1] = t.y, v[4 * k + 2] = t.z, v[4 * k + 3] = t.w;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < DIM; ++k) v[k] = __ldg(x + i * DIM + k);
-    }
-}
-
-template <int DIM>
-struct Regs {
-    const f32 (&v)[DIM];
-    __device__ __forceinline__ f32 operator()(u32 k) const { return v[k]; }
-};
-
-// DIM > 0: the dimension at compile time; 0: any dimension, read from memory.
 template <int KIND, int DIM, bool VEC>
-__global__ void __launch_bounds__(32 * DN_WARPS)
+__global__ void __launch_bounds__(32 * dtile::kWarps)
 k_dense(const f32* __restrict__ x, u32 n, u32 dim, f32 p, f32* __restrict__ mat, u32* __restrict__ rowmax) {
     if (blockIdx.y > blockIdx.x) return;   // below the diagonal: written by the mirror tile
-    __shared__ f32 tile[DN_T][DN_T + 1];
-    __shared__ u32 cmax[DN_T], rmax[DN_T];
-    const u32 i0 = blockIdx.y * DN_T, j0 = blockIdx.x * DN_T;
-    const bool diag = i0 == j0;
-    const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x < DN_T) cmax[threadIdx.x] = rmax[threadIdx.x] = 0u;
-    __syncthreads();
-    const u32 rows = min(u32(DN_T), n - i0), cols = min(u32(DN_T), n - j0);
-    u32 cm[2] = {0u, 0u};
-    if constexpr (DIM > 0) {
-        f32 xj[2][DIM];
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            const u32 cc = lane + 32 * c;
-            if (cc < cols) load_point<DIM, VEC>(x, j0 + cc, xj[c]);
-            else {
-#pragma unroll
-                for (int k = 0; k < DIM; ++k) xj[c][k] = 0.0f;
-            }
-        }
-#pragma unroll 2
-        for (u32 r = w; r < rows; r += DN_WARPS) {
-            const u32 i = i0 + r;
-            f32 xi[DIM];
-            load_point<DIM, VEC>(x, i, xi);
-            f32* row = mat + u64(i) * n + j0;
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                const u32 cc = lane + 32 * c;
-                if (cc < cols) {
-                    const f32 d = (i == j0 + cc) ? 0.0f : metric_dist(KIND, p, Regs<DIM>{xi}, Regs<DIM>{xj[c]}, DIM);
-                    row[cc] = d;
-                    tile[r][cc] = d;
-                    cm[c] = max(cm[c], __float_as_uint(d));
-                }
-            }
-        }
-    } else {
-        for (u32 r = w; r < rows; r += DN_WARPS) {
-            const u32 i = i0 + r;
-            f32* row = mat + u64(i) * n + j0;
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                const u32 cc = lane + 32 * c;
-                if (cc < cols) {
-                    const f32 d = (i == j0 + cc) ? 0.0f
-                                                 : metric_dist(KIND, p, Row{x + u64(i) * dim},
-                                                               Row{x + u64(j0 + cc) * dim}, dim);
-                    row[cc] = d;
-                    tile[r][cc] = d;
-                    cm[c] = max(cm[c], __float_as_uint(d));
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int c = 0; c < 2; ++c)
-        if (lane + 32 * c < cols) atomicMax(&cmax[lane + 32 * c], cm[c]);
-    __syncthreads();
-    if (!diag) {
-        // the transpose: entry (r, c) to (j0 + c, i0 + r), lanes along r
-        u32 rm[2] = {0u, 0u};
-        for (u32 c = w; c < cols; c += DN_WARPS) {
-            f32* row = mat + u64(j0 + c) * n + i0;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const u32 r = lane + 32 * h;
-                if (r < rows) {
-                    const f32 d = tile[r][c];
-                    row[r] = d;
-                    rm[h] = max(rm[h], __float_as_uint(d));
-                }
-            }
-        }
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-            if (lane + 32 * h < rows) atomicMax(&rmax[lane + 32 * h], rm[h]);
-        __syncthreads();
-    }
-    if (rowmax && threadIdx.x < DN_T) {
-        if (threadIdx.x < cols) atomicMax(&rowmax[j0 + threadIdx.x], cmax[threadIdx.x]);
-        if (!diag && threadIdx.x < rows) atomicMax(&rowmax[i0 + threadIdx.x], rmax[threadIdx.x]);
-    }
+    __shared__ dtile::Smem<DN_T> sm;
+    dtile::sym_tile<KIND, DIM, VEC, DN_T>(x, n, dim, p, mat, rowmax, blockIdx.y * DN_T, blockIdx.x * DN_T, sm);
 }
 
 template <int KIND, int DIM>
@@ -150,9 +31,9 @@ void launch_dk(u32 n, cudaStream_t s, const f32* x, u32 dim, f32 p, f32* mat, u3
     const dim3 grid(nb, nb);
     constexpr bool kVec = DIM > 0 && DIM % 4 == 0;   // rows of whole 16-byte groups
     if (kVec && (reinterpret_cast<uintptr_t>(x) & 15) == 0)
-        k_dense<KIND, DIM, kVec><<<grid, 32 * DN_WARPS, 0, s>>>(x, n, dim, p, mat, rowmax);
+        k_dense<KIND, DIM, kVec><<<grid, 32 * dtile::kWarps, 0, s>>>(x, n, dim, p, mat, rowmax);
     else
-        k_dense<KIND, DIM, false><<<grid, 32 * DN_WARPS, 0, s>>>(x, n, dim, p, mat, rowmax);
+        k_dense<KIND, DIM, false><<<grid, 32 * dtile::kWarps, 0, s>>>(x, n, dim, p, mat, rowmax);
 }
 
 // (Lp indexes the coordinates at run time: above four dimensions its register
