@@ -166,13 +166,27 @@ k_rs_upsweep(const u64* __restrict__ keys, TM tm, int shift, u32 width, u32* __r
     // atomic a thread instead of one a key on a single counter.
     const u64 base = tlo + u64(threadIdx.x) * RS_ITEMS;
     u64 kv[RS_ITEMS];
-    if (base + RS_ITEMS <= n && (reinterpret_cast<uintptr_t>(keys + base) & 15) == 0) {   // 16-byte loads
+    const bool aligned = (reinterpret_cast<uintptr_t>(keys + base) & 15) == 0;
+    if (base + RS_ITEMS <= n && aligned) {   // 16-byte loads
         const ulonglong2* p = reinterpret_cast<const ulonglong2*>(keys + base);
 #pragma unroll
         for (int i = 0; i < RS_ITEMS / 2; ++i) {
             const ulonglong2 v = p[i];
             kv[2 * i] = v.x;
             kv[2 * i + 1] = v.y;
+        }
+    } else if (base + RS_ITEMS + 1 <= n && base > tlo) {
+        // a run starting 8 bytes past a 16-byte boundary (a segment may
+        // start anywhere): the aligned pairs from the key before it, which
+        // belongs to the previous thread's run and is dropped
+        const ulonglong2* p = reinterpret_cast<const ulonglong2*>(keys + base - 1);
+        u64 prev = p[0].y;
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS / 2; ++i) {
+            const ulonglong2 v = p[i + 1];
+            kv[2 * i] = prev;
+            kv[2 * i + 1] = v.x;
+            prev = v.y;
         }
     } else {
 #pragma unroll
