@@ -140,3 +140,27 @@ def test_knn_front_h_above_packed_key_range_vs_oracle():
     e = O.emergent(csr=csr, n=n, cidx=o["cidx"], cd=o["cd"])
     assert np.array_equal(r["cf"], e["emi"])
     assert np.array_equal(r["ca"], e["emf"])
+
+
+@pytest.mark.parametrize("n,bad", [(3000, math.nan), (6000, math.inf)])
+def test_device_entries_reject_non_finite(n, bad):
+    """The device-pointer entry points that index by kNN list entries check
+    the points on the device, read before the first such kernel: a
+    non-finite coordinate is the reference's invalid-argument error (never a
+    short list read past its end), and the context keeps working."""
+    x = np.ascontiguousarray(synth.gmm(n, 32, 6, n), np.float32)
+    bad_x = x.copy()
+    bad_x[n // 2, 7] = bad
+    c = ctx()
+    kind, p = capi.metric_parse("l2")
+    for run in (lambda: ops.knn_graph(c, dev(bad_x), 15, "l2"), lambda: ops.mst_deaths(c, dev(bad_x), "l2")):
+        with pytest.raises(ValueError, match="non-finite coordinate"):
+            run()
+    xd = dev(bad_x)
+    out = capi.KnnFrontOut()
+    assert c.L.tt_knn_front(c.h, xd.data_ptr(), n, 32, kind, p, 15, 1, C.byref(out)) == capi.ERR_INVALID
+    assert "non-finite coordinate" in c.L.tt_last_error(c.h).decode()
+    d = ops.mst_deaths(c, dev(x), "l2")
+    assert np.array_equal(host(d).view(np.uint32), np.sort(host(d)).view(np.uint32))
+    rp, ci, w = ops.knn_graph(c, dev(x), 15, "l2")
+    assert host(rp).view(np.uint64)[-1] == ci.numel()

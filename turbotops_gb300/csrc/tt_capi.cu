@@ -56,6 +56,26 @@ __global__ void k_nonfinite(const f32* __restrict__ x, u64 count, u32* __restric
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
 }
 
+// The same test storing 1 into a flag when some coordinate is not finite
+// (every writer stores the same value), four floats a load when aligned.
+__global__ void k_nonfinite_store(const f32* __restrict__ x, u64 count, unsigned* flag) {
+    u32 bad = 0;
+    const u64 stride = u64(gridDim.x) * blockDim.x;
+    const u64 t0 = u64(blockIdx.x) * blockDim.x + threadIdx.x;
+    u64 head = 0;   // floats before the first 16-byte boundary
+    if ((reinterpret_cast<uintptr_t>(x) & 15) != 0) head = min(count, u64((16 - (reinterpret_cast<uintptr_t>(x) & 15)) / 4));
+    for (u64 i = t0; i < head; i += stride) bad |= (__float_as_uint(x[i]) & 0x7f800000u) == 0x7f800000u;
+    const float4* v = reinterpret_cast<const float4*>(x + head);
+    const u64 nv = (count - head) / 4;
+    for (u64 i = t0; i < nv; i += stride) {
+        const float4 f = __ldg(v + i);
+        bad |= ((__float_as_uint(f.x) & 0x7f800000u) == 0x7f800000u) | ((__float_as_uint(f.y) & 0x7f800000u) == 0x7f800000u) |
+               ((__float_as_uint(f.z) & 0x7f800000u) == 0x7f800000u) | ((__float_as_uint(f.w) & 0x7f800000u) == 0x7f800000u);
+    }
+    for (u64 i = head + nv * 4 + t0; i < count; i += stride) bad |= (__float_as_uint(x[i]) & 0x7f800000u) == 0x7f800000u;
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *reinterpret_cast<volatile unsigned*>(flag) = 1u;
+}
+
 void check_finite_dev(tt_ctx* c, const f32* x, u64 count) {
     if (!count) return;
     u32* flag = c->arena.get<u32>(S_MISC2, 4);
@@ -80,15 +100,19 @@ namespace tt {
 void check_finite_async(tt_ctx* c, const f32* x, u64 count) {
     c->fin_pending = false;
     if (!count) return;
-    if (!c->fin_host) TT_CUDA(cudaMallocHost(&c->fin_host, sizeof(unsigned)));
+    if (!c->fin_host) {
+        TT_CUDA(cudaHostAlloc(&c->fin_host, sizeof(unsigned), cudaHostAllocMapped));
+        TT_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&c->fin_dev), c->fin_host, 0));
+    }
     if (!c->fin_ev) TT_CUDA(cudaEventCreateWithFlags(&c->fin_ev, cudaEventDisableTiming));
-    u32* flag = c->arena.get<u32>(S_MISC2, 4);
-    TT_CUDA(cudaMemsetAsync(flag, 0, sizeof(u32), c->stream));
-    const u32 grid = u32(std::min<u64>((count + 255) / 256, 4ull * u64(c->sms)));
-    k_nonfinite<<<grid, 256, 0, c->stream>>>(x, count, flag);
+    // the flag lives in mapped page-locked memory: the kernel stores into it
+    // directly, so nothing but the kernel itself sits in the stream (the
+    // previous call's kernel has completed: its event was waited for)
+    *reinterpret_cast<volatile unsigned*>(c->fin_host) = 0u;
+    const u32 grid = u32(std::min<u64>((count + 1023) / 1024, 4ull * u64(c->sms)));
+    k_nonfinite_store<<<grid, 256, 0, c->stream>>>(x, count, c->fin_dev);
     TT_LAUNCH("k_nonfinite");
     ++c->launches;
-    TT_CUDA(cudaMemcpyAsync(c->fin_host, flag, sizeof(u32), cudaMemcpyDeviceToHost, c->stream));
     TT_CUDA(cudaEventRecord(c->fin_ev, c->stream));
     c->fin_pending = true;
 }
@@ -389,6 +413,8 @@ int tt_knn_graph(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, 
         u64* rp = c->arena.get<u64>(S_OUT0, u64(n) + 1);
         u32* ci = nullptr;
         f32* w = nullptr;
+        // a NaN leaves a list short: the graph build reads the check first
+        check_finite_async(c, x, u64(n) * dim);
         const u64 nnz = knn_graph(c, x, n, dim, kind, p, nullptr, kk, rp, &ci, &w);
         out->n = n;
         out->nnz = nnz;
@@ -419,7 +445,9 @@ int tt_radius_graph(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kin
 int tt_mst_deaths(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, float p, float* deaths) {
     return guard(c, [&] {
         check_metric(kind, p);
+        check_finite_async(c, x, u64(n) * dim);   // read before the rounds index anything by a list entry
         mst_deaths(c, x, n, dim, kind, p, deaths);
+        settle_finite(c);
     });
 }
 
@@ -477,6 +505,7 @@ int tt_knn_front(tt_ctx* c, const float* x, uint32_t n, uint32_t dim, int kind, 
         if (k == 0) invalid("persistence: k must be >= 1");
         if (!out) invalid("gb300: null output");
         if (n > kPackedMaxN) invalid("gb300: tt_knn_front's packed edge keys support n <= 131072 vertices");
+        check_finite_async(c, x, u64(n) * dim);   // read by the graph build (a NaN leaves a list short)
         u64* rp = nullptr;
         u32* ci = nullptr;
         f32* w = nullptr;

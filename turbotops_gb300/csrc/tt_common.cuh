@@ -162,7 +162,8 @@ struct tt_ctx {
     cudaEvent_t aux_ev = nullptr;
     unsigned long long* tc_host = nullptr;   // page-locked: the tensor-core kNN's error word and counters
     bool tc_pending = false;                 // ... copied there, not yet read (deferred to a later sync)
-    unsigned* fin_host = nullptr;   // page-locked: the points' non-finite flag (check_finite_async)
+    unsigned* fin_host = nullptr;   // mapped page-locked: the points' non-finite flag (check_finite_async)
+    unsigned* fin_dev = nullptr;    // ... its device address
     cudaEvent_t fin_ev = nullptr;   // ... its copy recorded
     bool fin_pending = false;       // ... not yet read
     cudaStream_t side = nullptr;    // kernels overlapped with the main stream's (created on first use)

@@ -154,6 +154,7 @@ u64 mst_deaths(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, f32* de
         kid = c->arena.get<u32>(S_KNN_I, u64(n) * K + 1);
         kd = c->arena.get<f32>(S_KNN_D, u64(n) * K + 1);
         knn_exact(c, x, n, dim, kind, p, K, kid, kd, false);
+        settle_finite(c);   // a pending check of the points: a NaN leaves a list short
     }
     u32* kb = lists ? c->arena.get<u32>(S_MST_KB, n + 1) : nullptr;
     u32* qlist = lists ? c->arena.get<u32>(S_MST_Q, n + 2) : nullptr;
