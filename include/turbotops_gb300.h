@@ -164,7 +164,9 @@ typedef struct tt_csr_out {
 } tt_csr_out;
 
 /* knn_lists_exact + knn_graph (graph.hpp:211-225, :286-304): the symmetric
- * kNN graph, rows sorted by neighbour id, weights d(i, j). */
+ * kNN graph, rows sorted by neighbour id, weights d(i, j). A non-finite
+ * coordinate is TT_ERR_INVALID ("persistence: non-finite coordinate"), as
+ * for PointCloud; it is checked on the device. */
 int tt_knn_graph(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
                  tt_csr_out* out);
 
@@ -175,7 +177,7 @@ int tt_radius_graph(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, i
 /* mst::h0 (mst.hpp:25-99): the n - 1 minimum-spanning-tree weights of the
  * complete graph, ascending, into deaths_dev (capacity n). The reference's
  * bars follow: deaths > threshold add essential classes, deaths > 0 are
- * finite bars. */
+ * finite bars. Non-finite coordinates: TT_ERR_INVALID, as tt_knn_graph. */
 int tt_mst_deaths(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, float* deaths_dev);
 
 /* Host-buffer form of tt_knn_graph (what the reference's
@@ -198,7 +200,8 @@ typedef struct tt_knn_front_out {
 
 /* knn_lists_exact -> knn_graph -> Reducer::dim0 of rips::compute_graph
  * (turbotops.hpp:260-298, threshold +inf), all on the device. n <= 131072
- * (packed edge keys, as tt_dim0); tt_knn_front_h takes any n. */
+ * (packed edge keys, as tt_dim0); tt_knn_front_h takes any n. Non-finite
+ * coordinates: TT_ERR_INVALID, as tt_knn_graph. */
 int tt_knn_front(tt_ctx* ctx, const float* x_dev, uint32_t n, uint32_t dim, int kind, float p, uint32_t k,
                  uint32_t maxdim, tt_knn_front_out* out);
 
