@@ -94,6 +94,8 @@ struct CsrRows {
 // bit range, known with the count).
 template <typename Rows>
 __global__ void k_edge_count(Rows rows, u32 n, f32 thr, u64* __restrict__ cnt, u32* __restrict__ dmm) {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
     u32 lo = 0xffffffffu, hi = 0;
@@ -145,6 +147,8 @@ __global__ void k_edge_count(Rows rows, u32 n, f32 thr, u64* __restrict__ cnt, u
 template <typename Rows>
 __global__ void k_edge_fill(Rows rows, u32 n, f32 thr, const u64* __restrict__ off, u64 m, int redzed,
                             u64* __restrict__ skey, u64* __restrict__ sidx, u32* __restrict__ err) {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
     for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
@@ -180,6 +184,8 @@ __global__ void k_edge_fill(Rows rows, u32 n, f32 thr, const u64* __restrict__ o
 // the edge that index order puts at q.
 __global__ void k_edge_pack(const u64* __restrict__ skey, const u64* __restrict__ sidx, u64 m, int redzed, int wide,
                             u64* __restrict__ keys, u32* __restrict__ inv) {
+    pdl_wait();
+    pdl_trigger();
     for (u64 r = u64(blockIdx.x) * blockDim.x + threadIdx.x; r < m; r += u64(gridDim.x) * blockDim.x) {
         const u64 k = skey[r];
         if (wide) {
@@ -194,6 +200,8 @@ __global__ void k_edge_pack(const u64* __restrict__ skey, const u64* __restrict_
 
 __global__ void k_apparent_dense(const f32* __restrict__ mat, u32 n, const u64* __restrict__ keys, EdgeFmt fmt, u64 m,
                                  u8* __restrict__ app, u32* __restrict__ emw, u8* __restrict__ emf) {
+    pdl_wait();
+    pdl_trigger();
     const DenseCx cx{mat, n};
     const int lane = threadIdx.x & 31;
     const u64 warps = (u64(gridDim.x) * blockDim.x) >> 5;
@@ -268,6 +276,8 @@ struct CsrCx {
 __global__ void __launch_bounds__(256, 8)
     k_apparent_csr(CsrCx cx, const u64* __restrict__ keys, EdgeFmt fmt, const u32* __restrict__ inv, u64 m,
                    u8* __restrict__ app, u32* __restrict__ emw, u8* __restrict__ emf) {
+    pdl_wait();
+    pdl_trigger();
     for (u64 t = u64(blockIdx.x) * blockDim.x + threadIdx.x; t < m; t += u64(gridDim.x) * blockDim.x) {
         const u64 e = inv[t];
         const u64 key = keys[e];
@@ -312,6 +322,8 @@ __global__ void __launch_bounds__(256, 8)
 // Borůvka over edge ranks (rank = position in the sorted array).
 // --------------------------------------------------------------------------
 __global__ void k_iota(u32* __restrict__ p, u32 n) {
+    pdl_wait();
+    pdl_trigger();
     for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) p[v] = v;
 }
 
@@ -323,6 +335,8 @@ __global__ void k_iota(u32* __restrict__ p, u32 n) {
 __global__ void k_bv_offer(const u64* __restrict__ keys, EdgeFmt fmt, const u32* __restrict__ live,
                            const u32* __restrict__ nlive_in, u32 m, const u32* __restrict__ comp,
                            u32* __restrict__ best, u32* __restrict__ live_out, u32* __restrict__ nlive_out) {
+    pdl_wait();
+    pdl_trigger();
     const u32 lane = threadIdx.x & 31;
     const bool all = nlive_in == nullptr;
     const u32 nlive = all ? m : *nlive_in;
@@ -358,6 +372,8 @@ __global__ void k_bv_hook(const u64* __restrict__ keys, EdgeFmt fmt, const u32* 
                           const u32* __restrict__ best,
                           u32* __restrict__ parent, u8* __restrict__ tree, u32 n, u32* __restrict__ hooks,
                           const u32* __restrict__ live) {
+    pdl_wait();
+    pdl_trigger();
     if (*live == 0) return;
     u32 mine = 0;
     for (u32 c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
@@ -378,6 +394,8 @@ __global__ void k_bv_hook(const u64* __restrict__ keys, EdgeFmt fmt, const u32* 
 
 __global__ void k_bv_flatten(const u32* __restrict__ parent, u32* __restrict__ comp, u32* __restrict__ best, u32 n,
                              const u32* __restrict__ live) {
+    pdl_wait();
+    pdl_trigger();
     if (*live == 0) return;   // no hook this round: parents, components and offers unchanged
     for (u32 v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         u32 r = parent[v];
@@ -394,6 +412,8 @@ __global__ void k_bv_flatten(const u32* __restrict__ parent, u32* __restrict__ c
 // scan counts both without a carry between the halves).
 __global__ void k_flags_dim0(const u64* __restrict__ keys, EdgeFmt fmt, const u8* __restrict__ tree,
                              const u8* __restrict__ app, u64 m, int want_cols, u64* __restrict__ f) {
+    pdl_wait();
+    pdl_trigger();
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
         const bool t = tree[e];
         f[e] = (u64(t && fmt.d(keys[e]) > 0.0f) << 32) | u64(want_cols && !t && !(app && app[e]));
@@ -406,6 +426,8 @@ __global__ void k_emit_dim0(const u64* __restrict__ keys, EdgeFmt fmt, const u8*
                             const u64* __restrict__ o2, const u64* __restrict__ tot,
                             f32* __restrict__ h0, u64* __restrict__ h0_edge, u64* __restrict__ cidx,
                             f32* __restrict__ cd, u64* __restrict__ emi, u8* __restrict__ emf_out) {
+    pdl_wait();
+    pdl_trigger();
     const u64 ncols = tot[0] & 0xffffffffull;
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += u64(gridDim.x) * blockDim.x) {
         const u64 key = keys[e];
@@ -472,9 +494,9 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
         TT_CUDA(cudaMemsetAsync(dmm, 0xff, sizeof(u32), c->stream));
         TT_CUDA(cudaMemsetAsync(dmm + 1, 0, sizeof(u32), c->stream));
         if (cx.mat)
-            k_edge_count<<<g, 256, 0, c->stream>>>(DenseRows{cx.mat, n}, n, cx.thr, off, dmm);
+            launch_pdl(k_edge_count<DenseRows>, g, 256, 0, c->stream, DenseRows{cx.mat, n}, n, cx.thr, off, dmm);
         else
-            k_edge_count<<<g, 256, 0, c->stream>>>(CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off, dmm);
+            launch_pdl(k_edge_count<CsrRows>, g, 256, 0, c->stream, CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off, dmm);
         TT_LAUNCH("k_edge_count");
         ++c->launches;
         scan_exclusive<u64>(c, off, off, n, off + n);
@@ -499,17 +521,18 @@ static u64 sorted_edge_keys(tt_ctx* c, const Complex& cx, int redzed, u64** keys
         u64* skey = c->arena.get<u64>(S_EDGE_SORT, m + 1);
         u64* sidx = c->arena.get<u64>(S_EDGE_IDX, m + 1);
         if (cx.mat)
-            k_edge_fill<<<g, 256, 0, c->stream>>>(DenseRows{cx.mat, n}, n, cx.thr, off, m, redzed, skey, sidx, err);
+            launch_pdl(k_edge_fill<DenseRows>, g, 256, 0, c->stream, DenseRows{cx.mat, n}, n, cx.thr, off, m, redzed, skey,
+                       sidx, err);
         else
-            k_edge_fill<<<g, 256, 0, c->stream>>>(CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off, m, redzed, skey,
-                                                  sidx, err);
+            launch_pdl(k_edge_fill<CsrRows>, g, 256, 0, c->stream, CsrRows{cx.rp, cx.ci, cx.w}, n, cx.thr, off, m, redzed,
+                       skey, sidx, err);
         TT_LAUNCH("k_edge_fill");
         u64* kb = c->arena.get<u64>(S_SORT_A, m);
         // a stable sort on the distance bits that differ (none: already in order)
         const bool sw = dbits > 0 && radix_sort<u32>(c, skey, static_cast<u32*>(nullptr), m, kb,
                                                      static_cast<u32*>(nullptr), dbits, 32);
         u32* inv = c->arena.get<u32>(S_EDGE_INV, m + 1);
-        k_edge_pack<<<grid_for(m, 256), 256, 0, c->stream>>>(sw ? kb : skey, sidx, m, redzed, wide, keys, inv);
+        launch_pdl(k_edge_pack, grid_for(m, 256), 256, 0, c->stream, sw ? kb : skey, sidx, m, redzed, wide, keys, inv);
         if (wide) *eidx_out = sidx;
         TT_LAUNCH("k_edge_pack");
         c->launches += 2;
@@ -544,13 +567,13 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
         u32* inv = c->arena.get<u32>(S_EDGE_INV, m + 1);
         const cudaStream_t s = c->stream;
         if (cx.mat)
-            k_apparent_dense<<<grid_for(m * 32, 256), 256, 0, s>>>(cx.mat, n, out.keys, fmt, m, app, emw, emf);
+            launch_pdl(k_apparent_dense, grid_for(m * 32, 256), 256, 0, s, cx.mat, n, out.keys, fmt, m, app, emw, emf);
         else
             // six of the eight resident blocks an SM: the forest's short
             // kernels then always find free slots instead of waiting for a
             // wave of scan blocks to retire (measured: kNN front end of
             // 100,000 points, dim0 0.04 ms shorter than with all eight)
-            k_apparent_csr<<<std::min<u32>(grid_for(m, 256), 6 * kSMs), 256, 0, s>>>(
+            launch_pdl(k_apparent_csr, std::min<u32>(grid_for(m, 256), 6 * kSMs), 256, 0, s, 
                 CsrCx{cx.rp, cx.ci, cx.w}, out.keys, fmt, inv, m, app, emw, emf);
         TT_LAUNCH("k_apparent");
         ++c->launches;
@@ -567,8 +590,8 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
     u32* ctr = c->arena.get<u32>(S_MISC1, 2 * kRounds);   // per round: live count, hooks
     u64 total_hooks = 0;
     if (n) {
-        k_iota<<<grid_for(n, 256), 256, 0, fs>>>(comp, n);
-        k_iota<<<grid_for(n, 256), 256, 0, fs>>>(parent, n);
+        launch_pdl(k_iota, grid_for(n, 256), 256, 0, fs, comp, n);
+        launch_pdl(k_iota, grid_for(n, 256), 256, 0, fs, parent, n);
         TT_CUDA(cudaMemsetAsync(best, 0xff, sizeof(u32) * n, fs));
         c->launches += 2;
         TT_CUDA(cudaMemsetAsync(ctr, 0, 2 * kRounds * sizeof(u32), fs));
@@ -579,11 +602,11 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
         for (int round = 0; known && round < kRounds;) {
             const int first = round;
             for (int q = 0; q < kPerTrip && round < kRounds; ++q, ++round) {
-                k_bv_offer<<<grid_for(known, 256), 256, 0, fs>>>(
+                launch_pdl(k_bv_offer, grid_for(known, 256), 256, 0, fs, 
                     out.keys, fmt, live0, round ? ctr + 2 * (round - 1) : nullptr, u32(m), comp, best, live1, ctr + 2 * round);
-                k_bv_hook<<<grid_for(n, 256), 256, 0, fs>>>(out.keys, fmt, comp, best, parent, tree, n,
+                launch_pdl(k_bv_hook, grid_for(n, 256), 256, 0, fs, out.keys, fmt, comp, best, parent, tree, n,
                                                            ctr + 2 * round + 1, ctr + 2 * round);
-                k_bv_flatten<<<grid_for(n, 256), 256, 0, fs>>>(parent, comp, best, n, ctr + 2 * round);
+                launch_pdl(k_bv_flatten, grid_for(n, 256), 256, 0, fs, parent, comp, best, n, ctr + 2 * round);
                 TT_LAUNCH("boruvka");
                 c->launches += 3;
                 std::swap(live0, live1);
@@ -605,7 +628,7 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
     u64* o2 = f2 + m + 2;
     u64* tot = c->arena.get<u64>(S_COUNT, 4);
     if (m) {
-        k_flags_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, fmt, tree, out.app, m, want_cols, f2);
+        launch_pdl(k_flags_dim0, grid_for(m, 256), 256, 0, c->stream, out.keys, fmt, tree, out.app, m, want_cols, f2);
         TT_LAUNCH("k_flags_dim0");
         scan_exclusive<u64>(c, f2, o2, m, tot);
         c->launches += 1;
@@ -623,7 +646,7 @@ void dim0(tt_ctx* c, const Complex& cx, u32 maxdim, Dim0Out& out, u64 m_known) {
         out.emf = c->arena.get<u8>(S_OUT4, ncols + 1);
         out.h0_edge = c->arena.get<u64>(S_OUT5, nh0 + 1);
         if (m) {
-            k_emit_dim0<<<grid_for(m, 256), 256, 0, c->stream>>>(out.keys, fmt, tree, out.app, emw, emf, m, want_cols,
+            launch_pdl(k_emit_dim0, grid_for(m, 256), 256, 0, c->stream, out.keys, fmt, tree, out.app, emw, emf, m, want_cols,
                                                                  o2, tot, out.h0, out.h0_edge, out.cidx, out.cd,
                                                                  out.emi, out.emf);
             TT_LAUNCH("k_emit_dim0");

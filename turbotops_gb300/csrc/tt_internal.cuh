@@ -20,6 +20,29 @@ __host__ __device__ inline u64 key_rips(f32 d, u64 idx) {
 constexpr u32 kPackedMaxN = 131072;
 
 // Simplex index helpers (combinatorial number system, rips.hpp:505-580).
+// Programmatic dependent launch: a kernel launched with launch_pdl may start
+// while the previous kernel of its stream finishes; pdl_wait (first thing in
+// such a kernel) waits until that kernel has completed and its writes are
+// visible, and pdl_trigger lets the next one start. Both do nothing in a
+// kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    TT_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...));
+}
+
 __device__ __forceinline__ void decode_edge(u64 idx, u32& a, u32& b) {
     // rips.hpp decode, nv = 2 closed form (:549-557): a > b. The FP32 closed
     // form is within one of the answer for idx < 2^40 (relative error below

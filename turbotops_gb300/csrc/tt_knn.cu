@@ -133,6 +133,8 @@ __device__ __forceinline__ u32 warp_rank_row(const u32* __restrict__ col, const 
 // Row i holds its own list (k entries, slots off[i] .. off[i] + k - 1 in
 // list order) and the entries naming i (after them, atomic cursor).
 __global__ void k_graph_deg(const u32* __restrict__ ids, u32 n, u32 k, unsigned long long* __restrict__ deg) {
+    pdl_wait();
+    pdl_trigger();
     const u64 total = u64(n) * k;
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += u64(gridDim.x) * blockDim.x) {
         if (e % k == 0) atomicAdd(&deg[e / k], (unsigned long long)k);
@@ -143,6 +145,8 @@ __global__ void k_graph_deg(const u32* __restrict__ ids, u32 n, u32 k, unsigned 
 __global__ void k_graph_fill(const u32* __restrict__ ids, const f32* __restrict__ d, u32 n, u32 k,
                              const u64* __restrict__ off, u32* __restrict__ cur, u32* __restrict__ col,
                              f32* __restrict__ w) {
+    pdl_wait();
+    pdl_trigger();
     const u64 total = u64(n) * k;
     for (u64 e = u64(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += u64(gridDim.x) * blockDim.x) {
         const u32 i = u32(e / k), j = ids[e];
@@ -164,6 +168,8 @@ __global__ void k_graph_rowsort(const u64* __restrict__ off, u32 n, const u32* _
                                 const f32* __restrict__ w, u32* __restrict__ scol, f32* __restrict__ sw,
                                 unsigned long long* __restrict__ ucnt, u32* __restrict__ overflow,
                                 u32* __restrict__ longs) {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
     for (u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
@@ -195,6 +201,8 @@ __global__ void __launch_bounds__(kLongThreads) k_graph_rowsort_long(const u64* 
                                                                      const f32* __restrict__ w, u32* __restrict__ scol,
                                                                      f32* __restrict__ sw,
                                                                      unsigned long long* __restrict__ ucnt) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ unsigned long long key[kRowSortMax];
     __shared__ u32 uc;
     const u32 tid = threadIdx.x;
@@ -244,6 +252,8 @@ __global__ void __launch_bounds__(kLongThreads) k_graph_rowsort_long(const u64* 
 __global__ void k_graph_emit(const u64* __restrict__ off, u32 n, const u32* __restrict__ scol,
                              const f32* __restrict__ sw, const u64* __restrict__ rp, u32* __restrict__ ci,
                              f32* __restrict__ wout, const u32* __restrict__ overflow) {
+    pdl_wait();
+    pdl_trigger();
     if (*overflow) return;
     const int lane = threadIdx.x & 31;
     const u32 warps = (gridDim.x * blockDim.x) >> 5;
@@ -281,6 +291,8 @@ namespace {
 // strided pivot points, the pivots' rows staged in shared memory.
 __global__ void k_pivot_cell(const f32* __restrict__ x, u32 n, u32 dim, u32 P, u64* __restrict__ key,
                              u32* __restrict__ val) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ f32 pv[];   // P x dim
     for (u32 t = threadIdx.x; t < P * dim; t += blockDim.x) pv[t] = x[(u64(t / dim) * n / P) * dim + t % dim];
     __syncthreads();
@@ -311,7 +323,7 @@ static const u32* pivot_order(tt_ctx* c, const f32* x, u32 n, u32 dim) {
     const u32 P = std::max<u32>(2, std::min<u32>(128, n / 1536));
     u64* key = c->arena.get<u64>(S_TC_KEYS, n);
     u32* val = c->arena.get<u32>(S_TC_VALS, n);
-    k_pivot_cell<<<std::min<u32>(div_up(n, 256), 8 * u32(c->sms)), 256, sizeof(f32) * P * dim, c->stream>>>(
+    launch_pdl(k_pivot_cell, std::min<u32>(div_up(n, 256), 8 * u32(c->sms)), 256, sizeof(f32) * P * dim, c->stream, 
         x, n, dim, P, key, val);
     TT_LAUNCH("k_pivot_cell");
     ++c->launches;
@@ -362,7 +374,7 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         u32* ovf = cur + n;
         TT_CUDA(cudaMemsetAsync(off, 0, (u64(n) + 1) * sizeof(u64), c->stream));
         TT_CUDA(cudaMemsetAsync(cur, 0, (u64(n) + 1) * sizeof(u32), c->stream));
-        k_graph_deg<<<grid_for(u64(n) * k, 256), 256, 0, c->stream>>>(kid, n, k,
+        launch_pdl(k_graph_deg, grid_for(u64(n) * k, 256), 256, 0, c->stream, kid, n, k,
                                                                         reinterpret_cast<unsigned long long*>(off));
         TT_LAUNCH("k_graph_deg");
         scan_exclusive<u64>(c, off, off, n, off + n);
@@ -370,14 +382,14 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         f32* cw = reinterpret_cast<f32*>(col + m + 1);
         u32* scol = c->arena.get<u32>(S_GRAPH_TMP, 2 * m + 2);
         f32* sw = reinterpret_cast<f32*>(scol + m + 1);
-        k_graph_fill<<<grid_for(u64(n) * k, 256), 256, 0, c->stream>>>(kid, kd, n, k, off, cur, col, cw);
+        launch_pdl(k_graph_fill, grid_for(u64(n) * k, 256), 256, 0, c->stream, kid, kd, n, k, off, cur, col, cw);
         TT_LAUNCH("k_graph_fill");
         u32* longs = c->arena.get<u32>(S_GRAPH_LONG, u64(n) + 1);
         TT_CUDA(cudaMemsetAsync(longs, 0, sizeof(u32), c->stream));
-        k_graph_rowsort<<<gw, 256, 0, c->stream>>>(off, n, col, cw, scol, sw,
+        launch_pdl(k_graph_rowsort, gw, 256, 0, c->stream, off, n, col, cw, scol, sw,
                                                     reinterpret_cast<unsigned long long*>(ucnt), ovf, longs);
         TT_LAUNCH("k_graph_rowsort");
-        k_graph_rowsort_long<<<std::min<u32>(n, 8 * u32(c->sms)), kLongThreads, 0, c->stream>>>(
+        launch_pdl(k_graph_rowsort_long, std::min<u32>(n, 8 * u32(c->sms)), kLongThreads, 0, c->stream, 
             off, longs, col, cw, scol, sw, reinterpret_cast<unsigned long long*>(ucnt));
         TT_LAUNCH("k_graph_rowsort_long");
         c->launches += 4;
@@ -388,7 +400,7 @@ u64 knn_graph(tt_ctx* c, const f32* x, u32 n, u32 dim, int kind, f32 p, const u3
         scan_exclusive<u64>(c, ucnt, rp, n, rp + n);
         u32* ci = c->arena.get<u32>(S_GRAPH_CI, m + 1);
         f32* w = c->arena.get<f32>(S_GRAPH_W, m + 1);
-        k_graph_emit<<<gw, 256, 0, c->stream>>>(off, n, scol, sw, rp, ci, w, ovf);
+        launch_pdl(k_graph_emit, gw, 256, 0, c->stream, off, n, scol, sw, rp, ci, w, ovf);
         TT_LAUNCH("k_graph_emit");
         ++c->launches;
         u32 overflow = 0;

@@ -324,6 +324,8 @@ __device__ __forceinline__ u32 spiral_tile(u32 B, u32 s, u32 ntiles) {
 constexpr int PIV_THREADS = 1024;
 __global__ void __launch_bounds__(PIV_THREADS) k_tc_pivots(const f32* __restrict__ x, u32 n, u32 P,
                                                           f32* __restrict__ piv, u32* __restrict__ rank) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ f32 psm[];
     f32* pv = psm;                       // P x (TC_DIM + 1)
     f32* dm = psm + P * (TC_DIM + 1);    // P x P
@@ -372,6 +374,8 @@ __global__ void __launch_bounds__(PIV_THREADS) k_tc_pivots(const f32* __restrict
 // nearest-pivot choice leaves the lists unchanged).
 __global__ void k_tc_assign(const f32* __restrict__ x, u32 n, const f32* __restrict__ piv, const u32* __restrict__ rank,
                             u32 P, u64* __restrict__ key, u32* __restrict__ val) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ float4 sp4[];      // P x 8 float4, then P norms
     f32* pn = reinterpret_cast<f32*>(sp4 + P * 8);
     for (u32 t = threadIdx.x; t < P * 8; t += blockDim.x) sp4[t] = reinterpret_cast<const float4*>(piv)[t];
@@ -422,6 +426,8 @@ __global__ void k_tc_assign(const f32* __restrict__ x, u32 n, const f32* __restr
 // First position of each cell (chain rank) in the rank-sorted keys; cell P
 // ends the array.
 __global__ void k_tc_cells(const u64* __restrict__ skey, u32 n, u32 P, u32* __restrict__ cell_off) {
+    pdl_wait();
+    pdl_trigger();
     for (u32 p = blockIdx.x * blockDim.x + threadIdx.x; p <= P; p += gridDim.x * blockDim.x) {
         u32 lo = 0, hi = n;
         while (lo < hi) {
@@ -442,6 +448,8 @@ __host__ __device__ __forceinline__ u32 sub_count(u32 s) { return s / 128u < 1u 
 
 __global__ void k_tc_subpiv(const f32* __restrict__ x, const u32* __restrict__ perm, const u32* __restrict__ cell_off,
                             u32 P, f32* __restrict__ spv, f32* __restrict__ spn) {
+    pdl_wait();
+    pdl_trigger();
     const u32 wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (wid >= P * 16) return;
     const u32 cell = wid >> 4, j = wid & 15u;
@@ -459,6 +467,8 @@ __global__ void k_tc_assign2(const f32* __restrict__ x, u32 n, const u64* __rest
                              const u32* __restrict__ perm, const u32* __restrict__ cell_off,
                              const f32* __restrict__ spv, const f32* __restrict__ spn, u64* __restrict__ key2,
                              u32* __restrict__ val2) {
+    pdl_wait();
+    pdl_trigger();
     const u32 r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const u32 cell = u32(skey[r]);
@@ -517,6 +527,8 @@ __global__ void k_tc_assign2(const f32* __restrict__ x, u32 n, const u64* __rest
 __global__ void __launch_bounds__(TC_N) k_tc_tiles(const f32* __restrict__ x, u32 n, const u32* __restrict__ perm,
                                                   f32* __restrict__ xh, unsigned char* __restrict__ pack,
                                                   f32* __restrict__ nq, f32* __restrict__ eq, f32* __restrict__ stats) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ f32 rows[TC_N][TC_DIM + 1];
     __shared__ f32 part[4][TC_DIM];
     __shared__ f32 cent[TC_DIM];
@@ -641,6 +653,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap map, const unsigned char* __restric
          u32 n, u32 k, const f32* __restrict__ nq,
          const f32* __restrict__ stats, u32* __restrict__ ids, f32* __restrict__ dists, u32* __restrict__ next_block,
          u32* __restrict__ err, unsigned long long* __restrict__ counters) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ unsigned char smem_raw[];
     Shared& S = *reinterpret_cast<Shared*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const u32 tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1403,9 +1417,9 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists, bool de
         u32* val = c->arena.get<u32>(S_TC_VALS, n);
         const size_t psmem = (size_t(P) * (TC_DIM + 1) + size_t(P) * P) * sizeof(f32);
         TT_CUDA(cudaFuncSetAttribute(k_tc_pivots, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psmem)));
-        k_tc_pivots<<<1, PIV_THREADS, psmem, c->stream>>>(x, n, P, piv, rank);
+        launch_pdl(k_tc_pivots, 1, PIV_THREADS, psmem, c->stream, x, n, P, piv, rank);
         TT_LAUNCH("k_tc_pivots");
-        k_tc_assign<<<div_up(div_up(n, 2), 256), 256, P * (TC_DIM + 1) * sizeof(f32), c->stream>>>(x, n, piv, rank,
+        launch_pdl(k_tc_assign, div_up(div_up(n, 2), 256), 256, P * (TC_DIM + 1) * sizeof(f32), c->stream, x, n, piv, rank,
                                                                                                      P, key, val);
         TT_LAUNCH("k_tc_assign");
         c->launches += 2;
@@ -1423,13 +1437,13 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists, bool de
             u32* cell_off = c->arena.get<u32>(S_TC_CELL, u64(P) + 2);
             u64* key2 = c->arena.get<u64>(S_TC_KEY2, n);
             u32* val2 = c->arena.get<u32>(S_TC_VAL2, n);
-            k_tc_cells<<<1, 256, 0, c->stream>>>(skey, n, P, cell_off);
+            launch_pdl(k_tc_cells, 1, 256, 0, c->stream, skey, n, P, cell_off);
             TT_LAUNCH("k_tc_cells");
             f32* spv = c->arena.get<f32>(S_TC_SPV, u64(P) * 16 * (TC_DIM + 1));
             f32* spn = spv + u64(P) * 16 * TC_DIM;
-            k_tc_subpiv<<<div_up(u64(P) * 16 * 32, 256), 256, 0, c->stream>>>(x, perm, cell_off, P, spv, spn);
+            launch_pdl(k_tc_subpiv, div_up(u64(P) * 16 * 32, 256), 256, 0, c->stream, x, perm, cell_off, P, spv, spn);
             TT_LAUNCH("k_tc_subpiv");
-            k_tc_assign2<<<div_up(n, 256), 256, 0, c->stream>>>(x, n, skey, perm, cell_off, spv, spn, key2, val2);
+            launch_pdl(k_tc_assign2, div_up(n, 256), 256, 0, c->stream, x, n, skey, perm, cell_off, spv, spn, key2, val2);
             TT_LAUNCH("k_tc_assign2");
             c->launches += 3;
             perm = radix_sort<u32>(c, key2, val2, n, kb, vb, bits + 4) ? vb : val2;
@@ -1444,7 +1458,7 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists, bool de
     unsigned long long* cnt = c->arena.get<unsigned long long>(S_COUNT, 2);
     TT_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(u32), c->stream));
     TT_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
-    k_tc_tiles<<<ntiles, TC_N, 0, c->stream>>>(x, n, perm, xh, pack, nq, eq, stats);
+    launch_pdl(k_tc_tiles, ntiles, TC_N, 0, c->stream, x, n, perm, xh, pack, nq, eq, stats);
     TT_LAUNCH("k_tc_tiles");
     CUtensorMap map;
     const cuuint64_t gdim[2] = {cuuint64_t(TC_DIM), cuuint64_t(n)};
@@ -1457,7 +1471,7 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists, bool de
     if (r != CUDA_SUCCESS) throw Error(TT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
     TT_CUDA(cudaFuncSetAttribute(k_knn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)));
     const u32 grid = std::min<u32>(ntiles, 2 * u32(c->sms));
-    k_knn_tc<<<grid, 128, TC_SMEM, c->stream>>>(map, pack, eq, n, k, nq, stats, ids, dists, ctl, ctl + 1, cnt);
+    launch_pdl(k_knn_tc, grid, 128, TC_SMEM, c->stream, map, pack, eq, n, k, nq, stats, ids, dists, ctl, ctl + 1, cnt);
     TT_LAUNCH("k_knn_tc");
     c->launches += 2;
     if (!c->tc_host) TT_CUDA(cudaMallocHost(&c->tc_host, 4 * sizeof(unsigned long long)));

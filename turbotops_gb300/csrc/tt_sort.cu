@@ -60,6 +60,8 @@ __device__ T block_exclusive_scan(T v, T* warp_tot, T* total) {
 
 template <typename T>
 __global__ void k_tile_sums(const T* __restrict__ in, u64 n, T* __restrict__ sums) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ T wt[32];
     __shared__ T tot;
     const u64 base = u64(blockIdx.x) * SCAN_TILE;
@@ -76,6 +78,8 @@ __global__ void k_tile_sums(const T* __restrict__ in, u64 n, T* __restrict__ sum
 template <typename T>
 __global__ void k_tile_scan(const T* __restrict__ in, u64 n, const T* __restrict__ offs,
                             T* __restrict__ out, T* __restrict__ total) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ T wt[32];
     __shared__ T tot;
     const u64 base = u64(blockIdx.x) * SCAN_TILE + u64(threadIdx.x) * SCAN_ITEMS;
@@ -153,6 +157,8 @@ __device__ __forceinline__ u32 warp_peers(u32 dg) {
 template <int BINS, typename TM>
 __global__ void __launch_bounds__(RS_THREADS)
 k_rs_upsweep(const u64* __restrict__ keys, TM tm, int shift, u32 width, u32* __restrict__ hist) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ u32 h[RS_WARPS][BINS];
     if (!tm.valid(blockIdx.x)) return;   // past the list: no keys, no counts
     u64 tlo, n;   // this tile's keys: [tlo, n)
@@ -224,6 +230,8 @@ __global__ void __launch_bounds__(RS_THREADS)
 k_rs_scatter(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __restrict__ vin,
              V* __restrict__ vout, u64 n, const unsigned long long* __restrict__ ndev, int shift, u32 width,
              const u32* __restrict__ offs, u32 tiles) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ u32 cnt[RS_WARPS][RS_BINS];   // per-warp running count, then warp prefix
     __shared__ u32 gbase[RS_BINS];
     if (ndev) n = min(n, u64(*ndev));
@@ -293,6 +301,8 @@ template <typename V, bool VALS, typename TM>
 __global__ void __launch_bounds__(RS_THREADS)
 k_rs_scatter_local(const u64* __restrict__ kin, u64* __restrict__ kout, const V* __restrict__ vin,
                    V* __restrict__ vout, TM tm, int shift, u32 width, const u32* __restrict__ offs) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ u64 skey[RS_TILE];
     __shared__ V sval[VALS ? RS_TILE : 1];
     __shared__ u32 cnt[RS_WARPS][RS_LBINS];   // per-warp running count, then warp prefix
@@ -436,7 +446,7 @@ void scan_exclusive(tt_ctx* c, const T* in, T* out, u64 n, T* total, int depth) 
     }
     const u64 tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (tiles == 1) {
-        k_tile_scan<T><<<1, SCAN_THREADS, 0, c->stream>>>(in, n, nullptr, out, total);
+        launch_pdl(k_tile_scan<T>, 1, SCAN_THREADS, 0, c->stream, in, n, static_cast<const T*>(nullptr), out, total);
         TT_LAUNCH("k_tile_scan");
         c->launches += 1;
         return;
@@ -445,16 +455,18 @@ void scan_exclusive(tt_ctx* c, const T* in, T* out, u64 n, T* total, int depth) 
     // sums[0..tiles) tile totals, sums[tiles..2 tiles) their exclusive scan;
     // each recursion level has its own scratch slot
     T* sums = c->arena.get<T>(depth == 0 ? S_SCAN : depth == 1 ? S_SCAN2 : S_SCAN3, 2 * tiles + 2);
-    k_tile_sums<T><<<u32(tiles), SCAN_THREADS, 0, c->stream>>>(in, n, sums);
+    launch_pdl(k_tile_sums<T>, u32(tiles), SCAN_THREADS, 0, c->stream, in, n, sums);
     TT_LAUNCH("k_tile_sums");
     if (tiles <= SCAN_TILE) {
-        k_tile_scan<T><<<1, SCAN_THREADS, 0, c->stream>>>(sums, tiles, nullptr, sums + tiles, nullptr);
+        launch_pdl(k_tile_scan<T>, 1, SCAN_THREADS, 0, c->stream, static_cast<const T*>(sums), tiles,
+                   static_cast<const T*>(nullptr), sums + tiles, static_cast<T*>(nullptr));
         TT_LAUNCH("k_tile_scan");
         c->launches += 1;
     } else {
         scan_exclusive<T>(c, sums, sums + tiles, tiles, nullptr, depth + 1);
     }
-    k_tile_scan<T><<<u32(tiles), SCAN_THREADS, 0, c->stream>>>(in, n, sums + tiles, out, total);
+    launch_pdl(k_tile_scan<T>, u32(tiles), SCAN_THREADS, 0, c->stream, in, n, static_cast<const T*>(sums + tiles), out,
+               total);
     TT_LAUNCH("k_tile_scan");
     c->launches += 2;
 }
@@ -500,20 +512,24 @@ bool radix_sort(tt_ctx* c, u64* keys, V* vals, u64 n, u64* kbuf, V* vbuf, int fo
         const int width = (lo_bit + bits - shift + (passes - q) - 1) / (passes - q);
         const FlatTiles tm{n, ndev, tiles};
         if (local)
-            k_rs_upsweep<RS_LBINS><<<tiles, RS_THREADS, 0, c->stream>>>(ka, tm, shift, u32(width), hist);
+            launch_pdl(k_rs_upsweep<RS_LBINS, FlatTiles>, tiles, RS_THREADS, 0, c->stream, static_cast<const u64*>(ka), tm, shift,
+                       u32(width), hist);
         else
-            k_rs_upsweep<RS_BINS><<<tiles, RS_THREADS, 0, c->stream>>>(ka, tm, shift, u32(width), hist);
+            launch_pdl(k_rs_upsweep<RS_BINS, FlatTiles>, tiles, RS_THREADS, 0, c->stream, static_cast<const u64*>(ka), tm, shift,
+                       u32(width), hist);
         TT_LAUNCH("k_rs_upsweep");
         scan_exclusive<u32>(c, hist, hist, u64(tiles) << width, nullptr, 0);
         if (local && va)
-            k_rs_scatter_local<V, true><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, tm, shift, u32(width),
-                                                                             hist);
+            launch_pdl(k_rs_scatter_local<V, true, FlatTiles>, tiles, RS_THREADS, 0, c->stream,
+                       static_cast<const u64*>(ka), kb, static_cast<const V*>(va), vb, tm, shift, u32(width),
+                       static_cast<const u32*>(hist));
         else if (local)
-            k_rs_scatter_local<V, false><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, tm, shift, u32(width),
-                                                                              hist);
+            launch_pdl(k_rs_scatter_local<V, false, FlatTiles>, tiles, RS_THREADS, 0, c->stream,
+                       static_cast<const u64*>(ka), kb, static_cast<const V*>(va), vb, tm, shift, u32(width),
+                       static_cast<const u32*>(hist));
         else
-            k_rs_scatter<V><<<tiles, RS_THREADS, 0, c->stream>>>(ka, kb, va, vb, n, ndev, shift, u32(width), hist,
-                                                                 tiles);
+            launch_pdl(k_rs_scatter<V>, tiles, RS_THREADS, 0, c->stream, static_cast<const u64*>(ka), kb,
+                       static_cast<const V*>(va), vb, n, ndev, shift, u32(width), static_cast<const u32*>(hist), tiles);
         TT_LAUNCH("k_rs_scatter");
         c->launches += 2;
         std::swap(ka, kb);
@@ -548,11 +564,13 @@ bool radix_sort_segments(tt_ctx* c, u64* keys, u64* kbuf, const u64* seg_off, co
     const SegTiles tm{tl, seg_off, ntiles_dev};
     for (int q = 0; q < passes; ++q) {
         const int width = (lo_bit + bits - shift + (passes - q) - 1) / (passes - q);
-        k_rs_upsweep<RS_LBINS><<<ntiles, RS_THREADS, 0, c->stream>>>(ka, tm, shift, u32(width), hist);
+        launch_pdl(k_rs_upsweep<RS_LBINS, SegTiles>, ntiles, RS_THREADS, 0, c->stream, static_cast<const u64*>(ka), tm, shift,
+                   u32(width), hist);
         TT_LAUNCH("k_rs_upsweep");
         scan_exclusive<u32>(c, hist, hist, hist_entries, nullptr, 0);
-        k_rs_scatter_local<u32, false><<<ntiles, RS_THREADS, 0, c->stream>>>(ka, kb, nullptr, nullptr, tm, shift,
-                                                                              u32(width), hist);
+        launch_pdl(k_rs_scatter_local<u32, false, SegTiles>, ntiles, RS_THREADS, 0, c->stream,
+                   static_cast<const u64*>(ka), kb, static_cast<const u32*>(nullptr), static_cast<u32*>(nullptr), tm,
+                   shift, u32(width), static_cast<const u32*>(hist));
         TT_LAUNCH("k_rs_scatter");
         c->launches += 2;
         std::swap(ka, kb);
