@@ -368,17 +368,19 @@ __global__ void __launch_bounds__(PIV_THREADS) k_tc_pivots(const f32* __restrict
     }
 }
 
-// key[i] = chain rank of the nearest pivot of point i (ties to the lower
-// pivot index), val[i] = i. Two points a thread; the distance order comes
+// key[i] = the nearest pivot of point i (ties to the lower pivot index; the
+// pivots are rows floor(p n / P), read from x, so this runs beside the chain
+// of k_tc_pivots and k_tc_rank maps the index to the chain's rank), val[i] =
+// i. Two points a thread; the distance order comes
 // from |p|^2 - 2 x.p (the assignment only shapes the tile order: any
 // nearest-pivot choice leaves the lists unchanged).
-__global__ void k_tc_assign(const f32* __restrict__ x, u32 n, const f32* __restrict__ piv, const u32* __restrict__ rank,
-                            u32 P, u64* __restrict__ key, u32* __restrict__ val) {
+__global__ void k_tc_assign(const f32* __restrict__ x, u32 n, u32 P, u64* __restrict__ key, u32* __restrict__ val) {
     pdl_wait();
     pdl_trigger();
-    extern __shared__ float4 sp4[];      // P x 8 float4, then P norms
+    extern __shared__ float4 sp4[];      // P x 8 float4 (the pivots: rows floor(p n / P)), then P norms
     f32* pn = reinterpret_cast<f32*>(sp4 + P * 8);
-    for (u32 t = threadIdx.x; t < P * 8; t += blockDim.x) sp4[t] = reinterpret_cast<const float4*>(piv)[t];
+    for (u32 t = threadIdx.x; t < P * 8; t += blockDim.x)
+        sp4[t] = __ldg(reinterpret_cast<const float4*>(x + (u64(t / 8) * n / P) * TC_DIM) + t % 8);
     __syncthreads();
     for (u32 p = threadIdx.x; p < P; p += blockDim.x) {
         f32 s = 0.0f;
@@ -415,12 +417,18 @@ __global__ void k_tc_assign(const f32* __restrict__ x, u32 n, const f32* __restr
         if (e0 < d0) d0 = e0, b0 = p;
         if (e1 < d1) d1 = e1, b1 = p;
     }
-    key[i0] = rank[b0];
+    key[i0] = b0;
     val[i0] = i0;
     if (i0 + 1 < n) {
-        key[i0 + 1] = rank[b1];
+        key[i0 + 1] = b1;
         val[i0 + 1] = i0 + 1;
     }
+}
+
+// key[i] = chain rank of point i's nearest pivot (k_tc_assign leaves the
+// pivot's index: the chain runs beside it, on the side stream).
+__global__ void k_tc_rank(const u32* __restrict__ rank, u32 n, u64* __restrict__ key) {
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) key[i] = rank[u32(key[i])];
 }
 
 // First position of each cell (chain rank) in the rank-sorted keys; cell P
@@ -1417,11 +1425,19 @@ void knn_tc(tt_ctx* c, const f32* x, u32 n, u32 k, u32* ids, f32* dists, bool de
         u32* val = c->arena.get<u32>(S_TC_VALS, n);
         const size_t psmem = (size_t(P) * (TC_DIM + 1) + size_t(P) * P) * sizeof(f32);
         TT_CUDA(cudaFuncSetAttribute(k_tc_pivots, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psmem)));
-        launch_pdl(k_tc_pivots, 1, PIV_THREADS, psmem, c->stream, x, n, P, piv, rank);
-        TT_LAUNCH("k_tc_pivots");
-        launch_pdl(k_tc_assign, div_up(div_up(n, 2), 256), 256, P * (TC_DIM + 1) * sizeof(f32), c->stream, x, n, piv, rank,
-                                                                                                     P, key, val);
-        TT_LAUNCH("k_tc_assign");
+        {   // the pivot chain (one CTA) on the side stream, beside the assignment
+            SideScope side(c);
+            const cudaStream_t ps = side.fork();
+            k_tc_pivots<<<1, PIV_THREADS, psmem, ps>>>(x, n, P, piv, rank);
+            TT_LAUNCH("k_tc_pivots");
+            launch_pdl(k_tc_assign, div_up(div_up(n, 2), 256), 256, P * (TC_DIM + 1) * sizeof(f32), c->stream, x, n, P,
+                       key, val);
+            TT_LAUNCH("k_tc_assign");
+            side.join();
+        }
+        k_tc_rank<<<std::min<u32>(div_up(n, 256), 4 * u32(c->sms)), 256, 0, c->stream>>>(rank, n, key);
+        TT_LAUNCH("k_tc_rank");
+        c->launches += 1;
         c->launches += 2;
         perm = val;
         u64* skey = key;
